@@ -1,0 +1,286 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 MRiLab scan engine (one JSON line on rank 0).
+
+Metric: spin*pool*steps/s -- active isochromats (voxel x spin) x pools x
+sequence steps with dt > 0 integrated per second -- on the two-pool exchange
+3D multi-echo GRE workload (128 x 128 x 32 voxels, 4 spins, free + myelin
+water exchanging, 8 Rx coils, 6 echoes; 32 x 8 phase/partition encodes of
+128 samples), seeded synthetic data.
+
+* ``value``: device throughput of a prepared scan (inputs resident in HBM,
+  ``mrl_plan_execute``), each of K steps one whole scan timed with CUDA
+  events on the launching stream, L2 flushed between steps.
+* ``e2e``: the same metric through ``mrl_scan`` -- the call the mex layer
+  makes -- with host buffers; host<->device copies are inside the region.
+* ``roofline``: FP32-pipe bound of the scan kernel from the algorithmic op
+  table (flops per isochromat-pool-step), against FP32 and MUFU peaks
+  measured on this GPU by ``libmrl_peaks.so``.
+* ``cpu_baseline``: the reference scan algorithm on the host cores (the
+  single-precision oracle port, all threads) on a bounded sample of the same
+  workload.
+
+``--impl reference`` times that CPU implementation alone (the reference's
+own CPU path; there is no GPU reference on this path) and prints its line.
+Multi-GPU: one independent scan per rank (voxel ranges shard with no data
+exchange; "replicas"), value = all ranks' units / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "spin*pool*steps/s"
+UNIT = "spin*pool*steps/s"
+
+# Algorithmic op table per isochromat-pool-step (FMA = 2 flops; MUFU =
+# sin, cos, rsqrt, ex2, lg2).
+OPS = dict(free_flops=17, free_mufu=2, rf_flops=50, rf_mufu=5, tx_flops=4, tx_mufu=2, exch_flops=8,
+           bound_flops=3, recv_flops=8)
+
+
+def workload_args(name, n_tr):
+    from mrilab_gb300 import phantoms
+
+    if name == "config2":
+        sc = phantoms.config2_me_gre(seed=0, n_tr=n_tr)
+        desc = dict(workload="two-pool exchange 3D multi-echo GRE, 128x128x32 voxels, 4 spins, 8 Rx, "
+                             "6 echoes, 32x8 encodes x 128 samples", model="me", voxels=128 * 128 * 32, spins=4,
+                    pools=2, rx=8, trs=int(sc.VCtl["TRNum"]))
+    elif name == "config1":
+        sc = phantoms.config1_gre(seed=0, n_tr=n_tr)
+        desc = dict(workload="single-pool 2D GRE, 64x64, 64 phase encodes x 64 samples", model="normal",
+                    voxels=64 * 64, spins=1, pools=1, rx=1, trs=int(sc.VCtl["TRNum"]))
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return sc, desc
+
+
+def op_counts(work, desc):
+    """Algorithmic FP32 flops and MUFU ops of one scan from the op table."""
+    iso_pools = work["units"] / max(1, work["steps"])
+    steps, rf, samples = work["steps"], work["rf_steps"], work["samples"]
+    P = desc["pools"]
+    flops = iso_pools * (rf * OPS["rf_flops"] + (steps - rf) * OPS["free_flops"])
+    mufu = iso_pools * (rf * OPS["rf_mufu"] + (steps - rf) * OPS["free_mufu"])
+    if desc["model"] in ("me", "gm"):
+        flops += iso_pools * steps * (P - 1) * OPS["exch_flops"]
+    flops += samples * iso_pools * desc["rx"] * OPS["recv_flops"]
+    return flops, mufu
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    from mrilab_gb300 import build
+
+    lib = ctypes.CDLL(build.PEAKS)
+    lib.mrl_probe_peaks.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    f, m = ctypes.c_double(), ctypes.c_double()
+    lib.mrl_probe_peaks(ctypes.byref(f), ctypes.byref(m))
+    return f.value, m.value
+
+
+def cpu_baseline(sc, target_s=12.0):
+    """The reference scan algorithm on the host cores (single-precision
+    oracle port, all threads) on the first steps of the same workload."""
+    import oracle
+
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    probe = oracle.run_port(sc, "f32", threads=threads, max_steps=8)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    steps = int(max(8, min(probe["steps"] * target_s / dt, 10**7)))
+    t0 = time.perf_counter()
+    out = oracle.run_port(sc, "f32", threads=threads, max_steps=steps)
+    el = time.perf_counter() - t0
+    units = sc.units() / max(1, count_steps(sc)) * out["steps"]
+    return dict(value=units / el, unit=UNIT, cores=threads, kind="port",
+                sample=f"first {out['steps']} dt>0 steps of the workload ({units:.3g} units, {el:.1f} s)")
+
+
+def count_steps(sc):
+    return int(np.count_nonzero(np.diff(sc.VSeq["utsLine"]) > 0))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config2", choices=["config2", "config1"])
+    ap.add_argument("--n-tr", type=int, default=None, help="TRs of the workload (default: all)")
+    ap.add_argument("--numerics", default="accurate", choices=["accurate", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    sc, desc = workload_args(args.workload, args.n_tr)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        vals = []
+        base = None
+        for i in range(args.warmup + args.steps):
+            base = cpu_baseline(sc, target_s=8.0)
+            if i >= args.warmup:
+                vals.append(base["value"])
+        v = float(np.mean(vals))
+        print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                          "scaling": "weak", "dtype": "f32", "data": "synthetic", "config": desc,
+                          "cpu_baseline": dict(base, value=v),
+                          "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                          "vs_baseline": None}))
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from mrilab_gb300 import engine
+
+    plan = engine.Plan(sc, numerics=args.numerics, gpu_index=local)
+    work = plan.work()
+    stream = torch.cuda.Stream()
+    flush = torch.empty(int(256 * 2**20), dtype=torch.uint8, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        plan.execute(stream.cuda_stream)
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(local) as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.fill_(1)  # L2 flush between timed scans (outside the events)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.execute(stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    out = plan.download()
+    total_ms = float(np.sum(times))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = work["units"] * args.steps * world / (total_ms * 1e-3)
+
+    # e2e through the C ABI with host buffers (what the mex layer calls)
+    e2e_runs = max(1, min(args.steps, 2))
+    e2e_t = []
+    tm = None
+    for _ in range(e2e_runs):
+        t0 = time.perf_counter()
+        engine.scan(sc, numerics=args.numerics, gpu_index=local)
+        e2e_t.append(time.perf_counter() - t0)
+        tm = engine.last_timing()
+    e2e_value = work["units"] * world / float(np.mean(e2e_t))
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    fp32_tf, mufu_g = peaks()
+    flops, mufu = op_counts(work, desc)
+    ms_per_scan = total_ms / args.steps
+    scan_share = tm["scan_ms"] / max(1e-9, tm["scan_ms"] + tm["reduce_ms"])
+    scan_ms = ms_per_scan * scan_share
+    achieved_tf = flops / (scan_ms * 1e-3) / 1e12
+    achieved_mufu = mufu / (scan_ms * 1e-3) / 1e9
+    roof = {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_tf, "unit": "TFLOP/s",
+            "frac": achieved_tf / fp32_tf, "traffic": None,
+            "mufu": {"achieved": achieved_mufu, "peak": mufu_g, "unit": "Gop/s", "frac": achieved_mufu / mufu_g},
+            "peak_source": "measured on this GPU by libmrl_peaks.so (FFMA / MUFU.SIN chains)",
+            "kernel": "scan kernel", "share_of_step": scan_share,
+            "flops_per_scan": flops, "mufu_per_scan": mufu, "scan_kernel_ms_per_scan": scan_ms}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_scan, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(desc, numerics=args.numerics, l2="flushed between timed steps (256 MiB write)",
+                       units_per_step=work["units"], steps_per_scan=work["steps"], samples=work["samples"]),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": tm["h2d_bytes"],
+                "d2h_bytes_per_step": tm["d2h_bytes"], "ms_per_step": float(np.mean(e2e_t)) * 1e3},
+        "gpu_launches": work["launches"] * args.steps,
+        "roofline": roof,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(sc)
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,198 @@
+/*
+ * mrl_scan.h -- C ABI of the GB300 MRiLab scan engine (libmrl_scan.so).
+ *
+ * The engine replaces the discrete Bloch integration behind MRiLab's mex
+ * engines.  Those engines take no arguments and read/mutate the MATLAB
+ * globals VObj, VMag, VCoi, VCtl, VSeq, VVar and VSig in place
+ * (Lib/src/engine/GPUEngine/DoScanAtGPU.cu:76-214); this ABI passes the same
+ * arrays explicitly, as plain pointers in MATLAB's column-major layout, so a
+ * thin mex layer (mrilab_gb300/csrc/mex_wrappers.cpp) or any FFI can bind it.
+ * No type here depends on MATLAB, CUDA or PyTorch.
+ *
+ * Layouts (V = ny*nx*nz voxels, S spins, P pools, Tx/Rx coils, A samples):
+ *   per-voxel maps            [V]           dB0, Gzgrid, Gygrid, Gxgrid
+ *   per-pool maps             [P][V]        Rho, T1, T2
+ *   isochromat maps           [P][S][V]     Mx, My, Mz, dWRnd
+ *   exchange channels         [nK][V]       K (layout depends on the model)
+ *   coil maps                 [Tx|Rx][V]    TxCoilmg/pe, RxCoilx/y
+ *   signal                    [P][Rx][A]    Sx, Sy (double)
+ * with the voxel index v = y + ny*(x + nx*z).
+ */
+#ifndef MRL_SCAN_H
+#define MRL_SCAN_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MRL_ABI_VERSION 1
+
+/* Tissue models: one per reference engine. */
+typedef enum {
+    MRL_MODEL_NORMAL = 0, /* DoScanAtGPU      (BlochKernel.cuh): independent pools */
+    MRL_MODEL_ME = 1,     /* DoMEScanAtGPU    (BlochKernelME.cuh): exchanging free pools,
+                             K channel t*P+p = rate t->p */
+    MRL_MODEL_MT = 2,     /* DoMTScanAtGPU    (BlochKernelMT.cuh): free + bound pool,
+                             K channel 1 = K12 (free->bound), 2 = K21 */
+    MRL_MODEL_CEST = 3,   /* DoCESTScanAtGPU  (BlochKernelCEST.cuh): free, MT-bound, CEST
+                             pools; channel t-1 = free->t, t+P-2 = t->free,
+                             0 = free->MT, P-1 = MT->free */
+    MRL_MODEL_GM = 4      /* DoGMScanAtGPU    (BlochKernelGM.cuh): TypeFlag 0 free / 1 bound,
+                             K channel p*P+t = rate t->p */
+} mrl_model;
+
+/* Arithmetic of the integrator. */
+typedef enum {
+    /* FP32 state and arithmetic; gradient/off-resonance phase carried in
+     * FP64 so long trains do not drift; compared with the all-FP64 oracle. */
+    MRL_NUMERICS_ACCURATE = 0,
+    /* The reference engine's own single-precision operation order
+     * (BlochKernel.h for one pool, BlochKernel*.cuh otherwise), evaluated
+     * without fused multiply-add and with correctly rounded FP32 math, for
+     * bit-level parity studies against the reference CPU engine. */
+    MRL_NUMERICS_REFERENCE = 1
+} mrl_numerics;
+
+typedef enum {
+    MRL_OK = 0,
+    MRL_ERR_ARG = -1,         /* inconsistent sizes, NULL pointers, bad model */
+    MRL_ERR_CUDA = -2,        /* a CUDA call failed (see mrl_last_error) */
+    MRL_ERR_NOMEM = -3,       /* device or host allocation failed */
+    MRL_ERR_EXT = -4,         /* an Ext plugin callback reported an error */
+    MRL_ERR_TIMEOUT = -5,     /* a bounded device wait gave up */
+    MRL_ERR_UNSUPPORTED = -6, /* a size the build does not support */
+    MRL_ERR_NO_DEVICE = -7    /* no usable CUDA device */
+} mrl_status;
+
+/* VObj (Src/Main/DoDataTypeConv.m:34-64) */
+typedef struct {
+    int ny, nx, nz;      /* spin-matrix rows, columns, slices */
+    int spin_num;        /* SpinNum */
+    int type_num;        /* TypeNum (pools) */
+    double gyro;         /* Gyro, rad/s/T */
+    const float *rho, *t1, *t2; /* [P][V] */
+    const float *k;      /* [k_channels][V], NULL for MRL_MODEL_NORMAL */
+    int k_channels;
+    const double *type_flag; /* [P], MRL_MODEL_GM only */
+    float *mx, *my, *mz; /* [P][S][V], updated in place */
+} mrl_object;
+
+/* VMag */
+typedef struct {
+    const float *db0;    /* [V], tesla */
+    const float *dwrnd;  /* [P][S][V], rad/s */
+    const float *gzgrid, *gygrid, *gxgrid; /* [V], metres */
+} mrl_field;
+
+/* VCoi */
+typedef struct {
+    int tx_num, rx_num;
+    double tx_default, rx_default; /* nonzero: uniform coil, maps ignored */
+    const float *tx_mg, *tx_pe;    /* [Tx][V] */
+    const float *rx_x, *rx_y;      /* [Rx][V] */
+} mrl_coils;
+
+/* VCtl */
+typedef struct {
+    const double *cs;    /* [P] chemical shift, Hz */
+    int tr_num;
+    int run_mode;        /* 0 scan; 1 = per-step history (requires sig.mxs..) */
+    int gpu_index;       /* cudaSetDevice index */
+    int numerics;        /* mrl_numerics */
+} mrl_control;
+
+/* VSeq lines (Src/Main/DoPulseGen.m:43-111) */
+typedef struct {
+    const double *uts, *ts, *rf_amp, *rf_phase, *rf_freq, *rf_coil;
+    const double *gz, *gy, *gx, *adc, *ext;
+    const double *flags; /* [len(ts)][6] */
+    int n_uts, n_ts, n_rf, n_gz, n_gy, n_gx, n_adc, n_ext;
+} mrl_sequence;
+
+/* VVar: the pulse-packet cursor, read at entry and written back at exit
+ * and around every Ext callback (DoScanAtGPU.cu:378-477).  Any pointer may
+ * be NULL, in which case the engine keeps that field internally. */
+typedef struct {
+    double *t, *dt, *rf_amp, *rf_phase, *rf_freq, *rf_coil, *rf_ref;
+    double *gz, *gy, *gx, *adc, *ext, *kz, *ky, *kx, *gpu_fetch;
+    int *utsi, *rfi, *gzi, *gyi, *gxi, *adci, *exti, *tr_count;
+} mrl_state;
+
+/* VSig */
+typedef struct {
+    double *sx, *sy;         /* [P][Rx][A]; each acquired sample is assigned */
+    double *kz, *ky, *kx;    /* [A]; accumulated (+=) like the reference */
+    int signal_num;          /* A */
+    float *mxs, *mys, *mzs;  /* RunMode 1 history [len(uts)][P][S][V], may be NULL */
+    double *muts;            /* RunMode 1 step times [len(uts)], may be NULL */
+} mrl_signal;
+
+typedef struct {
+    int abi_version;         /* MRL_ABI_VERSION */
+    int model;               /* mrl_model */
+    mrl_object obj;
+    mrl_field mag;
+    mrl_coils coil;
+    mrl_control ctl;
+    mrl_sequence seq;
+    mrl_state var;
+    mrl_signal sig;
+} mrl_scan_args;
+
+/* Ext events.  At every Ext sample whose value is nonzero the engine
+ * finishes the steps before it, makes Sx/Sy and the VVar cursor current on
+ * the host and calls the callback twice, mirroring DoScanAtGPU.cu:565-660:
+ *   what = MRL_EXT_FETCH : return nonzero to have the magnetisation
+ *                          (obj.mx/my/mz) written back to the host before
+ *                          the plugin runs and read again after it;
+ *   what = MRL_EXT_PLUGIN: run the plugin; return 0 on success.
+ * The callback may replace any pointer in *args (MATLAB may reallocate);
+ * the engine re-reads them after each call. */
+enum { MRL_EXT_FETCH = 1, MRL_EXT_PLUGIN = 2 };
+typedef int (*mrl_ext_fn)(void *user, mrl_scan_args *args, int what);
+
+/* Run a scan.  Replaces the integration behind the mex entry points
+ * DoScanAtGPU / DoMEScanAtGPU / DoMTScanAtGPU / DoCESTScanAtGPU /
+ * DoGMScanAtGPU (each `void mexFunction(int, mxArray*[], int, const
+ * mxArray*[])`, e.g. Lib/src/engine/GPUEngine/DoScanAtGPU.cu:76), with the
+ * model selected by args->model.  Returns an mrl_status. */
+int mrl_scan(mrl_scan_args *args, mrl_ext_fn ext, void *user);
+
+/* Prepared scans.  A plan uploads the active voxels, decodes the whole
+ * sequence and sizes every device buffer once; mrl_plan_execute then
+ * re-runs the scan from the initial magnetisation entirely on the device
+ * (asynchronously on `stream`, a cudaStream_t or NULL for the legacy
+ * stream), and mrl_plan_download writes Sx/Sy and the final Mx/My/Mz into
+ * the host arrays named by `args`.  Sequences with Ext events need the
+ * callback path of mrl_scan and are rejected (MRL_ERR_UNSUPPORTED).  No
+ * counterpart in the reference, which re-uploads everything per call
+ * (DoScanAtGPU.cu:257-334). */
+typedef struct mrl_plan mrl_plan;
+int mrl_plan_create(const mrl_scan_args *args, mrl_plan **out);
+int mrl_plan_execute(mrl_plan *plan, void *stream);
+int mrl_plan_download(mrl_plan *plan, mrl_scan_args *args);
+/* Work of one execution: isochromat-pool-steps (active isochromats x pools
+ * x dt>0 steps), dt>0 steps, of which rf-on steps, acquired samples, kernel
+ * launches. */
+int mrl_plan_work(const mrl_plan *plan, long long out[5]);
+void mrl_plan_destroy(mrl_plan *plan);
+
+/* Human-readable text for a status code (reference: errors were printed
+ * with mexPrintf or raised with mexErrMsgTxt, DoScanAtGPU.cu:231-242,566). */
+const char *mrl_status_string(int status);
+
+/* Detail of the last failure on the calling thread ("" if none). */
+const char *mrl_last_error(void);
+
+/* Timing of the last mrl_scan on the calling thread: [0] whole call (ms),
+ * [1] device time of the scan kernels (ms), [2] device time of the receive
+ * reduction (ms), [3] host-to-device copies (ms), [4] device-to-host copies
+ * (ms), [5] kernel launches, [6] bytes copied host-to-device, [7] bytes
+ * copied device-to-host.  New in this engine; the reference has no
+ * counterpart. */
+int mrl_last_timing(double out[8]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,192 @@
+// Sequence decoder (see decode.h).  Restates DoScanAtGPU.cu:339-477 and the
+// Ext/TR-boundary bookkeeping around it (:478-481,662-763).
+#include "decode.h"
+
+#include <cmath>
+
+namespace mrl {
+
+namespace {
+constexpr double kPi = 3.14159265359;  // the reference's constant (DoScanAtGPU.cu:68)
+
+// Smaller-magnitude end of the interval starting at line[idx]
+// (DoScanAtGPU.cu:429-455).
+inline double hold(const double *line, int n, int idx) {
+    int nxt = idx + 1 < n - 1 ? idx + 1 : n - 1;
+    if (std::fabs(line[idx]) <= std::fabs(line[nxt])) return line[idx];
+    return line[idx + 1 < n ? idx + 1 : n - 1];
+}
+}  // namespace
+
+void load_state(DecodeState &s, const mrl_state &v, int tx) {
+#define LD(f) \
+    if (v.f) s.f = *v.f;
+    LD(t) LD(dt) LD(rf_coil) LD(rf_ref) LD(gz) LD(gy) LD(gx) LD(adc) LD(ext) LD(kz) LD(ky) LD(kx) LD(gpu_fetch)
+    LD(utsi) LD(rfi) LD(gzi) LD(gyi) LD(gxi) LD(adci) LD(exti) LD(tr_count)
+#undef LD
+    for (int c = 0; c < tx; ++c) {
+        if (v.rf_amp) s.rf_amp[c] = v.rf_amp[c];
+        if (v.rf_phase) s.rf_phase[c] = v.rf_phase[c];
+        if (v.rf_freq) s.rf_freq[c] = v.rf_freq[c];
+    }
+}
+
+void store_state(const DecodeState &s, mrl_state &v, int tx) {
+#define ST(f) \
+    if (v.f) *v.f = s.f;
+    ST(t) ST(dt) ST(rf_coil) ST(gz) ST(gy) ST(gx) ST(adc) ST(ext) ST(kz) ST(ky) ST(kx)
+    ST(utsi) ST(rfi) ST(gzi) ST(gyi) ST(gxi) ST(adci) ST(exti) ST(tr_count)
+#undef ST
+    for (int c = 0; c < tx; ++c) {
+        if (v.rf_amp) v.rf_amp[c] = s.rf_amp[c];
+        if (v.rf_phase) v.rf_phase[c] = s.rf_phase[c];
+        if (v.rf_freq) v.rf_freq[c] = s.rf_freq[c];
+    }
+}
+
+namespace {
+// Second half of a time point: Ext cursor, packet reset, TR count.
+void finish_time_point(DecodeState &s, int tx, bool ext_flag, double flag_sum, double dt) {
+    if (ext_flag) s.exti++;
+    if (flag_sum == 0) {  // no channel fired: reset the pulse packet (:463-472)
+        for (int c = 0; c < tx; ++c) s.rf_amp[c] = s.rf_phase[c] = s.rf_freq[c] = 0;
+        s.gz = s.gy = s.gx = 0;
+        s.adc = 0;
+        s.ext = 0;
+    }
+    if (dt < 0) s.tr_count++;  // TR boundary (:759-762)
+}
+}  // namespace
+
+void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx, double gyro, mrl_signal &sig,
+                      DecodeChunk &out) {
+    const int stride = record_stride_f4(tx) * 4;
+    out.records.clear();
+    out.step_adc.clear();
+    out.n_steps = 0;
+    out.n_rf_steps = 0;
+    out.adc_begin = s.signali;
+    out.stopped_at_ext = false;
+    if (s.pend_active) {
+        finish_time_point(s, tx, s.pend_ext, s.pend_flag_sum, s.pend_dt);
+        s.pend_active = false;
+    }
+    const int max_step = q.n_ts;
+    while (!s.done) {
+        if (s.i >= max_step) {
+            s.done = true;
+            break;
+        }
+        double flag[6] = {0, 0, 0, 0, 0, 0};
+        auto add_flags = [&](int k) {
+            for (int f = 0; f < 6; ++f) flag[f] += q.flags[(long)k * 6 + f];
+        };
+        // entries with equal times merge (:346-376); the reference reads
+        // tsLine[i+1] one past the end at i = MaxStep-1: treated as different
+        if (s.i + 1 >= max_step || q.ts[s.i] != q.ts[s.i + 1]) {
+            add_flags(s.i);
+            s.i++;
+        } else {
+            add_flags(s.i);
+            while (s.i + 1 < max_step && q.ts[s.i] == q.ts[s.i + 1]) {
+                add_flags(s.i + 1);
+                s.i++;
+                if (s.i == max_step - 1) break;
+            }
+            s.i++;
+        }
+        const int nu = q.n_uts;
+        const int cur = s.utsi < nu ? s.utsi : nu - 1;
+        const int nxt = cur + 1 < nu - 1 ? cur + 1 : nu - 1;
+        s.t = q.uts[cur];
+        s.dt = q.uts[nxt] - q.uts[cur];
+        s.utsi = nxt;
+        const double dt = s.dt;
+
+        if (flag[0] >= 1) {  // rf: one update per merged rf entry (:385-419)
+            for (int j = 0; j < flag[0]; ++j) {
+                if (s.rfi >= q.n_rf) break;
+                s.rf_coil = q.rf_coil[s.rfi];
+                int txi = (int)s.rf_coil;
+                for (int k = s.rfi + 1; k < q.n_rf; ++k) {
+                    if (s.rf_coil == q.rf_coil[k]) {
+                        if (txi >= 1 && txi <= tx) {
+                            const int a = s.rfi;
+                            s.rf_amp[txi - 1] = std::fabs(q.rf_amp[a]) <= std::fabs(q.rf_amp[k]) ? q.rf_amp[a] : q.rf_amp[k];
+                            s.rf_phase[txi - 1] =
+                                std::fabs(q.rf_phase[a]) <= std::fabs(q.rf_phase[k]) ? q.rf_phase[a] : q.rf_phase[k];
+                            s.rf_freq[txi - 1] = std::fabs(q.rf_freq[a]) <= std::fabs(q.rf_freq[k]) ? q.rf_freq[a] : q.rf_freq[k];
+                        }
+                        break;
+                    }
+                }
+                s.rfi++;
+            }
+            // a negative amplitude becomes a phase shift of pi (:413-418)
+            for (int c = 0; c < tx; ++c) {
+                if (s.rf_amp[c] < 0) {
+                    s.rf_amp[c] = std::fabs(s.rf_amp[c]);
+                    s.rf_phase[c] = s.rf_phase[c] + kPi;
+                }
+            }
+        }
+        if (flag[1] == 1 && s.gzi < q.n_gz) s.gz = hold(q.gz, q.n_gz, s.gzi++);
+        if (flag[2] == 1 && s.gyi < q.n_gy) s.gy = hold(q.gy, q.n_gy, s.gyi++);
+        if (flag[3] == 1 && s.gxi < q.n_gx) s.gx = hold(q.gx, q.n_gx, s.gxi++);
+        s.adc = 0;
+        if (flag[4] == 1 && s.adci < q.n_adc) s.adc = q.adc[s.adci++];
+
+        if (dt > 0) {
+            const size_t base = out.records.size();
+            out.records.resize(base + stride, 0.f);
+            float *r = &out.records[base];
+            r[0] = (float)dt;
+            r[1] = (float)s.gz;
+            r[2] = (float)s.gy;
+            r[3] = (float)s.gx;
+            r[4] = (float)s.rf_amp[0];
+            r[5] = (float)s.rf_phase[0];
+            r[6] = (float)s.rf_freq[0];
+            r[7] = (float)s.adc;
+            for (int c = 1; c < tx; ++c) {
+                r[4 + 4 * c + 0] = (float)s.rf_amp[c];
+                r[4 + 4 * c + 1] = (float)s.rf_phase[c];
+                r[4 + 4 * c + 2] = (float)s.rf_freq[c];
+            }
+            bool rf_on = false;
+            for (int c = 0; c < tx; ++c) rf_on |= (float)s.rf_amp[c] != 0.f;
+            out.n_rf_steps += rf_on;
+            out.step_adc.push_back(s.adc == 1 ? s.signali : -1);
+            out.n_steps++;
+        }
+        if (s.adc == 1) {  // k-space position of the sample (:466-472)
+            if (s.signali < sig.signal_num) {
+                if (sig.kz) sig.kz[s.signali] += s.kz;
+                if (sig.ky) sig.ky[s.signali] += s.ky;
+                if (sig.kx) sig.kx[s.signali] += s.kx;
+            }
+            s.signali++;
+        }
+        s.kz += s.gz * dt * (gyro / (2 * kPi));
+        s.ky += s.gy * dt * (gyro / (2 * kPi));
+        s.kx += s.gx * dt * (gyro / (2 * kPi));
+
+        const bool ext_flag = flag[5] == 1;
+        const double flag_sum = flag[0] + flag[1] + flag[2] + flag[3] + flag[4] + flag[5];
+        if (ext_flag && s.exti < q.n_ext) {
+            s.ext = q.ext[s.exti];
+            if (s.ext != 0) {  // stop: the engine flushes, then runs the plugin
+                s.pend_active = true;
+                s.pend_ext = ext_flag;
+                s.pend_flag_sum = flag_sum;
+                s.pend_dt = dt;
+                out.stopped_at_ext = true;
+                break;
+            }
+        }
+        finish_time_point(s, tx, ext_flag, flag_sum, dt);
+    }
+    out.adc_end = s.signali;
+}
+
+}  // namespace mrl

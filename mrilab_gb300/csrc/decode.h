@@ -1,0 +1,59 @@
+// Sequence decoder: turns VSeq lines into per-step records for the device.
+//
+// Restates the host loop of the reference GPU engines
+// (Lib/src/engine/GPUEngine/DoScanAtGPU.cu:339-477): entries of tsLine that
+// share one time are merged by OR-ing (summing) their channel flags; at each
+// unique time the rf / gradient values are updated by sample-and-hold of the
+// smaller-magnitude end of the interval; a time point with no flag resets
+// the pulse packet to zero; steps with dt > 0 are emitted; dt < 0 marks a TR
+// boundary.  The decoder stops at every Ext sample with a nonzero value so
+// the engine can run the plugin and then resume with the (possibly edited)
+// VVar cursor.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "../../include/mrl_scan.h"
+
+namespace mrl {
+
+constexpr int kMaxTx = 8;
+
+// Device step record: float4 {dt, Gz, Gy, Gx}, float4 {amp0, phase0, freq0,
+// adc}, then one float4 {amp, phase, freq, 0} per extra Tx coil.
+inline int record_stride_f4(int tx_num) { return 2 + (tx_num - 1); }
+
+struct DecodeState {
+    // VVar
+    double t = 0, dt = 0, rf_coil = 0, rf_ref = 0;
+    double rf_amp[kMaxTx] = {0}, rf_phase[kMaxTx] = {0}, rf_freq[kMaxTx] = {0};
+    double gz = 0, gy = 0, gx = 0, adc = 0, ext = 0, kz = 0, ky = 0, kx = 0, gpu_fetch = 0;
+    int utsi = 0, rfi = 0, gzi = 0, gyi = 0, gxi = 0, adci = 0, exti = 0, tr_count = 0;
+    // decoder position
+    int i = 0;        // tsLine cursor
+    int signali = 0;  // next ADC sample index
+    bool done = false;
+    // second half of a time point interrupted by an Ext stop
+    bool pend_active = false, pend_ext = false;
+    double pend_flag_sum = 0, pend_dt = 0;
+};
+
+struct DecodeChunk {
+    std::vector<float> records;      // n_steps * stride floats
+    std::vector<int> step_adc;       // per step: ADC sample index, or -1
+    int64_t n_steps = 0;
+    int adc_begin = 0, adc_end = 0;  // sample indices acquired in this chunk
+    int n_rf_steps = 0;              // steps with rf on
+    bool stopped_at_ext = false;     // true: an Ext callback is due now
+};
+
+void load_state(DecodeState &s, const mrl_state &v, int tx_num);
+void store_state(const DecodeState &s, mrl_state &v, int tx_num);
+
+// Decode until the next nonzero Ext sample or the end of the sequence.
+// K-space positions of acquired samples are accumulated into sig.kx/ky/kz.
+void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx_num, double gyro, mrl_signal &sig,
+                      DecodeChunk &out);
+
+}  // namespace mrl

@@ -1,0 +1,739 @@
+// mrl_scan: host side of the GB300 scan engine.
+//
+// One call replaces the body of a reference GPU mex engine
+// (Lib/src/engine/GPUEngine/DoScanAtGPU.cu:215-787 and its ME/MT/CEST/GM
+// variants): bind inputs, upload the active voxels once, decode the
+// sequence, integrate on the device, sum the receive signal, service Ext
+// callbacks, and write the results back in place.
+//
+// Differences in structure from the reference (results are the same):
+//   * voxels whose pools are all empty (T1, T2 or Rho zero) are compacted
+//     away before upload instead of being skipped inside the kernel;
+//   * the magnetisation stays on the device for the whole scan: kernels are
+//     launched per block of steps, not per TR, and only Ext events bring
+//     data back to the host;
+//   * the receive sum is reduced on the device in FP64 instead of
+//     downloading per-column partial signals every TR.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mrl_scan.h"
+#include "decode.h"
+#include "scan_launch.h"
+
+namespace mrl {
+
+namespace {
+
+thread_local std::string g_err;
+thread_local double g_timing[8];
+
+void set_err(const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+
+constexpr double kPiRef = 3.14159265359;
+
+// Receive reduction: Sx/Sy[pool][coil][signal] = sum over blocks of the
+// per-block partial sums, in FP64, then demodulated by rfRef
+// (BlochKernel.cuh:160-170 applies the same rotation per isochromat).
+__global__ void reduce_partials(const float2 *__restrict__ partial, int nblk, int a_launch, int npairs, int rx,
+                                const int *__restrict__ amap, int A, double *sx, double *sy, double cr, double sr) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= a_launch * npairs) return;
+    const int a = o / npairs;
+    const int pair = o - a * npairs;
+    double x = 0.0, y = 0.0;
+    for (int b = 0; b < nblk; ++b) {
+        const float2 p = partial[((long long)b * a_launch + a) * npairs + pair];
+        x += (double)p.x;
+        y += (double)p.y;
+    }
+    const int sig = amap[a];
+    if (sig < 0 || sig >= A) return;
+    const int t = pair / rx;
+    const int c = pair - t * rx;
+    const long long idx = ((long long)t * rx + c) * A + sig;
+    sx[idx] = cr * x - sr * y;
+    sy[idx] = sr * x + cr * y;
+}
+
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t ensure(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) n = std::max<size_t>(count, 1);
+        return e;
+    }
+};
+
+struct ModelInfo {
+    int km;        // KModel
+    int nsamp;     // pools with a receive signal slot that can be nonzero
+    int nk;        // exchange channels read
+    bool gm;
+};
+
+// Active-voxel rule of each model: the reference kernels skip a pool (or,
+// for MT/CEST, the whole voxel) whose T1, T2 or Rho is zero
+// (BlochKernel.cuh:103, BlochKernelGM.cuh:176, BlochKernelMT.cuh:123).
+bool voxel_active(const mrl_scan_args &a, int km, long long v, long long V) {
+    const int P = a.obj.type_num;
+    auto pool = [&](int t) {
+        return a.obj.t1[t * V + v] != 0.f && a.obj.t2[t * V + v] != 0.f && a.obj.rho[t * V + v] != 0.f;
+    };
+    if (km == KM_MT || km == KM_CEST) return pool(0);
+    for (int t = 0; t < P; ++t)
+        if (pool(t)) return true;
+    return false;
+}
+
+struct Scanner {
+    mrl_scan_args *args;
+    mrl_ext_fn ext;
+    void *user;
+    ModelInfo mi{};
+    int P = 0, S = 0, TX = 0, RX = 0, A = 0, NS = 1, tpv = 1, stride4 = 2;
+    long long V = 0;
+    int n_act = 0;
+    std::vector<long long> act;  // compact index -> voxel
+    cudaStream_t st = nullptr;
+    DevBuf<float> d_f;           // all per-voxel float fields, packed
+    DevBuf<float> d_m;           // mx | my | mz
+    DevBuf<float2> d_rx;
+    DevBuf<float4> d_rec;
+    DevBuf<float2> d_part;
+    DevBuf<int> d_amap;
+    DevBuf<double> d_sx, d_sy;
+    DevBuf<int> d_err;
+    // offsets into d_f
+    size_t o_gx = 0, o_gy = 0, o_gz = 0, o_db0 = 0, o_txmg = 0, o_txpe = 0, o_rho = 0, o_t1 = 0, o_t2 = 0, o_k = 0,
+           o_dwr = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_scan, ev_red;
+    int launches = 0;
+    double h2d_ms = 0, d2h_ms = 0, h2d_bytes = 0, d2h_bytes = 0;
+
+    ~Scanner() {
+        for (auto &e : ev_scan) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
+        for (auto &e : ev_red) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    int fail_cuda(cudaError_t e, const char *what) {
+        set_err("%s: %s", what, cudaGetErrorString(e));
+        return MRL_ERR_CUDA;
+    }
+
+    int validate() {
+        const mrl_scan_args &a = *args;
+        if (a.abi_version != MRL_ABI_VERSION) return set_err("abi_version %d, expected %d", a.abi_version, MRL_ABI_VERSION), MRL_ERR_ARG;
+        P = a.obj.type_num;
+        S = a.obj.spin_num;
+        TX = a.coil.tx_num;
+        RX = a.coil.rx_num;
+        A = a.sig.signal_num;
+        V = (long long)a.obj.ny * a.obj.nx * a.obj.nz;
+        if (V <= 0 || P < 1 || S < 1 || TX < 1 || RX < 1 || A < 0)
+            return set_err("bad sizes V=%lld P=%d S=%d Tx=%d Rx=%d A=%d", V, P, S, TX, RX, A), MRL_ERR_ARG;
+        if (V > (1LL << 31) / std::max(1, P * S)) return set_err("spin matrix too large"), MRL_ERR_UNSUPPORTED;
+        if (!a.obj.rho || !a.obj.t1 || !a.obj.t2 || !a.obj.mx || !a.obj.my || !a.obj.mz || !a.mag.db0 ||
+            !a.mag.dwrnd || !a.mag.gzgrid || !a.mag.gygrid || !a.mag.gxgrid || !a.coil.tx_mg || !a.coil.tx_pe ||
+            !a.obj.gyro)
+            return set_err("missing input array"), MRL_ERR_ARG;
+        if (a.coil.rx_default == 0 && (!a.coil.rx_x || !a.coil.rx_y)) return set_err("missing Rx coil maps"), MRL_ERR_ARG;
+        if (A > 0 && (!a.sig.sx || !a.sig.sy)) return set_err("missing signal arrays"), MRL_ERR_ARG;
+        if (!a.seq.uts || !a.seq.ts || !a.seq.flags || a.seq.n_ts < 1 || a.seq.n_uts < 1)
+            return set_err("empty sequence"), MRL_ERR_ARG;
+        if (TX > 4) return set_err("TxCoilNum %d > 4 not supported", TX), MRL_ERR_UNSUPPORTED;
+        if (P > kMaxPool) return set_err("TypeNum %d > %d not supported", P, kMaxPool), MRL_ERR_UNSUPPORTED;
+        if (a.ctl.run_mode == 1) return set_err("RunMode 1 (per-step history) is not supported yet"), MRL_ERR_UNSUPPORTED;
+        switch (a.model) {
+        case MRL_MODEL_NORMAL:
+            if (P > 3) return set_err("normal model supports TypeNum <= 3"), MRL_ERR_UNSUPPORTED;
+            mi = {KM_NORMAL, P, 0, false};
+            break;
+        case MRL_MODEL_ME:
+        case MRL_MODEL_GM:
+            if (P > 5) return set_err("exchange models support TypeNum <= 5"), MRL_ERR_UNSUPPORTED;
+            mi = {KM_EXCH, P, P * P, a.model == MRL_MODEL_GM};
+            if (mi.gm && !a.obj.type_flag) return set_err("GM model needs TypeFlag"), MRL_ERR_ARG;
+            break;
+        case MRL_MODEL_MT:
+            if (P != 2) return set_err("MT model needs TypeNum == 2"), MRL_ERR_ARG;
+            mi = {KM_MT, 1, 4, false};
+            break;
+        case MRL_MODEL_CEST:
+            if (P < 2 || P > 6) return set_err("CEST model supports 2 <= TypeNum <= 6"), MRL_ERR_UNSUPPORTED;
+            mi = {KM_CEST, 1, 2 * (P - 1), false};
+            break;
+        default:
+            return set_err("unknown model %d", a.model), MRL_ERR_ARG;
+        }
+        if (mi.nk > 0 && (!a.obj.k || a.obj.k_channels < mi.nk))
+            return set_err("K needs %d channels, got %d", mi.nk, a.obj.k ? a.obj.k_channels : 0), MRL_ERR_ARG;
+        NS = spins_per_thread(S);
+        tpv = S / NS;
+        stride4 = record_stride_f4(TX);
+        return MRL_OK;
+    }
+
+    // Gather the active voxels into structure-of-arrays form and upload.
+    int upload_object() {
+        const mrl_scan_args &a = *args;
+        act.clear();
+        for (long long v = 0; v < V; ++v)
+            if (voxel_active(a, mi.km, v, V)) act.push_back(v);
+        n_act = (int)act.size();
+        const size_t n = std::max(1, n_act);
+        size_t off = 0;
+        auto take = [&](size_t cnt) {
+            size_t o = off;
+            off += cnt;
+            return o;
+        };
+        o_gx = take(n), o_gy = take(n), o_gz = take(n), o_db0 = take(n);
+        o_txmg = take(n * TX), o_txpe = take(n * TX);
+        o_rho = take(n * P), o_t1 = take(n * P), o_t2 = take(n * P);
+        o_k = take(n * std::max(1, mi.nk));
+        o_dwr = take(n * P * S);
+        std::vector<float> hf(off, 0.f);
+        std::vector<float> hm(3 * n * P * S, 0.f);
+        std::vector<float2> hr(a.coil.rx_default == 0 ? n * RX : 1, make_float2(0.f, 0.f));
+        const int nk = mi.nk;
+        for (int i = 0; i < n_act; ++i) {
+            const long long v = act[i];
+            hf[o_gx + i] = a.mag.gxgrid[v];
+            hf[o_gy + i] = a.mag.gygrid[v];
+            hf[o_gz + i] = a.mag.gzgrid[v];
+            hf[o_db0 + i] = a.mag.db0[v];
+            for (int c = 0; c < TX; ++c) {
+                hf[o_txmg + c * n + i] = a.coil.tx_mg[c * V + v];
+                hf[o_txpe + c * n + i] = a.coil.tx_pe[c * V + v];
+            }
+            for (int t = 0; t < P; ++t) {
+                hf[o_rho + t * n + i] = a.obj.rho[t * V + v];
+                hf[o_t1 + t * n + i] = a.obj.t1[t * V + v];
+                hf[o_t2 + t * n + i] = a.obj.t2[t * V + v];
+                for (int s = 0; s < S; ++s) {
+                    const long long src = ((long long)t * S + s) * V + v;
+                    const size_t dst = ((size_t)t * S + s) * n + i;
+                    hf[o_dwr + dst] = a.mag.dwrnd[src];
+                    hm[dst] = a.obj.mx[src];
+                    hm[(size_t)n * P * S + dst] = a.obj.my[src];
+                    hm[(size_t)2 * n * P * S + dst] = a.obj.mz[src];
+                }
+            }
+            for (int k = 0; k < nk; ++k) hf[o_k + k * n + i] = a.obj.k[k * V + v];
+            if (a.coil.rx_default == 0)
+                for (int c = 0; c < RX; ++c)
+                    hr[c * n + i] = make_float2(a.coil.rx_x[c * V + v], a.coil.rx_y[c * V + v]);
+        }
+        cudaError_t e;
+        if ((e = d_f.ensure(off)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(object)");
+        if ((e = d_m.ensure(hm.size())) != cudaSuccess) return fail_cuda(e, "cudaMalloc(state)");
+        if ((e = d_rx.ensure(hr.size())) != cudaSuccess) return fail_cuda(e, "cudaMalloc(coils)");
+        auto t0 = std::chrono::steady_clock::now();
+        if ((e = cudaMemcpyAsync(d_f.p, hf.data(), off * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return fail_cuda(e, "upload object");
+        h2d_bytes += (double)off * sizeof(float) + hm.size() * sizeof(float) + hr.size() * sizeof(float2);
+        if ((e = cudaMemcpyAsync(d_m.p, hm.data(), hm.size() * sizeof(float), cudaMemcpyHostToDevice, st)) !=
+            cudaSuccess)
+            return fail_cuda(e, "upload state");
+        if ((e = cudaMemcpyAsync(d_rx.p, hr.data(), hr.size() * sizeof(float2), cudaMemcpyHostToDevice, st)) !=
+            cudaSuccess)
+            return fail_cuda(e, "upload coils");
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e, "upload sync");
+        h2d_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return MRL_OK;
+    }
+
+    // Copy the device magnetisation back into the caller's arrays.
+    int download_state() {
+        mrl_scan_args &a = *args;
+        const size_t n = std::max(1, n_act);
+        std::vector<float> hm(3 * n * P * S);
+        auto t0 = std::chrono::steady_clock::now();
+        cudaError_t e = cudaMemcpyAsync(hm.data(), d_m.p, hm.size() * sizeof(float), cudaMemcpyDeviceToHost, st);
+        d2h_bytes += (double)hm.size() * sizeof(float);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail_cuda(e, "download state");
+        d2h_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        for (int i = 0; i < n_act; ++i) {
+            const long long v = act[i];
+            for (int t = 0; t < P; ++t)
+                for (int s = 0; s < S; ++s) {
+                    const long long dst = ((long long)t * S + s) * V + v;
+                    const size_t src = ((size_t)t * S + s) * n + i;
+                    a.obj.mx[dst] = hm[src];
+                    a.obj.my[dst] = hm[(size_t)n * P * S + src];
+                    a.obj.mz[dst] = hm[(size_t)2 * n * P * S + src];
+                }
+        }
+        return MRL_OK;
+    }
+
+    // Copy acquired samples [a0, a1) of every (pool, coil) row to the host.
+    int download_signal(int a0, int a1) {
+        if (a1 <= a0 || A == 0) return MRL_OK;
+        a1 = std::min(a1, A);
+        if (a1 <= a0) return MRL_OK;
+        mrl_scan_args &a = *args;
+        const size_t pitch = (size_t)A * sizeof(double);
+        d2h_bytes += 2.0 * (a1 - a0) * sizeof(double) * P * RX;
+        auto t0 = std::chrono::steady_clock::now();
+        cudaError_t e = cudaMemcpy2DAsync(a.sig.sx + a0, pitch, d_sx.p + a0, pitch, (size_t)(a1 - a0) * sizeof(double),
+                                          (size_t)P * RX, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(a.sig.sy + a0, pitch, d_sy.p + a0, pitch, (size_t)(a1 - a0) * sizeof(double),
+                                  (size_t)P * RX, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail_cuda(e, "download signal");
+        d2h_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return MRL_OK;
+    }
+
+    ScanLaunch make_launch(double rf_ref) {
+        const mrl_scan_args &a = *args;
+        const size_t n = std::max(1, n_act);
+        ScanLaunch L{};
+        L.n_act = n_act;
+        L.S = S;
+        L.tx = TX;
+        L.rx = RX;
+        L.nsamp = mi.nsamp;
+        L.npairs = mi.nsamp * RX;
+        L.tpv = tpv;
+        L.gyro = (float)a.obj.gyro;
+        L.rx_default = a.coil.rx_default != 0;
+        L.exch_gm = mi.gm ? 1 : 0;
+        L.gxg = d_f.p + o_gx;
+        L.gyg = d_f.p + o_gy;
+        L.gzg = d_f.p + o_gz;
+        L.db0 = d_f.p + o_db0;
+        L.txmg = d_f.p + o_txmg;
+        L.txpe = d_f.p + o_txpe;
+        L.rxc = d_rx.p;
+        L.rho = d_f.p + o_rho;
+        L.t1 = d_f.p + o_t1;
+        L.t2 = d_f.p + o_t2;
+        L.kch = d_f.p + o_k;
+        L.dwrnd = d_f.p + o_dwr;
+        L.mx = d_m.p;
+        L.my = d_m.p + n * P * S;
+        L.mz = d_m.p + 2 * n * P * S;
+        L.stride4 = stride4;
+        L.err = d_err.p;
+        for (int t = 0; t < kMaxPool; ++t) {
+            L.cs2pi[t] = t < P && a.ctl.cs ? (float)(2 * kPiRef * (double)(float)a.ctl.cs[t]) : 0.f;
+            L.kind[t] = (mi.gm && t < P) ? (int)a.obj.type_flag[t] : 0;
+        }
+        (void)rf_ref;
+        return L;
+    }
+
+    struct LaunchDesc {
+        long long s0, s1;
+        int a_off, a_count;
+    };
+    std::vector<LaunchDesc> plan_launches;
+    std::vector<int> amap_host;
+    long long n_steps_total = 0, n_rf_total = 0;
+    int n_adc_total = 0;
+
+    long long n_blocks() const {
+        const long long nthreads = (long long)n_act * tpv;
+        return std::max(1LL, (nthreads + kBlock - 1) / kBlock);
+    }
+
+    // Split a decoded chunk into launches whose receive partials fit the
+    // budget (MRL_PARTIAL_MB, default 1 GiB), upload its step records and
+    // ADC map, and size the partial buffer.
+    int prepare_chunk(const DecodeChunk &ch, std::vector<LaunchDesc> &out) {
+        out.clear();
+        amap_host.clear();
+        if (ch.n_steps == 0) return MRL_OK;
+        const int npairs = mi.nsamp * RX;
+        const char *env = getenv("MRL_PARTIAL_MB");
+        const double budget = (env ? atof(env) : 1024.0) * 1048576.0;
+        const long long a_max =
+            std::max(1LL, (long long)(budget / ((double)n_blocks() * npairs * sizeof(float2))));
+        long long s0 = 0;
+        int a_off = 0, a_cnt = 0, a_peak = 0;
+        for (long long q = 0; q < ch.n_steps; ++q) {
+            if (ch.step_adc[q] < 0) continue;
+            if (a_cnt == a_max) {
+                out.push_back({s0, q, a_off, a_cnt});
+                a_peak = std::max(a_peak, a_cnt);
+                s0 = q;
+                a_off += a_cnt;
+                a_cnt = 0;
+            }
+            amap_host.push_back(ch.step_adc[q]);
+            a_cnt++;
+        }
+        out.push_back({s0, ch.n_steps, a_off, a_cnt});
+        a_peak = std::max(a_peak, a_cnt);
+        cudaError_t e;
+        if ((e = d_rec.ensure(ch.records.size() / 4)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(steps)");
+        if ((e = d_amap.ensure(std::max<size_t>(1, amap_host.size()))) != cudaSuccess)
+            return fail_cuda(e, "cudaMalloc(amap)");
+        if ((e = d_part.ensure((size_t)n_blocks() * std::max(1, a_peak) * npairs)) != cudaSuccess)
+            return fail_cuda(e, "cudaMalloc(partials)");
+        auto t0 = std::chrono::steady_clock::now();
+        if ((e = cudaMemcpyAsync(d_rec.p, ch.records.data(), ch.records.size() * sizeof(float), cudaMemcpyHostToDevice,
+                                 st)) != cudaSuccess)
+            return fail_cuda(e, "upload steps");
+        h2d_bytes += (double)ch.records.size() * sizeof(float) + amap_host.size() * sizeof(int);
+        if (!amap_host.empty() &&
+            (e = cudaMemcpyAsync(d_amap.p, amap_host.data(), amap_host.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                 st)) != cudaSuccess)
+            return fail_cuda(e, "upload amap");
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e, "upload steps");
+        h2d_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return MRL_OK;
+    }
+
+    // Enqueue the launches of a prepared chunk on `stream` (no host sync).
+    int enqueue(const std::vector<LaunchDesc> &ls, double rf_ref, cudaStream_t stream, bool timed) {
+        if (ls.empty()) return MRL_OK;
+        ScanLaunch L = make_launch(rf_ref);
+        L.rec = d_rec.p;
+        L.partial = d_part.p;
+        const int nblk = (int)n_blocks();
+        const size_t smem = scan_smem_bytes(stride4, mi.nsamp);
+        const double cr = std::cos(-rf_ref), sr = std::sin(-rf_ref);
+        cudaError_t e;
+        for (const LaunchDesc &d : ls) {
+            L.s0 = d.s0;
+            L.s1 = d.s1;
+            L.a_launch = d.a_count;
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (timed) {
+                cudaEventCreate(&e0);
+                cudaEventCreate(&e1);
+                ev_scan.push_back({e0, e1});
+                cudaEventRecord(e0, stream);
+            }
+            if (n_act > 0) {
+                dim3 grid(nblk);
+                switch (mi.km) {
+                case KM_NORMAL: e = launch_scan_ref_normal(P, NS, grid, smem, stream, L); break;
+                case KM_EXCH: e = launch_scan_ref_exch(P, NS, grid, smem, stream, L); break;
+                case KM_MT: e = launch_scan_ref_mt(P, NS, grid, smem, stream, L); break;
+                default: e = launch_scan_ref_cest(P, NS, grid, smem, stream, L); break;
+                }
+                if (e != cudaSuccess) return fail_cuda(e, "scan kernel launch");
+                launches++;
+            }
+            if (timed) cudaEventRecord(e1, stream);
+            if (d.a_count > 0 && n_act > 0) {
+                cudaEvent_t r0 = nullptr, r1 = nullptr;
+                if (timed) {
+                    cudaEventCreate(&r0);
+                    cudaEventCreate(&r1);
+                    ev_red.push_back({r0, r1});
+                    cudaEventRecord(r0, stream);
+                }
+                const int tot = d.a_count * L.npairs;
+                reduce_partials<<<(tot + 255) / 256, 256, 0, stream>>>(d_part.p, nblk, d.a_count, L.npairs, RX,
+                                                                       d_amap.p + d.a_off, A, d_sx.p, d_sy.p, cr, sr);
+                if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "reduce launch");
+                launches++;
+                if (timed) cudaEventRecord(r1, stream);
+            }
+        }
+        return MRL_OK;
+    }
+
+    int run_chunk(const DecodeChunk &ch, double rf_ref) {
+        std::vector<LaunchDesc> ls;
+        int rc = prepare_chunk(ch, ls);
+        if (rc) return rc;
+        if ((rc = enqueue(ls, rf_ref, st, true))) return rc;
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail_cuda(e, "scan kernels");
+        return MRL_OK;
+    }
+
+    int setup() {
+        int rc = validate();
+        if (rc) return rc;
+        cudaError_t e;
+        int dev = args->ctl.gpu_index;
+        if ((e = cudaSetDevice(dev)) != cudaSuccess) {
+            set_err("cudaSetDevice(%d): %s", dev, cudaGetErrorString(e));
+            return e == cudaErrorNoDevice || e == cudaErrorInvalidDevice ? MRL_ERR_NO_DEVICE : MRL_ERR_CUDA;
+        }
+        if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess)
+            return fail_cuda(e, "cudaStreamCreate");
+        if ((e = d_err.ensure(1)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(err)");
+        cudaMemsetAsync(d_err.p, 0, sizeof(int), st);
+        const size_t nsig = (size_t)P * RX * std::max(A, 1);
+        if ((e = d_sx.ensure(nsig)) != cudaSuccess || (e = d_sy.ensure(nsig)) != cudaSuccess)
+            return fail_cuda(e, "cudaMalloc(signal)");
+        cudaMemsetAsync(d_sx.p, 0, nsig * sizeof(double), st);
+        cudaMemsetAsync(d_sy.p, 0, nsig * sizeof(double), st);
+        return upload_object();
+    }
+
+    int check_device_status() {
+        int herr = 0;
+        cudaError_t e = cudaMemcpy(&herr, d_err.p, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail_cuda(e, "read status");
+        if (herr) {
+            set_err("a device wait timed out (status bits %d)", herr);
+            return MRL_ERR_TIMEOUT;
+        }
+        return MRL_OK;
+    }
+
+    int run() {
+        int rc = setup();
+        if (rc) return rc;
+        cudaError_t e;
+
+        DecodeState ds;
+        load_state(ds, args->var, TX);
+        ds.i = 0;
+        ds.signali = 0;
+        DecodeChunk ch;
+        int signal_synced = 0;
+        for (;;) {
+            decode_until_ext(ds, args->seq, TX, args->obj.gyro, args->sig, ch);
+            const double rf_ref = args->var.rf_ref ? *args->var.rf_ref : 0.0;
+            if ((rc = run_chunk(ch, rf_ref))) return rc;
+            if (!ch.stopped_at_ext) break;
+            // Ext event: make the signal and the cursor current, then run
+            // DoGPUFetch / DoExtPlugin (DoScanAtGPU.cu:565-660)
+            if ((rc = download_signal(signal_synced, ds.signali))) return rc;
+            signal_synced = ds.signali;
+            store_state(ds, args->var, TX);
+            if (ext) {
+                const int fetch = ext(user, args, MRL_EXT_FETCH);
+                if (fetch && (rc = download_state())) return rc;
+                if (ext(user, args, MRL_EXT_PLUGIN) != 0) {
+                    set_err("Ext plugin returned an error");
+                    return MRL_ERR_EXT;
+                }
+                load_state(ds, args->var, TX);
+                if (fetch && (rc = upload_object())) return rc;
+            }
+        }
+        if ((rc = download_signal(signal_synced, ds.signali))) return rc;
+        if ((rc = download_state())) return rc;
+        store_state(ds, args->var, TX);
+        if ((rc = check_device_status())) return rc;
+        (void)e;
+        double scan_ms = 0, red_ms = 0;
+        for (auto &p : ev_scan) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, p.first, p.second);
+            scan_ms += ms;
+        }
+        for (auto &p : ev_red) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, p.first, p.second);
+            red_ms += ms;
+        }
+        g_timing[1] = scan_ms;
+        g_timing[2] = red_ms;
+        g_timing[3] = h2d_ms;
+        g_timing[4] = d2h_ms;
+        g_timing[5] = launches;
+        g_timing[6] = h2d_bytes;
+        g_timing[7] = d2h_bytes;
+        return MRL_OK;
+    }
+};
+
+}  // namespace
+}  // namespace mrl
+
+struct mrl_plan {
+    mrl::Scanner sc;
+    mrl_scan_args args{};
+    mrl::DevBuf<float> d_m0;
+    std::vector<mrl::Scanner::LaunchDesc> ls;
+    std::vector<double> kx, ky, kz;
+    double rf_ref = 0;
+    long long work[5] = {0, 0, 0, 0, 0};
+};
+
+extern "C" {
+
+int mrl_scan(mrl_scan_args *args, mrl_ext_fn ext, void *user) {
+    mrl::g_err.clear();
+    for (double &t : mrl::g_timing) t = 0;
+    if (!args) {
+        mrl::set_err("args is NULL");
+        return MRL_ERR_ARG;
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    auto t0 = std::chrono::steady_clock::now();
+    int rc;
+    {
+        mrl::Scanner sc;
+        sc.args = args;
+        sc.ext = ext;
+        sc.user = user;
+        rc = sc.run();
+    }
+    mrl::g_timing[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    cudaSetDevice(prev);
+    return rc;
+}
+
+int mrl_plan_create(const mrl_scan_args *args, mrl_plan **out) {
+    mrl::g_err.clear();
+    if (!args || !out) {
+        mrl::set_err("NULL argument");
+        return MRL_ERR_ARG;
+    }
+    *out = nullptr;
+    mrl_plan *p = new mrl_plan();
+    p->args = *args;
+    mrl::Scanner &sc = p->sc;
+    sc.args = &p->args;
+    sc.ext = nullptr;
+    sc.user = nullptr;
+    int rc = sc.setup();
+    if (rc) {
+        delete p;
+        return rc;
+    }
+    const int A = sc.A;
+    p->kx.assign(std::max(A, 1), 0.0);
+    p->ky.assign(std::max(A, 1), 0.0);
+    p->kz.assign(std::max(A, 1), 0.0);
+    mrl_signal sig = p->args.sig;
+    sig.kx = p->kx.data();
+    sig.ky = p->ky.data();
+    sig.kz = p->kz.data();
+    mrl::DecodeState ds;
+    mrl_state none{};
+    mrl::load_state(ds, none, sc.TX);
+    ds.tr_count = 0;
+    mrl::DecodeChunk ch;
+    mrl::decode_until_ext(ds, p->args.seq, sc.TX, p->args.obj.gyro, sig, ch);
+    if (ch.stopped_at_ext) {
+        mrl::set_err("the sequence has Ext events: use mrl_scan with a callback");
+        delete p;
+        return MRL_ERR_UNSUPPORTED;
+    }
+    if ((rc = sc.prepare_chunk(ch, p->ls))) {
+        delete p;
+        return rc;
+    }
+    p->rf_ref = args->var.rf_ref ? *args->var.rf_ref : 0.0;
+    cudaError_t e = p->d_m0.ensure(sc.d_m.n);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p->d_m0.p, sc.d_m.p, sc.d_m.n * sizeof(float), cudaMemcpyDeviceToDevice, sc.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sc.st);
+    if (e != cudaSuccess) {
+        sc.fail_cuda(e, "plan state copy");
+        delete p;
+        return MRL_ERR_CUDA;
+    }
+    // work units: active isochromat-pools x dt>0 steps
+    long long iso_pools = 0;
+    for (int i = 0; i < sc.n_act; ++i) {
+        const long long v = sc.act[i];
+        if (sc.mi.km == mrl::KM_MT || sc.mi.km == mrl::KM_CEST) {
+            iso_pools += sc.P;
+        } else {
+            for (int t = 0; t < sc.P; ++t)
+                iso_pools += args->obj.t1[t * sc.V + v] != 0.f && args->obj.t2[t * sc.V + v] != 0.f &&
+                             args->obj.rho[t * sc.V + v] != 0.f;
+        }
+    }
+    long long launches = 0;
+    for (auto &d : p->ls) launches += 1 + (d.a_count > 0 ? 1 : 0);
+    p->work[0] = iso_pools * sc.S * ch.n_steps;
+    p->work[1] = ch.n_steps;
+    p->work[2] = ch.n_rf_steps;
+    p->work[3] = ch.adc_end - ch.adc_begin;
+    p->work[4] = launches;
+    *out = p;
+    return MRL_OK;
+}
+
+int mrl_plan_execute(mrl_plan *p, void *stream) {
+    if (!p) return MRL_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(p->sc.d_m.p, p->d_m0.p, p->sc.d_m.n * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return p->sc.fail_cuda(e, "plan reset");
+    return p->sc.enqueue(p->ls, p->rf_ref, s, false);
+}
+
+int mrl_plan_download(mrl_plan *p, mrl_scan_args *args) {
+    if (!p || !args) return MRL_ERR_ARG;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return p->sc.fail_cuda(e, "plan sync");
+    int rc = p->sc.check_device_status();
+    if (rc) return rc;
+    mrl_scan_args *keep = p->sc.args;
+    p->sc.args = args;
+    rc = p->sc.download_signal(0, p->sc.A);
+    if (!rc) rc = p->sc.download_state();
+    p->sc.args = keep;
+    for (int i = 0; i < p->sc.A; ++i) {
+        if (args->sig.kx) args->sig.kx[i] = p->kx[i];
+        if (args->sig.ky) args->sig.ky[i] = p->ky[i];
+        if (args->sig.kz) args->sig.kz[i] = p->kz[i];
+    }
+    return rc;
+}
+
+int mrl_plan_work(const mrl_plan *p, long long out[5]) {
+    if (!p || !out) return MRL_ERR_ARG;
+    for (int i = 0; i < 5; ++i) out[i] = p->work[i];
+    return MRL_OK;
+}
+
+void mrl_plan_destroy(mrl_plan *p) { delete p; }
+
+const char *mrl_status_string(int status) {
+    switch (status) {
+    case MRL_OK: return "ok";
+    case MRL_ERR_ARG: return "invalid argument";
+    case MRL_ERR_CUDA: return "CUDA error";
+    case MRL_ERR_NOMEM: return "out of memory";
+    case MRL_ERR_EXT: return "Ext plugin error";
+    case MRL_ERR_TIMEOUT: return "device wait timed out";
+    case MRL_ERR_UNSUPPORTED: return "unsupported configuration";
+    case MRL_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+const char *mrl_last_error(void) { return mrl::g_err.c_str(); }
+
+int mrl_last_timing(double out[8]) {
+    if (!out) return MRL_ERR_ARG;
+    for (int i = 0; i < 8; ++i) out[i] = mrl::g_timing[i];
+    return MRL_OK;
+}
+
+}  // extern "C"

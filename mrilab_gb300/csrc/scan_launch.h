@@ -1,0 +1,26 @@
+// Host-side launchers of the scan kernels, one per tissue model (each
+// model's instantiations live in their own translation unit so they build
+// in parallel).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "scan_kernel.cuh"
+
+namespace mrl {
+
+// Spins handled per thread for a given SpinNum: all of them when S <= 4 and
+// S is 1, 2 or 4; otherwise one spin per thread.
+inline int spins_per_thread(int S) { return (S == 4 || S == 2) ? S : 1; }
+
+// Dynamic shared memory of one block.
+inline size_t scan_smem_bytes(int stride4, int nsamp) {
+    return 128 + (size_t)2 * kChunk * stride4 * 16 + (size_t)kAdcTile * nsamp * (kBlock + 1) * 8;
+}
+
+cudaError_t launch_scan_ref_normal(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
+cudaError_t launch_scan_ref_exch(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
+cudaError_t launch_scan_ref_mt(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
+cudaError_t launch_scan_ref_cest(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
+
+}  // namespace mrl

@@ -1,0 +1,246 @@
+"""Python binding of the scan engine's C ABI (``include/mrl_scan.h``).
+
+``scan(sc, ...)`` runs one MRiLab scan on the GPU through ``mrl_scan`` --
+the same call the mex wrappers make -- with the seven MATLAB structs of a
+``phantoms.Scan`` passed as host arrays, exactly as the reference engines
+receive them (``Lib/src/engine/GPUEngine/DoScanAtGPU.cu:117-214``).  There
+is no CPU fallback: if ``libmrl_scan.so`` is missing or no GPU is usable the
+call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Callable, Dict, Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmrl_scan.so")
+
+MODEL = {"normal": 0, "me": 1, "mt": 2, "cest": 3, "gm": 4}
+NUMERICS = {"accurate": 0, "reference": 1}
+EXT_FETCH, EXT_PLUGIN = 1, 2
+ABI_VERSION = 1
+
+_d = ctypes.POINTER(ctypes.c_double)
+_f = ctypes.POINTER(ctypes.c_float)
+_i = ctypes.POINTER(ctypes.c_int)
+
+
+class Object(ctypes.Structure):
+    _fields_ = [("ny", ctypes.c_int), ("nx", ctypes.c_int), ("nz", ctypes.c_int), ("spin_num", ctypes.c_int),
+                ("type_num", ctypes.c_int), ("gyro", ctypes.c_double), ("rho", _f), ("t1", _f), ("t2", _f),
+                ("k", _f), ("k_channels", ctypes.c_int), ("type_flag", _d), ("mx", _f), ("my", _f), ("mz", _f)]
+
+
+class Field(ctypes.Structure):
+    _fields_ = [("db0", _f), ("dwrnd", _f), ("gzgrid", _f), ("gygrid", _f), ("gxgrid", _f)]
+
+
+class Coils(ctypes.Structure):
+    _fields_ = [("tx_num", ctypes.c_int), ("rx_num", ctypes.c_int), ("tx_default", ctypes.c_double),
+                ("rx_default", ctypes.c_double), ("tx_mg", _f), ("tx_pe", _f), ("rx_x", _f), ("rx_y", _f)]
+
+
+class Control(ctypes.Structure):
+    _fields_ = [("cs", _d), ("tr_num", ctypes.c_int), ("run_mode", ctypes.c_int), ("gpu_index", ctypes.c_int),
+                ("numerics", ctypes.c_int)]
+
+
+class Sequence(ctypes.Structure):
+    _fields_ = [(n, _d) for n in ("uts", "ts", "rf_amp", "rf_phase", "rf_freq", "rf_coil", "gz", "gy", "gx",
+                                  "adc", "ext", "flags")] + \
+               [(n, ctypes.c_int) for n in ("n_uts", "n_ts", "n_rf", "n_gz", "n_gy", "n_gx", "n_adc", "n_ext")]
+
+
+class State(ctypes.Structure):
+    _fields_ = [(n, _d) for n in ("t", "dt", "rf_amp", "rf_phase", "rf_freq", "rf_coil", "rf_ref", "gz", "gy",
+                                  "gx", "adc", "ext", "kz", "ky", "kx", "gpu_fetch")] + \
+               [(n, _i) for n in ("utsi", "rfi", "gzi", "gyi", "gxi", "adci", "exti", "tr_count")]
+
+
+class Signal(ctypes.Structure):
+    _fields_ = [("sx", _d), ("sy", _d), ("kz", _d), ("ky", _d), ("kx", _d), ("signal_num", ctypes.c_int),
+                ("mxs", _f), ("mys", _f), ("mzs", _f), ("muts", _d)]
+
+
+class ScanArgs(ctypes.Structure):
+    _fields_ = [("abi_version", ctypes.c_int), ("model", ctypes.c_int), ("obj", Object), ("mag", Field),
+                ("coil", Coils), ("ctl", Control), ("seq", Sequence), ("var", State), ("sig", Signal)]
+
+
+EXT_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ScanArgs), ctypes.c_int)
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def library() -> ctypes.CDLL:
+    """Load libmrl_scan.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() (no CPU fallback exists)")
+        lib = ctypes.CDLL(LIB_PATH)
+        lib.mrl_scan.argtypes = [ctypes.POINTER(ScanArgs), EXT_FN, ctypes.c_void_p]
+        lib.mrl_scan.restype = ctypes.c_int
+        lib.mrl_status_string.argtypes = [ctypes.c_int]
+        lib.mrl_status_string.restype = ctypes.c_char_p
+        lib.mrl_last_error.restype = ctypes.c_char_p
+        lib.mrl_last_timing.argtypes = [ctypes.POINTER(ctypes.c_double)]
+        lib.mrl_last_timing.restype = ctypes.c_int
+        _lib = lib
+    return _lib
+
+
+class ScanError(RuntimeError):
+    def __init__(self, status: int, detail: str):
+        super().__init__(f"mrl_scan failed ({status}): {detail}")
+        self.status = status
+
+
+def _flat(a, dtype):
+    return np.ascontiguousarray(np.asarray(a, dtype).ravel(order="F"))
+
+
+class HostScan:
+    """Column-major host copies of a Scan's arrays, bound into ScanArgs."""
+
+    def __init__(self, sc, model: Optional[str] = None, numerics: str = "accurate", gpu_index: int = 0):
+        self.sc = sc
+        o, m, c, ctl, q, v, sig = sc.VObj, sc.VMag, sc.VCoi, sc.VCtl, sc.VSeq, sc.VVar, sc.VSig
+        self.keep = {}
+        K = self.keep
+        f32 = lambda k, a: K.setdefault(k, _flat(a, np.float32))
+        f64 = lambda k, a: K.setdefault(k, _flat(a, np.float64))
+        i32 = lambda k, a: K.setdefault(k, _flat(a, np.int32))
+        p = lambda a, t: a.ctypes.data_as(t)
+        a = ScanArgs()
+        a.abi_version = ABI_VERSION
+        a.model = MODEL[model or sc.model]
+        Y, X, Z = o["Rho"].shape[:3]
+        V = Y * X * Z
+        ob = a.obj
+        ob.ny, ob.nx, ob.nz = Y, X, Z
+        ob.spin_num, ob.type_num = int(o["SpinNum"]), int(o["TypeNum"])
+        ob.gyro = float(o["Gyro"])
+        ob.rho, ob.t1, ob.t2 = p(f32("rho", o["Rho"]), _f), p(f32("t1", o["T1"]), _f), p(f32("t2", o["T2"]), _f)
+        if "K" in o:
+            ob.k = p(f32("k", o["K"]), _f)
+            ob.k_channels = K["k"].size // V
+        if "TypeFlag" in o:
+            ob.type_flag = p(f64("tf", o["TypeFlag"]), _d)
+        ob.mx, ob.my, ob.mz = (p(f32("mx", o["Mx"]), _f), p(f32("my", o["My"]), _f), p(f32("mz", o["Mz"]), _f))
+        fm = a.mag
+        fm.db0, fm.dwrnd = p(f32("db0", m["dB0"]), _f), p(f32("dwrnd", m["dWRnd"]), _f)
+        fm.gzgrid, fm.gygrid, fm.gxgrid = (p(f32("gzg", m["Gzgrid"]), _f), p(f32("gyg", m["Gygrid"]), _f),
+                                           p(f32("gxg", m["Gxgrid"]), _f))
+        co = a.coil
+        co.tx_num, co.rx_num = int(c["TxCoilNum"]), int(c["RxCoilNum"])
+        co.tx_default, co.rx_default = float(c["TxCoilDefault"]), float(c["RxCoilDefault"])
+        co.tx_mg, co.tx_pe = p(f32("txmg", c["TxCoilmg"]), _f), p(f32("txpe", c["TxCoilpe"]), _f)
+        co.rx_x, co.rx_y = p(f32("rxx", c["RxCoilx"]), _f), p(f32("rxy", c["RxCoily"]), _f)
+        ct = a.ctl
+        ct.cs = p(f64("cs", ctl["CS"]), _d)
+        ct.tr_num, ct.run_mode = int(ctl["TRNum"]), int(ctl["RunMode"])
+        ct.gpu_index = gpu_index
+        ct.numerics = NUMERICS[numerics]
+        sq = a.seq
+        for fld, key in [("uts", "utsLine"), ("ts", "tsLine"), ("rf_amp", "rfAmpLine"), ("rf_phase", "rfPhaseLine"),
+                         ("rf_freq", "rfFreqLine"), ("rf_coil", "rfCoilLine"), ("gz", "GzAmpLine"),
+                         ("gy", "GyAmpLine"), ("gx", "GxAmpLine"), ("adc", "ADCLine"), ("ext", "ExtLine"),
+                         ("flags", "flagsLine")]:
+            setattr(sq, fld, p(f64("seq_" + fld, q[key]), _d))
+        sq.n_uts, sq.n_ts = q["utsLine"].size, q["tsLine"].size
+        sq.n_rf, sq.n_gz, sq.n_gy, sq.n_gx = (q["rfAmpLine"].size, q["GzAmpLine"].size, q["GyAmpLine"].size,
+                                              q["GxAmpLine"].size)
+        sq.n_adc, sq.n_ext = q["ADCLine"].size, q["ExtLine"].size
+        st = a.var
+        for fld, key in [("t", "t"), ("dt", "dt"), ("rf_amp", "rfAmp"), ("rf_phase", "rfPhase"),
+                         ("rf_freq", "rfFreq"), ("rf_coil", "rfCoil"), ("rf_ref", "rfRef"), ("gz", "GzAmp"),
+                         ("gy", "GyAmp"), ("gx", "GxAmp"), ("adc", "ADC"), ("ext", "Ext"), ("kz", "Kz"),
+                         ("ky", "Ky"), ("kx", "Kx"), ("gpu_fetch", "gpuFetch")]:
+            setattr(st, fld, p(f64("var_" + fld, v[key]), _d))
+        for fld, key in [("utsi", "utsi"), ("rfi", "rfi"), ("gzi", "Gzi"), ("gyi", "Gyi"), ("gxi", "Gxi"),
+                         ("adci", "ADCi"), ("exti", "Exti"), ("tr_count", "TRCount")]:
+            setattr(st, fld, p(i32("var_" + fld, v[key]), _i))
+        sg = a.sig
+        sg.sx, sg.sy = p(f64("sx", sig["Sx"]), _d), p(f64("sy", sig["Sy"]), _d)
+        sg.kz, sg.ky, sg.kx = p(f64("skz", sig["Kz"]), _d), p(f64("sky", sig["Ky"]), _d), p(f64("skx", sig["Kx"]), _d)
+        sg.signal_num = int(sig["SignalNum"])
+        self.args = a
+
+    def outputs(self) -> Dict[str, np.ndarray]:
+        K = self.keep
+        return dict(Sx=K["sx"], Sy=K["sy"], Kx=K["skx"], Ky=K["sky"], Kz=K["skz"], Mx=K["mx"], My=K["my"],
+                    Mz=K["mz"], TRCount=int(K["var_tr_count"][0]), utsi=int(K["var_utsi"][0]))
+
+
+def last_timing() -> Dict[str, float]:
+    buf = (ctypes.c_double * 8)()
+    library().mrl_last_timing(buf)
+    return dict(total_ms=buf[0], scan_ms=buf[1], reduce_ms=buf[2], h2d_ms=buf[3], d2h_ms=buf[4],
+                launches=int(buf[5]), h2d_bytes=int(buf[6]), d2h_bytes=int(buf[7]))
+
+
+def run(hs: HostScan, ext: Optional[Callable[[ScanArgs, int], int]] = None) -> Dict[str, np.ndarray]:
+    lib = library()
+    cb = EXT_FN(lambda user, args, what: int(ext(args.contents, what)) if ext else 0)
+    rc = lib.mrl_scan(ctypes.byref(hs.args), cb, None)
+    if rc != 0:
+        raise ScanError(rc, lib.mrl_last_error().decode())
+    return hs.outputs()
+
+
+def scan(sc, model: Optional[str] = None, numerics: str = "accurate", gpu_index: int = 0,
+         ext: Optional[Callable[[ScanArgs, int], int]] = None) -> Dict[str, np.ndarray]:
+    """Run ``sc`` (a phantoms.Scan) on the GPU; returns Sx, Sy, Kx, Ky, Kz and
+    the final Mx, My, Mz (flattened column-major), leaving ``sc`` unchanged."""
+    return run(HostScan(sc, model=model, numerics=numerics, gpu_index=gpu_index), ext)
+
+
+class Plan:
+    """A prepared scan (``mrl_plan``): inputs resident on the device, the
+    sequence decoded once; ``execute(stream)`` re-runs the whole scan from
+    the initial magnetisation without host work."""
+
+    def __init__(self, sc, model: Optional[str] = None, numerics: str = "accurate", gpu_index: int = 0):
+        lib = library()
+        lib.mrl_plan_create.argtypes = [ctypes.POINTER(ScanArgs), ctypes.POINTER(ctypes.c_void_p)]
+        lib.mrl_plan_execute.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        lib.mrl_plan_download.argtypes = [ctypes.c_void_p, ctypes.POINTER(ScanArgs)]
+        lib.mrl_plan_work.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
+        lib.mrl_plan_destroy.argtypes = [ctypes.c_void_p]
+        self.lib = lib
+        self.host = HostScan(sc, model=model, numerics=numerics, gpu_index=gpu_index)
+        self.ptr = ctypes.c_void_p()
+        rc = lib.mrl_plan_create(ctypes.byref(self.host.args), ctypes.byref(self.ptr))
+        if rc != 0:
+            raise ScanError(rc, lib.mrl_last_error().decode())
+
+    def work(self) -> Dict[str, int]:
+        buf = (ctypes.c_longlong * 5)()
+        self.lib.mrl_plan_work(self.ptr, buf)
+        return dict(units=buf[0], steps=buf[1], rf_steps=buf[2], samples=buf[3], launches=buf[4])
+
+    def execute(self, stream: int = 0) -> None:
+        rc = self.lib.mrl_plan_execute(self.ptr, ctypes.c_void_p(stream))
+        if rc != 0:
+            raise ScanError(rc, self.lib.mrl_last_error().decode())
+
+    def download(self) -> Dict[str, np.ndarray]:
+        rc = self.lib.mrl_plan_download(self.ptr, ctypes.byref(self.host.args))
+        if rc != 0:
+            raise ScanError(rc, self.lib.mrl_last_error().decode())
+        return self.host.outputs()
+
+    def close(self) -> None:
+        if self.ptr:
+            self.lib.mrl_plan_destroy(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

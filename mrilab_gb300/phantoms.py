@@ -1,0 +1,446 @@
+"""Seeded synthetic scans: MATLAB-style globals for the scan engine.
+
+``Scan`` holds the seven structs an MRiLab engine reads (VObj, VMag, VCoi,
+VCtl, VSeq, VVar, VSig) as dicts of numpy arrays with the shapes and dtypes
+that ``Src/Main/DoPreScan.m`` builds and ``Src/Main/DoDataTypeConv.m:19-138``
+fixes:
+
+* per-voxel maps are ``[Y, X, Z]`` (rows = y, columns = x), pool maps add a
+  trailing pool axis, isochromat maps ``[Y, X, Z, Spin, Pool]``;
+* magnetisation starts at ``Rho / SpinNum`` along z (DoPreScan.m:409-414);
+* intravoxel dephasing ``dWRnd = (1/T2* - 1/T2) * tan(pi (u_i - 1/2))`` with
+  ``u = linspace(0.01, 0.99, SpinNum)`` (DoPreScan.m:381-390);
+* exchange rates are kept as a canonical per-voxel matrix ``rates[..., t, p]``
+  = rate from pool t to pool p and laid out into ``VObj.K`` per model by
+  ``k_layout`` (ME: channel t*P+p; GM: channel p*P+t; MT: channels 1 and 2;
+  CEST: channels t-1 / t+P-2 -- BlochKernel{ME,GM,MT,CEST}.cuh).
+
+The workloads are the five benchmark configurations, each with a ``scale``
+knob so tests can run shrunken copies.
+"""
+from __future__ import annotations
+
+import copy
+from dataclasses import dataclass, field
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import seq as S
+
+GAMMA = S.GAMMA_H
+MODELS = ("normal", "me", "mt", "cest", "gm")
+
+
+@dataclass
+class Scan:
+    VObj: Dict[str, np.ndarray]
+    VMag: Dict[str, np.ndarray]
+    VCoi: Dict[str, np.ndarray]
+    VCtl: Dict[str, np.ndarray]
+    VSeq: Dict[str, np.ndarray]
+    VVar: Dict[str, np.ndarray]
+    VSig: Dict[str, np.ndarray]
+    model: str = "normal"
+    rates: Optional[np.ndarray] = None
+    info: Dict[str, object] = field(default_factory=dict)
+
+    def structs(self):
+        return dict(VObj=self.VObj, VMag=self.VMag, VCoi=self.VCoi, VCtl=self.VCtl,
+                    VSeq=self.VSeq, VVar=self.VVar, VSig=self.VSig)
+
+    def copy(self) -> "Scan":
+        return copy.deepcopy(self)
+
+    @property
+    def dims(self):
+        return self.VObj["Rho"].shape[:3]
+
+    @property
+    def signal_num(self) -> int:
+        return int(self.VSig["SignalNum"])
+
+    def units(self) -> int:
+        """Work units: active isochromats x pools x steps with dt > 0."""
+        rho = self.VObj["Rho"]
+        t1 = self.VObj["T1"]
+        t2 = self.VObj["T2"]
+        if self.model in ("mt", "cest"):
+            act = (rho[..., 0] != 0) & (t1[..., 0] != 0) & (t2[..., 0] != 0)
+            n_iso_pool = int(act.sum()) * rho.shape[3]
+        elif self.model == "normal":
+            act = (rho != 0) & (t1 != 0) & (t2 != 0)
+            n_iso_pool = int(act.sum())
+        else:
+            act = (rho != 0) & (t1 != 0) & (t2 != 0)
+            n_iso_pool = int(act.sum())
+        uts = self.VSeq["utsLine"]
+        n_steps = int(np.count_nonzero(np.diff(uts) > 0))
+        return n_iso_pool * int(self.VObj["SpinNum"]) * n_steps
+
+
+def k_layout(model: str, rates: np.ndarray) -> np.ndarray:
+    """Lay a canonical rate matrix ``rates[Y,X,Z,t,p]`` (t -> p) out as VObj.K."""
+    Y, X, Z, P, _ = rates.shape
+    if model == "me":
+        K = np.zeros((Y, X, Z, P * P), np.float32)
+        for t in range(P):
+            for p in range(P):
+                K[..., t * P + p] = rates[..., t, p]
+    elif model == "gm":
+        K = np.zeros((Y, X, Z, P * P), np.float32)
+        for t in range(P):
+            for p in range(P):
+                K[..., p * P + t] = rates[..., t, p]
+    elif model == "mt":
+        K = np.zeros((Y, X, Z, 4), np.float32)
+        K[..., 1] = rates[..., 0, 1]  # free -> bound (K12)
+        K[..., 2] = rates[..., 1, 0]  # bound -> free (K21)
+    elif model == "cest":
+        K = np.zeros((Y, X, Z, 2 * (P - 1)), np.float32)
+        K[..., 0] = rates[..., 0, 1]          # free -> MT
+        K[..., P - 1] = rates[..., 1, 0]      # MT -> free
+        for t in range(2, P):
+            K[..., t - 1] = rates[..., 0, t]  # free -> CEST t
+            K[..., t + P - 2] = rates[..., t, 0]  # CEST t -> free
+    else:
+        raise ValueError(model)
+    return K
+
+
+def _grids(shape, res):
+    Y, X, Z = shape
+    x = (np.arange(X) - (X - 1) / 2) * res[0]
+    y = (np.arange(Y) - (Y - 1) / 2) * res[1]
+    z = (np.arange(Z) - (Z - 1) / 2) * res[2]
+    gx, gy, gz = np.meshgrid(x, y, z)  # [Y, X, Z], as DoPreScan's meshgrid
+    return gx.astype(np.float32), gy.astype(np.float32), gz.astype(np.float32)
+
+
+def assemble(rho, t1, t2, *, spin_num=1, t2star=None, db0_hz=None, res=(1e-3, 1e-3, 1e-3),
+             cs_hz=None, model="normal", rates=None, type_flag=None, tx_mg=None, tx_pe=None,
+             rx=None, seqlines=None, tr_num=1, seed=0) -> Scan:
+    """Build the seven structs from pool maps ``[Y, X, Z, P]``."""
+    rho = np.asarray(rho, np.float32)
+    t1 = np.asarray(t1, np.float32)
+    t2 = np.asarray(t2, np.float32)
+    if rho.ndim == 3:
+        rho, t1, t2 = rho[..., None], t1[..., None], t2[..., None]
+    Y, X, Z, P = rho.shape
+    Sn = int(spin_num)
+    gx, gy, gz = _grids((Y, X, Z), res)
+
+    mz = np.zeros((Y, X, Z, Sn, P), np.float32)
+    for t in range(P):
+        mz[..., t] = (rho[..., t].astype(np.float64) / Sn)[..., None].astype(np.float32)
+    dwrnd = np.zeros((Y, X, Z, Sn, P), np.float32)
+    if Sn > 1 and t2star is not None:
+        u = np.linspace(0.01, 0.99, Sn)
+        for t in range(P):
+            with np.errstate(divide="ignore", invalid="ignore"):
+                r2p = np.where(t2[..., t] > 0, 1.0 / t2star[..., t] - 1.0 / t2[..., t], 0.0)
+            for i in range(Sn):
+                dwrnd[..., i, t] = (r2p * np.tan(np.pi * (u[i] - 0.5))).astype(np.float32)
+    db0 = np.zeros((Y, X, Z), np.float32) if db0_hz is None else (2 * np.pi * db0_hz / GAMMA).astype(np.float32)
+
+    if tx_mg is None:
+        tx_mg = np.ones((Y, X, Z, 1), np.float32)
+        tx_pe = np.zeros((Y, X, Z, 1), np.float32)
+        tx_default = 1.0
+    else:
+        tx_default = 0.0
+    if rx is None:
+        rxx = np.ones((Y, X, Z, 1), np.float32)
+        rxy = np.zeros((Y, X, Z, 1), np.float32)
+        rx_default = 1.0
+    else:
+        rxx, rxy = np.asarray(rx[0], np.float32), np.asarray(rx[1], np.float32)
+        rx_default = 0.0
+    ntx, nrx = tx_mg.shape[3], rxx.shape[3]
+
+    vobj = dict(Gyro=np.float64(GAMMA), Mx=np.zeros_like(mz), My=np.zeros_like(mz), Mz=mz,
+                Rho=rho, T1=t1, T2=t2, SpinNum=np.int32(Sn), TypeNum=np.int32(P),
+                ChemShift=np.float64(0.0))
+    if model != "normal":
+        vobj["K"] = k_layout(model, rates)
+    if model == "gm":
+        vobj["TypeFlag"] = np.asarray(type_flag, np.float64)
+    vmag = dict(dB0=db0, dWRnd=dwrnd, Gzgrid=gz, Gygrid=gy, Gxgrid=gx)
+    vcoi = dict(TxCoilmg=np.asarray(tx_mg, np.float32), TxCoilpe=np.asarray(tx_pe, np.float32),
+                RxCoilx=rxx, RxCoily=rxy, TxCoilNum=np.int32(ntx), RxCoilNum=np.int32(nrx),
+                TxCoilDefault=np.float64(tx_default), RxCoilDefault=np.float64(rx_default))
+    cs = np.zeros(P) if cs_hz is None else np.asarray(cs_hz, np.float64)
+    vctl = dict(CS=cs.astype(np.float64), TRNum=np.int32(tr_num), RunMode=np.int32(0),
+                MaxThreadNum=np.int32(1), ActiveThreadNum=np.int32(0), GPUIndex=np.int32(0))
+    nsig = int(np.count_nonzero(seqlines["ADCLine"] == 1))
+    vvar = dict(t=np.float64(0), dt=np.float64(0), rfAmp=np.zeros(ntx), rfPhase=np.zeros(ntx),
+                rfFreq=np.zeros(ntx), rfCoil=np.float64(0), rfRef=np.float64(0),
+                GzAmp=np.float64(0), GyAmp=np.float64(0), GxAmp=np.float64(0),
+                ADC=np.float64(0), Ext=np.float64(0), Kz=np.float64(0), Ky=np.float64(0),
+                Kx=np.float64(0), gpuFetch=np.float64(0),
+                utsi=np.int32(0), rfi=np.int32(0), Gzi=np.int32(0), Gyi=np.int32(0),
+                Gxi=np.int32(0), ADCi=np.int32(0), Exti=np.int32(0), TRCount=np.int32(1),
+                SliceCount=np.int32(1), PhaseCount=np.int32(1))
+    vsig = dict(Sx=np.zeros(nsig * P * nrx), Sy=np.zeros(nsig * P * nrx),
+                Kz=np.zeros(nsig), Ky=np.zeros(nsig), Kx=np.zeros(nsig),
+                Mx=np.zeros_like(mz), My=np.zeros_like(mz), Mz=mz.copy(),
+                Muts=np.float64(0), SignalNum=np.int32(nsig))
+    return Scan(vobj, vmag, vcoi, vctl, dict(seqlines), vvar, vsig, model=model, rates=rates,
+                info=dict(seed=seed))
+
+
+# ---------------------------------------------------------------------------
+# sequences
+# ---------------------------------------------------------------------------
+
+def gre_lines(*, n_read, n_pe, n_par=1, fov=(0.24, 0.24, 0.24), tr_ms=20.0, te_ms=(5.0,),
+              flip=30.0, rf_ms=2.0, rf_raster_us=10.0, tbw=4.0, bw_hz=32000.0,
+              spoil=True, n_tr=None, ext_every=0, gamma=GAMMA):
+    """Cartesian (multi-echo) gradient echo, 2D (n_par=1) or 3D.
+
+    RF: windowed sinc; slab gradient on z during RF, rephased after;
+    phase encode on y (and partition encode on z); monopolar readouts on x
+    centred at each TE (ms, from the RF centre) with a rewinder between
+    echoes; a spoiler lobe after the last echo.
+    """
+    dwell_ns = int(round(1e9 / bw_hz))
+    rf_ns = int(round(rf_ms * 1e6))
+    raster_ns = int(round(rf_raster_us * 1e3))
+    tr_ns = int(round(tr_ms * 1e6))
+    ramp = 100_000  # 0.1 ms ramps
+    gread = 2 * np.pi / (gamma * fov[0] * dwell_ns * S.NS)
+    ro_ns = n_read * dwell_ns
+    rf_center = rf_ns // 2
+    gslab = 2 * np.pi / (gamma * fov[2] * 4 * raster_ns * S.NS) * 0.05  # mild slab gradient
+    trs = []
+    total = n_pe * n_par if n_tr is None else n_tr
+    for i in range(total):
+        ipe = i % n_pe
+        ipar = (i // n_pe) % n_par
+        tr = S.TR(tr_ns)
+        t_rf, a_rf = S.sinc_rf(0, rf_ns, raster_ns, flip, tbw)
+        tr.rf(t_rf, a_rf)
+        tr.trap("z", 0, rf_ns, gslab, ramp_ns=raster_ns)
+        # encoding window between the RF end and the first readout
+        first_ro = rf_center + int(round(te_ms[0] * 1e6)) - ro_ns // 2
+        enc0 = rf_ns + 20_000
+        enc1 = first_ro - 20_000
+        if enc1 - enc0 < 4 * ramp:
+            raise ValueError("TE too short for the encoding lobes")
+        dur = (enc1 - enc0 - 2 * ramp) * S.NS
+        ky = (ipe - n_pe // 2) / fov[1]
+        tr.trap("y", enc0, enc1, 2 * np.pi * ky / (gamma * dur), ramp_ns=ramp)
+        gz_area = -gslab * (rf_ns - 2 * raster_ns) * S.NS / 2
+        if n_par > 1:
+            kz = (ipar - n_par // 2) / fov[2]
+            gz_area += 2 * np.pi * kz / gamma
+        tr.trap("z", enc0, enc1, gz_area / dur, ramp_ns=ramp)
+        pre_area = -gread * (n_read // 2) * dwell_ns * S.NS
+        tr.trap("x", enc0, enc1, pre_area / dur, ramp_ns=ramp)
+        adc_times = []
+        prev_end = None
+        for e, te in enumerate(te_ms):
+            ro_start = rf_center + int(round(te * 1e6)) - (n_read // 2) * dwell_ns
+            if prev_end is not None:
+                # rewind the full readout lobe before the next echo
+                g0, g1 = prev_end + 20_000, ro_start - ramp - 20_000
+                if g1 - g0 < 3 * ramp:
+                    raise ValueError("echo spacing too short")
+                rdur = (g1 - g0 - 2 * ramp) * S.NS
+                tr.trap("x", g0, g1, -gread * ro_ns * S.NS / rdur, ramp_ns=ramp)
+            tr.trap("x", ro_start - ramp, ro_start + ro_ns + ramp, gread, ramp_ns=ramp)
+            adc_times += list(ro_start + dwell_ns * np.arange(n_read))
+            prev_end = ro_start + ro_ns + ramp
+        tr.adc_t += [0]
+        tr.adc_v += [0.0]
+        tr.adc(adc_times)
+        tr.adc_t += [tr_ns]
+        tr.adc_v += [0.0]
+        if spoil and prev_end + 2_500_000 < tr_ns:
+            tr.trap("x", prev_end + 50_000, prev_end + 2_050_000, 4 * gread, ramp_ns=ramp)
+        if ext_every and (i % ext_every == ext_every - 1):
+            tr.ext_t += [0]
+            tr.ext_v += [0.0]
+            tr.ext(prev_end + 10_000, 1.0)
+            tr.ext_t += [tr_ns]
+            tr.ext_v += [0.0]
+        trs.append(tr)
+    return S.concat(trs), total
+
+
+# ---------------------------------------------------------------------------
+# the five workloads
+# ---------------------------------------------------------------------------
+
+def config1_gre(seed=0, n=64, n_tr=None) -> Scan:
+    """Plain single-pool 2D GRE: n x n x 1, three concentric disks, dB0 ~ N(0, 10 Hz)."""
+    rng = np.random.default_rng(seed)
+    Y = X = n
+    yy, xx = np.mgrid[0:Y, 0:X]
+    r = np.hypot((xx - (X - 1) / 2) / (X / 2), (yy - (Y - 1) / 2) / (Y / 2))
+    rho = np.zeros((Y, X, 1), np.float32)
+    t1 = np.zeros_like(rho)
+    t2 = np.zeros_like(rho)
+    for rmax, T1, T2, M0 in [(0.9, 0.8, 0.08, 0.7), (0.6, 1.3, 0.11, 0.8), (0.3, 4.0, 2.0, 1.0)]:
+        m = (r <= rmax)[..., None]
+        rho[m], t1[m], t2[m] = M0, T1, T2
+    db0 = rng.normal(0.0, 10.0, (Y, X, 1))
+    fov = 0.24
+    lines, ntr = gre_lines(n_read=n, n_pe=n, fov=(fov, fov, fov), tr_ms=20.0, te_ms=(5.0,),
+                           flip=30.0, rf_ms=2.0, rf_raster_us=10.0, tbw=4.0, bw_hz=32000.0,
+                           n_tr=n_tr)
+    return assemble(rho, t1, t2, db0_hz=db0, res=(fov / X, fov / Y, 0.005), seqlines=lines,
+                    tr_num=ntr, seed=seed)
+
+
+def _cylinder_coils(shape, res, n_coils, rng):
+    Y, X, Z = shape
+    gx, gy, gz = _grids(shape, res)
+    radius = 0.6 * max(X * res[0], Y * res[1])
+    sigma = 0.5 * radius
+    mags, phs = [], []
+    for c in range(n_coils):
+        th = 2 * np.pi * c / n_coils
+        cx, cy = radius * np.cos(th), radius * np.sin(th)
+        cz = (rng.uniform(-0.3, 0.3)) * Z * res[2]
+        d2 = (gx - cx) ** 2 + (gy - cy) ** 2 + (gz - cz) ** 2
+        mags.append(np.exp(-d2 / (2 * sigma**2)))
+        phs.append(th + 2 * np.pi * (gx * np.cos(th) + gy * np.sin(th)) / (4 * radius))
+    mag = np.stack(mags, -1)
+    ph = np.stack(phs, -1)
+    return (mag * np.cos(ph)).astype(np.float32), (mag * np.sin(ph)).astype(np.float32)
+
+
+def config2_me_gre(seed=0, nx=128, ny=128, nz=32, n_pe=32, n_par=8, n_read=128, spins=4,
+                   n_coils=8, n_tr=None, model="me") -> Scan:
+    """Two-pool exchange 3D multi-echo GRE with 8 Rx coils (precision study).
+
+    Free water (T1 1000 / T2 60 ms) and myelin water (T1 400 / T2 12 ms),
+    myelin fraction ~ U(0, 0.25), exchange k ~ U(2, 20) 1/s from myelin to
+    free water (detailed balance sets the reverse rate), dB0 ~ N(0, 25 Hz),
+    4 spins per voxel with intravoxel dephasing, 6 echoes at TE 2..22 ms,
+    ``n_pe`` x ``n_par`` phase/partition encodes of ``n_read`` samples.
+    """
+    rng = np.random.default_rng(seed)
+    Y, X, Z = ny, nx, nz
+    yy, xx, zz = np.meshgrid(np.arange(Y), np.arange(X), np.arange(Z), indexing="ij")
+    r = np.hypot((xx - (X - 1) / 2) / (X / 2), (yy - (Y - 1) / 2) / (Y / 2))
+    inside = r <= 0.85
+    f = rng.uniform(0.0, 0.25, (Y, X, Z))
+    rho = np.zeros((Y, X, Z, 2), np.float32)
+    rho[..., 0] = np.where(inside, 1.0 - f, 0.0)
+    rho[..., 1] = np.where(inside, f, 0.0)
+    t1 = np.zeros_like(rho)
+    t2 = np.zeros_like(rho)
+    t1[..., 0], t2[..., 0] = np.where(inside, 1.0, 0.0), np.where(inside, 0.060, 0.0)
+    t1[..., 1], t2[..., 1] = np.where(inside, 0.4, 0.0), np.where(inside, 0.012, 0.0)
+    # a myelin fraction of exactly 0 leaves that pool empty (Rho == 0)
+    k = rng.uniform(2.0, 20.0, (Y, X, Z))
+    rates = np.zeros((Y, X, Z, 2, 2), np.float32)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rates[..., 1, 0] = np.where(inside, k, 0.0)
+        rates[..., 0, 1] = np.where(inside & (f < 1), k * f / np.maximum(1 - f, 1e-6), 0.0)
+    db0 = rng.normal(0.0, 25.0, (Y, X, Z))
+    t2star = np.stack([np.full((Y, X, Z), 0.040), np.full((Y, X, Z), 0.010)], -1)
+    fov = (0.24, 0.24, 0.24 * Z / X)
+    res = (fov[0] / X, fov[1] / Y, fov[2] / Z)
+    rxx, rxy = _cylinder_coils((Y, X, Z), res, n_coils, rng)
+    lines, ntr = gre_lines(n_read=n_read, n_pe=n_pe, n_par=n_par, fov=fov, tr_ms=25.0,
+                           te_ms=(2.0, 6.0, 10.0, 14.0, 18.0, 22.0), flip=20.0, rf_ms=0.5,
+                           rf_raster_us=10.0, tbw=2.0, bw_hz=64000.0, n_tr=n_tr)
+    tf = np.zeros(2) if model == "gm" else None
+    return assemble(rho, t1, t2, spin_num=spins, t2star=t2star, db0_hz=db0, res=res,
+                    model=model, rates=rates, type_flag=tf, rx=(rxx, rxy), seqlines=lines,
+                    tr_num=ntr, seed=seed)
+
+
+def sat_gre_lines(*, n_read=16, n_pe=4, fov=0.2, tr_ms=30.0, sat_offsets_hz=(1500.0,), sat_ms=4.0,
+                  sat_b1_ut=2.0, sat_raster_us=20.0, flip=15.0, bw_hz=32000.0, gamma=GAMMA):
+    """Saturation-prepared GRE: per TR a block of Gaussian saturation pulses
+    at ``sat_offsets_hz`` (one offset per TR, cycled), then a hard
+    excitation and one Cartesian readout -- the MT/CEST workloads' shape."""
+    dwell = int(round(1e9 / bw_hz))
+    raster = int(round(sat_raster_us * 1e3))
+    sat_ns = int(round(sat_ms * 1e6))
+    tr_ns = int(round(tr_ms * 1e6))
+    ramp = 100_000
+    gread = 2 * np.pi / (gamma * fov * dwell * S.NS)
+    trs = []
+    for i in range(n_pe):
+        tr = S.TR(tr_ns)
+        off = sat_offsets_hz[i % len(sat_offsets_hz)]
+        n = sat_ns // raster + 1
+        t = np.arange(n, dtype=np.int64) * raster
+        env = np.exp(-0.5 * ((t - sat_ns / 2) / (sat_ns / 5)) ** 2)
+        env[0] = env[-1] = 0.0
+        tr.rf(t, sat_b1_ut * 1e-6 * env, 0.0, off)
+        t_ex = sat_ns + 1_000_000
+        t_hr, a_hr = S.hard_rf(t_ex, 200_000, flip)
+        tr.rf(t_hr, a_hr)
+        ro = t_ex + 2_000_000
+        ky = (i - n_pe // 2) / fov
+        dur = (1_600_000 - 2 * ramp) * S.NS
+        tr.trap("y", t_ex + 250_000, t_ex + 1_850_000, 2 * np.pi * ky / (gamma * dur), ramp_ns=ramp)
+        tr.trap("x", t_ex + 250_000, t_ex + 1_850_000, -gread * (n_read // 2) * dwell * S.NS / dur, ramp_ns=ramp)
+        tr.trap("x", ro - ramp, ro + n_read * dwell + ramp, gread, ramp_ns=ramp)
+        tr.adc_t += [0]
+        tr.adc_v += [0.0]
+        tr.adc(ro + dwell * np.arange(n_read))
+        tr.adc_t += [tr_ns]
+        tr.adc_v += [0.0]
+        trs.append(tr)
+    return S.concat(trs), n_pe
+
+
+def small_multipool(model: str, seed=0, n=8, nz=1, pools=2, spins=1, coils=1, n_tr=3, seq="gre") -> Scan:
+    """A small random multi-pool scan for parity tests of the ME/MT/CEST/GM
+    models: random tissue per voxel, rates obeying detailed balance."""
+    rng = np.random.default_rng(seed)
+    Y = X = n
+    Z = nz
+    P = pools
+    yy, xx = np.mgrid[0:Y, 0:X]
+    inside2d = np.hypot(xx - (X - 1) / 2, yy - (Y - 1) / 2) <= 0.45 * n
+    inside = np.repeat(inside2d[..., None], Z, axis=2)
+    frac = rng.uniform(0.02, 0.2, (Y, X, Z, P))
+    frac[..., 0] = 1.0
+    rho = (frac * inside[..., None]).astype(np.float32)
+    t1 = np.where(inside[..., None], rng.uniform(0.3, 1.5, (Y, X, Z, P)), 0).astype(np.float32)
+    t2 = np.where(inside[..., None], rng.uniform(0.01, 0.1, (Y, X, Z, P)), 0).astype(np.float32)
+    type_flag = None
+    if model in ("mt", "cest"):
+        t2[..., 1] = np.where(inside, 12e-6, 0)  # bound pool T2 (s)
+    if model == "gm":
+        type_flag = np.zeros(P)
+        type_flag[-1] = 1.0
+        t2[..., -1] = np.where(inside, 10e-6, 0)
+    rates = np.zeros((Y, X, Z, P, P), np.float32)
+    for p in range(1, P):
+        k = rng.uniform(10, 500, (Y, X, Z))
+        if model in ("me", "gm"):
+            rates[..., p, 0] = np.where(inside, k, 0)
+            rates[..., 0, p] = np.where(inside, k * rho[..., p] / np.maximum(rho[..., 0], 1e-6), 0)
+            if model == "me" and P > 2 and p == P - 1:
+                k2 = rng.uniform(5, 50, (Y, X, Z))
+                rates[..., p, 1] = np.where(inside, k2, 0)
+                rates[..., 1, p] = np.where(inside, k2 * rho[..., p] / np.maximum(rho[..., 1], 1e-6), 0)
+        else:  # mt / cest: exchange with free water only
+            rates[..., p, 0] = np.where(inside, k, 0)
+            rates[..., 0, p] = np.where(inside, k * rho[..., p] / np.maximum(rho[..., 0], 1e-6), 0)
+    db0 = rng.normal(0.0, 20.0, (Y, X, Z))
+    cs = np.zeros(P)
+    if model == "cest":
+        cs[2:] = rng.choice([3.5 * 128.0, 2.0 * 128.0, -3.5 * 128.0], P - 2, replace=False)
+    elif model in ("me", "gm"):
+        cs[1:] = rng.uniform(-50, 50, P - 1)
+    fov = 0.2
+    res = (fov / X, fov / Y, 0.005)
+    rx = _cylinder_coils((Y, X, Z), res, coils, rng) if coils > 1 else None
+    if seq == "sat":
+        lines, ntr = sat_gre_lines(n_read=n, n_pe=n_tr, fov=fov, sat_offsets_hz=(1500.0, -800.0, 400.0))
+    else:
+        lines, ntr = gre_lines(n_read=n, n_pe=n_tr, fov=(fov, fov, fov), tr_ms=12.0, te_ms=(4.0,), flip=25.0,
+                               rf_ms=1.0, rf_raster_us=10.0, tbw=2.0, bw_hz=32000.0)
+    t2s = np.maximum(t2 * 0.5, 1e-6) if spins > 1 else None
+    return assemble(rho, t1, t2, spin_num=spins, t2star=t2s, db0_hz=db0, res=res, cs_hz=cs, model=model,
+                    rates=rates, type_flag=type_flag, rx=rx, seqlines=lines, tr_num=ntr, seed=seed)

@@ -1,0 +1,77 @@
+"""Regenerate the golden fixtures from the reference engine itself.
+
+Runs the reference CPU engine (``Lib/src/engine/CPUEngine/DoScanAtCPU.cpp``,
+compiled unmodified against the project's mex/IPP stand-ins into
+``oracle/_ref`` -- available only where the reference tree is mounted) on
+seeded single-pool scans and stores its outputs, together with the all-FP64
+oracle's outputs on the same inputs, as small ``.npz`` files.  The scans are
+rebuilt from their seeds by ``mrilab_gb300.phantoms`` at test time.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from mrilab_gb300 import phantoms  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+MULTIPOOL = {
+    # name: small_multipool kwargs; the reference's own kernels (compiled as
+    # host C, oracle/_ref/libmrl_refkern.so) produce the golden signal
+    "mp_me_p2_s2_c2": dict(model="me", seed=3, pools=2, spins=2, coils=2, seq="gre"),
+    "mp_me_p3_s1_c1": dict(model="me", seed=3, pools=3, spins=1, coils=1, seq="gre"),
+    "mp_gm_p3_s2_c2": dict(model="gm", seed=3, pools=3, spins=2, coils=2, seq="sat"),
+    "mp_mt_p2_s2_c2": dict(model="mt", seed=3, pools=2, spins=2, coils=2, seq="sat"),
+    "mp_cest_p4_s2_c2": dict(model="cest", seed=3, pools=4, spins=2, coils=2, seq="sat"),
+}
+
+CASES = {
+    # name: (builder kwargs)
+    "gre2d_n16_tr4_seed1": dict(seed=1, n=16, n_tr=4),
+    "gre2d_n32_tr8_seed2": dict(seed=2, n=32, n_tr=8),
+    "gre2d_n64_full_seed0": dict(seed=0, n=64),
+}
+
+
+def main():
+    oracle.build()
+    if not oracle.ref_available():
+        raise SystemExit("the reference engine is not built (needs the reference tree)")
+    for name, kw in CASES.items():
+        sc = phantoms.config1_gre(**kw)
+        ref = oracle.run_ref_cpu(sc, threads=1)
+        f64 = oracle.run_port(sc, "f64")
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            builder=np.array("config1_gre"), kwargs=np.array(repr(kw)),
+            ref_Sx=ref["Sx"], ref_Sy=ref["Sy"], ref_Kx=ref["Kx"], ref_Ky=ref["Ky"], ref_Kz=ref["Kz"],
+            ref_Mz=ref["Mz"], ref_Mx=ref["Mx"], ref_My=ref["My"],
+            f64_Sx=f64["Sx"], f64_Sy=f64["Sy"],
+        )
+        s_ref = ref["Sx"] + 1j * ref["Sy"]
+        s64 = f64["Sx"] + 1j * f64["Sy"]
+        print(name, "reference vs FP64 oracle: %.3e" % (np.linalg.norm(s_ref - s64) / np.linalg.norm(s64)))
+    for name, kw in MULTIPOOL.items():
+        sc = phantoms.small_multipool(**kw)
+        ref = oracle.run_ref_kernel(sc)
+        f64 = oracle.run_port(sc, "f64")
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            builder=np.array("small_multipool"), kwargs=np.array(repr(kw)),
+            ref_Sx=ref["Sx"], ref_Sy=ref["Sy"], ref_Mz=ref["Mz"], ref_Mx=ref["Mx"], ref_My=ref["My"],
+            f64_Sx=f64["Sx"], f64_Sy=f64["Sy"],
+        )
+        s_ref = ref["Sx"] + 1j * ref["Sy"]
+        s64 = f64["Sx"] + 1j * f64["Sy"]
+        print(name, "reference kernels vs FP64 oracle: %.3e" % (np.linalg.norm(s_ref - s64) / np.linalg.norm(s64)))
+
+
+if __name__ == "__main__":
+    main()

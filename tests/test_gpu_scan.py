@@ -1,0 +1,144 @@
+"""GPU parity of the scan engine, called through the C ABI (libmrl_scan.so)
+and through the mex wrappers, against the reference's recorded outputs and
+the CPU oracle."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import ROOT, load_golden, rel_l2, signal
+from mrilab_gb300 import engine, mexsim, phantoms
+
+pytestmark = pytest.mark.gpu
+
+SINGLE = ["gre2d_n16_tr4_seed1", "gre2d_n32_tr8_seed2", "gre2d_n64_full_seed0"]
+MULTI = ["mp_me_p2_s2_c2", "mp_me_p3_s1_c1", "mp_gm_p3_s2_c2", "mp_mt_p2_s2_c2", "mp_cest_p4_s2_c2"]
+
+# Reference-order numerics: relative L2 of the complex signal against the
+# reference CPU engine's own output (its float rounding reproduced op by op;
+# transcendentals differ by < 1 ulp between libm and the device).
+TOL_REF_CPU = 1e-5
+# Multi-pool models against the reference's kernels run on the CPU in
+# double-per-operation arithmetic: both sit at float-rounding distance
+# (~1e-5) from the FP64 oracle.
+TOL_REF_KERN = 3e-5
+# Against the single-precision oracle port on the same inputs.
+TOL_PORT = 1e-5
+
+
+@pytest.mark.parametrize("name", SINGLE)
+def test_reference_numerics_match_reference_cpu_engine(built, name):
+    sc, g = load_golden(name)
+    out = engine.scan(sc, numerics="reference")
+    ref = g["ref_Sx"] + 1j * g["ref_Sy"]
+    err = rel_l2(signal(out), ref)
+    print(f"{name}: GPU vs reference CPU engine {err:.3e}")
+    assert err <= TOL_REF_CPU
+    np.testing.assert_allclose(out["Kx"], g["ref_Kx"], atol=1e-9)
+    np.testing.assert_allclose(out["Ky"], g["ref_Ky"], atol=1e-9)
+    np.testing.assert_allclose(out["Mz"], g["ref_Mz"], atol=5e-5)
+
+
+@pytest.mark.parametrize("name", MULTI)
+def test_reference_numerics_multipool_models(built, name):
+    sc, g = load_golden(name)
+    out = engine.scan(sc, numerics="reference")
+    ref = g["ref_Sx"] + 1j * g["ref_Sy"]
+    err_ref = rel_l2(signal(out), ref)
+    port = oracle.run_port(sc, "f32")
+    err_port = rel_l2(signal(out), signal(port))
+    print(f"{name}: GPU vs reference kernels {err_ref:.3e}, vs port {err_port:.3e}")
+    assert err_ref <= TOL_REF_KERN
+    assert err_port <= TOL_PORT
+    np.testing.assert_allclose(out["Mz"], port["Mz"], atol=1e-4)
+
+
+def test_mex_wrapper_path(built):
+    """DoScanAtGPU through the mex stand-in: globals in, globals out."""
+    sc, g = load_golden("gre2d_n16_tr4_seed1")
+    ms = mexsim.MexSession()
+    for k, v in sc.structs().items():
+        ms.set_global(k, v)
+    ms.set_field("VCtl", "Numerics", np.float64(1.0))
+    ms.call(os.path.join(ROOT, "mrilab_gb300", "mex", "DoScanAtGPU.so"))
+    sx = ms.get("VSig", "Sx").ravel(order="F")
+    sy = ms.get("VSig", "Sy").ravel(order="F")
+    assert rel_l2(sx + 1j * sy, g["ref_Sx"] + 1j * g["ref_Sy"]) <= TOL_REF_CPU
+    assert int(ms.get("VVar", "TRCount").ravel()[0]) == 4
+
+
+@pytest.mark.parametrize("wrapper,name", [("DoMEScanAtGPU", "mp_me_p2_s2_c2"), ("DoMTScanAtGPU", "mp_mt_p2_s2_c2"),
+                                          ("DoCESTScanAtGPU", "mp_cest_p4_s2_c2"), ("DoGMScanAtGPU", "mp_gm_p3_s2_c2")])
+def test_multipool_mex_wrappers(built, wrapper, name):
+    sc, g = load_golden(name)
+    ms = mexsim.MexSession()
+    for k, v in sc.structs().items():
+        ms.set_global(k, v)
+    ms.set_field("VCtl", "Numerics", np.float64(1.0))
+    ms.call(os.path.join(ROOT, "mrilab_gb300", "mex", wrapper + ".so"))
+    sx = ms.get("VSig", "Sx").ravel(order="F")
+    sy = ms.get("VSig", "Sy").ravel(order="F")
+    assert rel_l2(sx + 1j * sy, g["ref_Sx"] + 1j * g["ref_Sy"]) <= TOL_REF_KERN
+
+
+def test_plan_matches_scan_and_reruns(built):
+    sc, g = load_golden("gre2d_n32_tr8_seed2")
+    direct = engine.scan(sc, numerics="reference")
+    plan = engine.Plan(sc, numerics="reference")
+    w = plan.work()
+    assert w["samples"] == sc.signal_num and w["units"] > 0
+    for _ in range(2):  # re-execution restarts from the initial state
+        plan.execute()
+        out = plan.download()
+        assert rel_l2(signal(out), signal(direct)) <= 1e-12
+    plan.close()
+
+
+def test_ext_plugin_callback(built):
+    """An Ext plugin that spoils the transverse magnetisation (DoExtPlugin
+    case 6) sees the state after the step that starts at the Ext sample."""
+    sc = phantoms.config1_gre(seed=4, n=8, n_tr=3)
+    lines, _ = phantoms.gre_lines(n_read=8, n_pe=3, fov=(0.24,) * 3, tr_ms=20.0, te_ms=(5.0,), flip=30.0,
+                                  rf_ms=2.0, rf_raster_us=10.0, tbw=4.0, bw_hz=32000.0, ext_every=1)
+    sc.VSeq = lines
+    hs = engine.HostScan(sc, numerics="reference")
+    calls = []
+
+    def cb(args, what):
+        calls.append(what)
+        if what == engine.EXT_FETCH:
+            return 1
+        hs.keep["mx"][:] = 0
+        hs.keep["my"][:] = 0
+        return 0
+
+    out = engine.run(hs, cb)
+    assert calls == [engine.EXT_FETCH, engine.EXT_PLUGIN] * 3
+    base = engine.scan(sc, numerics="reference")
+    assert rel_l2(signal(out), signal(base)) > 1e-3
+    # a plugin error propagates as a status code
+    hs2 = engine.HostScan(sc, numerics="reference")
+    with pytest.raises(engine.ScanError) as e:
+        engine.run(hs2, lambda args, what: 0 if what == engine.EXT_FETCH else 1)
+    assert e.value.status == -4
+
+
+def test_empty_object_gives_zero_signal(built):
+    sc = phantoms.config1_gre(seed=0, n=8, n_tr=2)
+    sc.VObj["Rho"][:] = 0
+    sc.VObj["Mz"][:] = 0
+    out = engine.scan(sc, numerics="reference")
+    assert np.all(out["Sx"] == 0) and np.all(out["Sy"] == 0)
+    assert np.count_nonzero(out["Kx"]) > 0
+
+
+def test_multiple_partial_launches(built, monkeypatch):
+    """A tiny partial budget splits the scan into many launches; the signal
+    is unchanged."""
+    sc, g = load_golden("gre2d_n16_tr4_seed1")
+    monkeypatch.setenv("MRL_PARTIAL_MB", "0.0001")
+    out = engine.scan(sc, numerics="reference")
+    t = engine.last_timing()
+    assert t["launches"] > 8
+    assert rel_l2(signal(out), g["ref_Sx"] + 1j * g["ref_Sy"]) <= TOL_REF_CPU
