@@ -43,6 +43,10 @@ UNITS = {
     "scan_ref_exch.cu": ["-fmad=false"],
     "scan_ref_mt.cu": ["-fmad=false"],
     "scan_ref_cest.cu": ["-fmad=false"],
+    "scan_fast_normal.cu": [],
+    "scan_fast_exch.cu": [],
+    "scan_fast_mt.cu": [],
+    "scan_fast_cest.cu": [],
     "decode.cpp": None,  # host C++
 }
 

@@ -3,6 +3,7 @@
 #include "decode.h"
 
 #include <cmath>
+#include <cstring>
 
 namespace mrl {
 
@@ -62,6 +63,7 @@ void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx, double gyro
                       DecodeChunk &out) {
     const int stride = record_stride_f4(tx) * 4;
     out.records.clear();
+    out.steps.clear();
     out.step_adc.clear();
     out.n_steps = 0;
     out.n_rf_steps = 0;
@@ -153,6 +155,18 @@ void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx, double gyro
                 r[4 + 4 * c + 1] = (float)s.rf_phase[c];
                 r[4 + 4 * c + 2] = (float)s.rf_freq[c];
             }
+            StepInfo si;
+            si.dt = dt;
+            si.gz = s.gz;
+            si.gy = s.gy;
+            si.gx = s.gx;
+            for (int c = 0; c < kMaxTx; ++c) {
+                si.amp[c] = c < tx ? s.rf_amp[c] : 0.0;
+                si.phase[c] = c < tx ? s.rf_phase[c] : 0.0;
+                si.freq[c] = c < tx ? s.rf_freq[c] : 0.0;
+            }
+            si.adc = s.adc == 1 ? s.signali : -1;
+            out.steps.push_back(si);
             bool rf_on = false;
             for (int c = 0; c < tx; ++c) rf_on |= (float)s.rf_amp[c] != 0.f;
             out.n_rf_steps += rf_on;
@@ -187,6 +201,70 @@ void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx, double gyro
         finish_time_point(s, tx, ext_flag, flag_sum, dt);
     }
     out.adc_end = s.signali;
+}
+
+namespace {
+inline void split(double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+}  // namespace
+
+void pack_fast_records(const DecodeChunk &ch, int tx, FrameMoments &fm, std::vector<float> &out) {
+    const int stride = fast_stride_f4(tx) * 4;
+    out.assign((size_t)ch.n_steps * stride, 0.f);
+    for (int64_t q = 0; q < ch.n_steps; ++q) {
+        const StepInfo &si = ch.steps[q];
+        float *r = &out[(size_t)q * stride];
+        bool rf = false;
+        double dw_rf = 0;
+        for (int c = 0; c < tx; ++c) {
+            if ((float)si.amp[c] != 0.f) {
+                rf = true;
+                dw_rf += 2 * kPi * si.freq[c];
+            }
+        }
+        int flags = 0;
+        if (si.adc >= 0) flags |= kFlagAdc;
+        if (rf) flags |= kFlagRf;
+        const bool new_dt = si.dt != fm.last_dt;
+        const bool new_state = new_dt || si.gx != fm.last_gx || si.gy != fm.last_gy || si.gz != fm.last_gz;
+        if (new_dt) flags |= kFlagDt;
+        if (new_state) flags |= kFlagState;
+        if (new_state || rf || fm.since_anchor >= kAnchorEvery) {
+            flags |= kFlagAnchor;
+            fm.since_anchor = 0;
+        }
+        fm.since_anchor++;
+        fm.last_dt = si.dt;
+        fm.last_gx = si.gx;
+        fm.last_gy = si.gy;
+        fm.last_gz = si.gz;
+        r[0] = (float)si.dt;
+        r[1] = (float)si.gz;
+        r[2] = (float)si.gy;
+        r[3] = (float)si.gx;
+        r[4] = (float)(si.amp[0] * std::cos(si.phase[0]));
+        r[5] = (float)(si.amp[0] * std::sin(si.phase[0]));
+        r[6] = (float)dw_rf;
+        std::memcpy(&r[7], &flags, sizeof(int));
+        split(fm.t, r[8], r[9]);
+        split(fm.kx, r[10], r[11]);
+        split(fm.ky, r[12], r[13]);
+        split(fm.kz, r[14], r[15]);
+        for (int c = 1; c < tx; ++c) {
+            r[16 + 4 * (c - 1) + 0] = (float)(si.amp[c] * std::cos(si.phase[c]));
+            r[16 + 4 * (c - 1) + 1] = (float)(si.amp[c] * std::sin(si.phase[c]));
+            r[16 + 4 * (c - 1) + 2] = (float)si.freq[c];
+            r[16 + 4 * (c - 1) + 3] = (float)std::fabs(si.amp[c]);
+        }
+        if (!rf) {  // the frame advances over steps without rf
+            fm.t += si.dt;
+            fm.kx += si.gx * si.dt;
+            fm.ky += si.gy * si.dt;
+            fm.kz += si.gz * si.dt;
+        }
+    }
 }
 
 }  // namespace mrl

@@ -39,7 +39,15 @@ struct DecodeState {
     double pend_flag_sum = 0, pend_dt = 0;
 };
 
+// One dt > 0 step in double precision, as decoded.
+struct StepInfo {
+    double dt, gz, gy, gx;
+    double amp[kMaxTx], phase[kMaxTx], freq[kMaxTx];
+    int adc;  // ADC sample index, or -1
+};
+
 struct DecodeChunk {
+    std::vector<StepInfo> steps;     // dt > 0 steps
     std::vector<float> records;      // n_steps * stride floats
     std::vector<int> step_adc;       // per step: ADC sample index, or -1
     int64_t n_steps = 0;
@@ -50,6 +58,30 @@ struct DecodeChunk {
 
 void load_state(DecodeState &s, const mrl_state &v, int tx_num);
 void store_state(const DecodeState &s, mrl_state &v, int tx_num);
+
+// Moments of the frame phase, accumulated over steps without rf (the rf
+// steps rotate the magnetisation explicitly): elapsed time and gradient
+// areas, in double precision, carried across chunks.
+struct FrameMoments {
+    double t = 0, kx = 0, ky = 0, kz = 0;
+    double last_dt = -1, last_gx = 0, last_gy = 0, last_gz = 0;
+    int since_anchor = 1 << 30;
+};
+
+// Step record of the MRL_NUMERICS_ACCURATE integrator (16 floats + 4 per
+// extra Tx coil):
+//   {dt, Gz, Gy, Gx}
+//   {Re A0, Im A0, 2*pi*sum of rf frequencies of the active coils, flags}
+//   {T hi, T lo, Kx hi, Kx lo}      moments at the start of the step
+//   {Ky hi, Ky lo, Kz hi, Kz lo}
+//   {Re Ac, Im Ac, freq c, |Ac|} for every coil c >= 1
+// with Ac = amp_c * exp(i phase_c) the complex rf amplitude, and flag bits
+// kFlagAdc, kFlagRf, kFlagAnchor (recompute the frame phasors exactly),
+// kFlagState (dt or gradient changed), kFlagDt (dt changed).
+enum : int { kFlagAdc = 1, kFlagRf = 2, kFlagAnchor = 4, kFlagState = 8, kFlagDt = 16 };
+constexpr int kAnchorEvery = 8;
+inline int fast_stride_f4(int tx_num) { return 4 + (tx_num - 1); }
+void pack_fast_records(const DecodeChunk &ch, int tx_num, FrameMoments &fm, std::vector<float> &out);
 
 // Decode until the next nonzero Ext sample or the end of the sequence.
 // K-space positions of acquired samples are accumulated into sig.kx/ky/kz.

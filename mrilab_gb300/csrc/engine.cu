@@ -127,6 +127,12 @@ struct Scanner {
     DevBuf<int> d_amap;
     DevBuf<double> d_sx, d_sy;
     DevBuf<int> d_err;
+    // accurate integrator: frame coefficients and moments
+    bool fast = false;
+    FrameMoments fmom;
+    DevBuf<float2> d_f2;  // omega [4][n] | wres [P][S][n] | txc [Tx][n]
+    size_t o_om = 0, o_wr = 0, o_txc = 0;
+    std::vector<float> frec;
     // offsets into d_f
     size_t o_gx = 0, o_gy = 0, o_gz = 0, o_db0 = 0, o_txmg = 0, o_txpe = 0, o_rho = 0, o_t1 = 0, o_t2 = 0, o_k = 0,
            o_dwr = 0;
@@ -192,9 +198,24 @@ struct Scanner {
         }
         if (mi.nk > 0 && (!a.obj.k || a.obj.k_channels < mi.nk))
             return set_err("K needs %d channels, got %d", mi.nk, a.obj.k ? a.obj.k_channels : 0), MRL_ERR_ARG;
+        fast = a.ctl.numerics == MRL_NUMERICS_ACCURATE;
+        if (a.ctl.numerics != MRL_NUMERICS_ACCURATE && a.ctl.numerics != MRL_NUMERICS_REFERENCE)
+            return set_err("unknown numerics %d", a.ctl.numerics), MRL_ERR_ARG;
+        if (fast && TX > 1) {
+            bool bound = mi.km == KM_MT || mi.km == KM_CEST;
+            if (mi.gm)
+                for (int t = 0; t < P; ++t) bound |= (int)a.obj.type_flag[t] == 1;
+            if (bound)
+                return set_err("bound-pool saturation with several Tx coils needs MRL_NUMERICS_REFERENCE"),
+                       MRL_ERR_UNSUPPORTED;
+        }
         NS = spins_per_thread(S);
+        if (const char *e = getenv("MRL_SPINS_PER_THREAD")) {
+            const int ns = atoi(e);
+            if ((ns == 1 || ns == 2 || ns == 4) && S % ns == 0) NS = ns;
+        }
         tpv = S / NS;
-        stride4 = record_stride_f4(TX);
+        stride4 = fast ? fast_stride_f4(TX) : record_stride_f4(TX);
         return MRL_OK;
     }
 
@@ -249,7 +270,44 @@ struct Scanner {
                 for (int c = 0; c < RX; ++c)
                     hr[c * n + i] = make_float2(a.coil.rx_x[c * V + v], a.coil.rx_y[c * V + v]);
         }
+        std::vector<float2> h2;
+        if (fast) {
+            // frame coefficients in double, split into (hi, lo) float pairs
+            o_om = 0;
+            o_wr = 4 * n;
+            o_txc = o_wr + (size_t)P * S * n;
+            h2.assign(o_txc + (size_t)TX * n, make_float2(0.f, 0.f));
+            auto split = [](double v) {
+                const float hi = (float)v;
+                return make_float2(hi, (float)(v - (double)hi));
+            };
+            const double g = a.obj.gyro;
+            for (int i = 0; i < n_act; ++i) {
+                const long long v = act[i];
+                h2[0 * n + i] = split(g * (double)a.mag.db0[v]);
+                h2[1 * n + i] = split(g * (double)a.mag.gxgrid[v]);
+                h2[2 * n + i] = split(g * (double)a.mag.gygrid[v]);
+                h2[3 * n + i] = split(g * (double)a.mag.gzgrid[v]);
+                for (int t = 0; t < P; ++t) {
+                    const double cs = a.ctl.cs ? 2 * kPiRef * a.ctl.cs[t] : 0.0;
+                    for (int s2 = 0; s2 < S; ++s2)
+                        h2[o_wr + ((size_t)t * S + s2) * n + i] =
+                            split((double)a.mag.dwrnd[((long long)t * S + s2) * V + v] + cs);
+                }
+                for (int c = 0; c < TX; ++c) {
+                    const double mg = a.coil.tx_mg[c * V + v], pe = a.coil.tx_pe[c * V + v];
+                    h2[o_txc + (size_t)c * n + i] = make_float2((float)(mg * std::cos(pe)), (float)(mg * std::sin(pe)));
+                }
+            }
+        }
         cudaError_t e;
+        if (fast) {
+            if ((e = d_f2.ensure(h2.size())) != cudaSuccess) return fail_cuda(e, "cudaMalloc(frame)");
+            if ((e = cudaMemcpyAsync(d_f2.p, h2.data(), h2.size() * sizeof(float2), cudaMemcpyHostToDevice, st)) !=
+                cudaSuccess)
+                return fail_cuda(e, "upload frame");
+            h2d_bytes += (double)h2.size() * sizeof(float2);
+        }
         if ((e = d_f.ensure(off)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(object)");
         if ((e = d_m.ensure(hm.size())) != cudaSuccess) return fail_cuda(e, "cudaMalloc(state)");
         if ((e = d_rx.ensure(hr.size())) != cudaSuccess) return fail_cuda(e, "cudaMalloc(coils)");
@@ -394,17 +452,22 @@ struct Scanner {
         }
         out.push_back({s0, ch.n_steps, a_off, a_cnt});
         a_peak = std::max(a_peak, a_cnt);
+        const std::vector<float> *recs = &ch.records;
+        if (fast) {
+            pack_fast_records(ch, TX, fmom, frec);
+            recs = &frec;
+        }
         cudaError_t e;
-        if ((e = d_rec.ensure(ch.records.size() / 4)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(steps)");
+        if ((e = d_rec.ensure(recs->size() / 4)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(steps)");
         if ((e = d_amap.ensure(std::max<size_t>(1, amap_host.size()))) != cudaSuccess)
             return fail_cuda(e, "cudaMalloc(amap)");
         if ((e = d_part.ensure((size_t)n_blocks() * std::max(1, a_peak) * npairs)) != cudaSuccess)
             return fail_cuda(e, "cudaMalloc(partials)");
         auto t0 = std::chrono::steady_clock::now();
-        if ((e = cudaMemcpyAsync(d_rec.p, ch.records.data(), ch.records.size() * sizeof(float), cudaMemcpyHostToDevice,
-                                 st)) != cudaSuccess)
+        if ((e = cudaMemcpyAsync(d_rec.p, recs->data(), recs->size() * sizeof(float), cudaMemcpyHostToDevice, st)) !=
+            cudaSuccess)
             return fail_cuda(e, "upload steps");
-        h2d_bytes += (double)ch.records.size() * sizeof(float) + amap_host.size() * sizeof(int);
+        h2d_bytes += (double)recs->size() * sizeof(float) + amap_host.size() * sizeof(int);
         if (!amap_host.empty() &&
             (e = cudaMemcpyAsync(d_amap.p, amap_host.data(), amap_host.size() * sizeof(int), cudaMemcpyHostToDevice,
                                  st)) != cudaSuccess)
@@ -437,11 +500,27 @@ struct Scanner {
             }
             if (n_act > 0) {
                 dim3 grid(nblk);
-                switch (mi.km) {
-                case KM_NORMAL: e = launch_scan_ref_normal(P, NS, grid, smem, stream, L); break;
-                case KM_EXCH: e = launch_scan_ref_exch(P, NS, grid, smem, stream, L); break;
-                case KM_MT: e = launch_scan_ref_mt(P, NS, grid, smem, stream, L); break;
-                default: e = launch_scan_ref_cest(P, NS, grid, smem, stream, L); break;
+                if (fast) {
+                    FastLaunch F;
+                    F.b = L;
+                    const size_t n = std::max(1, n_act);
+                    F.omega = d_f2.p + o_om;
+                    F.wres = d_f2.p + o_wr;
+                    F.txc = d_f2.p + o_txc;
+                    (void)n;
+                    switch (mi.km) {
+                    case KM_NORMAL: e = launch_scan_fast_normal(P, NS, grid, smem, stream, F); break;
+                    case KM_EXCH: e = launch_scan_fast_exch(P, NS, grid, smem, stream, F); break;
+                    case KM_MT: e = launch_scan_fast_mt(P, NS, grid, smem, stream, F); break;
+                    default: e = launch_scan_fast_cest(P, NS, grid, smem, stream, F); break;
+                    }
+                } else {
+                    switch (mi.km) {
+                    case KM_NORMAL: e = launch_scan_ref_normal(P, NS, grid, smem, stream, L); break;
+                    case KM_EXCH: e = launch_scan_ref_exch(P, NS, grid, smem, stream, L); break;
+                    case KM_MT: e = launch_scan_ref_mt(P, NS, grid, smem, stream, L); break;
+                    default: e = launch_scan_ref_cest(P, NS, grid, smem, stream, L); break;
+                    }
                 }
                 if (e != cudaSuccess) return fail_cuda(e, "scan kernel launch");
                 launches++;

@@ -1,0 +1,566 @@
+// The MRL_NUMERICS_ACCURATE scan kernel: the same sequence model and tissue
+// models as scan_ref_kernel (BlochKernel{,ME,MT,CEST,GM}.cuh), integrated
+// in single precision in a rotating frame so that it is both faster and
+// closer to the exact (FP64) solution than the reference's own FP32 code.
+//
+// Frame.  Each isochromat-pool keeps its magnetisation in a frame rotating
+// with its free precession: m_lab = m_frame * P, P = exp(-i Phi), with
+//   Phi = gamma (dB0 T + x Kx + y Ky + z Kz) + w_res T,
+// T and K the elapsed time and gradient areas over the steps without rf
+// (moments carried on the host in FP64 and passed as hi/lo float pairs),
+// and w_res = dWRnd + 2 pi CS the isochromat's residual frequency (hi/lo).
+// Free precession therefore never rotates m: only the phasor P advances,
+// by a factor (1 + d) with d = exp(-i theta) - 1 evaluated once per change
+// of (dt, G); P is recomputed exactly from the moments (double-float
+// arithmetic, Cody-Waite reduction) at every change of (dt, G), every rf
+// step and at least every kAnchorEvery steps, so its error never
+// accumulates.  An rf step rotates m_frame about the effective field with
+// the rf azimuth shifted by -Phi (exact identity of the reference's closed
+// form, BlochKernel.cuh:241-254).
+//
+// Coefficients close to 1 are applied in "1 - y" form: relaxation
+// exp(-dt/T) = 1 - y with y = -expm1(-dt/T), exchange exp(-k dt) likewise,
+// so repeated multiplication does not accumulate the rounding of a stored
+// factor.  The receive sum rotates each frame back to the lab with P.
+#pragma once
+
+#include "decode.h"
+#include "scan_kernel.cuh"
+
+namespace mrl {
+
+struct FastLaunch {
+    ScanLaunch b;             // shared fields; b.rec points at fast records
+    const float2 *omega;      // [4][n_act] (hi, lo) of gamma*dB0, gamma*x, gamma*y, gamma*z
+    const float2 *wres;       // [P][S][n_act] (hi, lo) residual frequency, rad/s
+    const float2 *txc;        // [tx][n_act] TxCoilmg * exp(i TxCoilpe)
+};
+
+// ---- double-float helpers ------------------------------------------------
+struct df {
+    float hi, lo;
+};
+
+__device__ __forceinline__ df two_prod(float a, float b) {
+    const float p = a * b;
+    return {p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ df two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+
+// (a_hi + a_lo) * (b_hi + b_lo), unnormalised
+__device__ __forceinline__ df df_mul(float ah, float al, float bh, float bl) {
+    df p = two_prod(ah, bh);
+    p.lo = fmaf(ah, bl, fmaf(al, bh, p.lo));
+    return p;
+}
+
+__device__ __forceinline__ df df_add(df a, df b) {
+    df s = two_sum(a.hi, b.hi);
+    s.lo += a.lo + b.lo;
+    return s;
+}
+
+// exp(-i phi) for a double-float phase, reduced modulo 2 pi.
+__device__ __forceinline__ float2 phasor(df phi) {
+    constexpr float kInv2Pi = 0.15915494309189535f;
+    constexpr float kC1 = 6.28318548202514648f;     // float(2 pi)
+    constexpr float kC2 = -1.7484555314695172e-07f; // 2 pi - kC1
+    const float k = rintf(phi.hi * kInv2Pi);
+    float r = fmaf(-k, kC1, phi.hi);
+    r = fmaf(-k, kC2, r);
+    r += phi.lo;
+    float s, c;
+    sincosf(r, &s, &c);
+    return make_float2(c, -s);
+}
+
+// exp(-i theta) - 1, accurate for small theta.
+__device__ __forceinline__ float2 phase_step(float theta) {
+    float s, c;
+    sincosf(0.5f * theta, &s, &c);
+    return make_float2(-2.f * s * s, -2.f * s * c);
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+__device__ __forceinline__ float2 cmul_conj(float2 a, float2 b) {  // a * conj(b)
+    return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+
+// y = 1 - exp(-x)
+__device__ __forceinline__ float one_minus_exp(float x) { return -expm1f(-x); }
+
+// Rotation of the frame magnetisation by an rf step: angle alpha about
+// n = (cb cos PHI, -cb sin PHI, sb) in the sense of the reference's closed
+// form (verified identity: R = cos a I - sin a [n]x + (1 - cos a) n n^T).
+__device__ __forceinline__ void rf_rotate(float &x, float &y, float &z, float dW, float b, float2 uphi, float dt) {
+    const float q = fmaf(dW, dW, b * b);
+    if (q == 0.f) return;
+    const float rn = rsqrtf(q);
+    const float Bm = q * rn;
+    const float cb = fabsf(b) * rn;
+    const float sb = copysignf(1.f, b) * dW * rn;
+    float sh, ch;
+    sincosf(0.5f * Bm * dt, &sh, &ch);
+    const float sa = 2.f * sh * ch;
+    const float omc = 2.f * sh * sh;  // 1 - cos(alpha)
+    const float ca = 1.f - omc;
+    const float nx = cb * uphi.x, ny = -cb * uphi.y, nz = sb;
+    const float cx = ny * z - nz * y, cy = nz * x - nx * z, cz = nx * y - ny * x;
+    const float k = omc * fmaf(nx, x, fmaf(ny, y, nz * z));
+    const float x2 = fmaf(ca, x, fmaf(-sa, cx, k * nx));
+    const float y2 = fmaf(ca, y, fmaf(-sa, cy, k * ny));
+    const float z2 = fmaf(ca, z, fmaf(-sa, cz, k * nz));
+    x = x2;
+    y = y2;
+    z = z2;
+}
+
+template <int MODEL, int P, int NS>
+__global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
+    const ScanLaunch &L = F.b;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    float4 *rbuf = reinterpret_cast<float4 *>(smem + 128);
+    const int rstride = L.stride4;
+    float2 *mbuf = reinterpret_cast<float2 *>(rbuf + 2 * kChunk * rstride);
+    constexpr int kRow = kBlock + 1;
+    constexpr bool kFreeAll = MODEL == KM_NORMAL || MODEL == KM_EXCH;
+
+    const int tid = threadIdx.x;
+    const long long gt = (long long)blockIdx.x * kBlock + tid;
+    const int v = (int)(gt / L.tpv);
+    const int sg = (int)(gt % L.tpv);
+    const bool active = v < L.n_act;
+    const int n = L.n_act;
+
+    float X[NS][P], Y[NS][P], Z[NS][P];
+    float2 Ph[NS][P], D[NS][P];
+    float Wh[NS][P], Wl[NS][P];
+    float rhoS[P], it1[P], it2[P], t2v[P], y1[P], y2[P];
+    unsigned act = 0;
+    float2 om[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    float2 tx0 = make_float2(0.f, 0.f);
+    float db0 = 0.f;
+    constexpr int kNK = MODEL == KM_EXCH ? P * P : (MODEL == KM_MT ? 2 : (MODEL == KM_CEST ? 2 * (P - 1) : 1));
+    float kc[kNK];
+#pragma unroll
+    for (int i = 0; i < kNK; ++i) kc[i] = 0.f;
+#pragma unroll
+    for (int t = 0; t < P; ++t) {
+        rhoS[t] = it1[t] = it2[t] = t2v[t] = y1[t] = y2[t] = 0.f;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            X[s][t] = Y[s][t] = Z[s][t] = Wh[s][t] = Wl[s][t] = 0.f;
+            Ph[s][t] = make_float2(1.f, 0.f);
+            D[s][t] = make_float2(0.f, 0.f);
+        }
+    }
+    if (active) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) om[i] = F.omega[(long long)i * n + v];
+        tx0 = F.txc[v];
+        db0 = L.db0[v];
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+            const float r = L.rho[(long long)t * n + v], T1 = L.t1[(long long)t * n + v],
+                        T2 = L.t2[(long long)t * n + v];
+            rhoS[t] = r / (float)L.S;
+            it1[t] = T1 != 0.f ? 1.f / T1 : 0.f;
+            it2[t] = T2 != 0.f ? 1.f / T2 : 0.f;
+            t2v[t] = T2;
+            if (T1 != 0.f && T2 != 0.f && r != 0.f) act |= 1u << t;
+        }
+        if (MODEL == KM_MT) {
+            kc[0] = L.kch[1LL * n + v];
+            kc[1] = L.kch[2LL * n + v];
+        } else if (MODEL != KM_NORMAL) {
+#pragma unroll
+            for (int i = 0; i < kNK; ++i) kc[i] = L.kch[(long long)i * n + v];
+        }
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const int sp = sg * NS + s;
+#pragma unroll
+            for (int t = 0; t < P; ++t) {
+                const long long i = ((long long)t * L.S + sp) * n + v;
+                X[s][t] = L.mx[i];
+                Y[s][t] = L.my[i];
+                Z[s][t] = L.mz[i];
+                const float2 w = F.wres[i];
+                Wh[s][t] = w.x;
+                Wl[s][t] = w.y;
+            }
+        }
+    }
+    // the isochromats enter the frame at the start of the launch: m_frame = m_lab / P
+    bool entered = false;
+    // exchange / MT coefficients, cached per dt
+    float yo[P], fin[P][P];
+#pragma unroll
+    for (int t = 0; t < P; ++t) {
+        yo[t] = 0.f;
+#pragma unroll
+        for (int p = 0; p < P; ++p) fin[t][p] = 0.f;
+    }
+    float mt_y1k = 0.f, mt_y21 = 0.f, mt_y1bk = 0.f, mt_y1b = 0.f, mt_y12 = 0.f;
+    LineshapeCache lc;
+    const float gyro = L.gyro;
+
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const long long nsteps = L.s1 - L.s0;
+    const int nchunks = (int)((nsteps + kChunk - 1) / kChunk);
+    auto issue = [&](int k) {
+        const long long first = L.s0 + (long long)k * kChunk;
+        const long long cnt = min((long long)kChunk, L.s1 - first);
+        const uint32_t bytes = (uint32_t)(cnt * rstride * 16);
+        mbar_expect_tx(&bar[k & 1], bytes);
+        bulk_g2s(rbuf + (k & 1) * kChunk * rstride, L.rec + first * rstride, bytes, &bar[k & 1]);
+    };
+    if (tid == 0 && nchunks > 0) issue(0);
+
+    int a_fill = 0, a_base = 0;
+    auto flush = [&]() {
+        __syncthreads();
+        const int nout = L.npairs * a_fill;
+        for (int o = tid; o < nout; o += kBlock) {
+            const int pair = o / a_fill;
+            const int a = o - pair * a_fill;
+            const int t = pair / L.rx;
+            const int c = pair - t * L.rx;
+            float sx = 0.f, sy = 0.f;
+            const float2 *row = mbuf + (a * L.nsamp + t) * kRow;
+            const long long vb = (long long)blockIdx.x * kBlock;
+            for (int j = 0; j < kBlock; ++j) {
+                const long long vj = (vb + j) / L.tpv;
+                if (vj >= n) break;
+                const float2 m = row[j];
+                if (L.rx_default) {
+                    sx += m.x;
+                    sy += m.y;
+                } else {
+                    const float2 r = L.rxc[(long long)c * n + vj];
+                    sx = fmaf(m.x, r.x, fmaf(m.y, r.y, sx));
+                    sy = fmaf(m.y, r.x, fmaf(-m.x, r.y, sy));
+                }
+            }
+            L.partial[((long long)blockIdx.x * L.a_launch + a_base + a) * L.npairs + pair] = make_float2(sx, sy);
+        }
+        a_base += a_fill;
+        a_fill = 0;
+        __syncthreads();
+    };
+
+    bool ok = true;
+    for (int k = 0; k < nchunks && ok; ++k) {
+        if (tid == 0 && k + 1 < nchunks) issue(k + 1);
+        ok = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, L.err);
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) {
+            if (tid == 0) mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, L.err);
+            break;
+        }
+        const float4 *cb = rbuf + (k & 1) * kChunk * rstride;
+        const int cnt = (int)min((long long)kChunk, nsteps - (long long)k * kChunk);
+        for (int q = 0; q < cnt; ++q) {
+            const float4 r0 = cb[q * rstride];
+            const float4 r1 = cb[q * rstride + 1];
+            int flags = __float_as_int(r1.w);
+            if (k == 0 && q == 0) flags |= kFlagState | kFlagDt;  // a launch may start inside a run
+            const float dt = r0.x;
+
+            // ---- frame phasors ---------------------------------------------
+            if (active && ((flags & kFlagAnchor) || !entered)) {
+                const float4 r2 = cb[q * rstride + 2];
+                const float4 r3 = cb[q * rstride + 3];
+                df phc = df_mul(om[0].x, om[0].y, r2.x, r2.y);
+                phc = df_add(phc, df_mul(om[1].x, om[1].y, r2.z, r2.w));
+                phc = df_add(phc, df_mul(om[2].x, om[2].y, r3.x, r3.y));
+                phc = df_add(phc, df_mul(om[3].x, om[3].y, r3.z, r3.w));
+#pragma unroll
+                for (int s = 0; s < NS; ++s)
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        const float2 pn = phasor(df_add(phc, df_mul(Wh[s][t], Wl[s][t], r2.x, r2.y)));
+                        if (!entered) {  // m_frame = m_lab * conj(P)
+                            const float2 m = cmul_conj(make_float2(X[s][t], Y[s][t]), pn);
+                            X[s][t] = m.x;
+                            Y[s][t] = m.y;
+                        }
+                        Ph[s][t] = pn;
+                    }
+                entered = true;
+            }
+            const float gzt = r0.y, gyt = r0.z, gxt = r0.w;
+            // instantaneous common off-resonance (rad/s)
+            const float wc = fmaf(om[3].x, gzt, fmaf(om[2].x, gyt, fmaf(om[1].x, gxt, om[0].x)));
+            if (active && (flags & kFlagState)) {
+#pragma unroll
+                for (int s = 0; s < NS; ++s)
+#pragma unroll
+                    for (int t = 0; t < P; ++t) D[s][t] = phase_step((wc + Wh[s][t]) * dt);
+            }
+            if (active && (flags & kFlagDt)) {
+#pragma unroll
+                for (int t = 0; t < P; ++t) {
+                    y1[t] = one_minus_exp(dt * it1[t]);
+                    y2[t] = one_minus_exp(dt * it2[t]);
+                }
+                if (MODEL == KM_EXCH) {
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        float ko = 0.f;  // exp(-sum k_out dt) = 1 - ko
+                        float ksum = 0.f;
+#pragma unroll
+                        for (int p = 0; p < P; ++p) {
+                            fin[t][p] = 0.f;
+                            if (L.exch_gm && p == t) continue;
+                            const float kgo = L.exch_gm ? kc[p * P + t] : kc[t * P + p];
+                            const float kin = L.exch_gm ? kc[t * P + p] : kc[p * P + t];
+                            ksum += kgo;
+                            if (kin != 0.f) fin[t][p] = one_minus_exp(dt * kin);
+                        }
+                        ko = one_minus_exp(dt * ksum);
+                        yo[t] = ko;
+                    }
+                } else if (MODEL == KM_MT || MODEL == KM_CEST) {
+                    const float K12 = kc[0];
+                    const float K21 = MODEL == KM_MT ? kc[1] : kc[P - 1];
+                    mt_y1k = one_minus_exp(dt * (it1[0] + K12));
+                    mt_y21 = one_minus_exp(dt * K21);
+                    mt_y1bk = one_minus_exp(dt * (it1[1] + K21));
+                    mt_y1b = one_minus_exp(dt * it1[1]);
+                    mt_y12 = one_minus_exp(dt * K12);
+                    if (MODEL == KM_CEST) {
+                        float ksum = 0.f;
+#pragma unroll
+                        for (int t = 2; t < P; ++t) {
+                            const float kgo = kc[t - 1], kin = kc[t + P - 2];
+                            ksum += kgo;
+                            fin[0][t] = kin != 0.f ? one_minus_exp(dt * kin) : 0.f;
+                            yo[t] = kin != 0.f ? one_minus_exp(dt * kin) : 0.f;
+                            fin[t][0] = kgo != 0.f ? one_minus_exp(dt * kgo) : 0.f;
+                        }
+                        yo[0] = one_minus_exp(dt * ksum);
+                    }
+                }
+            }
+
+            // ---- receive, before the step's rotation ------------------------
+            if (flags & kFlagAdc) {
+                float2 *tile = mbuf + a_fill * L.nsamp * kRow;
+#pragma unroll
+                for (int t = 0; t < P; ++t) {
+                    if (t >= L.nsamp) break;
+                    float sx = 0.f, sy = 0.f;
+                    const bool sampled = (MODEL != KM_EXCH) || (L.kind[t] == 0);
+#pragma unroll
+                    for (int s = 0; s < NS; ++s) {
+                        const float2 m = cmul(make_float2(X[s][t], Y[s][t]), Ph[s][t]);
+                        sx += m.x;
+                        sy += m.y;
+                    }
+                    tile[t * kRow + tid] = (active && sampled) ? make_float2(sx, sy) : make_float2(0.f, 0.f);
+                }
+                if (++a_fill == kAdcTile) flush();
+            }
+            if (!active) continue;
+
+            const bool rf = (flags & kFlagRf) != 0;
+            float b = 0.f;
+            float2 u0 = make_float2(1.f, 0.f);  // exp(i PHI) before the frame shift
+            float w_sat[P];                       // bound-pool saturation rates
+#pragma unroll
+            for (int t = 0; t < P; ++t) w_sat[t] = 0.f;
+            if (rf) {
+                // complex B1 = sum_c TxCoilmg_c exp(i pe_c) * amp_c exp(i phase_c)
+                float2 B = cmul(tx0, make_float2(r1.x, r1.y));
+                for (int c = 1; c < L.tx && c < 4; ++c) {
+                    const float4 rc = cb[q * rstride + 3 + c];
+                    const float2 t2 = cmul(F.txc[(long long)c * n + v], make_float2(rc.x, rc.y));
+                    B.x += t2.x;
+                    B.y += t2.y;
+                }
+                const float Bm = sqrtf(fmaf(B.x, B.x, B.y * B.y));
+                b = Bm * gyro;
+                if (Bm > 0.f) u0 = make_float2(B.x / Bm, -B.y / Bm);  // conj(B)/|B|
+                if (MODEL != KM_NORMAL) {
+                    // bound pools: W = pi (gamma TxCoilmg |amp|)^2 G(rf offset, T2b) with the
+                    // reference's lineshape rule (single transmit coil)
+                    const float b1 = sqrtf(fmaf(r1.x, r1.x, r1.y * r1.y)) * sqrtf(fmaf(tx0.x, tx0.x, tx0.y * tx0.y));
+                    const float freq = r1.z * 0.15915494309189535f;
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        const bool bound = (MODEL == KM_EXCH) ? (L.kind[t] == 1) : (t == 1);
+                        if (!bound) continue;
+                        if (lc.t2b != t2v[t] || lc.freq != freq) {
+                            lc.freq = freq;
+                            lc.t2b = t2v[t];
+                            lc.g = lineshape(freq, db0, gyro, t2v[t]);
+                        }
+                        w_sat[t] = (float)(kPiRef * (double)((b1 * gyro) * (b1 * gyro)) * (double)lc.g);
+                    }
+                }
+            }
+            const float wrf = r1.z;  // 2 pi sum of active rf frequencies
+
+#pragma unroll
+            for (int s = 0; s < NS; ++s) {
+                float2 Pprev[P];
+#pragma unroll
+                for (int t = 0; t < P; ++t) Pprev[t] = Ph[s][t];
+                float px[P], py[P], pz[P];
+#pragma unroll
+                for (int t = 0; t < P; ++t) {
+                    px[t] = X[s][t];
+                    py[t] = Y[s][t];
+                    pz[t] = Z[s][t];
+                }
+                // rotation (rf) or frame advance (free precession)
+#pragma unroll
+                for (int t = 0; t < P; ++t) {
+                    const bool free_pool =
+                        kFreeAll ? (MODEL == KM_NORMAL || L.kind[t] == 0) : (t == 0 || (MODEL == KM_CEST && t >= 2));
+                    if (!free_pool) continue;
+                    if (MODEL != KM_MT && MODEL != KM_CEST && !(act >> t & 1u)) continue;
+                    if (rf) {
+                        const float dW = wc + Wh[s][t] + wrf;
+                        const float2 uphi = cmul(u0, Ph[s][t]);
+                        rf_rotate(X[s][t], Y[s][t], Z[s][t], dW, b, uphi, dt);
+                    } else {
+                        const float2 p = Ph[s][t];
+                        const float2 d = D[s][t];
+                        Ph[s][t] = make_float2(fmaf(p.x, d.x, fmaf(-p.y, d.y, p.x)), fmaf(p.x, d.y, fmaf(p.y, d.x, p.y)));
+                    }
+                }
+                // relaxation and exchange
+                if (MODEL == KM_NORMAL) {
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        if (!(act >> t & 1u)) continue;
+                        X[s][t] = fmaf(-y2[t], X[s][t], X[s][t]);
+                        Y[s][t] = fmaf(-y2[t], Y[s][t], Y[s][t]);
+                        Z[s][t] = fmaf(y1[t], rhoS[t] - Z[s][t], Z[s][t]);
+                    }
+                } else if (MODEL == KM_EXCH) {
+                    float nx[P], ny[P], nz[P];
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        nx[t] = X[s][t];
+                        ny[t] = Y[s][t];
+                        nz[t] = Z[s][t];
+                    }
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        if (!(act >> t & 1u)) continue;
+                        const int kind = L.kind[t];
+                        if (kind != 0 && kind != 1) continue;
+                        const bool bound = kind == 1;
+                        float x = nx[t], y = ny[t], z = nz[t];
+                        float ix = 0.f, iy = 0.f, iz = 0.f;
+#pragma unroll
+                        for (int p = 0; p < P; ++p) {
+                            const float f = fin[t][p];
+                            if (f == 0.f) continue;
+                            iz = fmaf(f, pz[p], iz);
+                            if (!bound && L.kind[p] == 0) {
+                                // m_p(prev) carried into t's frame after the step
+                                const float2 rel = cmul_conj(Pprev[p], Ph[s][t]);
+                                const float2 m = cmul(make_float2(px[p], py[p]), rel);
+                                ix = fmaf(f, m.x, ix);
+                                iy = fmaf(f, m.y, iy);
+                            }
+                        }
+                        if (bound) {
+                            if (rf) z = fmaf(-one_minus_exp(w_sat[t] * dt), z, z);
+                        } else {
+                            x = fmaf(-y2[t], x, x);
+                            y = fmaf(-y2[t], y, y);
+                            x = fmaf(-yo[t], x, x) + ix;
+                            y = fmaf(-yo[t], y, y) + iy;
+                            X[s][t] = x;
+                            Y[s][t] = y;
+                        }
+                        z = fmaf(-y1[t], z, z);
+                        Z[s][t] = fmaf(-yo[t], z, z) + iz + rhoS[t] * y1[t];
+                    }
+                } else {  // MT / CEST
+                    float x = X[s][0], y = Y[s][0], z = Z[s][0];
+                    const float zb0 = pz[1], z0 = pz[0];
+                    x = fmaf(-y2[0], x, x);
+                    y = fmaf(-y2[0], y, y);
+                    if (MODEL == KM_MT) {
+                        z = fmaf(-mt_y1k, z, z) + rhoS[0] * y1[0] + zb0 * mt_y21;
+                    } else {
+                        float ix = 0.f, iy = 0.f, iz = 0.f;
+#pragma unroll
+                        for (int t = 2; t < P; ++t) {
+                            const float f = fin[0][t];
+                            if (f == 0.f) continue;
+                            const float2 rel = cmul_conj(Pprev[t], Ph[s][0]);
+                            const float2 m = cmul(make_float2(px[t], py[t]), rel);
+                            ix = fmaf(f, m.x, ix);
+                            iy = fmaf(f, m.y, iy);
+                            iz = fmaf(f, pz[t], iz);
+                        }
+                        x = fmaf(-yo[0], x, x) + ix;
+                        y = fmaf(-yo[0], y, y) + iy;
+                        z = fmaf(-mt_y1k, z, z);
+                        z = fmaf(-yo[0], z, z) + iz + zb0 * mt_y21 + rhoS[0] * y1[0];
+#pragma unroll
+                        for (int t = 2; t < P; ++t) {
+                            float cx = X[s][t], cy = Y[s][t], cz = Z[s][t];
+                            cx = fmaf(-y2[t], cx, cx);
+                            cy = fmaf(-y2[t], cy, cy);
+                            cz = fmaf(-y1[t], cz, cz);
+                            const float f = fin[t][0];
+                            const float2 rel = cmul_conj(Pprev[0], Ph[s][t]);
+                            const float2 m = cmul(make_float2(px[0], py[0]), rel);
+                            X[s][t] = fmaf(-yo[t], cx, cx) + f * m.x;
+                            Y[s][t] = fmaf(-yo[t], cy, cy) + f * m.y;
+                            Z[s][t] = fmaf(-yo[t], cz, cz) + f * z0 + rhoS[t] * y1[t];
+                        }
+                    }
+                    float bz = zb0;
+                    if (rf) bz = fmaf(-one_minus_exp(w_sat[1] * dt), bz, bz);
+                    Z[s][1] = fmaf(-mt_y1bk, bz, bz) + rhoS[1] * mt_y1b + z0 * mt_y12;
+                    X[s][0] = x;
+                    Y[s][0] = y;
+                    Z[s][0] = z;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (a_fill > 0) flush();
+
+    if (active) {
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const int sp = sg * NS + s;
+#pragma unroll
+            for (int t = 0; t < P; ++t) {
+                // back to the lab frame: m_lab = m_frame * P
+                const float2 m = entered ? cmul(make_float2(X[s][t], Y[s][t]), Ph[s][t]) : make_float2(X[s][t], Y[s][t]);
+                const long long i = ((long long)t * L.S + sp) * n + v;
+                L.mx[i] = m.x;
+                L.my[i] = m.y;
+                L.mz[i] = Z[s][t];
+            }
+        }
+    }
+}
+
+}  // namespace mrl

@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include "scan_fast_kernel.cuh"
 #include "scan_kernel.cuh"
 
 namespace mrl {
@@ -22,5 +23,10 @@ cudaError_t launch_scan_ref_normal(int P, int NS, dim3 grid, size_t smem, cudaSt
 cudaError_t launch_scan_ref_exch(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
 cudaError_t launch_scan_ref_mt(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
 cudaError_t launch_scan_ref_cest(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
+
+cudaError_t launch_scan_fast_normal(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastLaunch &F);
+cudaError_t launch_scan_fast_exch(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastLaunch &F);
+cudaError_t launch_scan_fast_mt(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastLaunch &F);
+cudaError_t launch_scan_fast_cest(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastLaunch &F);
 
 }  // namespace mrl

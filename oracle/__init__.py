@@ -75,7 +75,7 @@ def build(force: bool = False) -> None:
     hdr = os.path.join(HERE, "port", "mrl_port_impl.h")
     if force or not os.path.exists(PORT_SO) or os.path.getmtime(PORT_SO) < max(
             os.path.getmtime(src), os.path.getmtime(hdr)):
-        subprocess.check_call(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", src, "-o", PORT_SO, "-lm"])
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", src, "-o", PORT_SO, "-lm"])
     if os.path.isdir(REFERENCE_ROOT):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref"])
 

@@ -142,3 +142,55 @@ def test_multiple_partial_launches(built, monkeypatch):
     t = engine.last_timing()
     assert t["launches"] > 8
     assert rel_l2(signal(out), g["ref_Sx"] + 1j * g["ref_Sy"]) <= TOL_REF_CPU
+
+
+# Accurate numerics: relative L2 of the complex signal against the all-FP64
+# oracle (the reference algorithm in double precision).
+TOL_FP64 = 1e-5
+
+
+@pytest.mark.parametrize("name", SINGLE)
+def test_accurate_numerics_vs_fp64_oracle(built, name):
+    sc, g = load_golden(name)
+    out = engine.scan(sc, numerics="accurate")
+    f64 = g["f64_Sx"] + 1j * g["f64_Sy"]
+    ref = g["ref_Sx"] + 1j * g["ref_Sy"]
+    err64 = rel_l2(signal(out), f64)
+    print(f"{name}: accurate GPU vs FP64 oracle {err64:.3e}; reference CPU engine vs FP64 {rel_l2(ref, f64):.3e}; "
+          f"GPU vs reference CPU engine {rel_l2(signal(out), ref):.3e}")
+    assert err64 <= TOL_FP64
+
+
+@pytest.mark.parametrize("name", MULTI)
+def test_accurate_multipool_vs_fp64_oracle(built, name):
+    sc, g = load_golden(name)
+    out = engine.scan(sc, numerics="accurate")
+    f64 = g["f64_Sx"] + 1j * g["f64_Sy"]
+    err64 = rel_l2(signal(out), f64)
+    print(f"{name}: accurate GPU vs FP64 oracle {err64:.3e}, reference kernels vs FP64 "
+          f"{rel_l2(g['ref_Sx'] + 1j * g['ref_Sy'], f64):.3e}")
+    assert err64 <= TOL_FP64
+
+
+@pytest.mark.parametrize("spt", ["1", "2", "4"])
+def test_accurate_spins_per_thread_agree(built, monkeypatch, spt):
+    """The spins-per-thread tiling (an autotuned knob) does not change results."""
+    sc, g = load_golden("mp_me_p2_s2_c2")
+    sc = phantoms.small_multipool("me", seed=5, pools=2, spins=4, coils=3, n_tr=2)
+    monkeypatch.setenv("MRL_SPINS_PER_THREAD", spt)
+    out = engine.scan(sc, numerics="accurate")
+    f64 = oracle.run_port(sc, "f64")
+    assert rel_l2(signal(out), signal(f64)) <= TOL_FP64
+
+
+def test_accurate_two_pool_3d_multiecho(built):
+    """The benchmark workload's structure (two exchanging pools, 4 spins with
+    intravoxel dephasing, 8 Rx coils, 6 echoes) on a shrunken object."""
+    sc = phantoms.config2_me_gre(seed=0, nx=16, ny=16, nz=4, n_pe=4, n_par=2, n_read=32, n_tr=3)
+    out = engine.scan(sc, numerics="accurate")
+    f64 = oracle.run_port(sc, "f64")
+    f32 = oracle.run_port(sc, "f32")
+    err = rel_l2(signal(out), signal(f64))
+    print(f"config2 shrunk: accurate GPU vs FP64 {err:.3e}; FP32 reference algorithm vs FP64 "
+          f"{rel_l2(signal(f32), signal(f64)):.3e}")
+    assert err <= TOL_FP64
