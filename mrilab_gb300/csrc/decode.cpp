@@ -4,6 +4,8 @@
 
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
+#include <algorithm>
 
 namespace mrl {
 
@@ -212,6 +214,8 @@ inline void split(double v, float &hi, float &lo) {
 
 void pack_fast_records(const DecodeChunk &ch, int tx, FrameMoments &fm, std::vector<float> &out) {
     const int stride = fast_stride_f4(tx) * 4;
+    int every = kAnchorEvery;
+    if (const char *e = std::getenv("MRL_ANCHOR_EVERY")) every = std::max(1, std::atoi(e));
     out.assign((size_t)ch.n_steps * stride, 0.f);
     for (int64_t q = 0; q < ch.n_steps; ++q) {
         const StepInfo &si = ch.steps[q];
@@ -231,7 +235,7 @@ void pack_fast_records(const DecodeChunk &ch, int tx, FrameMoments &fm, std::vec
         const bool new_state = new_dt || si.gx != fm.last_gx || si.gy != fm.last_gy || si.gz != fm.last_gz;
         if (new_dt) flags |= kFlagDt;
         if (new_state) flags |= kFlagState;
-        if (new_state || rf || fm.since_anchor >= kAnchorEvery) {
+        if (new_state || rf || fm.since_anchor >= every) {
             flags |= kFlagAnchor;
             fm.since_anchor = 0;
         }

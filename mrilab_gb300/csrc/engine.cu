@@ -323,6 +323,11 @@ struct Scanner {
             return fail_cuda(e, "upload coils");
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e, "upload sync");
         h2d_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (getenv("MRL_DEBUG")) {
+            double sx = 0, sz = 0;
+            for (size_t i = 0; i < n * P * S; ++i) sx += std::fabs(hm[i]), sz += hm[2 * n * P * S + i];
+            fprintf(stderr, "mrl: upload_object n_act=%d |Mx|=%g sum Mz=%g\n", n_act, sx, sz);
+        }
         return MRL_OK;
     }
 
@@ -337,6 +342,11 @@ struct Scanner {
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return fail_cuda(e, "download state");
         d2h_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (getenv("MRL_DEBUG")) {
+            double sx = 0;
+            for (size_t i = 0; i < n * P * S; ++i) sx += std::fabs(hm[i]);
+            fprintf(stderr, "mrl: download_state |Mx|=%g\n", sx);
+        }
         for (int i = 0; i < n_act; ++i) {
             const long long v = act[i];
             for (int t = 0; t < P; ++t)
@@ -484,7 +494,7 @@ struct Scanner {
         L.rec = d_rec.p;
         L.partial = d_part.p;
         const int nblk = (int)n_blocks();
-        const size_t smem = scan_smem_bytes(stride4, mi.nsamp);
+        const size_t smem = fast ? scan_fast_smem_bytes(stride4, mi.nsamp, RX) : scan_smem_bytes(stride4, mi.nsamp);
         const double cr = std::cos(-rf_ref), sr = std::sin(-rf_ref);
         cudaError_t e;
         for (const LaunchDesc &d : ls) {
@@ -610,6 +620,7 @@ struct Scanner {
             store_state(ds, args->var, TX);
             if (ext) {
                 const int fetch = ext(user, args, MRL_EXT_FETCH);
+                if (getenv("MRL_DEBUG")) fprintf(stderr, "mrl: Ext value %g, fetch %d\n", ds.ext, fetch);
                 if (fetch && (rc = download_state())) return rc;
                 if (ext(user, args, MRL_EXT_PLUGIN) != 0) {
                     set_err("Ext plugin returned an error");

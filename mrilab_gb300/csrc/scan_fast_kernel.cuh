@@ -74,8 +74,10 @@ __device__ __forceinline__ float2 phasor(df phi) {
     float r = fmaf(-k, kC1, phi.hi);
     r = fmaf(-k, kC2, r);
     r += phi.lo;
+    // |r| <= pi: the MUFU approximation's absolute error (~4e-7) is reset at
+    // every anchor, so it does not accumulate
     float s, c;
-    sincosf(r, &s, &c);
+    __sincosf(r, &s, &c);
     return make_float2(c, -s);
 }
 
@@ -130,8 +132,12 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     float4 *rbuf = reinterpret_cast<float4 *>(smem + 128);
     const int rstride = L.stride4;
-    float2 *mbuf = reinterpret_cast<float2 *>(rbuf + 2 * kChunk * rstride);
-    constexpr int kRow = kBlock + 1;
+    // coil sensitivities of the block's voxels, then per-warp receive sums
+    const int C4 = (L.rx + 3) & ~3;
+    float2 *rsm = reinterpret_cast<float2 *>(rbuf + 2 * kChunk * rstride);  // [C4][kBlock]
+    float *acc = reinterpret_cast<float *>(rsm + C4 * kBlock);              // [kAdcTile][warp][nsamp][C4][2]
+    constexpr int kWarps = kBlock / 32;
+    const int acc_row = L.nsamp * C4 * 2;
     constexpr bool kFreeAll = MODEL == KM_NORMAL || MODEL == KM_EXCH;
 
     const int tid = threadIdx.x;
@@ -200,6 +206,12 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
             }
         }
     }
+    // stage this thread's voxel's coil sensitivities (zero beyond the coil count)
+    for (int c = 0; c < C4; ++c) {
+        float2 r = make_float2(0.f, 0.f);
+        if (active && c < L.rx) r = L.rx_default ? make_float2(1.f, 0.f) : L.rxc[(long long)c * n + v];
+        rsm[c * kBlock + tid] = r;
+    }
     // the isochromats enter the frame at the start of the launch: m_frame = m_lab / P
     bool entered = false;
     // exchange / MT coefficients, cached per dt
@@ -232,29 +244,23 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
     if (tid == 0 && nchunks > 0) issue(0);
 
     int a_fill = 0, a_base = 0;
+    const int lane = tid & 31, warp = tid >> 5;
+    // flush: sum the per-warp receive sums of the tile and write one partial
+    // per (block, sample, pool, coil)
     auto flush = [&]() {
         __syncthreads();
-        const int nout = L.npairs * a_fill;
+        const int nout = a_fill * L.nsamp * L.rx;
         for (int o = tid; o < nout; o += kBlock) {
-            const int pair = o / a_fill;
-            const int a = o - pair * a_fill;
+            const int a = o / (L.nsamp * L.rx);
+            const int pair = o - a * (L.nsamp * L.rx);
             const int t = pair / L.rx;
             const int c = pair - t * L.rx;
             float sx = 0.f, sy = 0.f;
-            const float2 *row = mbuf + (a * L.nsamp + t) * kRow;
-            const long long vb = (long long)blockIdx.x * kBlock;
-            for (int j = 0; j < kBlock; ++j) {
-                const long long vj = (vb + j) / L.tpv;
-                if (vj >= n) break;
-                const float2 m = row[j];
-                if (L.rx_default) {
-                    sx += m.x;
-                    sy += m.y;
-                } else {
-                    const float2 r = L.rxc[(long long)c * n + vj];
-                    sx = fmaf(m.x, r.x, fmaf(m.y, r.y, sx));
-                    sy = fmaf(m.y, r.x, fmaf(-m.x, r.y, sy));
-                }
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) {
+                const float *row = acc + (a * kWarps + w) * acc_row + (t * C4 + c) * 2;
+                sx += row[0];
+                sy += row[1];
             }
             L.partial[((long long)blockIdx.x * L.a_launch + a_base + a) * L.npairs + pair] = make_float2(sx, sy);
         }
@@ -360,19 +366,54 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
 
             // ---- receive, before the step's rotation ------------------------
             if (flags & kFlagAdc) {
-                float2 *tile = mbuf + a_fill * L.nsamp * kRow;
+                float *arow = acc + (a_fill * kWarps + warp) * acc_row;
 #pragma unroll
                 for (int t = 0; t < P; ++t) {
                     if (t >= L.nsamp) break;
-                    float sx = 0.f, sy = 0.f;
+                    float mx = 0.f, my = 0.f;
                     const bool sampled = (MODEL != KM_EXCH) || (L.kind[t] == 0);
 #pragma unroll
                     for (int s = 0; s < NS; ++s) {
                         const float2 m = cmul(make_float2(X[s][t], Y[s][t]), Ph[s][t]);
-                        sx += m.x;
-                        sy += m.y;
+                        mx += m.x;
+                        my += m.y;
                     }
-                    tile[t * kRow + tid] = (active && sampled) ? make_float2(sx, sy) : make_float2(0.f, 0.f);
+                    if (!(active && sampled)) mx = my = 0.f;
+                    for (int g = 0; g < C4; g += 4) {
+                        // M conj(R) for 4 coils: sx = Mx Rx + My Ry, sy = My Rx - Mx Ry
+                        float vv[8];
+#pragma unroll
+                        for (int cc = 0; cc < 4; ++cc) {
+                            const float2 r = rsm[(g + cc) * kBlock + tid];
+                            vv[2 * cc] = fmaf(mx, r.x, my * r.y);
+                            vv[2 * cc + 1] = fmaf(my, r.x, -mx * r.y);
+                        }
+                        // warp transpose-reduction: after the three halving steps lane l
+                        // holds value (l >> 2) & 7 summed over lanes differing in bits 4..2
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const bool up = lane & 16;
+                            const float send = up ? vv[j] : vv[j + 4];
+                            const float keep = up ? vv[j + 4] : vv[j];
+                            vv[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+                        }
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) {
+                            const bool up = lane & 8;
+                            const float send = up ? vv[j] : vv[j + 2];
+                            const float keep = up ? vv[j + 2] : vv[j];
+                            vv[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+                        }
+                        {
+                            const bool up = lane & 4;
+                            const float send = up ? vv[0] : vv[1];
+                            const float keep = up ? vv[1] : vv[0];
+                            vv[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+                        }
+                        vv[0] += __shfl_xor_sync(0xffffffffu, vv[0], 2);
+                        vv[0] += __shfl_xor_sync(0xffffffffu, vv[0], 1);
+                        if ((lane & 3) == 0) arow[(t * C4 + g) * 2 + (lane >> 2)] = vv[0];
+                    }
                 }
                 if (++a_fill == kAdcTile) flush();
             }

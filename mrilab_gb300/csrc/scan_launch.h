@@ -18,6 +18,12 @@ inline int spins_per_thread(int S) { return (S == 4 || S == 2) ? S : 1; }
 inline size_t scan_smem_bytes(int stride4, int nsamp) {
     return 128 + (size_t)2 * kChunk * stride4 * 16 + (size_t)kAdcTile * nsamp * (kBlock + 1) * 8;
 }
+// ... of the accurate kernel: staged records, coil sensitivities of the
+// block's voxels and the per-warp receive tile.
+inline size_t scan_fast_smem_bytes(int stride4, int nsamp, int rx) {
+    const size_t c4 = (size_t)((rx + 3) & ~3);
+    return 128 + (size_t)2 * kChunk * stride4 * 16 + c4 * kBlock * 8 + (size_t)kAdcTile * (kBlock / 32) * nsamp * c4 * 2 * 4;
+}
 
 cudaError_t launch_scan_ref_normal(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
 cudaError_t launch_scan_ref_exch(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);

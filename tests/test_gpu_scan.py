@@ -37,7 +37,7 @@ def test_reference_numerics_match_reference_cpu_engine(built, name):
     assert err <= TOL_REF_CPU
     np.testing.assert_allclose(out["Kx"], g["ref_Kx"], atol=1e-9)
     np.testing.assert_allclose(out["Ky"], g["ref_Ky"], atol=1e-9)
-    np.testing.assert_allclose(out["Mz"], g["ref_Mz"], atol=5e-5)
+    assert rel_l2(out["Mz"], g["ref_Mz"]) <= 1e-5
 
 
 @pytest.mark.parametrize("name", MULTI)
