@@ -100,7 +100,7 @@ class ScanError(RuntimeError):
 
 
 def _flat(a, dtype):
-    return np.ascontiguousarray(np.asarray(a, dtype).ravel(order="F"))
+    return np.array(np.asarray(a, dtype).ravel(order="F"), dtype=dtype, copy=True)
 
 
 class HostScan:

@@ -117,6 +117,10 @@ def test_ext_plugin_callback(built):
     assert calls == [engine.EXT_FETCH, engine.EXT_PLUGIN] * 3
     base = engine.scan(sc, numerics="reference")
     assert rel_l2(signal(out), signal(base)) > 1e-3
+    # the same plugin in the CPU oracle (which runs it before the step that
+    # starts at the Ext sample; that step is a 10 us free precession here)
+    port = oracle.run_port(sc, "f32", ext_cb=lambda v, o: (o["Mx"].fill(0), o["My"].fill(0), 0)[-1])
+    assert rel_l2(signal(out), signal(port)) <= 1e-3
     # a plugin error propagates as a status code
     hs2 = engine.HostScan(sc, numerics="reference")
     with pytest.raises(engine.ScanError) as e:
