@@ -511,7 +511,7 @@ struct Scanner {
             if (n_act > 0) {
                 dim3 grid(nblk);
                 if (fast) {
-                    FastLaunch F;
+                    FastLaunch F{};
                     F.b = L;
                     const size_t n = std::max(1, n_act);
                     F.omega = d_f2.p + o_om;

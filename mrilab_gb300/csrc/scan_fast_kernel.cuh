@@ -116,10 +116,13 @@ __device__ __forceinline__ void rf_rotate(float &x, float &y, float &z, float dW
     const float ca = 1.f - omc;
     const float nx = cb * uphi.x, ny = -cb * uphi.y, nz = sb;
     const float cx = ny * z - nz * y, cy = nz * x - nx * z, cz = nx * y - ny * x;
-    const float k = omc * fmaf(nx, x, fmaf(ny, y, nz * z));
-    const float x2 = fmaf(ca, x, fmaf(-sa, cx, k * nx));
-    const float y2 = fmaf(ca, y, fmaf(-sa, cy, k * ny));
-    const float z2 = fmaf(ca, z, fmaf(-sa, cz, k * nz));
+    const float k = fmaf(nx, x, fmaf(ny, y, nz * z));
+    // increment form R M = M + (1 - cos a)((n.M) n - M) - sin a (n x M): the
+    // small increment is added to M with a single rounding
+    (void)ca;
+    const float x2 = x + fmaf(omc, fmaf(k, nx, -x), -sa * cx);
+    const float y2 = y + fmaf(omc, fmaf(k, ny, -y), -sa * cy);
+    const float z2 = z + fmaf(omc, fmaf(k, nz, -z), -sa * cz);
     x = x2;
     y = y2;
     z = z2;
