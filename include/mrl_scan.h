@@ -177,6 +177,38 @@ int mrl_plan_download(mrl_plan *plan, mrl_scan_args *args);
 int mrl_plan_work(const mrl_plan *plan, long long out[5]);
 void mrl_plan_destroy(mrl_plan *plan);
 
+/* Scan without allocating device memory.
+ *
+ * For callers that cannot call cudaMalloc themselves -- code running inside
+ * a host application or framework that owns the whole device heap (a
+ * MATLAB session handing over gpuArray storage, a serving process with a
+ * fixed memory pool), or code recording a CUDA graph, where allocation is
+ * not allowed -- this variant of the accurate scan kernel works entirely in
+ * buffers the caller already owns.  It has no counterpart in the reference,
+ * whose engines allocate and free every device array per call
+ * (DoScanAtGPU.cu:257-334,765-784).
+ *
+ * Pointers in `args`: obj.rho/t1/t2/k/mx/my/mz, mag.*, coil.tx_mg/tx_pe/
+ * rx_x/rx_y and sig.sx/sy are DEVICE pointers in the layouts above
+ * (uncompacted); seq.*, ctl.cs, obj.type_flag, var.* and sig.kx/ky/kz are
+ * host pointers.  Mx/My/Mz are updated in place and every acquired sample
+ * of Sx/Sy is assigned.  `d_steps` is a device buffer of `step_bytes`
+ * bytes for the decoded step records (16 floats per step; len(uts) * 64
+ * bytes always suffices).  Work is queued on `stream` (a cudaStream_t, NULL
+ * for the legacy stream) and the call returns when it has finished.
+ *
+ * Its only scratch is one statically allocated device array of 32 MiB
+ * (held by every GPU that loads the library until the process exits): a
+ * status word, the ADC map of one launch and the receive partial sums of
+ * (thread blocks x Rx x pools) per sample.  Objects for which a single
+ * sample does not fit are rejected with MRL_ERR_UNSUPPORTED.  The scratch
+ * is shared by every call: calls that overlap on the GPU (different
+ * streams or threads) race and must be serialised by the caller.  The
+ * first call on a device looks up the scratch's device address on that
+ * device (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  Limits: MRL_NUMERICS_ACCURATE, one Tx coil, no Ext events. */
+int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, void *stream);
+
 /* Human-readable text for a status code (reference: errors were printed
  * with mexPrintf or raised with mexErrMsgTxt, DoScanAtGPU.cu:231-242,566). */
 const char *mrl_status_string(int status);

@@ -20,6 +20,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -42,8 +43,6 @@ void set_err(const char *fmt, ...) {
     va_end(ap);
     g_err = buf;
 }
-
-constexpr double kPiRef = 3.14159265359;
 
 // Receive reduction: Sx/Sy[pool][coil][signal] = sum over blocks of the
 // per-block partial sums, in FP64, then demodulated by rfRef
@@ -657,6 +656,32 @@ struct Scanner {
     }
 };
 
+// ---- allocation-free scans (mrl_scan_noalloc) -------------------------------
+// Scratch of mrl_scan_noalloc: [status word, padded to 256 B][ADC map of one
+// launch (int)][receive partial sums (float2)].  One array per process per
+// device, shared by every call.
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {};
+
+// Device address of the scratch array on the current device.  Host code
+// only sees a host-side stand-in named g_noalloc_scratch; the device address
+// comes from cudaGetSymbolAddress, fetched once per device.
+cudaError_t noalloc_scratch(int dev, unsigned char **out) {
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+    return cudaSuccess;
+}
+
 }  // namespace
 }  // namespace mrl
 
@@ -803,6 +828,169 @@ int mrl_plan_work(const mrl_plan *p, long long out[5]) {
 }
 
 void mrl_plan_destroy(mrl_plan *p) { delete p; }
+
+int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, void *stream) {
+    using namespace mrl;
+    g_err.clear();
+    if (!args || !d_steps) {
+        set_err("NULL argument");
+        return MRL_ERR_ARG;
+    }
+    Scanner sc;  // validation only: nothing of it is allocated
+    sc.args = args;
+    int rc = sc.validate();
+    if (rc) return rc;
+    if (!sc.fast) {
+        set_err("mrl_scan_noalloc runs the MRL_NUMERICS_ACCURATE integrator only");
+        return MRL_ERR_UNSUPPORTED;
+    }
+    if (sc.TX != 1) {
+        set_err("mrl_scan_noalloc supports one Tx coil");
+        return MRL_ERR_UNSUPPORTED;
+    }
+    if (sc.V * sc.tpv > (long long)INT32_MAX) {
+        set_err("spin matrix too large");
+        return MRL_ERR_UNSUPPORTED;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaSetDevice(args->ctl.gpu_index);
+    if (e != cudaSuccess) {
+        set_err("cudaSetDevice(%d): %s", args->ctl.gpu_index, cudaGetErrorString(e));
+        return MRL_ERR_NO_DEVICE;
+    }
+    unsigned char *scratch = nullptr;
+    if ((e = noalloc_scratch(args->ctl.gpu_index, &scratch)) != cudaSuccess)
+        return sc.fail_cuda(e, "cudaGetSymbolAddress(scratch)");
+    int *d_status = reinterpret_cast<int *>(scratch);
+    // decode the whole sequence on the host
+    DecodeState ds;
+    load_state(ds, args->var, sc.TX);
+    DecodeChunk ch;
+    decode_until_ext(ds, args->seq, sc.TX, args->obj.gyro, args->sig, ch);
+    if (ch.stopped_at_ext) {
+        set_err("the sequence has Ext events: use mrl_scan with a callback");
+        return MRL_ERR_UNSUPPORTED;
+    }
+    store_state(ds, args->var, sc.TX);
+    FrameMoments fm;
+    std::vector<float> rec;
+    pack_fast_records(ch, sc.TX, fm, rec);
+    if (rec.size() * sizeof(float) > step_bytes) {
+        set_err("step buffer holds %zu bytes, %zu needed", step_bytes, rec.size() * sizeof(float));
+        return MRL_ERR_ARG;
+    }
+    // launches sized so that one launch's ADC map and partials fit the scratch
+    const int n = (int)sc.V;
+    const long long nblk = std::max(1LL, ((long long)n * sc.tpv + kBlock - 1) / kBlock);
+    const int npairs = sc.mi.nsamp * sc.RX;
+    const double per_sample = sizeof(int) + (double)nblk * npairs * sizeof(float2);
+    const long long a_cap = (long long)((kNoAllocScratchBytes - 256) / per_sample);
+    if (a_cap < 1) {
+        set_err("object too large for the %zu-byte scratch: one ADC sample needs %.0f bytes", kNoAllocScratchBytes,
+                per_sample);
+        return MRL_ERR_UNSUPPORTED;
+    }
+    int *d_amap = reinterpret_cast<int *>(scratch + 256);
+    float2 *d_part = reinterpret_cast<float2 *>(scratch + 256 + ((a_cap * sizeof(int) + 255) / 256) * 256);
+    if ((e = cudaMemsetAsync(d_status, 0, sizeof(int), st)) != cudaSuccess) return sc.fail_cuda(e, "status reset");
+    if ((e = cudaMemcpyAsync(d_steps, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice, st)) !=
+        cudaSuccess)
+        return sc.fail_cuda(e, "upload steps");
+    ScanLaunch L{};
+    L.n_act = n;
+    L.S = sc.S;
+    L.tx = sc.TX;
+    L.rx = sc.RX;
+    L.nsamp = sc.mi.nsamp;
+    L.npairs = npairs;
+    L.tpv = sc.tpv;
+    L.gyro = (float)args->obj.gyro;
+    L.rx_default = args->coil.rx_default != 0;
+    L.exch_gm = sc.mi.gm ? 1 : 0;
+    L.gxg = args->mag.gxgrid;
+    L.gyg = args->mag.gygrid;
+    L.gzg = args->mag.gzgrid;
+    L.db0 = args->mag.db0;
+    L.txmg = args->coil.tx_mg;
+    L.txpe = args->coil.tx_pe;
+    L.rho = args->obj.rho;
+    L.t1 = args->obj.t1;
+    L.t2 = args->obj.t2;
+    L.kch = args->obj.k;
+    L.dwrnd = args->mag.dwrnd;
+    L.mx = args->obj.mx;
+    L.my = args->obj.my;
+    L.mz = args->obj.mz;
+    L.rec = reinterpret_cast<const float4 *>(d_steps);
+    L.stride4 = sc.stride4;
+    L.err = d_status;
+    L.partial = d_part;
+    for (int t = 0; t < kMaxPool; ++t) {
+        L.cs2pi[t] = t < sc.P && args->ctl.cs ? (float)(2 * kPiRef * (double)(float)args->ctl.cs[t]) : 0.f;
+        L.kind[t] = (sc.mi.gm && t < sc.P) ? (int)args->obj.type_flag[t] : 0;
+    }
+    FastLaunch F{};
+    F.b = L;
+    F.direct = 1;
+    F.rx_x = args->coil.rx_x;
+    F.rx_y = args->coil.rx_y;
+    F.gam_hi = (float)args->obj.gyro;
+    F.gam_lo = (float)(args->obj.gyro - (double)F.gam_hi);
+    for (int t = 0; t < kMaxPool; ++t) {
+        const double w = (t < sc.P && args->ctl.cs) ? 2 * kPiRef * args->ctl.cs[t] : 0.0;
+        F.cs_hi[t] = (float)w;
+        F.cs_lo[t] = (float)(w - (double)F.cs_hi[t]);
+    }
+    const size_t smem = scan_fast_smem_bytes(sc.stride4, sc.mi.nsamp, sc.RX);
+    const double rf_ref = args->var.rf_ref ? *args->var.rf_ref : 0.0;
+    const double cr = std::cos(-rf_ref), sr = std::sin(-rf_ref);
+    // walk the steps, one launch per a_cap samples
+    long long s0 = 0;
+    std::vector<int> amap;
+    auto launch = [&](long long s1) -> int {
+        F.b.s0 = s0;
+        F.b.s1 = s1;
+        F.b.a_launch = (int)amap.size();
+        cudaError_t le;
+        if (!amap.empty() &&
+            (le = cudaMemcpyAsync(d_amap, amap.data(), amap.size() * sizeof(int), cudaMemcpyHostToDevice, st)) !=
+                cudaSuccess)
+            return sc.fail_cuda(le, "upload ADC map");
+        switch (sc.mi.km) {
+        case KM_NORMAL: le = launch_scan_fast_normal(sc.P, sc.NS, dim3((unsigned)nblk), smem, st, F); break;
+        case KM_EXCH: le = launch_scan_fast_exch(sc.P, sc.NS, dim3((unsigned)nblk), smem, st, F); break;
+        case KM_MT: le = launch_scan_fast_mt(sc.P, sc.NS, dim3((unsigned)nblk), smem, st, F); break;
+        default: le = launch_scan_fast_cest(sc.P, sc.NS, dim3((unsigned)nblk), smem, st, F); break;
+        }
+        if (le != cudaSuccess) return sc.fail_cuda(le, "scan kernel launch");
+        if (!amap.empty()) {
+            const int tot = (int)amap.size() * npairs;
+            reduce_partials<<<(tot + 255) / 256, 256, 0, st>>>(d_part, (int)nblk, (int)amap.size(), npairs, sc.RX,
+                                                               d_amap, sc.A, args->sig.sx, args->sig.sy, cr, sr);
+            if ((le = cudaGetLastError()) != cudaSuccess) return sc.fail_cuda(le, "reduce launch");
+        }
+        return MRL_OK;
+    };
+    for (long long q = 0; q < ch.n_steps; ++q) {
+        if (ch.step_adc[q] < 0) continue;
+        if ((long long)amap.size() == a_cap) {
+            if ((rc = launch(q))) return rc;
+            s0 = q;
+            amap.clear();
+        }
+        amap.push_back(ch.step_adc[q]);
+    }
+    if (ch.n_steps > 0 && (rc = launch(ch.n_steps))) return rc;
+    int status = 0;
+    if ((e = cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return sc.fail_cuda(e, "scan");
+    if (status) {
+        set_err("a device wait timed out (status bits %d)", status);
+        return MRL_ERR_TIMEOUT;
+    }
+    return MRL_OK;
+}
 
 const char *mrl_status_string(int status) {
     switch (status) {

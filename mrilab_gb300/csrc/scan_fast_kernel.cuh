@@ -34,6 +34,13 @@ struct FastLaunch {
     const float2 *omega;      // [4][n_act] (hi, lo) of gamma*dB0, gamma*x, gamma*y, gamma*z
     const float2 *wres;       // [P][S][n_act] (hi, lo) residual frequency, rad/s
     const float2 *txc;        // [tx][n_act] TxCoilmg * exp(i TxCoilpe)
+    // Direct layout (mrl_scan_noalloc): the arrays of ScanLaunch are the
+    // caller's uncompacted MATLAB arrays (n = every voxel), and the three
+    // derived fields above are computed here instead of being read.
+    int direct;
+    const float *rx_x, *rx_y; // [rx][n]
+    float gam_hi, gam_lo;     // gyromagnetic ratio split
+    float cs_hi[kMaxPool], cs_lo[kMaxPool];  // 2 pi CS[t] split
 };
 
 // ---- double-float helpers ------------------------------------------------
@@ -147,7 +154,7 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
     const long long gt = (long long)blockIdx.x * kBlock + tid;
     const int v = (int)(gt / L.tpv);
     const int sg = (int)(gt % L.tpv);
-    const bool active = v < L.n_act;
+    bool active = v < L.n_act;
     const int n = L.n_act;
 
     float X[NS][P], Y[NS][P], Z[NS][P];
@@ -173,10 +180,22 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
         }
     }
     if (active) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) om[i] = F.omega[(long long)i * n + v];
-        tx0 = F.txc[v];
         db0 = L.db0[v];
+        if (F.direct) {
+            const float g[4] = {db0, L.gxg[v], L.gyg[v], L.gzg[v]};
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const df p = df_mul(F.gam_hi, F.gam_lo, g[i], 0.f);
+                om[i] = make_float2(p.hi, p.lo);
+            }
+            float sp, cp;
+            sincosf(L.txpe[v], &sp, &cp);
+            tx0 = make_float2(L.txmg[v] * cp, L.txmg[v] * sp);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) om[i] = F.omega[(long long)i * n + v];
+            tx0 = F.txc[v];
+        }
 #pragma unroll
         for (int t = 0; t < P; ++t) {
             const float r = L.rho[(long long)t * n + v], T1 = L.t1[(long long)t * n + v],
@@ -203,16 +222,33 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                 X[s][t] = L.mx[i];
                 Y[s][t] = L.my[i];
                 Z[s][t] = L.mz[i];
-                const float2 w = F.wres[i];
-                Wh[s][t] = w.x;
-                Wl[s][t] = w.y;
+                if (F.direct) {
+                    const df w = two_sum(L.dwrnd[i], F.cs_hi[t]);
+                    Wh[s][t] = w.hi;
+                    Wl[s][t] = w.lo + F.cs_lo[t];
+                } else {
+                    const float2 w = F.wres[i];
+                    Wh[s][t] = w.x;
+                    Wl[s][t] = w.y;
+                }
             }
         }
+    }
+    if (F.direct) {
+        const bool any = (MODEL == KM_MT || MODEL == KM_CEST) ? (act & 1u) != 0 : act != 0;
+        if (!any) active = false;
     }
     // stage this thread's voxel's coil sensitivities (zero beyond the coil count)
     for (int c = 0; c < C4; ++c) {
         float2 r = make_float2(0.f, 0.f);
-        if (active && c < L.rx) r = L.rx_default ? make_float2(1.f, 0.f) : L.rxc[(long long)c * n + v];
+        if (active && c < L.rx) {
+            if (L.rx_default)
+                r = make_float2(1.f, 0.f);
+            else if (F.direct)
+                r = make_float2(F.rx_x[(long long)c * n + v], F.rx_y[(long long)c * n + v]);
+            else
+                r = L.rxc[(long long)c * n + v];
+        }
         rsm[c * kBlock + tid] = r;
     }
     // the isochromats enter the frame at the start of the launch: m_frame = m_lab / P
