@@ -145,6 +145,15 @@ struct Scanner {
         if (st) cudaStreamDestroy(st);
     }
 
+    // every pool of an exchange model is a free pool (ME, or GM without bound pools)
+    int all_free() const {
+        if (mi.km != KM_EXCH) return 0;
+        if (!mi.gm) return 1;
+        for (int t = 0; t < P; ++t)
+            if ((int)args->obj.type_flag[t] != 0) return 0;
+        return 1;
+    }
+
     int fail_cuda(cudaError_t e, const char *what) {
         set_err("%s: %s", what, cudaGetErrorString(e));
         return MRL_ERR_CUDA;
@@ -516,6 +525,7 @@ struct Scanner {
                     F.omega = d_f2.p + o_om;
                     F.wres = d_f2.p + o_wr;
                     F.txc = d_f2.p + o_txc;
+                    F.all_free = all_free();
                     (void)n;
                     switch (mi.km) {
                     case KM_NORMAL: e = launch_scan_fast_normal(P, NS, grid, smem, stream, F); break;
@@ -932,6 +942,7 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
     FastLaunch F{};
     F.b = L;
     F.direct = 1;
+    F.all_free = sc.all_free();
     F.rx_x = args->coil.rx_x;
     F.rx_y = args->coil.rx_y;
     F.gam_hi = (float)args->obj.gyro;

@@ -38,6 +38,7 @@ struct FastLaunch {
     // caller's uncompacted MATLAB arrays (n = every voxel), and the three
     // derived fields above are computed here instead of being read.
     int direct;
+    int all_free;             // KM_EXCH: every pool is free (ME, or GM without bound pools)
     const float *rx_x, *rx_y; // [rx][n]
     float gam_hi, gam_lo;     // gyromagnetic ratio split
     float cs_hi[kMaxPool], cs_lo[kMaxPool];  // 2 pi CS[t] split
@@ -103,6 +104,41 @@ __device__ __forceinline__ float2 cmul_conj(float2 a, float2 b) {  // a * conj(b
     return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
 }
 
+// ---- receive contraction on the tensor cores --------------------------------
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+// D += A (16x8, row) * B (8x8, col), TF32 inputs, FP32 accumulate
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Three-term TF32 product (big*big + big*small + small*big): FP32-level
+// accuracy from the TF32 pipes.
+__device__ __forceinline__ void mma_3xtf32(float (&d)[4], const float (&a)[4], const float (&b)[2]) {
+    uint32_t ab[4], as[4], bb[2], bs[2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        ab[i] = to_tf32(a[i]);
+        as[i] = to_tf32(a[i] - __uint_as_float(ab[i]));
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        bb[i] = to_tf32(b[i]);
+        bs[i] = to_tf32(b[i] - __uint_as_float(bb[i]));
+    }
+    mma_tf32(d, as, bb);
+    mma_tf32(d, ab, bs);
+    mma_tf32(d, ab, bb);
+}
+
 // y = 1 - exp(-x)
 __device__ __forceinline__ float one_minus_exp(float x) { return -expm1f(-x); }
 
@@ -142,12 +178,16 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     float4 *rbuf = reinterpret_cast<float4 *>(smem + 128);
     const int rstride = L.stride4;
-    // coil sensitivities of the block's voxels, then per-warp receive sums
+    // receive tile: one row per (sample, sampled pool), one float2 column per
+    // thread; the coil sensitivities of the threads' voxels; per-warp sums
+    constexpr int kNSampP = (MODEL == KM_MT || MODEL == KM_CEST) ? 1 : P;
+    constexpr int kTile = (16 / kNSampP) < 1 ? 1 : 16 / kNSampP;  // samples per flush
+    constexpr int kTRow = kBlock + 2;                             // padded row (float2)
     const int C4 = (L.rx + 3) & ~3;
-    float2 *rsm = reinterpret_cast<float2 *>(rbuf + 2 * kChunk * rstride);  // [C4][kBlock]
-    float *acc = reinterpret_cast<float *>(rsm + C4 * kBlock);              // [kAdcTile][warp][nsamp][C4][2]
+    float2 *mtile = reinterpret_cast<float2 *>(rbuf + 2 * kFastChunk * rstride);  // [16][kTRow]
+    float2 *rsm = mtile + 16 * kTRow;                                              // [C4][kTRow]
+    float *red = reinterpret_cast<float *>(rsm + C4 * kTRow);                      // [warp][16][2*C4]
     constexpr int kWarps = kBlock / 32;
-    const int acc_row = L.nsamp * C4 * 2;
     constexpr bool kFreeAll = MODEL == KM_NORMAL || MODEL == KM_EXCH;
 
     const int tid = threadIdx.x;
@@ -249,7 +289,7 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
             else
                 r = L.rxc[(long long)c * n + v];
         }
-        rsm[c * kBlock + tid] = r;
+        rsm[c * kTRow + tid] = r;
     }
     // the isochromats enter the frame at the start of the launch: m_frame = m_lab / P
     bool entered = false;
@@ -272,36 +312,61 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
     }
     __syncthreads();
     const long long nsteps = L.s1 - L.s0;
-    const int nchunks = (int)((nsteps + kChunk - 1) / kChunk);
+    const int nchunks = (int)((nsteps + kFastChunk - 1) / kFastChunk);
     auto issue = [&](int k) {
-        const long long first = L.s0 + (long long)k * kChunk;
-        const long long cnt = min((long long)kChunk, L.s1 - first);
+        const long long first = L.s0 + (long long)k * kFastChunk;
+        const long long cnt = min((long long)kFastChunk, L.s1 - first);
         const uint32_t bytes = (uint32_t)(cnt * rstride * 16);
         mbar_expect_tx(&bar[k & 1], bytes);
-        bulk_g2s(rbuf + (k & 1) * kChunk * rstride, L.rec + first * rstride, bytes, &bar[k & 1]);
+        bulk_g2s(rbuf + (k & 1) * kFastChunk * rstride, L.rec + first * rstride, bytes, &bar[k & 1]);
     };
     if (tid == 0 && nchunks > 0) issue(0);
 
     int a_fill = 0, a_base = 0;
     const int lane = tid & 31, warp = tid >> 5;
-    // flush: sum the per-warp receive sums of the tile and write one partial
-    // per (block, sample, pool, coil)
+    // flush: S[row][2c + {x,y}] = sum over threads of m(row) conj(R_c): a
+    // (16 x 2*128) x (2*128 x 2*C4) real GEMM, split by warps along the
+    // thread (voxel) dimension, on the tensor cores; then the warp slices are
+    // added and one partial per (block, sample, pool, coil) is written
     auto flush = [&]() {
         __syncthreads();
-        const int nout = a_fill * L.nsamp * L.rx;
+        const int g = lane >> 2, tig = lane & 3;
+        for (int nt = 0; nt < C4 / 4; ++nt) {
+            float d[4] = {0.f, 0.f, 0.f, 0.f};
+            const int c = nt * 4 + (g >> 1), cmp = g & 1;
+#pragma unroll
+            for (int ks = 0; ks < 8; ++ks) {
+                const int k0 = warp * 64 + ks * 8 + tig, k1 = k0 + 4;
+                const int j0 = k0 >> 1, j1 = k1 >> 1, ri0 = k0 & 1, ri1 = k1 & 1;
+                const float2 m00 = mtile[g * kTRow + j0], m10 = mtile[(g + 8) * kTRow + j0];
+                const float2 m01 = mtile[g * kTRow + j1], m11 = mtile[(g + 8) * kTRow + j1];
+                const float a[4] = {ri0 ? m00.y : m00.x, ri0 ? m10.y : m10.x, ri1 ? m01.y : m01.x,
+                                    ri1 ? m11.y : m11.x};
+                // B[2j + ri][2c + cmp]: (x,x) = rx, (x,y) = -ry, (y,x) = ry, (y,y) = rx
+                const float2 r0 = rsm[c * kTRow + j0], r1 = rsm[c * kTRow + j1];
+                const float b[2] = {cmp ? (ri0 ? r0.x : -r0.y) : (ri0 ? r0.y : r0.x),
+                                    cmp ? (ri1 ? r1.x : -r1.y) : (ri1 ? r1.y : r1.x)};
+                mma_3xtf32(d, a, b);
+            }
+            float *rw = red + warp * 16 * (2 * C4);
+            rw[g * (2 * C4) + nt * 8 + 2 * tig] = d[0];
+            rw[g * (2 * C4) + nt * 8 + 2 * tig + 1] = d[1];
+            rw[(g + 8) * (2 * C4) + nt * 8 + 2 * tig] = d[2];
+            rw[(g + 8) * (2 * C4) + nt * 8 + 2 * tig + 1] = d[3];
+        }
+        __syncthreads();
+        const int nout = a_fill * kNSampP * L.rx;
         for (int o = tid; o < nout; o += kBlock) {
-            const int a = o / (L.nsamp * L.rx);
-            const int pair = o - a * (L.nsamp * L.rx);
-            const int t = pair / L.rx;
-            const int c = pair - t * L.rx;
+            const int row = o / L.rx;  // = a * kNSampP + t
+            const int c = o - row * L.rx;
+            const int a = row / kNSampP, t = row - a * kNSampP;
             float sx = 0.f, sy = 0.f;
 #pragma unroll
             for (int w = 0; w < kWarps; ++w) {
-                const float *row = acc + (a * kWarps + w) * acc_row + (t * C4 + c) * 2;
-                sx += row[0];
-                sy += row[1];
+                sx += red[(w * 16 + row) * (2 * C4) + 2 * c];
+                sy += red[(w * 16 + row) * (2 * C4) + 2 * c + 1];
             }
-            L.partial[((long long)blockIdx.x * L.a_launch + a_base + a) * L.npairs + pair] = make_float2(sx, sy);
+            L.partial[((long long)blockIdx.x * L.a_launch + a_base + a) * L.npairs + t * L.rx + c] = make_float2(sx, sy);
         }
         a_base += a_fill;
         a_fill = 0;
@@ -317,8 +382,8 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
             if (tid == 0) mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, L.err);
             break;
         }
-        const float4 *cb = rbuf + (k & 1) * kChunk * rstride;
-        const int cnt = (int)min((long long)kChunk, nsteps - (long long)k * kChunk);
+        const float4 *cb = rbuf + (k & 1) * kFastChunk * rstride;
+        const int cnt = (int)min((long long)kFastChunk, nsteps - (long long)k * kFastChunk);
         for (int q = 0; q < cnt; ++q) {
             const float4 r0 = cb[q * rstride];
             const float4 r1 = cb[q * rstride + 1];
@@ -355,7 +420,10 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
 #pragma unroll
                 for (int s = 0; s < NS; ++s)
 #pragma unroll
-                    for (int t = 0; t < P; ++t) D[s][t] = phase_step((wc + Wh[s][t]) * dt);
+                    for (int t = 0; t < P; ++t)
+                        D[s][t] = (MODEL == KM_MT || MODEL == KM_CEST || (act >> t & 1u))
+                                      ? phase_step((wc + Wh[s][t]) * dt)
+                                      : make_float2(0.f, 0.f);
             }
             if (active && (flags & kFlagDt)) {
 #pragma unroll
@@ -403,14 +471,24 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                 }
             }
 
-            // ---- receive, before the step's rotation ------------------------
-            if (flags & kFlagAdc) {
-                float *arow = acc + (a_fill * kWarps + warp) * acc_row;
+            if (active && (flags & kFlagDt) && MODEL != KM_MT && MODEL != KM_CEST) {
+                // an empty pool keeps its magnetisation: neutral coefficients
+                // instead of branches keep the per-pool updates straight-line
 #pragma unroll
                 for (int t = 0; t < P; ++t) {
-                    if (t >= L.nsamp) break;
+                    if (act >> t & 1u) continue;
+                    y1[t] = y2[t] = yo[t] = 0.f;
+#pragma unroll
+                    for (int p = 0; p < P; ++p) fin[t][p] = 0.f;
+                }
+            }
+
+            // ---- receive, before the step's rotation ------------------------
+            if (flags & kFlagAdc) {
+#pragma unroll
+                for (int t = 0; t < kNSampP; ++t) {
                     float mx = 0.f, my = 0.f;
-                    const bool sampled = (MODEL != KM_EXCH) || (L.kind[t] == 0);
+                    const bool sampled = (MODEL != KM_EXCH) || F.all_free || (L.kind[t] == 0);
 #pragma unroll
                     for (int s = 0; s < NS; ++s) {
                         const float2 m = cmul(make_float2(X[s][t], Y[s][t]), Ph[s][t]);
@@ -418,43 +496,9 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                         my += m.y;
                     }
                     if (!(active && sampled)) mx = my = 0.f;
-                    for (int g = 0; g < C4; g += 4) {
-                        // M conj(R) for 4 coils: sx = Mx Rx + My Ry, sy = My Rx - Mx Ry
-                        float vv[8];
-#pragma unroll
-                        for (int cc = 0; cc < 4; ++cc) {
-                            const float2 r = rsm[(g + cc) * kBlock + tid];
-                            vv[2 * cc] = fmaf(mx, r.x, my * r.y);
-                            vv[2 * cc + 1] = fmaf(my, r.x, -mx * r.y);
-                        }
-                        // warp transpose-reduction: after the three halving steps lane l
-                        // holds value (l >> 2) & 7 summed over lanes differing in bits 4..2
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            const bool up = lane & 16;
-                            const float send = up ? vv[j] : vv[j + 4];
-                            const float keep = up ? vv[j + 4] : vv[j];
-                            vv[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-                        }
-#pragma unroll
-                        for (int j = 0; j < 2; ++j) {
-                            const bool up = lane & 8;
-                            const float send = up ? vv[j] : vv[j + 2];
-                            const float keep = up ? vv[j + 2] : vv[j];
-                            vv[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-                        }
-                        {
-                            const bool up = lane & 4;
-                            const float send = up ? vv[0] : vv[1];
-                            const float keep = up ? vv[1] : vv[0];
-                            vv[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-                        }
-                        vv[0] += __shfl_xor_sync(0xffffffffu, vv[0], 2);
-                        vv[0] += __shfl_xor_sync(0xffffffffu, vv[0], 1);
-                        if ((lane & 3) == 0) arow[(t * C4 + g) * 2 + (lane >> 2)] = vv[0];
-                    }
+                    mtile[(a_fill * kNSampP + t) * kTRow + tid] = make_float2(mx, my);
                 }
-                if (++a_fill == kAdcTile) flush();
+                if (++a_fill == kTile) flush();
             }
             if (!active) continue;
 
@@ -507,6 +551,58 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                     px[t] = X[s][t];
                     py[t] = Y[s][t];
                     pz[t] = Z[s][t];
+                }
+                if (MODEL == KM_NORMAL || (MODEL == KM_EXCH && F.all_free)) {
+                    // every pool free: straight-line updates of all pools
+                    if (rf) {
+#pragma unroll
+                        for (int t = 0; t < P; ++t) {
+                            float x = X[s][t], y = Y[s][t], z = Z[s][t];
+                            rf_rotate(x, y, z, wc + Wh[s][t] + wrf, b, cmul(u0, Ph[s][t]), dt);
+                            const bool on = act >> t & 1u;
+                            X[s][t] = on ? x : X[s][t];
+                            Y[s][t] = on ? y : Y[s][t];
+                            Z[s][t] = on ? z : Z[s][t];
+                        }
+                    } else {
+#pragma unroll
+                        for (int t = 0; t < P; ++t) {
+                            const float2 p = Ph[s][t], d = D[s][t];
+                            Ph[s][t] = make_float2(fmaf(p.x, d.x, fmaf(-p.y, d.y, p.x)), fmaf(p.x, d.y, fmaf(p.y, d.x, p.y)));
+                        }
+                    }
+                    if (MODEL == KM_NORMAL) {
+#pragma unroll
+                        for (int t = 0; t < P; ++t) {
+                            X[s][t] = fmaf(-y2[t], X[s][t], X[s][t]);
+                            Y[s][t] = fmaf(-y2[t], Y[s][t], Y[s][t]);
+                            Z[s][t] = fmaf(y1[t], rhoS[t] - Z[s][t], Z[s][t]);
+                        }
+                    } else {
+                        // inflow uses every pool's magnetisation before the step, in the lab
+                        // frame, carried into the receiving pool's frame after the step
+                        float2 ml[P];
+#pragma unroll
+                        for (int p = 0; p < P; ++p) ml[p] = cmul(make_float2(px[p], py[p]), Pprev[p]);
+#pragma unroll
+                        for (int t = 0; t < P; ++t) {
+                            float ix = 0.f, iy = 0.f, iz = 0.f;
+#pragma unroll
+                            for (int p = 0; p < P; ++p) {
+                                ix = fmaf(fin[t][p], ml[p].x, ix);
+                                iy = fmaf(fin[t][p], ml[p].y, iy);
+                                iz = fmaf(fin[t][p], pz[p], iz);
+                            }
+                            const float2 in = cmul_conj(make_float2(ix, iy), Ph[s][t]);
+                            float x = fmaf(-y2[t], X[s][t], X[s][t]);
+                            float y = fmaf(-y2[t], Y[s][t], Y[s][t]);
+                            float z = fmaf(-y1[t], Z[s][t], Z[s][t]);
+                            X[s][t] = fmaf(-yo[t], x, x) + in.x;
+                            Y[s][t] = fmaf(-yo[t], y, y) + in.y;
+                            Z[s][t] = fmaf(-yo[t], z, z) + iz + rhoS[t] * y1[t];
+                        }
+                    }
+                    continue;
                 }
                 // rotation (rf) or frame advance (free precession)
 #pragma unroll
@@ -588,7 +684,6 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
 #pragma unroll
                         for (int t = 2; t < P; ++t) {
                             const float f = fin[0][t];
-                            if (f == 0.f) continue;
                             const float2 rel = cmul_conj(Pprev[t], Ph[s][0]);
                             const float2 m = cmul(make_float2(px[t], py[t]), rel);
                             ix = fmaf(f, m.x, ix);

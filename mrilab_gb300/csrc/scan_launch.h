@@ -21,8 +21,10 @@ inline size_t scan_smem_bytes(int stride4, int nsamp) {
 // ... of the accurate kernel: staged records, coil sensitivities of the
 // block's voxels and the per-warp receive tile.
 inline size_t scan_fast_smem_bytes(int stride4, int nsamp, int rx) {
+    (void)nsamp;
     const size_t c4 = (size_t)((rx + 3) & ~3);
-    return 128 + (size_t)2 * kChunk * stride4 * 16 + c4 * kBlock * 8 + (size_t)kAdcTile * (kBlock / 32) * nsamp * c4 * 2 * 4;
+    const size_t row = kBlock + 2;
+    return 128 + (size_t)2 * kFastChunk * stride4 * 16 + 16 * row * 8 + c4 * row * 8 + (kBlock / 32) * 16 * 2 * c4 * 4;
 }
 
 cudaError_t launch_scan_ref_normal(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
