@@ -8,7 +8,9 @@
 //
 // Differences in structure from the reference (results are the same):
 //   * voxels whose pools are all empty (T1, T2 or Rho zero) are compacted
-//     away before upload instead of being skipped inside the kernel;
+//     away instead of being skipped inside the kernel: the caller's arrays
+//     are uploaded as they are and gathered on the device, and the final
+//     magnetisation is scattered back on the device and downloaded whole;
 //   * the magnetisation stays on the device for the whole scan: kernels are
 //     launched per block of steps, not per TR, and only Ext events bring
 //     data back to the host;
@@ -68,6 +70,108 @@ __global__ void reduce_partials(const float2 *__restrict__ partial, int nblk, in
     sy[idx] = sr * x + cr * y;
 }
 
+// ---- object staging on the device -------------------------------------------
+// The caller's column-major arrays are uploaded unchanged into one raw
+// buffer; gather_object builds the compacted structure-of-arrays the scan
+// kernels read (active voxels only, index i -> voxel act[i]) and, for the
+// accurate integrator, the frame coefficients in FP64 split into (hi, lo)
+// float pairs.  scatter_state writes the compacted magnetisation back into
+// the raw arrays, which are then downloaded into the caller's arrays whole.
+struct RawObject {
+    const float *gx, *gy, *gz, *db0;  // [V]
+    const float *txmg, *txpe;         // [Tx][V]
+    const float *rho, *t1, *t2;       // [P][V]
+    const float *k;                   // [nk][V]
+    const float *dwr;                 // [P][S][V]
+    float *mx, *my, *mz;              // [P][S][V]
+    const float *rxx, *rxy;           // [Rx][V], null for the default coil
+};
+
+struct GatherArgs {
+    RawObject r;
+    const int *act;
+    int n_act, n, P, S, TX, RX, nk;
+    long long V;
+    float *f;  // d_f base
+    size_t o_gx, o_gy, o_gz, o_db0, o_txmg, o_txpe, o_rho, o_t1, o_t2, o_k, o_dwr;
+    float *m;       // d_m: mx | my | mz, [P][S][n] each
+    float2 *rxc;    // [Rx][n]
+    float2 *f2;     // frame coefficients, null for reference numerics
+    size_t o_om, o_wr, o_txc;
+    double gyro;
+    double cs2pi[kMaxPool];  // 2 pi CS[t]
+};
+
+__device__ __forceinline__ float2 split_df(double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+
+__global__ void gather_object(GatherArgs G) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= G.n_act) return;
+    const long long v = G.act[i];
+    const long long V = G.V;
+    const size_t n = (size_t)G.n;
+    const RawObject &r = G.r;
+    float *f = G.f;
+    const float gx = r.gx[v], gy = r.gy[v], gz = r.gz[v], db0 = r.db0[v];
+    f[G.o_gx + i] = gx;
+    f[G.o_gy + i] = gy;
+    f[G.o_gz + i] = gz;
+    f[G.o_db0 + i] = db0;
+    for (int c = 0; c < G.TX; ++c) {
+        const float mg = r.txmg[c * V + v], pe = r.txpe[c * V + v];
+        f[G.o_txmg + c * n + i] = mg;
+        f[G.o_txpe + c * n + i] = pe;
+        if (G.f2) {
+            double sp, cp;
+            sincos((double)pe, &sp, &cp);
+            G.f2[G.o_txc + c * n + i] = make_float2((float)((double)mg * cp), (float)((double)mg * sp));
+        }
+    }
+    const size_t ns = n * G.P * G.S;
+    for (int t = 0; t < G.P; ++t) {
+        f[G.o_rho + t * n + i] = r.rho[t * V + v];
+        f[G.o_t1 + t * n + i] = r.t1[t * V + v];
+        f[G.o_t2 + t * n + i] = r.t2[t * V + v];
+        for (int s = 0; s < G.S; ++s) {
+            const long long src = ((long long)t * G.S + s) * V + v;
+            const size_t dst = ((size_t)t * G.S + s) * n + i;
+            const float w = r.dwr[src];
+            f[G.o_dwr + dst] = w;
+            G.m[dst] = r.mx[src];
+            G.m[ns + dst] = r.my[src];
+            G.m[2 * ns + dst] = r.mz[src];
+            if (G.f2) G.f2[G.o_wr + dst] = split_df((double)w + G.cs2pi[t]);
+        }
+    }
+    for (int k = 0; k < G.nk; ++k) f[G.o_k + k * n + i] = r.k[k * V + v];
+    if (r.rxx)
+        for (int c = 0; c < G.RX; ++c) G.rxc[c * n + i] = make_float2(r.rxx[c * V + v], r.rxy[c * V + v]);
+    if (G.f2) {
+        G.f2[G.o_om + 0 * n + i] = split_df(G.gyro * (double)db0);
+        G.f2[G.o_om + 1 * n + i] = split_df(G.gyro * (double)gx);
+        G.f2[G.o_om + 2 * n + i] = split_df(G.gyro * (double)gy);
+        G.f2[G.o_om + 3 * n + i] = split_df(G.gyro * (double)gz);
+    }
+}
+
+__global__ void scatter_state(const float *__restrict__ m, const int *__restrict__ act, int n_act, int n, int PS,
+                              long long V, float *mx, float *my, float *mz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_act) return;
+    const long long v = act[i];
+    const size_t ns = (size_t)n * PS;
+    for (int ts = 0; ts < PS; ++ts) {
+        const size_t src = (size_t)ts * n + i;
+        const long long dst = (long long)ts * V + v;
+        mx[dst] = m[src];
+        my[dst] = m[ns + src];
+        mz[dst] = m[2 * ns + src];
+    }
+}
+
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
@@ -116,7 +220,7 @@ struct Scanner {
     int P = 0, S = 0, TX = 0, RX = 0, A = 0, NS = 1, tpv = 1, stride4 = 2;
     long long V = 0;
     int n_act = 0;
-    std::vector<long long> act;  // compact index -> voxel
+    std::vector<int> act;        // compact index -> voxel
     cudaStream_t st = nullptr;
     DevBuf<float> d_f;           // all per-voxel float fields, packed
     DevBuf<float> d_m;           // mx | my | mz
@@ -130,6 +234,9 @@ struct Scanner {
     bool fast = false;
     FrameMoments fmom;
     DevBuf<float2> d_f2;  // omega [4][n] | wres [P][S][n] | txc [Tx][n]
+    DevBuf<float> d_raw;  // the caller's arrays as uploaded (RawObject)
+    DevBuf<int> d_act;    // compact index -> voxel, on the device
+    RawObject raw{};
     size_t o_om = 0, o_wr = 0, o_txc = 0;
     std::vector<float> frec;
     // offsets into d_f
@@ -152,6 +259,16 @@ struct Scanner {
         for (int t = 0; t < P; ++t)
             if ((int)args->obj.type_flag[t] != 0) return 0;
         return 1;
+    }
+
+    // MRL_DEBUG: host phase times on stderr
+    const bool dbg = getenv("MRL_DEBUG") != nullptr;
+    std::chrono::steady_clock::time_point t_phase = std::chrono::steady_clock::now();
+    void phase(const char *name) {
+        if (!dbg) return;
+        const auto now = std::chrono::steady_clock::now();
+        fprintf(stderr, "mrl: %-16s %9.3f ms\n", name, std::chrono::duration<double, std::milli>(now - t_phase).count());
+        t_phase = now;
     }
 
     int fail_cuda(cudaError_t e, const char *what) {
@@ -227,12 +344,13 @@ struct Scanner {
         return MRL_OK;
     }
 
-    // Gather the active voxels into structure-of-arrays form and upload.
+    // Upload the caller's arrays unchanged and gather the active voxels into
+    // structure-of-arrays form on the device (gather_object).
     int upload_object() {
         const mrl_scan_args &a = *args;
         act.clear();
         for (long long v = 0; v < V; ++v)
-            if (voxel_active(a, mi.km, v, V)) act.push_back(v);
+            if (voxel_active(a, mi.km, v, V)) act.push_back((int)v);
         n_act = (int)act.size();
         const size_t n = std::max(1, n_act);
         size_t off = 0;
@@ -246,126 +364,126 @@ struct Scanner {
         o_rho = take(n * P), o_t1 = take(n * P), o_t2 = take(n * P);
         o_k = take(n * std::max(1, mi.nk));
         o_dwr = take(n * P * S);
-        std::vector<float> hf(off, 0.f);
-        std::vector<float> hm(3 * n * P * S, 0.f);
-        std::vector<float2> hr(a.coil.rx_default == 0 ? n * RX : 1, make_float2(0.f, 0.f));
-        const int nk = mi.nk;
-        for (int i = 0; i < n_act; ++i) {
-            const long long v = act[i];
-            hf[o_gx + i] = a.mag.gxgrid[v];
-            hf[o_gy + i] = a.mag.gygrid[v];
-            hf[o_gz + i] = a.mag.gzgrid[v];
-            hf[o_db0 + i] = a.mag.db0[v];
-            for (int c = 0; c < TX; ++c) {
-                hf[o_txmg + c * n + i] = a.coil.tx_mg[c * V + v];
-                hf[o_txpe + c * n + i] = a.coil.tx_pe[c * V + v];
-            }
-            for (int t = 0; t < P; ++t) {
-                hf[o_rho + t * n + i] = a.obj.rho[t * V + v];
-                hf[o_t1 + t * n + i] = a.obj.t1[t * V + v];
-                hf[o_t2 + t * n + i] = a.obj.t2[t * V + v];
-                for (int s = 0; s < S; ++s) {
-                    const long long src = ((long long)t * S + s) * V + v;
-                    const size_t dst = ((size_t)t * S + s) * n + i;
-                    hf[o_dwr + dst] = a.mag.dwrnd[src];
-                    hm[dst] = a.obj.mx[src];
-                    hm[(size_t)n * P * S + dst] = a.obj.my[src];
-                    hm[(size_t)2 * n * P * S + dst] = a.obj.mz[src];
-                }
-            }
-            for (int k = 0; k < nk; ++k) hf[o_k + k * n + i] = a.obj.k[k * V + v];
-            if (a.coil.rx_default == 0)
-                for (int c = 0; c < RX; ++c)
-                    hr[c * n + i] = make_float2(a.coil.rx_x[c * V + v], a.coil.rx_y[c * V + v]);
-        }
-        std::vector<float2> h2;
         if (fast) {
-            // frame coefficients in double, split into (hi, lo) float pairs
             o_om = 0;
             o_wr = 4 * n;
             o_txc = o_wr + (size_t)P * S * n;
-            h2.assign(o_txc + (size_t)TX * n, make_float2(0.f, 0.f));
-            auto split = [](double v) {
-                const float hi = (float)v;
-                return make_float2(hi, (float)(v - (double)hi));
-            };
-            const double g = a.obj.gyro;
-            for (int i = 0; i < n_act; ++i) {
-                const long long v = act[i];
-                h2[0 * n + i] = split(g * (double)a.mag.db0[v]);
-                h2[1 * n + i] = split(g * (double)a.mag.gxgrid[v]);
-                h2[2 * n + i] = split(g * (double)a.mag.gygrid[v]);
-                h2[3 * n + i] = split(g * (double)a.mag.gzgrid[v]);
-                for (int t = 0; t < P; ++t) {
-                    const double cs = a.ctl.cs ? 2 * kPiRef * a.ctl.cs[t] : 0.0;
-                    for (int s2 = 0; s2 < S; ++s2)
-                        h2[o_wr + ((size_t)t * S + s2) * n + i] =
-                            split((double)a.mag.dwrnd[((long long)t * S + s2) * V + v] + cs);
-                }
-                for (int c = 0; c < TX; ++c) {
-                    const double mg = a.coil.tx_mg[c * V + v], pe = a.coil.tx_pe[c * V + v];
-                    h2[o_txc + (size_t)c * n + i] = make_float2((float)(mg * std::cos(pe)), (float)(mg * std::sin(pe)));
-                }
-            }
+        }
+        phase("active voxels");
+        const bool rxmap = a.coil.rx_default == 0;
+        // raw buffer: the caller's arrays back to back, in the order below
+        const size_t Vs = (size_t)V, PSV = (size_t)P * S * Vs;
+        struct Piece {
+            const float *host;
+            size_t count;
+        };
+        const Piece pieces[] = {{a.mag.gxgrid, Vs},
+                                {a.mag.gygrid, Vs},
+                                {a.mag.gzgrid, Vs},
+                                {a.mag.db0, Vs},
+                                {a.coil.tx_mg, (size_t)TX * Vs},
+                                {a.coil.tx_pe, (size_t)TX * Vs},
+                                {a.obj.rho, (size_t)P * Vs},
+                                {a.obj.t1, (size_t)P * Vs},
+                                {a.obj.t2, (size_t)P * Vs},
+                                {mi.nk > 0 ? a.obj.k : nullptr, (size_t)mi.nk * Vs},
+                                {a.mag.dwrnd, PSV},
+                                {a.obj.mx, PSV},
+                                {a.obj.my, PSV},
+                                {a.obj.mz, PSV},
+                                {rxmap ? a.coil.rx_x : nullptr, rxmap ? (size_t)RX * Vs : 0},
+                                {rxmap ? a.coil.rx_y : nullptr, rxmap ? (size_t)RX * Vs : 0}};
+        constexpr int kPieces = sizeof(pieces) / sizeof(pieces[0]);
+        size_t roff[kPieces], rtot = 0;
+        for (int q = 0; q < kPieces; ++q) {
+            roff[q] = rtot;
+            rtot += (pieces[q].count + 63) & ~size_t(63);  // 256-byte aligned pieces
         }
         cudaError_t e;
-        if (fast) {
-            if ((e = d_f2.ensure(h2.size())) != cudaSuccess) return fail_cuda(e, "cudaMalloc(frame)");
-            if ((e = cudaMemcpyAsync(d_f2.p, h2.data(), h2.size() * sizeof(float2), cudaMemcpyHostToDevice, st)) !=
-                cudaSuccess)
-                return fail_cuda(e, "upload frame");
-            h2d_bytes += (double)h2.size() * sizeof(float2);
-        }
+        if ((e = d_raw.ensure(rtot)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(raw object)");
+        if ((e = d_act.ensure(n)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(voxel map)");
         if ((e = d_f.ensure(off)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(object)");
-        if ((e = d_m.ensure(hm.size())) != cudaSuccess) return fail_cuda(e, "cudaMalloc(state)");
-        if ((e = d_rx.ensure(hr.size())) != cudaSuccess) return fail_cuda(e, "cudaMalloc(coils)");
+        if ((e = d_m.ensure(3 * n * P * S)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(state)");
+        if ((e = d_rx.ensure(rxmap ? n * RX : 1)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(coils)");
+        if (fast && (e = d_f2.ensure(o_txc + (size_t)TX * n)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(frame)");
         auto t0 = std::chrono::steady_clock::now();
-        if ((e = cudaMemcpyAsync(d_f.p, hf.data(), off * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
-            return fail_cuda(e, "upload object");
-        h2d_bytes += (double)off * sizeof(float) + hm.size() * sizeof(float) + hr.size() * sizeof(float2);
-        if ((e = cudaMemcpyAsync(d_m.p, hm.data(), hm.size() * sizeof(float), cudaMemcpyHostToDevice, st)) !=
-            cudaSuccess)
-            return fail_cuda(e, "upload state");
-        if ((e = cudaMemcpyAsync(d_rx.p, hr.data(), hr.size() * sizeof(float2), cudaMemcpyHostToDevice, st)) !=
-            cudaSuccess)
-            return fail_cuda(e, "upload coils");
+        for (int q = 0; q < kPieces; ++q) {
+            if (!pieces[q].host || pieces[q].count == 0) continue;
+            if ((e = cudaMemcpyAsync(d_raw.p + roff[q], pieces[q].host, pieces[q].count * sizeof(float),
+                                     cudaMemcpyHostToDevice, st)) != cudaSuccess)
+                return fail_cuda(e, "upload object");
+            h2d_bytes += (double)pieces[q].count * sizeof(float);
+        }
+        if (n_act > 0) {
+            if ((e = cudaMemcpyAsync(d_act.p, act.data(), (size_t)n_act * sizeof(int), cudaMemcpyHostToDevice, st)) !=
+                cudaSuccess)
+                return fail_cuda(e, "upload voxel map");
+            h2d_bytes += (double)n_act * sizeof(int);
+        }
+        raw.gx = d_raw.p + roff[0];
+        raw.gy = d_raw.p + roff[1];
+        raw.gz = d_raw.p + roff[2];
+        raw.db0 = d_raw.p + roff[3];
+        raw.txmg = d_raw.p + roff[4];
+        raw.txpe = d_raw.p + roff[5];
+        raw.rho = d_raw.p + roff[6];
+        raw.t1 = d_raw.p + roff[7];
+        raw.t2 = d_raw.p + roff[8];
+        raw.k = d_raw.p + roff[9];
+        raw.dwr = d_raw.p + roff[10];
+        raw.mx = d_raw.p + roff[11];
+        raw.my = d_raw.p + roff[12];
+        raw.mz = d_raw.p + roff[13];
+        raw.rxx = rxmap ? d_raw.p + roff[14] : nullptr;
+        raw.rxy = rxmap ? d_raw.p + roff[15] : nullptr;
+        if (n_act > 0) {
+            GatherArgs G{};
+            G.r = raw;
+            G.act = d_act.p;
+            G.n_act = n_act;
+            G.n = (int)n;
+            G.P = P;
+            G.S = S;
+            G.TX = TX;
+            G.RX = RX;
+            G.nk = mi.nk;
+            G.V = V;
+            G.f = d_f.p;
+            G.o_gx = o_gx, G.o_gy = o_gy, G.o_gz = o_gz, G.o_db0 = o_db0, G.o_txmg = o_txmg, G.o_txpe = o_txpe;
+            G.o_rho = o_rho, G.o_t1 = o_t1, G.o_t2 = o_t2, G.o_k = o_k, G.o_dwr = o_dwr;
+            G.m = d_m.p;
+            G.rxc = d_rx.p;
+            G.f2 = fast ? d_f2.p : nullptr;
+            G.o_om = o_om, G.o_wr = o_wr, G.o_txc = o_txc;
+            G.gyro = a.obj.gyro;
+            for (int t = 0; t < kMaxPool; ++t) G.cs2pi[t] = (t < P && a.ctl.cs) ? 2 * kPiRef * a.ctl.cs[t] : 0.0;
+            gather_object<<<(n_act + 255) / 256, 256, 0, st>>>(G);
+            if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "gather launch");
+        }
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e, "upload sync");
         h2d_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-        if (getenv("MRL_DEBUG")) {
-            double sx = 0, sz = 0;
-            for (size_t i = 0; i < n * P * S; ++i) sx += std::fabs(hm[i]), sz += hm[2 * n * P * S + i];
-            fprintf(stderr, "mrl: upload_object n_act=%d |Mx|=%g sum Mz=%g\n", n_act, sx, sz);
-        }
+        phase("upload object");
+        if (dbg) fprintf(stderr, "mrl: upload_object n_act=%d of %lld voxels\n", n_act, V);
         return MRL_OK;
     }
 
     // Copy the device magnetisation back into the caller's arrays.
     int download_state() {
         mrl_scan_args &a = *args;
+        if (n_act == 0) return MRL_OK;  // nothing was integrated
         const size_t n = std::max(1, n_act);
-        std::vector<float> hm(3 * n * P * S);
+        const size_t PSV = (size_t)P * S * V;
         auto t0 = std::chrono::steady_clock::now();
-        cudaError_t e = cudaMemcpyAsync(hm.data(), d_m.p, hm.size() * sizeof(float), cudaMemcpyDeviceToHost, st);
-        d2h_bytes += (double)hm.size() * sizeof(float);
+        scatter_state<<<(n_act + 255) / 256, 256, 0, st>>>(d_m.p, d_act.p, n_act, (int)n, P * S, V, raw.mx, raw.my,
+                                                          raw.mz);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(a.obj.mx, raw.mx, PSV * sizeof(float), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(a.obj.my, raw.my, PSV * sizeof(float), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(a.obj.mz, raw.mz, PSV * sizeof(float), cudaMemcpyDeviceToHost, st);
+        d2h_bytes += 3.0 * PSV * sizeof(float);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return fail_cuda(e, "download state");
         d2h_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-        if (getenv("MRL_DEBUG")) {
-            double sx = 0;
-            for (size_t i = 0; i < n * P * S; ++i) sx += std::fabs(hm[i]);
-            fprintf(stderr, "mrl: download_state |Mx|=%g\n", sx);
-        }
-        for (int i = 0; i < n_act; ++i) {
-            const long long v = act[i];
-            for (int t = 0; t < P; ++t)
-                for (int s = 0; s < S; ++s) {
-                    const long long dst = ((long long)t * S + s) * V + v;
-                    const size_t src = ((size_t)t * S + s) * n + i;
-                    a.obj.mx[dst] = hm[src];
-                    a.obj.my[dst] = hm[(size_t)n * P * S + src];
-                    a.obj.mz[dst] = hm[(size_t)2 * n * P * S + src];
-                }
-        }
         return MRL_OK;
     }
 
@@ -475,6 +593,7 @@ struct Scanner {
             pack_fast_records(ch, TX, fmom, frec);
             recs = &frec;
         }
+        phase("pack records");
         cudaError_t e;
         if ((e = d_rec.ensure(recs->size() / 4)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(steps)");
         if ((e = d_amap.ensure(std::max<size_t>(1, amap_host.size()))) != cudaSuccess)
@@ -492,6 +611,7 @@ struct Scanner {
             return fail_cuda(e, "upload amap");
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e, "upload steps");
         h2d_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        phase("upload steps");
         return MRL_OK;
     }
 
@@ -571,12 +691,14 @@ struct Scanner {
         if ((rc = enqueue(ls, rf_ref, st, true))) return rc;
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return fail_cuda(e, "scan kernels");
+        phase("scan kernels");
         return MRL_OK;
     }
 
     int setup() {
         int rc = validate();
         if (rc) return rc;
+        phase("validate");
         cudaError_t e;
         int dev = args->ctl.gpu_index;
         if ((e = cudaSetDevice(dev)) != cudaSuccess) {
@@ -592,6 +714,7 @@ struct Scanner {
             return fail_cuda(e, "cudaMalloc(signal)");
         cudaMemsetAsync(d_sx.p, 0, nsig * sizeof(double), st);
         cudaMemsetAsync(d_sy.p, 0, nsig * sizeof(double), st);
+        phase("device setup");
         return upload_object();
     }
 
@@ -619,6 +742,7 @@ struct Scanner {
         int signal_synced = 0;
         for (;;) {
             decode_until_ext(ds, args->seq, TX, args->obj.gyro, args->sig, ch);
+            phase("decode");
             const double rf_ref = args->var.rf_ref ? *args->var.rf_ref : 0.0;
             if ((rc = run_chunk(ch, rf_ref))) return rc;
             if (!ch.stopped_at_ext) break;
@@ -640,7 +764,9 @@ struct Scanner {
             }
         }
         if ((rc = download_signal(signal_synced, ds.signali))) return rc;
+        phase("download signal");
         if ((rc = download_state())) return rc;
+        phase("download state");
         store_state(ds, args->var, TX);
         if ((rc = check_device_status())) return rc;
         (void)e;

@@ -99,8 +99,19 @@ class ScanError(RuntimeError):
         self.status = status
 
 
-def _flat(a, dtype):
-    return np.array(np.asarray(a, dtype).ravel(order="F"), dtype=dtype, copy=True)
+def _flat(a, dtype, copy=True):
+    """Column-major flat array of ``a``.  Arrays the engine writes (magnetisation,
+    signal, pulse-packet cursor) are always copies, so a scan leaves the
+    caller's structs unchanged; read-only inputs that already have MATLAB's
+    layout and the right type are passed through without a copy."""
+    a = np.asarray(a, dtype)
+    if not copy and a.flags.f_contiguous:
+        return a.reshape(-1, order="F")
+    return a.flatten(order="F")
+
+
+# host arrays mrl_scan writes into
+_WRITTEN = frozenset({"mx", "my", "mz", "sx", "sy", "skz", "sky", "skx"})
 
 
 class HostScan:
@@ -111,9 +122,10 @@ class HostScan:
         o, m, c, ctl, q, v, sig = sc.VObj, sc.VMag, sc.VCoi, sc.VCtl, sc.VSeq, sc.VVar, sc.VSig
         self.keep = {}
         K = self.keep
-        f32 = lambda k, a: K.setdefault(k, _flat(a, np.float32))
-        f64 = lambda k, a: K.setdefault(k, _flat(a, np.float64))
-        i32 = lambda k, a: K.setdefault(k, _flat(a, np.int32))
+        # inputs the engine only reads may alias the caller's arrays
+        f32 = lambda k, a: K.setdefault(k, _flat(a, np.float32, copy=k in _WRITTEN))
+        f64 = lambda k, a: K.setdefault(k, _flat(a, np.float64, copy=k in _WRITTEN or k.startswith("var_")))
+        i32 = lambda k, a: K.setdefault(k, _flat(a, np.int32, copy=True))
         p = lambda a, t: a.ctypes.data_as(t)
         a = ScanArgs()
         a.abi_version = ABI_VERSION

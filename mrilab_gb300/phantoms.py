@@ -185,6 +185,11 @@ def assemble(rho, t1, t2, *, spin_num=1, t2star=None, db0_hz=None, res=(1e-3, 1e
                 Kz=np.zeros(nsig), Ky=np.zeros(nsig), Kx=np.zeros(nsig),
                 Mx=np.zeros_like(mz), My=np.zeros_like(mz), Mz=mz.copy(),
                 Muts=np.float64(0), SignalNum=np.int32(nsig))
+    # MATLAB's column-major layout, which is what the engine binds
+    for d in (vobj, vmag, vcoi, vsig):
+        for k, a in d.items():
+            if isinstance(a, np.ndarray) and a.ndim > 1:
+                d[k] = np.asfortranarray(a)
     return Scan(vobj, vmag, vcoi, vctl, dict(seqlines), vvar, vsig, model=model, rates=rates,
                 info=dict(seed=seed))
 
