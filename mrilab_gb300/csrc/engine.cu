@@ -818,6 +818,18 @@ cudaError_t noalloc_scratch(int dev, unsigned char **out) {
     return cudaSuccess;
 }
 
+// Device sine/cosine of the accurate kernel on caller-given arguments: the
+// hook of its accuracy test (not part of the scan interface).
+__global__ void sincos_probe(const float *x, float *sn, float *cs, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        float a, b;
+        sincos_cw(x[i], a, b);
+        sn[i] = a;
+        cs[i] = b;
+    }
+}
+
 }  // namespace
 }  // namespace mrl
 
@@ -1144,6 +1156,28 @@ const char *mrl_status_string(int status) {
 }
 
 const char *mrl_last_error(void) { return mrl::g_err.c_str(); }
+
+// Test hook (not declared in mrl_scan.h): sin and cos of n host floats as
+// the accurate kernel computes them, on the current device.
+int mrl_selftest_sincos(const float *x, float *sn, float *cs, int n) {
+    using namespace mrl;
+    if (!x || !sn || !cs || n < 0) return MRL_ERR_ARG;
+    if (n == 0) return MRL_OK;
+    DevBuf<float> d;
+    cudaError_t e = d.ensure((size_t)3 * n);
+    if (e == cudaSuccess) e = cudaMemcpy(d.p, x, (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        sincos_probe<<<(n + 255) / 256, 256>>>(d.p, d.p + n, d.p + 2 * n, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(sn, d.p + n, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(cs, d.p + 2 * n, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_err("selftest sincos: %s", cudaGetErrorString(e));
+        return MRL_ERR_CUDA;
+    }
+    return MRL_OK;
+}
 
 int mrl_last_timing(double out[8]) {
     if (!out) return MRL_ERR_ARG;

@@ -6,7 +6,7 @@ namespace mrl {
 namespace {
 template <int P, int NS>
 cudaError_t go(dim3 grid, size_t smem, cudaStream_t st, const FastLaunch &F) {
-    auto k = scan_fast_kernel<KM_CEST, P, NS>;
+    auto k = scan_fast_kernel<KM_CEST, P, NS, false>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k<<<grid, kBlock, smem, st>>>(F);

@@ -38,7 +38,8 @@ struct FastLaunch {
     // caller's uncompacted MATLAB arrays (n = every voxel), and the three
     // derived fields above are computed here instead of being read.
     int direct;
-    int all_free;             // KM_EXCH: every pool is free (ME, or GM without bound pools)
+    int all_free;             // KM_EXCH: every pool is free (ME, or GM without bound pools): selects
+                              // the FREE instantiation
     const float *rx_x, *rx_y; // [rx][n]
     float gam_hi, gam_lo;     // gyromagnetic ratio split
     float cs_hi[kMaxPool], cs_lo[kMaxPool];  // 2 pi CS[t] split
@@ -89,10 +90,45 @@ __device__ __forceinline__ float2 phasor(df phi) {
     return make_float2(c, -s);
 }
 
+// sin and cos of x: Cody-Waite reduction (Cody and Waite, Software Manual
+// for the Elementary Functions, 1980) x = k pi/2 + r with pi/2 split in
+// three floats and fused multiply-adds, |r| <= pi/4, then the Taylor series
+// of sin (to r^11) and cos (to r^12) by Horner's rule; truncation error
+// below 1e-11 on |r| <= pi/4.  Small arguments (k = 0) keep full relative
+// accuracy.  Meant for |x| well below 2^22 (rotation angles of one step).
+__device__ __forceinline__ void sincos_cw(float x, float &sn, float &cs) {
+    constexpr float kTwoOverPi = 0.636619746685028076f;
+    constexpr float kC1 = 1.57079637050628662f;       // float(pi / 2)
+    constexpr float kC2 = -4.37113882867379300e-08f;  // float(pi / 2 - kC1)
+    constexpr float kC3 = -1.77635683940025046e-15f;  // pi / 2 - kC1 - kC2
+    const float k = rintf(x * kTwoOverPi);
+    float r = fmaf(-k, kC1, x);
+    r = fmaf(-k, kC2, r);
+    r = fmaf(-k, kC3, r);
+    const float r2 = r * r;
+    float ps = -1.f / 39916800.f;
+    ps = fmaf(ps, r2, 1.f / 362880.f);
+    ps = fmaf(ps, r2, -1.f / 5040.f);
+    ps = fmaf(ps, r2, 1.f / 120.f);
+    ps = fmaf(ps, r2, -1.f / 6.f);
+    const float sr = fmaf(ps * r2, r, r);
+    float pc = 1.f / 479001600.f;
+    pc = fmaf(pc, r2, -1.f / 3628800.f);
+    pc = fmaf(pc, r2, 1.f / 40320.f);
+    pc = fmaf(pc, r2, -1.f / 720.f);
+    pc = fmaf(pc, r2, 1.f / 24.f);
+    pc = fmaf(pc, r2, -0.5f);
+    const float cr = fmaf(pc, r2, 1.f);
+    const int q = (int)k & 3;
+    const float a = (q & 1) ? cr : sr, b = (q & 1) ? sr : cr;
+    sn = (q & 2) ? -a : a;
+    cs = ((q + 1) & 2) ? -b : b;
+}
+
 // exp(-i theta) - 1, accurate for small theta.
 __device__ __forceinline__ float2 phase_step(float theta) {
     float s, c;
-    sincosf(0.5f * theta, &s, &c);
+    sincos_cw(0.5f * theta, s, c);
     return make_float2(-2.f * s * s, -2.f * s * c);
 }
 
@@ -120,23 +156,11 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// Three-term TF32 product (big*big + big*small + small*big): FP32-level
-// accuracy from the TF32 pipes.
-__device__ __forceinline__ void mma_3xtf32(float (&d)[4], const float (&a)[4], const float (&b)[2]) {
-    uint32_t ab[4], as[4], bb[2], bs[2];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        ab[i] = to_tf32(a[i]);
-        as[i] = to_tf32(a[i] - __uint_as_float(ab[i]));
-    }
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        bb[i] = to_tf32(b[i]);
-        bs[i] = to_tf32(b[i] - __uint_as_float(bb[i]));
-    }
-    mma_tf32(d, as, bb);
-    mma_tf32(d, ab, bs);
-    mma_tf32(d, ab, bb);
+// (x, y) as TF32 (big, small) parts: x = big + small to ~2^-22 relative,
+// for the three-term TF32 product big*big + big*small + small*big
+__device__ __forceinline__ uint4 tf32_split2(float x, float y) {
+    const uint32_t xb = to_tf32(x), yb = to_tf32(y);
+    return make_uint4(xb, to_tf32(x - __uint_as_float(xb)), yb, to_tf32(y - __uint_as_float(yb)));
 }
 
 // y = 1 - exp(-x)
@@ -153,7 +177,7 @@ __device__ __forceinline__ void rf_rotate(float &x, float &y, float &z, float dW
     const float cb = fabsf(b) * rn;
     const float sb = copysignf(1.f, b) * dW * rn;
     float sh, ch;
-    sincosf(0.5f * Bm * dt, &sh, &ch);
+    sincos_cw(0.5f * Bm * dt, sh, ch);
     const float sa = 2.f * sh * ch;
     const float omc = 2.f * sh * sh;  // 1 - cos(alpha)
     const float ca = 1.f - omc;
@@ -171,22 +195,27 @@ __device__ __forceinline__ void rf_rotate(float &x, float &y, float &z, float dW
     z = z2;
 }
 
-template <int MODEL, int P, int NS>
+// FREE (KM_EXCH only): every pool is a free pool (ME, or GM without bound
+// pools); the instantiation then has only the straight-line update path.
+template <int MODEL, int P, int NS, bool FREE>
 __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
     const ScanLaunch &L = F.b;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     float4 *rbuf = reinterpret_cast<float4 *>(smem + 128);
     const int rstride = L.stride4;
-    // receive tile: one row per (sample, sampled pool), one float2 column per
-    // thread; the coil sensitivities of the threads' voxels; per-warp sums
+    // receive tile: one row per (sample, sampled pool), one column per thread
+    // holding its lab-frame transverse magnetisation as TF32 (big, small)
+    // parts (x big, x small, y big, y small); the coil sensitivities of the
+    // threads' voxels split the same way (x big, x small, y big, y small);
+    // per-warp sums of the contraction
     constexpr int kNSampP = (MODEL == KM_MT || MODEL == KM_CEST) ? 1 : P;
     constexpr int kTile = (16 / kNSampP) < 1 ? 1 : 16 / kNSampP;  // samples per flush
-    constexpr int kTRow = kBlock + 2;                             // padded row (float2)
+    constexpr int kTRow = kBlock + 2;                             // padded row (uint4)
     const int C4 = (L.rx + 3) & ~3;
-    float2 *mtile = reinterpret_cast<float2 *>(rbuf + 2 * kFastChunk * rstride);  // [16][kTRow]
-    float2 *rsm = mtile + 16 * kTRow;                                              // [C4][kTRow]
-    float *red = reinterpret_cast<float *>(rsm + C4 * kTRow);                      // [warp][16][2*C4]
+    uint4 *mtile = reinterpret_cast<uint4 *>(rbuf + 2 * kFastChunk * rstride);  // [16][kTRow]
+    uint4 *rsm = mtile + 16 * kTRow;                                             // [C4][kTRow]
+    float *red = reinterpret_cast<float *>(rsm + C4 * kTRow);                    // [warp][16][2*C4]
     constexpr int kWarps = kBlock / 32;
     constexpr bool kFreeAll = MODEL == KM_NORMAL || MODEL == KM_EXCH;
 
@@ -229,7 +258,7 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                 om[i] = make_float2(p.hi, p.lo);
             }
             float sp, cp;
-            sincosf(L.txpe[v], &sp, &cp);
+            sincos_cw(L.txpe[v], sp, cp);
             tx0 = make_float2(L.txmg[v] * cp, L.txmg[v] * sp);
         } else {
 #pragma unroll
@@ -289,7 +318,7 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
             else
                 r = L.rxc[(long long)c * n + v];
         }
-        rsm[c * kTRow + tid] = r;
+        rsm[c * kTRow + tid] = tf32_split2(r.x, r.y);
     }
     // the isochromats enter the frame at the start of the launch: m_frame = m_lab / P
     bool entered = false;
@@ -326,33 +355,49 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
     const int lane = tid & 31, warp = tid >> 5;
     // flush: S[row][2c + {x,y}] = sum over threads of m(row) conj(R_c): a
     // (16 x 2*128) x (2*128 x 2*C4) real GEMM, split by warps along the
-    // thread (voxel) dimension, on the tensor cores; then the warp slices are
-    // added and one partial per (block, sample, pool, coil) is written
+    // thread (voxel) dimension, on the tensor cores in the three-term TF32
+    // split (big*big + big*small + small*big, each term its own accumulator
+    // chain); then the warp slices are added and one
+    // partial per (block, sample, pool, coil) is written.
+    //   A[row][2j + ri] = (x, y)[ri] of thread j;  B[2j + ri][2c + cmp]:
+    //   (x,x) = rx, (y,x) = ry, (x,y) = -ry, (y,y) = rx.
     auto flush = [&]() {
         __syncthreads();
-        const int g = lane >> 2, tig = lane & 3;
-        for (int nt = 0; nt < C4 / 4; ++nt) {
-            float d[4] = {0.f, 0.f, 0.f, 0.f};
-            const int c = nt * 4 + (g >> 1), cmp = g & 1;
+        const int g = lane >> 2, tig = lane & 3, ri = tig & 1, cmp = g & 1;
+        const bool same = ri == cmp;                              // rx, else ry
+        const uint32_t sgn = (cmp && !ri) ? 0x80000000u : 0u;     // -ry
+        const uint2 *mt2 = reinterpret_cast<const uint2 *>(mtile);  // (big, small) pairs
+        const int nt_all = C4 / 4;
+        float *rw = red + warp * 16 * (2 * C4);
+        for (int nt = 0; nt < nt_all; ++nt) {
+            float acc[3][4];
+#pragma unroll
+            for (int u = 0; u < 3; ++u)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) acc[u][i] = 0.f;
+            const int c = nt * 4 + (g >> 1);
 #pragma unroll
             for (int ks = 0; ks < 8; ++ks) {
-                const int k0 = warp * 64 + ks * 8 + tig, k1 = k0 + 4;
-                const int j0 = k0 >> 1, j1 = k1 >> 1, ri0 = k0 & 1, ri1 = k1 & 1;
-                const float2 m00 = mtile[g * kTRow + j0], m10 = mtile[(g + 8) * kTRow + j0];
-                const float2 m01 = mtile[g * kTRow + j1], m11 = mtile[(g + 8) * kTRow + j1];
-                const float a[4] = {ri0 ? m00.y : m00.x, ri0 ? m10.y : m10.x, ri1 ? m01.y : m01.x,
-                                    ri1 ? m11.y : m11.x};
-                // B[2j + ri][2c + cmp]: (x,x) = rx, (x,y) = -ry, (y,x) = ry, (y,y) = rx
-                const float2 r0 = rsm[c * kTRow + j0], r1 = rsm[c * kTRow + j1];
-                const float b[2] = {cmp ? (ri0 ? r0.x : -r0.y) : (ri0 ? r0.y : r0.x),
-                                    cmp ? (ri1 ? r1.x : -r1.y) : (ri1 ? r1.y : r1.x)};
-                mma_3xtf32(d, a, b);
+                const int j0 = warp * 32 + ks * 4 + (tig >> 1), j1 = j0 + 2;
+                const uint2 a00 = mt2[(g * kTRow + j0) * 2 + ri], a10 = mt2[((g + 8) * kTRow + j0) * 2 + ri];
+                const uint2 a01 = mt2[(g * kTRow + j1) * 2 + ri], a11 = mt2[((g + 8) * kTRow + j1) * 2 + ri];
+                const uint32_t ab[4] = {a00.x, a10.x, a01.x, a11.x};
+                const uint32_t as[4] = {a00.y, a10.y, a01.y, a11.y};
+                const uint4 q0 = rsm[c * kTRow + j0], q1 = rsm[c * kTRow + j1];
+                const uint32_t bb[2] = {(same ? q0.x : q0.z) ^ sgn, (same ? q1.x : q1.z) ^ sgn};
+                const uint32_t bs[2] = {(same ? q0.y : q0.w) ^ sgn, (same ? q1.y : q1.w) ^ sgn};
+                mma_tf32(acc[0], as, bb);
+                mma_tf32(acc[1], ab, bs);
+                mma_tf32(acc[2], ab, bb);
             }
-            float *rw = red + warp * 16 * (2 * C4);
-            rw[g * (2 * C4) + nt * 8 + 2 * tig] = d[0];
-            rw[g * (2 * C4) + nt * 8 + 2 * tig + 1] = d[1];
-            rw[(g + 8) * (2 * C4) + nt * 8 + 2 * tig] = d[2];
-            rw[(g + 8) * (2 * C4) + nt * 8 + 2 * tig + 1] = d[3];
+            float d[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) d[i] = (acc[0][i] + acc[1][i]) + acc[2][i];
+            const int col = nt * 8 + 2 * tig;
+            rw[g * (2 * C4) + col] = d[0];
+            rw[g * (2 * C4) + col + 1] = d[1];
+            rw[(g + 8) * (2 * C4) + col] = d[2];
+            rw[(g + 8) * (2 * C4) + col + 1] = d[3];
         }
         __syncthreads();
         const int nout = a_fill * kNSampP * L.rx;
@@ -488,7 +533,7 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
 #pragma unroll
                 for (int t = 0; t < kNSampP; ++t) {
                     float mx = 0.f, my = 0.f;
-                    const bool sampled = (MODEL != KM_EXCH) || F.all_free || (L.kind[t] == 0);
+                    const bool sampled = (MODEL != KM_EXCH) || FREE || (L.kind[t] == 0);
 #pragma unroll
                     for (int s = 0; s < NS; ++s) {
                         const float2 m = cmul(make_float2(X[s][t], Y[s][t]), Ph[s][t]);
@@ -496,7 +541,7 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                         my += m.y;
                     }
                     if (!(active && sampled)) mx = my = 0.f;
-                    mtile[(a_fill * kNSampP + t) * kTRow + tid] = make_float2(mx, my);
+                    mtile[(a_fill * kNSampP + t) * kTRow + tid] = tf32_split2(mx, my);
                 }
                 if (++a_fill == kTile) flush();
             }
@@ -527,7 +572,7 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                     const float freq = r1.z * 0.15915494309189535f;
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
-                        const bool bound = (MODEL == KM_EXCH) ? (L.kind[t] == 1) : (t == 1);
+                        const bool bound = (MODEL == KM_EXCH) ? (!FREE && L.kind[t] == 1) : (t == 1);
                         if (!bound) continue;
                         if (lc.t2b != t2v[t] || lc.freq != freq) {
                             lc.freq = freq;
@@ -552,7 +597,7 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                     py[t] = Y[s][t];
                     pz[t] = Z[s][t];
                 }
-                if (MODEL == KM_NORMAL || (MODEL == KM_EXCH && F.all_free)) {
+                if (MODEL == KM_NORMAL || (MODEL == KM_EXCH && FREE)) {
                     // every pool free: straight-line updates of all pools
                     if (rf) {
 #pragma unroll

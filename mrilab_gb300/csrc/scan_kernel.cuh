@@ -32,7 +32,7 @@ namespace mrl {
 
 constexpr int kBlock = 128;
 constexpr int kChunk = 256;
-constexpr int kFastChunk = 128;  // steps per staged chunk of the accurate kernel
+constexpr int kFastChunk = 32;  // steps per staged chunk of the accurate kernel
 constexpr int kAdcTile = 16;
 constexpr int kMaxPool = 8;
 constexpr int kMaxPairs = 64 * kMaxPool;

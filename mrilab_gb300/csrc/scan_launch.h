@@ -24,7 +24,7 @@ inline size_t scan_fast_smem_bytes(int stride4, int nsamp, int rx) {
     (void)nsamp;
     const size_t c4 = (size_t)((rx + 3) & ~3);
     const size_t row = kBlock + 2;
-    return 128 + (size_t)2 * kFastChunk * stride4 * 16 + 16 * row * 8 + c4 * row * 8 + (kBlock / 32) * 16 * 2 * c4 * 4;
+    return 128 + (size_t)2 * kFastChunk * stride4 * 16 + 16 * row * 16 + c4 * row * 16 + (kBlock / 32) * 16 * 2 * c4 * 4;
 }
 
 cudaError_t launch_scan_ref_normal(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);

@@ -201,3 +201,33 @@ def test_accurate_two_pool_3d_multiecho(built):
     print(f"config2 shrunk: accurate GPU vs FP64 {err:.3e}; FP32 reference algorithm vs FP64 "
           f"{rel_l2(signal(f32), signal(f64)):.3e}")
     assert err <= TOL_FP64
+
+
+def test_device_sincos_error_bounds(built):
+    """The accurate kernel's own sine/cosine (Cody-Waite reduction + Taylor
+    polynomials) against FP64 sin/cos of the same float arguments: absolute
+    error within 2.5e-7 (about 2 ulp at 1) up to |x| = 1000, and relative
+    error of the sine within 3e-7 for the small per-step rotation angles."""
+    import ctypes
+
+    lib = engine.library()
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.mrl_selftest_sincos.argtypes = [fp, fp, fp, ctypes.c_int]
+    lib.mrl_selftest_sincos.restype = ctypes.c_int
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(-np.pi, np.pi, 200000), rng.uniform(-1000, 1000, 200000),
+                        np.geomspace(1e-9, 0.8, 20000), -np.geomspace(1e-9, 0.8, 20000),
+                        np.arange(-64, 65) * (np.pi / 4), [0.0]]).astype(np.float32)
+    sn = np.empty_like(x)
+    cs = np.empty_like(x)
+    rc = lib.mrl_selftest_sincos(x.ctypes.data_as(fp), sn.ctypes.data_as(fp), cs.ctypes.data_as(fp), x.size)
+    assert rc == 0
+    xd = x.astype(np.float64)
+    err_s = np.abs(sn - np.sin(xd))
+    err_c = np.abs(cs - np.cos(xd))
+    print(f"max abs error: sin {err_s.max():.2e}, cos {err_c.max():.2e}")
+    assert err_s.max() <= 2.5e-7 and err_c.max() <= 2.5e-7
+    small = np.abs(xd) <= 0.8
+    rel = err_s[small] / np.maximum(np.abs(np.sin(xd[small])), 1e-30)
+    print(f"max relative sine error for |x| <= 0.8: {rel.max():.2e}")
+    assert rel.max() <= 3e-7
