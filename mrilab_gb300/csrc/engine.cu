@@ -49,18 +49,51 @@ void set_err(const char *fmt, ...) {
 // Receive reduction: Sx/Sy[pool][coil][signal] = sum over blocks of the
 // per-block partial sums, in FP64, then demodulated by rfRef
 // (BlochKernel.cuh:160-170 applies the same rotation per isochromat).
-__global__ void reduce_partials(const float2 *__restrict__ partial, int nblk, int a_launch, int npairs, int rx,
-                                const int *__restrict__ amap, int A, double *sx, double *sy, double cr, double sr) {
-    const int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= a_launch * npairs) return;
+// A block takes 32 consecutive (sample, pool, coil) outputs; its 8 warps
+// split the scan blocks (warp w sums blocks w, w + 8, ...; 256-byte loads)
+// and their sums are added in a fixed order, so results are reproducible.
+constexpr int kRedWarps = 8;
+__global__ void __launch_bounds__(32 * kRedWarps)
+    reduce_partials(const float2 *__restrict__ partial, int nblk, int a_launch, int npairs, int rx,
+                    const int *__restrict__ amap, int A, double *sx, double *sy, double cr, double sr) {
+    __shared__ double2 red[kRedWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int o = blockIdx.x * 32 + lane;
+    const int tot = a_launch * npairs;
+    double x = 0.0, y = 0.0;
+    if (o < tot) {
+        const size_t stride = (size_t)a_launch * npairs;
+        const float2 *p = partial + o;
+        int b = w;
+        for (; b + 3 * kRedWarps < nblk; b += 4 * kRedWarps) {
+            const float2 p0 = p[(size_t)b * stride], p1 = p[(size_t)(b + kRedWarps) * stride];
+            const float2 p2 = p[(size_t)(b + 2 * kRedWarps) * stride], p3 = p[(size_t)(b + 3 * kRedWarps) * stride];
+            x += (double)p0.x;
+            y += (double)p0.y;
+            x += (double)p1.x;
+            y += (double)p1.y;
+            x += (double)p2.x;
+            y += (double)p2.y;
+            x += (double)p3.x;
+            y += (double)p3.y;
+        }
+        for (; b < nblk; b += kRedWarps) {
+            const float2 q = p[(size_t)b * stride];
+            x += (double)q.x;
+            y += (double)q.y;
+        }
+    }
+    red[w][lane] = make_double2(x, y);
+    __syncthreads();
+    if (w != 0 || o >= tot) return;
+    x = 0.0;
+    y = 0.0;
+    for (int k = 0; k < kRedWarps; ++k) {
+        x += red[k][lane].x;
+        y += red[k][lane].y;
+    }
     const int a = o / npairs;
     const int pair = o - a * npairs;
-    double x = 0.0, y = 0.0;
-    for (int b = 0; b < nblk; ++b) {
-        const float2 p = partial[((long long)b * a_launch + a) * npairs + pair];
-        x += (double)p.x;
-        y += (double)p.y;
-    }
     const int sig = amap[a];
     if (sig < 0 || sig >= A) return;
     const int t = pair / rx;
@@ -97,9 +130,8 @@ struct GatherArgs {
     float *m;       // d_m: mx | my | mz, [P][S][n] each
     float2 *rxc;    // [Rx][n]
     float2 *f2;     // frame coefficients, null for reference numerics
-    size_t o_om, o_wr, o_txc;
+    size_t o_om, o_txc;
     double gyro;
-    double cs2pi[kMaxPool];  // 2 pi CS[t]
 };
 
 __device__ __forceinline__ float2 split_df(double v) {
@@ -143,7 +175,6 @@ __global__ void gather_object(GatherArgs G) {
             G.m[dst] = r.mx[src];
             G.m[ns + dst] = r.my[src];
             G.m[2 * ns + dst] = r.mz[src];
-            if (G.f2) G.f2[G.o_wr + dst] = split_df((double)w + G.cs2pi[t]);
         }
     }
     for (int k = 0; k < G.nk; ++k) f[G.o_k + k * n + i] = r.k[k * V + v];
@@ -233,11 +264,11 @@ struct Scanner {
     // accurate integrator: frame coefficients and moments
     bool fast = false;
     FrameMoments fmom;
-    DevBuf<float2> d_f2;  // omega [4][n] | wres [P][S][n] | txc [Tx][n]
+    DevBuf<float2> d_f2;  // omega [4][n] | txc [Tx][n]
     DevBuf<float> d_raw;  // the caller's arrays as uploaded (RawObject)
     DevBuf<int> d_act;    // compact index -> voxel, on the device
     RawObject raw{};
-    size_t o_om = 0, o_wr = 0, o_txc = 0;
+    size_t o_om = 0, o_txc = 0;
     std::vector<float> frec;
     // offsets into d_f
     size_t o_gx = 0, o_gy = 0, o_gz = 0, o_db0 = 0, o_txmg = 0, o_txpe = 0, o_rho = 0, o_t1 = 0, o_t2 = 0, o_k = 0,
@@ -334,7 +365,7 @@ struct Scanner {
                 return set_err("bound-pool saturation with several Tx coils needs MRL_NUMERICS_REFERENCE"),
                        MRL_ERR_UNSUPPORTED;
         }
-        NS = spins_per_thread(S);
+        NS = spins_per_thread(S, P);
         if (const char *e = getenv("MRL_SPINS_PER_THREAD")) {
             const int ns = atoi(e);
             if ((ns == 1 || ns == 2 || ns == 4) && S % ns == 0) NS = ns;
@@ -366,8 +397,7 @@ struct Scanner {
         o_dwr = take(n * P * S);
         if (fast) {
             o_om = 0;
-            o_wr = 4 * n;
-            o_txc = o_wr + (size_t)P * S * n;
+            o_txc = 4 * n;
         }
         phase("active voxels");
         const bool rxmap = a.coil.rx_default == 0;
@@ -454,9 +484,8 @@ struct Scanner {
             G.m = d_m.p;
             G.rxc = d_rx.p;
             G.f2 = fast ? d_f2.p : nullptr;
-            G.o_om = o_om, G.o_wr = o_wr, G.o_txc = o_txc;
+            G.o_om = o_om, G.o_txc = o_txc;
             G.gyro = a.obj.gyro;
-            for (int t = 0; t < kMaxPool; ++t) G.cs2pi[t] = (t < P && a.ctl.cs) ? 2 * kPiRef * a.ctl.cs[t] : 0.0;
             gather_object<<<(n_act + 255) / 256, 256, 0, st>>>(G);
             if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "gather launch");
         }
@@ -559,9 +588,12 @@ struct Scanner {
         const long long nthreads = (long long)n_act * tpv;
         return std::max(1LL, (nthreads + kBlock - 1) / kBlock);
     }
+    // receive partial sums of one sample: one per block (reference order)
+    // or per warp (accurate kernel)
+    long long n_slices() const { return n_blocks() * partial_slices(fast); }
 
     // Split a decoded chunk into launches whose receive partials fit the
-    // budget (MRL_PARTIAL_MB, default 1 GiB), upload its step records and
+    // budget (MRL_PARTIAL_MB, default 4 GiB), upload its step records and
     // ADC map, and size the partial buffer.
     int prepare_chunk(const DecodeChunk &ch, std::vector<LaunchDesc> &out) {
         out.clear();
@@ -569,9 +601,9 @@ struct Scanner {
         if (ch.n_steps == 0) return MRL_OK;
         const int npairs = mi.nsamp * RX;
         const char *env = getenv("MRL_PARTIAL_MB");
-        const double budget = (env ? atof(env) : 1024.0) * 1048576.0;
+        const double budget = (env ? atof(env) : 4096.0) * 1048576.0;
         const long long a_max =
-            std::max(1LL, (long long)(budget / ((double)n_blocks() * npairs * sizeof(float2))));
+            std::max(1LL, (long long)(budget / ((double)n_slices() * npairs * sizeof(float2))));
         long long s0 = 0;
         int a_off = 0, a_cnt = 0, a_peak = 0;
         for (long long q = 0; q < ch.n_steps; ++q) {
@@ -598,7 +630,7 @@ struct Scanner {
         if ((e = d_rec.ensure(recs->size() / 4)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(steps)");
         if ((e = d_amap.ensure(std::max<size_t>(1, amap_host.size()))) != cudaSuccess)
             return fail_cuda(e, "cudaMalloc(amap)");
-        if ((e = d_part.ensure((size_t)n_blocks() * std::max(1, a_peak) * npairs)) != cudaSuccess)
+        if ((e = d_part.ensure((size_t)n_slices() * std::max(1, a_peak) * npairs)) != cudaSuccess)
             return fail_cuda(e, "cudaMalloc(partials)");
         auto t0 = std::chrono::steady_clock::now();
         if ((e = cudaMemcpyAsync(d_rec.p, recs->data(), recs->size() * sizeof(float), cudaMemcpyHostToDevice, st)) !=
@@ -622,7 +654,7 @@ struct Scanner {
         L.rec = d_rec.p;
         L.partial = d_part.p;
         const int nblk = (int)n_blocks();
-        const size_t smem = fast ? scan_fast_smem_bytes(stride4, mi.nsamp, RX) : scan_smem_bytes(stride4, mi.nsamp);
+        const size_t smem = fast ? scan_fast_smem_bytes(stride4, RX, P, NS) : scan_smem_bytes(stride4, mi.nsamp);
         const double cr = std::cos(-rf_ref), sr = std::sin(-rf_ref);
         cudaError_t e;
         for (const LaunchDesc &d : ls) {
@@ -643,9 +675,13 @@ struct Scanner {
                     F.b = L;
                     const size_t n = std::max(1, n_act);
                     F.omega = d_f2.p + o_om;
-                    F.wres = d_f2.p + o_wr;
                     F.txc = d_f2.p + o_txc;
                     F.all_free = all_free();
+                    for (int t = 0; t < kMaxPool; ++t) {  // 2 pi CS[t] as a (hi, lo) pair
+                        const double w = (t < P && args->ctl.cs) ? 2 * kPiRef * args->ctl.cs[t] : 0.0;
+                        F.cs_hi[t] = (float)w;
+                        F.cs_lo[t] = (float)(w - (double)F.cs_hi[t]);
+                    }
                     (void)n;
                     switch (mi.km) {
                     case KM_NORMAL: e = launch_scan_fast_normal(P, NS, grid, smem, stream, F); break;
@@ -674,7 +710,8 @@ struct Scanner {
                     cudaEventRecord(r0, stream);
                 }
                 const int tot = d.a_count * L.npairs;
-                reduce_partials<<<(tot + 255) / 256, 256, 0, stream>>>(d_part.p, nblk, d.a_count, L.npairs, RX,
+                reduce_partials<<<(tot + 31) / 32, 32 * kRedWarps, 0, stream>>>(d_part.p, (int)n_slices(), d.a_count,
+                                                                                  L.npairs, RX,
                                                                        d_amap.p + d.a_off, A, d_sx.p, d_sy.p, cr, sr);
                 if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "reduce launch");
                 launches++;
@@ -816,6 +853,16 @@ cudaError_t noalloc_scratch(int dev, unsigned char **out) {
     }
     *out = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
     return cudaSuccess;
+}
+
+// TF32 rounding of the receive contraction: integer form and the
+// hardware conversion side by side (hook of their equality test).
+__global__ void tf32_probe(const float *x, uint32_t *rn, uint32_t *cvt, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        rn[i] = tf32_rn(x[i]);
+        cvt[i] = to_tf32(x[i]);
+    }
 }
 
 // Device sine/cosine of the accurate kernel on caller-given arguments: the
@@ -1031,7 +1078,8 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
     const int n = (int)sc.V;
     const long long nblk = std::max(1LL, ((long long)n * sc.tpv + kBlock - 1) / kBlock);
     const int npairs = sc.mi.nsamp * sc.RX;
-    const double per_sample = sizeof(int) + (double)nblk * npairs * sizeof(float2);
+    const long long nslices = nblk * partial_slices(true);
+    const double per_sample = sizeof(int) + (double)nslices * npairs * sizeof(float2);
     const long long a_cap = (long long)((kNoAllocScratchBytes - 256) / per_sample);
     if (a_cap < 1) {
         set_err("object too large for the %zu-byte scratch: one ADC sample needs %.0f bytes", kNoAllocScratchBytes,
@@ -1090,7 +1138,7 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
         F.cs_hi[t] = (float)w;
         F.cs_lo[t] = (float)(w - (double)F.cs_hi[t]);
     }
-    const size_t smem = scan_fast_smem_bytes(sc.stride4, sc.mi.nsamp, sc.RX);
+    const size_t smem = scan_fast_smem_bytes(sc.stride4, sc.RX, sc.P, sc.NS);
     const double rf_ref = args->var.rf_ref ? *args->var.rf_ref : 0.0;
     const double cr = std::cos(-rf_ref), sr = std::sin(-rf_ref);
     // walk the steps, one launch per a_cap samples
@@ -1114,7 +1162,8 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
         if (le != cudaSuccess) return sc.fail_cuda(le, "scan kernel launch");
         if (!amap.empty()) {
             const int tot = (int)amap.size() * npairs;
-            reduce_partials<<<(tot + 255) / 256, 256, 0, st>>>(d_part, (int)nblk, (int)amap.size(), npairs, sc.RX,
+            reduce_partials<<<(tot + 31) / 32, 32 * kRedWarps, 0, st>>>(d_part, (int)nslices, (int)amap.size(), npairs,
+                                                                        sc.RX,
                                                                d_amap, sc.A, args->sig.sx, args->sig.sy, cr, sr);
             if ((le = cudaGetLastError()) != cudaSuccess) return sc.fail_cuda(le, "reduce launch");
         }
@@ -1174,6 +1223,28 @@ int mrl_selftest_sincos(const float *x, float *sn, float *cs, int n) {
     if (e == cudaSuccess) e = cudaMemcpy(cs, d.p + 2 * n, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {
         set_err("selftest sincos: %s", cudaGetErrorString(e));
+        return MRL_ERR_CUDA;
+    }
+    return MRL_OK;
+}
+
+// Test hook (not declared in mrl_scan.h): the accurate kernel's TF32
+// rounding and the hardware conversion of n host floats.
+int mrl_selftest_tf32(const float *x, uint32_t *rn, uint32_t *cvt, int n) {
+    using namespace mrl;
+    if (!x || !rn || !cvt || n < 0) return MRL_ERR_ARG;
+    if (n == 0) return MRL_OK;
+    DevBuf<uint32_t> d;
+    cudaError_t e = d.ensure((size_t)3 * n);
+    if (e == cudaSuccess) e = cudaMemcpy(d.p, x, (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        tf32_probe<<<(n + 255) / 256, 256>>>(reinterpret_cast<const float *>(d.p), d.p + n, d.p + 2 * n, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(rn, d.p + n, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(cvt, d.p + 2 * n, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_err("selftest tf32: %s", cudaGetErrorString(e));
         return MRL_ERR_CUDA;
     }
     return MRL_OK;

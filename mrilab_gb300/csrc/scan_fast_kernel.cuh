@@ -1,27 +1,32 @@
 // The MRL_NUMERICS_ACCURATE scan kernel: the same sequence model and tissue
 // models as scan_ref_kernel (BlochKernel{,ME,MT,CEST,GM}.cuh), integrated
-// in single precision in a rotating frame so that it is both faster and
+// in single precision in rotating frames so that it is both faster and
 // closer to the exact (FP64) solution than the reference's own FP32 code.
 //
-// Frame.  Each isochromat-pool keeps its magnetisation in a frame rotating
-// with its free precession: m_lab = m_frame * P, P = exp(-i Phi), with
-//   Phi = gamma (dB0 T + x Kx + y Ky + z Kz) + w_res T,
+// Frames.  Pool t of a voxel has one frame, shared by the voxel's spins:
+// m_lab = m_frame * P_t, P_t = exp(-i Phi_t), with
+//   Phi_t = gamma (dB0 T + x Kx + y Ky + z Kz) + 2 pi CS_t T,
 // T and K the elapsed time and gradient areas over the steps without rf
-// (moments carried on the host in FP64 and passed as hi/lo float pairs),
-// and w_res = dWRnd + 2 pi CS the isochromat's residual frequency (hi/lo).
-// Free precession therefore never rotates m: only the phasor P advances,
-// by a factor (1 + d) with d = exp(-i theta) - 1 evaluated once per change
-// of (dt, G); P is recomputed exactly from the moments (double-float
-// arithmetic, Cody-Waite reduction) at every change of (dt, G), every rf
-// step and at least every kAnchorEvery steps, so its error never
-// accumulates.  An rf step rotates m_frame about the effective field with
-// the rf azimuth shifted by -Phi (exact identity of the reference's closed
-// form, BlochKernel.cuh:241-254).
+// (moments carried on the host in FP64 and passed as hi/lo float pairs).
+// Between anchors P_t advances by a factor (1 + d_t), d_t = exp(-i theta) - 1
+// evaluated once per change of (dt, G); P_t is recomputed exactly from the
+// moments (double-float arithmetic, Cody-Waite reduction) at every change
+// of (dt, G), every rf step and at least every kAnchorEvery steps, so the
+// large gradient and off-resonance phases never accumulate rounding.  In
+// its pool's frame an isochromat only sees its own small residual
+// frequency dWRnd, relaxation and exchange: a free step is the increment
+//   m += dm m + sum_p f_tp (P_p,before / P_t,after) m_p,
+// dm = (1 - a) exp(-i dWRnd dt) - 1 in "1 - y" form (a the transverse decay
+// of the step), f_tp the exchange inflow.  An rf step rotates the frame
+// magnetisation about the effective field with the rf azimuth shifted by
+// -Phi_t (exact identity of the reference's closed form,
+// BlochKernel.cuh:241-254) while the frame holds still.
 //
 // Coefficients close to 1 are applied in "1 - y" form: relaxation
 // exp(-dt/T) = 1 - y with y = -expm1(-dt/T), exchange exp(-k dt) likewise,
 // so repeated multiplication does not accumulate the rounding of a stored
-// factor.  The receive sum rotates each frame back to the lab with P.
+// factor.  The receive sums a pool's spins in the frame and rotates the
+// sum back to the lab with P_t.
 #pragma once
 
 #include "decode.h"
@@ -32,10 +37,9 @@ namespace mrl {
 struct FastLaunch {
     ScanLaunch b;             // shared fields; b.rec points at fast records
     const float2 *omega;      // [4][n_act] (hi, lo) of gamma*dB0, gamma*x, gamma*y, gamma*z
-    const float2 *wres;       // [P][S][n_act] (hi, lo) residual frequency, rad/s
     const float2 *txc;        // [tx][n_act] TxCoilmg * exp(i TxCoilpe)
     // Direct layout (mrl_scan_noalloc): the arrays of ScanLaunch are the
-    // caller's uncompacted MATLAB arrays (n = every voxel), and the three
+    // caller's uncompacted MATLAB arrays (n = every voxel), and the two
     // derived fields above are computed here instead of being read.
     int direct;
     int all_free;             // KM_EXCH: every pool is free (ME, or GM without bound pools): selects
@@ -141,11 +145,16 @@ __device__ __forceinline__ float2 cmul_conj(float2 a, float2 b) {  // a * conj(b
 }
 
 // ---- receive contraction on the tensor cores --------------------------------
+// The hardware conversion, kept as the check of tf32_rn.
 __device__ __forceinline__ uint32_t to_tf32(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
     return r;
 }
+
+// x rounded to TF32 (10-bit mantissa), to nearest with ties away from zero:
+// the bits cvt.rna.tf32.f32 gives for finite x, in two integer operations.
+__device__ __forceinline__ uint32_t tf32_rn(float x) { return (__float_as_uint(x) + 0x1000u) & 0xffffe000u; }
 
 // D += A (16x8, row) * B (8x8, col), TF32 inputs, FP32 accumulate
 __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
@@ -154,13 +163,6 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], 
         "{%0,%1,%2,%3};"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// (x, y) as TF32 (big, small) parts: x = big + small to ~2^-22 relative,
-// for the three-term TF32 product big*big + big*small + small*big
-__device__ __forceinline__ uint4 tf32_split2(float x, float y) {
-    const uint32_t xb = to_tf32(x), yb = to_tf32(y);
-    return make_uint4(xb, to_tf32(x - __uint_as_float(xb)), yb, to_tf32(y - __uint_as_float(yb)));
 }
 
 // y = 1 - exp(-x)
@@ -195,29 +197,45 @@ __device__ __forceinline__ void rf_rotate(float &x, float &y, float &z, float dW
     z = z2;
 }
 
+// Pools with a frame: every pool but the bound pool (pool 1) of MT / CEST,
+// which has no transverse magnetisation.
+template <int MODEL>
+__device__ __forceinline__ constexpr bool has_frame(int t) {
+    return !((MODEL == KM_MT || MODEL == KM_CEST) && t == 1);
+}
+
 // FREE (KM_EXCH only): every pool is a free pool (ME, or GM without bound
-// pools); the instantiation then has only the straight-line update path.
+// pools); the instantiation then carries no pool-kind tests.
+// Resident blocks per SM the register allocation aims at: four (16 warps)
+// while a thread's isochromat state is small.
+template <int P, int NS>
+constexpr int fast_min_blocks() {
+    return (P <= 2 && P * NS <= 8) ? 4 : ((P <= 3 && P * NS <= 6) ? 3 : 2);
+}
+
 template <int MODEL, int P, int NS, bool FREE>
-__global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
+__global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>()) scan_fast_kernel(FastLaunch F) {
     const ScanLaunch &L = F.b;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     float4 *rbuf = reinterpret_cast<float4 *>(smem + 128);
     const int rstride = L.stride4;
+    constexpr bool kMTC = MODEL == KM_MT || MODEL == KM_CEST;
     // receive tile: one row per (sample, sampled pool), one column per thread
-    // holding its lab-frame transverse magnetisation as TF32 (big, small)
-    // parts (x big, x small, y big, y small); the coil sensitivities of the
-    // threads' voxels split the same way (x big, x small, y big, y small);
-    // per-warp sums of the contraction
-    constexpr int kNSampP = (MODEL == KM_MT || MODEL == KM_CEST) ? 1 : P;
+    // holding its lab-frame transverse magnetisation; the coil sensitivities
+    // of the threads' voxels; per-warp sums of the contraction; then
+    // per-thread values read only at anchors, state changes and rf steps:
+    // the isochromats' dWRnd and the low parts of gamma * (dB0, x, y, z)
+    constexpr int kNSampP = kMTC ? 1 : P;
     constexpr int kTile = (16 / kNSampP) < 1 ? 1 : 16 / kNSampP;  // samples per flush
-    constexpr int kTRow = kBlock + 2;                             // padded row (uint4)
-    const int C4 = (L.rx + 3) & ~3;
-    uint4 *mtile = reinterpret_cast<uint4 *>(rbuf + 2 * kFastChunk * rstride);  // [16][kTRow]
-    uint4 *rsm = mtile + 16 * kTRow;                                             // [C4][kTRow]
-    float *red = reinterpret_cast<float *>(rsm + C4 * kTRow);                    // [warp][16][2*C4]
+    constexpr int kTRow = kBlock + 2;                             // padded row (float2)
     constexpr int kWarps = kBlock / 32;
-    constexpr bool kFreeAll = MODEL == KM_NORMAL || MODEL == KM_EXCH;
+    const int C4 = (L.rx + 3) & ~3;
+    float2 *mtile = reinterpret_cast<float2 *>(rbuf + 2 * kFastChunk * rstride);  // [16][kTRow]
+    float2 *rsm = mtile + 16 * kTRow;                                              // [C4][kTRow]
+    float *wstage = reinterpret_cast<float *>(rsm + C4 * kTRow);                   // [warp][16][2*C4]
+    float *dwsm = wstage + kWarps * 16 * 2 * C4;                                   // [NS * P][kBlock]
+    float *omlo = dwsm + NS * P * kBlock;                                        // [4][kBlock]
 
     const int tid = threadIdx.x;
     const long long gt = (long long)blockIdx.x * kBlock + tid;
@@ -227,11 +245,11 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
     const int n = L.n_act;
 
     float X[NS][P], Y[NS][P], Z[NS][P];
-    float2 Ph[NS][P], D[NS][P];
-    float Wh[NS][P], Wl[NS][P];
+    float2 dm[NS][P];     // free-step increment of the frame magnetisation
+    float2 Pc[P], Dc[P];  // frame phasor of each pool and its free-step increment
     float rhoS[P], it1[P], it2[P], t2v[P], y1[P], y2[P];
     unsigned act = 0;
-    float2 om[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    float om[4] = {0.f, 0.f, 0.f, 0.f};  // high parts of gamma * (dB0, x, y, z)
     float2 tx0 = make_float2(0.f, 0.f);
     float db0 = 0.f;
     constexpr int kNK = MODEL == KM_EXCH ? P * P : (MODEL == KM_MT ? 2 : (MODEL == KM_CEST ? 2 * (P - 1) : 1));
@@ -241,11 +259,12 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
 #pragma unroll
     for (int t = 0; t < P; ++t) {
         rhoS[t] = it1[t] = it2[t] = t2v[t] = y1[t] = y2[t] = 0.f;
+        Pc[t] = make_float2(1.f, 0.f);
+        Dc[t] = make_float2(0.f, 0.f);
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
-            X[s][t] = Y[s][t] = Z[s][t] = Wh[s][t] = Wl[s][t] = 0.f;
-            Ph[s][t] = make_float2(1.f, 0.f);
-            D[s][t] = make_float2(0.f, 0.f);
+            X[s][t] = Y[s][t] = Z[s][t] = 0.f;
+            dm[s][t] = make_float2(0.f, 0.f);
         }
     }
     if (active) {
@@ -255,14 +274,19 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const df p = df_mul(F.gam_hi, F.gam_lo, g[i], 0.f);
-                om[i] = make_float2(p.hi, p.lo);
+                om[i] = p.hi;
+                omlo[i * kBlock + tid] = p.lo;
             }
             float sp, cp;
             sincos_cw(L.txpe[v], sp, cp);
             tx0 = make_float2(L.txmg[v] * cp, L.txmg[v] * sp);
         } else {
 #pragma unroll
-            for (int i = 0; i < 4; ++i) om[i] = F.omega[(long long)i * n + v];
+            for (int i = 0; i < 4; ++i) {
+                const float2 o = F.omega[(long long)i * n + v];
+                om[i] = o.x;
+                omlo[i * kBlock + tid] = o.y;
+            }
             tx0 = F.txc[v];
         }
 #pragma unroll
@@ -291,21 +315,34 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                 X[s][t] = L.mx[i];
                 Y[s][t] = L.my[i];
                 Z[s][t] = L.mz[i];
-                if (F.direct) {
-                    const df w = two_sum(L.dwrnd[i], F.cs_hi[t]);
-                    Wh[s][t] = w.hi;
-                    Wl[s][t] = w.lo + F.cs_lo[t];
-                } else {
-                    const float2 w = F.wres[i];
-                    Wh[s][t] = w.x;
-                    Wl[s][t] = w.y;
-                }
+                dwsm[(s * P + t) * kBlock + tid] = L.dwrnd[i];
             }
         }
     }
     if (F.direct) {
-        const bool any = (MODEL == KM_MT || MODEL == KM_CEST) ? (act & 1u) != 0 : act != 0;
+        const bool any = kMTC ? (act & 1u) != 0 : act != 0;
         if (!any) active = false;
+    }
+    // pools whose magnetisation the step integrates; the others keep their
+    // lab-frame magnetisation (the reference skips them)
+    unsigned evo = 0;
+#pragma unroll
+    for (int t = 0; t < P; ++t) {
+        bool e;
+        if (kMTC)
+            e = true;
+        else if (MODEL == KM_NORMAL || FREE)
+            e = (act >> t & 1u) != 0;
+        else
+            e = (act >> t & 1u) && (L.kind[t] == 0 || L.kind[t] == 1);
+        if (e) evo |= 1u << t;
+    }
+    // transverse pools among them (GM: free pools only)
+    unsigned tvo = evo;
+    if (MODEL == KM_EXCH && !FREE) {
+#pragma unroll
+        for (int t = 0; t < P; ++t)
+            if (L.kind[t] != 0) tvo &= ~(1u << t);
     }
     // stage this thread's voxel's coil sensitivities (zero beyond the coil count)
     for (int c = 0; c < C4; ++c) {
@@ -318,9 +355,9 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
             else
                 r = L.rxc[(long long)c * n + v];
         }
-        rsm[c * kTRow + tid] = tf32_split2(r.x, r.y);
+        rsm[c * kTRow + tid] = r;
     }
-    // the isochromats enter the frame at the start of the launch: m_frame = m_lab / P
+    // the isochromats enter their frames at the first step: m_frame = m_lab / P_t
     bool entered = false;
     // exchange / MT coefficients, cached per dt
     float yo[P], fin[P][P];
@@ -357,18 +394,19 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
     // (16 x 2*128) x (2*128 x 2*C4) real GEMM, split by warps along the
     // thread (voxel) dimension, on the tensor cores in the three-term TF32
     // split (big*big + big*small + small*big, each term its own accumulator
-    // chain); then the warp slices are added and one
-    // partial per (block, sample, pool, coil) is written.
+    // chain); then the warp slices are added and one partial per (block,
+    // sample, pool, coil) is written.
     //   A[row][2j + ri] = (x, y)[ri] of thread j;  B[2j + ri][2c + cmp]:
     //   (x,x) = rx, (y,x) = ry, (x,y) = -ry, (y,y) = rx.
     auto flush = [&]() {
         __syncthreads();
         const int g = lane >> 2, tig = lane & 3, ri = tig & 1, cmp = g & 1;
-        const bool same = ri == cmp;                              // rx, else ry
-        const uint32_t sgn = (cmp && !ri) ? 0x80000000u : 0u;     // -ry
-        const uint2 *mt2 = reinterpret_cast<const uint2 *>(mtile);  // (big, small) pairs
+        const int bcomp = (ri == cmp) ? 0 : 1;                 // rx, else ry
+        const uint32_t sgn = (cmp && !ri) ? 0x80000000u : 0u;  // -ry
+        const float *mt1 = reinterpret_cast<const float *>(mtile) + ri;
+        const float *rs1 = reinterpret_cast<const float *>(rsm) + bcomp;
         const int nt_all = C4 / 4;
-        float *rw = red + warp * 16 * (2 * C4);
+        float *rw = wstage + warp * 16 * (2 * C4);
         for (int nt = 0; nt < nt_all; ++nt) {
             float acc[3][4];
 #pragma unroll
@@ -379,13 +417,21 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
 #pragma unroll
             for (int ks = 0; ks < 8; ++ks) {
                 const int j0 = warp * 32 + ks * 4 + (tig >> 1), j1 = j0 + 2;
-                const uint2 a00 = mt2[(g * kTRow + j0) * 2 + ri], a10 = mt2[((g + 8) * kTRow + j0) * 2 + ri];
-                const uint2 a01 = mt2[(g * kTRow + j1) * 2 + ri], a11 = mt2[((g + 8) * kTRow + j1) * 2 + ri];
-                const uint32_t ab[4] = {a00.x, a10.x, a01.x, a11.x};
-                const uint32_t as[4] = {a00.y, a10.y, a01.y, a11.y};
-                const uint4 q0 = rsm[c * kTRow + j0], q1 = rsm[c * kTRow + j1];
-                const uint32_t bb[2] = {(same ? q0.x : q0.z) ^ sgn, (same ? q1.x : q1.z) ^ sgn};
-                const uint32_t bs[2] = {(same ? q0.y : q0.w) ^ sgn, (same ? q1.y : q1.w) ^ sgn};
+                const float a[4] = {mt1[2 * (g * kTRow + j0)], mt1[2 * ((g + 8) * kTRow + j0)],
+                                    mt1[2 * (g * kTRow + j1)], mt1[2 * ((g + 8) * kTRow + j1)]};
+                const float b[2] = {__uint_as_float(__float_as_uint(rs1[2 * (c * kTRow + j0)]) ^ sgn),
+                                    __uint_as_float(__float_as_uint(rs1[2 * (c * kTRow + j1)]) ^ sgn)};
+                uint32_t ab[4], as[4], bb[2], bs[2];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    ab[i] = tf32_rn(a[i]);
+                    as[i] = tf32_rn(a[i] - __uint_as_float(ab[i]));
+                }
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    bb[i] = tf32_rn(b[i]);
+                    bs[i] = tf32_rn(b[i] - __uint_as_float(bb[i]));
+                }
                 mma_tf32(acc[0], as, bb);
                 mma_tf32(acc[1], ab, bs);
                 mma_tf32(acc[2], ab, bb);
@@ -400,6 +446,7 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
             rw[(g + 8) * (2 * C4) + col + 1] = d[3];
         }
         __syncthreads();
+        const float *red = wstage;
         const int nout = a_fill * kNSampP * L.rx;
         for (int o = tid; o < nout; o += kBlock) {
             const int row = o / L.rx;  // = a * kNSampP + t
@@ -436,40 +483,33 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
             if (k == 0 && q == 0) flags |= kFlagState | kFlagDt;  // a launch may start inside a run
             const float dt = r0.x;
 
-            // ---- frame phasors ---------------------------------------------
+            // ---- frame phasors, exact from the moments ----------------------
             if (active && ((flags & kFlagAnchor) || !entered)) {
                 const float4 r2 = cb[q * rstride + 2];
                 const float4 r3 = cb[q * rstride + 3];
-                df phc = df_mul(om[0].x, om[0].y, r2.x, r2.y);
-                phc = df_add(phc, df_mul(om[1].x, om[1].y, r2.z, r2.w));
-                phc = df_add(phc, df_mul(om[2].x, om[2].y, r3.x, r3.y));
-                phc = df_add(phc, df_mul(om[3].x, om[3].y, r3.z, r3.w));
+                df phc = df_mul(om[0], omlo[0 * kBlock + tid], r2.x, r2.y);
+                phc = df_add(phc, df_mul(om[1], omlo[1 * kBlock + tid], r2.z, r2.w));
+                phc = df_add(phc, df_mul(om[2], omlo[2 * kBlock + tid], r3.x, r3.y));
+                phc = df_add(phc, df_mul(om[3], omlo[3 * kBlock + tid], r3.z, r3.w));
 #pragma unroll
-                for (int s = 0; s < NS; ++s)
+                for (int t = 0; t < P; ++t) {
+                    if (!has_frame<MODEL>(t)) continue;
+                    const float2 pn = phasor(df_add(phc, df_mul(F.cs_hi[t], F.cs_lo[t], r2.x, r2.y)));
+                    if (!entered) {
 #pragma unroll
-                    for (int t = 0; t < P; ++t) {
-                        const float2 pn = phasor(df_add(phc, df_mul(Wh[s][t], Wl[s][t], r2.x, r2.y)));
-                        if (!entered) {  // m_frame = m_lab * conj(P)
+                        for (int s = 0; s < NS; ++s) {  // m_frame = m_lab * conj(P)
                             const float2 m = cmul_conj(make_float2(X[s][t], Y[s][t]), pn);
                             X[s][t] = m.x;
                             Y[s][t] = m.y;
                         }
-                        Ph[s][t] = pn;
                     }
+                    Pc[t] = pn;
+                }
                 entered = true;
             }
             const float gzt = r0.y, gyt = r0.z, gxt = r0.w;
             // instantaneous common off-resonance (rad/s)
-            const float wc = fmaf(om[3].x, gzt, fmaf(om[2].x, gyt, fmaf(om[1].x, gxt, om[0].x)));
-            if (active && (flags & kFlagState)) {
-#pragma unroll
-                for (int s = 0; s < NS; ++s)
-#pragma unroll
-                    for (int t = 0; t < P; ++t)
-                        D[s][t] = (MODEL == KM_MT || MODEL == KM_CEST || (act >> t & 1u))
-                                      ? phase_step((wc + Wh[s][t]) * dt)
-                                      : make_float2(0.f, 0.f);
-            }
+            const float wc = fmaf(om[3], gzt, fmaf(om[2], gyt, fmaf(om[1], gxt, om[0])));
             if (active && (flags & kFlagDt)) {
 #pragma unroll
                 for (int t = 0; t < P; ++t) {
@@ -479,7 +519,6 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                 if (MODEL == KM_EXCH) {
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
-                        float ko = 0.f;  // exp(-sum k_out dt) = 1 - ko
                         float ksum = 0.f;
 #pragma unroll
                         for (int p = 0; p < P; ++p) {
@@ -490,10 +529,9 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                             ksum += kgo;
                             if (kin != 0.f) fin[t][p] = one_minus_exp(dt * kin);
                         }
-                        ko = one_minus_exp(dt * ksum);
-                        yo[t] = ko;
+                        yo[t] = one_minus_exp(dt * ksum);
                     }
-                } else if (MODEL == KM_MT || MODEL == KM_CEST) {
+                } else if (kMTC) {
                     const float K12 = kc[0];
                     const float K21 = MODEL == KM_MT ? kc[1] : kc[P - 1];
                     mt_y1k = one_minus_exp(dt * (it1[0] + K12));
@@ -514,17 +552,37 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                         yo[0] = one_minus_exp(dt * ksum);
                     }
                 }
+                if (!kMTC) {
+                    // a pool the step leaves alone gets neutral coefficients
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        if (evo >> t & 1u) continue;
+                        y1[t] = y2[t] = yo[t] = 0.f;
+#pragma unroll
+                        for (int p = 0; p < P; ++p) fin[t][p] = 0.f;
+                    }
+                }
             }
-
-            if (active && (flags & kFlagDt) && MODEL != KM_MT && MODEL != KM_CEST) {
-                // an empty pool keeps its magnetisation: neutral coefficients
-                // instead of branches keep the per-pool updates straight-line
+            if (active && (flags & kFlagState)) {
+#pragma unroll
+                for (int t = 0; t < P; ++t)
+                    if (has_frame<MODEL>(t)) Dc[t] = phase_step((wc + F.cs_hi[t]) * dt);
 #pragma unroll
                 for (int t = 0; t < P; ++t) {
-                    if (act >> t & 1u) continue;
-                    y1[t] = y2[t] = yo[t] = 0.f;
+                    if (!has_frame<MODEL>(t)) continue;
+                    // transverse decay of a free step: (1 - a) = (1 - y2)(1 - yo)
+                    const float a = (MODEL == KM_NORMAL || MODEL == KM_MT) ? y2[t]
+                                                                           : y2[t] + yo[t] - y2[t] * yo[t];
 #pragma unroll
-                    for (int p = 0; p < P; ++p) fin[t][p] = 0.f;
+                    for (int s = 0; s < NS; ++s) {
+                        if (tvo >> t & 1u) {
+                            const float2 p = phase_step(dwsm[(s * P + t) * kBlock + tid] * dt);
+                            dm[s][t] = make_float2(fmaf(p.x, 1.f - a, -a), p.y * (1.f - a));
+                        } else {
+                            // constant in the lab: m_frame turns back by the frame's step
+                            dm[s][t] = make_float2(Dc[t].x, -Dc[t].y);
+                        }
+                    }
                 }
             }
 
@@ -532,27 +590,60 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
             if (flags & kFlagAdc) {
 #pragma unroll
                 for (int t = 0; t < kNSampP; ++t) {
-                    float mx = 0.f, my = 0.f;
-                    const bool sampled = (MODEL != KM_EXCH) || FREE || (L.kind[t] == 0);
+                    float sx = 0.f, sy = 0.f;
 #pragma unroll
                     for (int s = 0; s < NS; ++s) {
-                        const float2 m = cmul(make_float2(X[s][t], Y[s][t]), Ph[s][t]);
-                        mx += m.x;
-                        my += m.y;
+                        sx += X[s][t];
+                        sy += Y[s][t];
                     }
-                    if (!(active && sampled)) mx = my = 0.f;
-                    mtile[(a_fill * kNSampP + t) * kTRow + tid] = tf32_split2(mx, my);
+                    float2 m = cmul(make_float2(sx, sy), Pc[t]);
+                    const bool sampled = (MODEL != KM_EXCH) || FREE || (L.kind[t] == 0);
+                    if (!(active && sampled)) m = make_float2(0.f, 0.f);
+                    mtile[(a_fill * kNSampP + t) * kTRow + tid] = m;
                 }
                 if (++a_fill == kTile) flush();
             }
             if (!active) continue;
 
             const bool rf = (flags & kFlagRf) != 0;
+            float2 Pprev[P];
+#pragma unroll
+            for (int t = 0; t < P; ++t) Pprev[t] = Pc[t];
+            if (!rf) {
+#pragma unroll
+                for (int t = 0; t < P; ++t) {
+                    if (!has_frame<MODEL>(t)) continue;
+                    const float2 p = Pc[t], d = Dc[t];
+                    Pc[t] = make_float2(fmaf(p.x, d.x, fmaf(-p.y, d.y, p.x)), fmaf(p.x, d.y, fmaf(p.y, d.x, p.y)));
+                }
+            }
+            // exchange inflow of transverse magnetisation between frames:
+            // fr[t][p] = f_tp P_p(before the step) conj(P_t(after))
+            float2 fr[P][P];
+            if (MODEL == KM_EXCH) {
+#pragma unroll
+                for (int t = 0; t < P; ++t)
+#pragma unroll
+                    for (int p = 0; p < P; ++p) {
+                        const float2 r = cmul_conj(Pprev[p], Pc[t]);
+                        const float f = (FREE || ((tvo >> t & 1u) && L.kind[p] == 0)) ? fin[t][p] : 0.f;
+                        fr[t][p] = make_float2(f * r.x, f * r.y);
+                    }
+            } else if (MODEL == KM_CEST) {
+#pragma unroll
+                for (int t = 2; t < P; ++t) {
+                    const float2 r0t = cmul_conj(Pprev[t], Pc[0]);
+                    const float2 rt0 = cmul_conj(Pprev[0], Pc[t]);
+                    fr[0][t] = make_float2(fin[0][t] * r0t.x, fin[0][t] * r0t.y);
+                    fr[t][0] = make_float2(fin[t][0] * rt0.x, fin[t][0] * rt0.y);
+                }
+            }
+
             float b = 0.f;
             float2 u0 = make_float2(1.f, 0.f);  // exp(i PHI) before the frame shift
-            float w_sat[P];                       // bound-pool saturation rates
+            float sat[P];                        // bound-pool saturation of the rf step
 #pragma unroll
-            for (int t = 0; t < P; ++t) w_sat[t] = 0.f;
+            for (int t = 0; t < P; ++t) sat[t] = 0.f;
             if (rf) {
                 // complex B1 = sum_c TxCoilmg_c exp(i pe_c) * amp_c exp(i phase_c)
                 float2 B = cmul(tx0, make_float2(r1.x, r1.y));
@@ -565,31 +656,32 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                 const float Bm = sqrtf(fmaf(B.x, B.x, B.y * B.y));
                 b = Bm * gyro;
                 if (Bm > 0.f) u0 = make_float2(B.x / Bm, -B.y / Bm);  // conj(B)/|B|
-                if (MODEL != KM_NORMAL) {
+                if (MODEL != KM_NORMAL && !(MODEL == KM_EXCH && FREE)) {
                     // bound pools: W = pi (gamma TxCoilmg |amp|)^2 G(rf offset, T2b) with the
                     // reference's lineshape rule (single transmit coil)
                     const float b1 = sqrtf(fmaf(r1.x, r1.x, r1.y * r1.y)) * sqrtf(fmaf(tx0.x, tx0.x, tx0.y * tx0.y));
                     const float freq = r1.z * 0.15915494309189535f;
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
-                        const bool bound = (MODEL == KM_EXCH) ? (!FREE && L.kind[t] == 1) : (t == 1);
+                        const bool bound = (MODEL == KM_EXCH) ? ((evo >> t & 1u) && L.kind[t] == 1) : (t == 1);
                         if (!bound) continue;
                         if (lc.t2b != t2v[t] || lc.freq != freq) {
                             lc.freq = freq;
                             lc.t2b = t2v[t];
                             lc.g = lineshape(freq, db0, gyro, t2v[t]);
                         }
-                        w_sat[t] = (float)(kPiRef * (double)((b1 * gyro) * (b1 * gyro)) * (double)lc.g);
+                        const float w = (float)(kPiRef * (double)((b1 * gyro) * (b1 * gyro)) * (double)lc.g);
+                        sat[t] = one_minus_exp(w * dt);
                     }
                 }
             }
             const float wrf = r1.z;  // 2 pi sum of active rf frequencies
+            float2 uphi[P];
+#pragma unroll
+            for (int t = 0; t < P; ++t) uphi[t] = rf ? cmul(u0, Pc[t]) : make_float2(1.f, 0.f);
 
 #pragma unroll
             for (int s = 0; s < NS; ++s) {
-                float2 Pprev[P];
-#pragma unroll
-                for (int t = 0; t < P; ++t) Pprev[t] = Ph[s][t];
                 float px[P], py[P], pz[P];
 #pragma unroll
                 for (int t = 0; t < P; ++t) {
@@ -597,167 +689,104 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
                     py[t] = Y[s][t];
                     pz[t] = Z[s][t];
                 }
-                if (MODEL == KM_NORMAL || (MODEL == KM_EXCH && FREE)) {
-                    // every pool free: straight-line updates of all pools
-                    if (rf) {
+                // ---- transverse ----------------------------------------------
+                if (rf) {
 #pragma unroll
-                        for (int t = 0; t < P; ++t) {
-                            float x = X[s][t], y = Y[s][t], z = Z[s][t];
-                            rf_rotate(x, y, z, wc + Wh[s][t] + wrf, b, cmul(u0, Ph[s][t]), dt);
-                            const bool on = act >> t & 1u;
-                            X[s][t] = on ? x : X[s][t];
-                            Y[s][t] = on ? y : Y[s][t];
-                            Z[s][t] = on ? z : Z[s][t];
-                        }
-                    } else {
-#pragma unroll
-                        for (int t = 0; t < P; ++t) {
-                            const float2 p = Ph[s][t], d = D[s][t];
-                            Ph[s][t] = make_float2(fmaf(p.x, d.x, fmaf(-p.y, d.y, p.x)), fmaf(p.x, d.y, fmaf(p.y, d.x, p.y)));
-                        }
+                    for (int t = 0; t < P; ++t) {
+                        if (!has_frame<MODEL>(t)) continue;
+                        float x = px[t], y = py[t], z = pz[t];
+                        const float dW = wc + dwsm[(s * P + t) * kBlock + tid] + F.cs_hi[t] + wrf;
+                        rf_rotate(x, y, z, dW, b, uphi[t], dt);
+                        const bool on = tvo >> t & 1u;
+                        X[s][t] = on ? x : px[t];
+                        Y[s][t] = on ? y : py[t];
+                        Z[s][t] = on ? z : pz[t];
                     }
-                    if (MODEL == KM_NORMAL) {
+                    // relaxation and inflow after the rotation (the frames hold still)
+                    if constexpr (MODEL == KM_NORMAL || MODEL == KM_MT) {
 #pragma unroll
                         for (int t = 0; t < P; ++t) {
+                            if (!has_frame<MODEL>(t)) continue;
                             X[s][t] = fmaf(-y2[t], X[s][t], X[s][t]);
                             Y[s][t] = fmaf(-y2[t], Y[s][t], Y[s][t]);
-                            Z[s][t] = fmaf(y1[t], rhoS[t] - Z[s][t], Z[s][t]);
                         }
                     } else {
-                        // inflow uses every pool's magnetisation before the step, in the lab
-                        // frame, carried into the receiving pool's frame after the step
-                        float2 ml[P];
-#pragma unroll
-                        for (int p = 0; p < P; ++p) ml[p] = cmul(make_float2(px[p], py[p]), Pprev[p]);
 #pragma unroll
                         for (int t = 0; t < P; ++t) {
-                            float ix = 0.f, iy = 0.f, iz = 0.f;
+                            if (!has_frame<MODEL>(t)) continue;
+                            float ix = 0.f, iy = 0.f;
 #pragma unroll
                             for (int p = 0; p < P; ++p) {
-                                ix = fmaf(fin[t][p], ml[p].x, ix);
-                                iy = fmaf(fin[t][p], ml[p].y, iy);
-                                iz = fmaf(fin[t][p], pz[p], iz);
+                                if (MODEL == KM_CEST && !((t == 0 && p >= 2) || (t >= 2 && p == 0))) continue;
+                                const float2 f = fr[t][p];
+                                ix = fmaf(f.x, px[p], fmaf(-f.y, py[p], ix));
+                                iy = fmaf(f.x, py[p], fmaf(f.y, px[p], iy));
                             }
-                            const float2 in = cmul_conj(make_float2(ix, iy), Ph[s][t]);
-                            float x = fmaf(-y2[t], X[s][t], X[s][t]);
-                            float y = fmaf(-y2[t], Y[s][t], Y[s][t]);
-                            float z = fmaf(-y1[t], Z[s][t], Z[s][t]);
-                            X[s][t] = fmaf(-yo[t], x, x) + in.x;
-                            Y[s][t] = fmaf(-yo[t], y, y) + in.y;
-                            Z[s][t] = fmaf(-yo[t], z, z) + iz + rhoS[t] * y1[t];
+                            const float x = fmaf(-y2[t], X[s][t], X[s][t]);
+                            const float y = fmaf(-y2[t], Y[s][t], Y[s][t]);
+                            X[s][t] = fmaf(-yo[t], x, x) + ix;
+                            Y[s][t] = fmaf(-yo[t], y, y) + iy;
                         }
                     }
-                    continue;
-                }
-                // rotation (rf) or frame advance (free precession)
-#pragma unroll
-                for (int t = 0; t < P; ++t) {
-                    const bool free_pool =
-                        kFreeAll ? (MODEL == KM_NORMAL || L.kind[t] == 0) : (t == 0 || (MODEL == KM_CEST && t >= 2));
-                    if (!free_pool) continue;
-                    if (MODEL != KM_MT && MODEL != KM_CEST && !(act >> t & 1u)) continue;
-                    if (rf) {
-                        const float dW = wc + Wh[s][t] + wrf;
-                        const float2 uphi = cmul(u0, Ph[s][t]);
-                        rf_rotate(X[s][t], Y[s][t], Z[s][t], dW, b, uphi, dt);
-                    } else {
-                        const float2 p = Ph[s][t];
-                        const float2 d = D[s][t];
-                        Ph[s][t] = make_float2(fmaf(p.x, d.x, fmaf(-p.y, d.y, p.x)), fmaf(p.x, d.y, fmaf(p.y, d.x, p.y)));
-                    }
-                }
-                // relaxation and exchange
-                if (MODEL == KM_NORMAL) {
+                } else {
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
-                        if (!(act >> t & 1u)) continue;
-                        X[s][t] = fmaf(-y2[t], X[s][t], X[s][t]);
-                        Y[s][t] = fmaf(-y2[t], Y[s][t], Y[s][t]);
-                        Z[s][t] = fmaf(y1[t], rhoS[t] - Z[s][t], Z[s][t]);
-                    }
-                } else if (MODEL == KM_EXCH) {
-                    float nx[P], ny[P], nz[P];
-#pragma unroll
-                    for (int t = 0; t < P; ++t) {
-                        nx[t] = X[s][t];
-                        ny[t] = Y[s][t];
-                        nz[t] = Z[s][t];
-                    }
-#pragma unroll
-                    for (int t = 0; t < P; ++t) {
-                        if (!(act >> t & 1u)) continue;
-                        const int kind = L.kind[t];
-                        if (kind != 0 && kind != 1) continue;
-                        const bool bound = kind == 1;
-                        float x = nx[t], y = ny[t], z = nz[t];
-                        float ix = 0.f, iy = 0.f, iz = 0.f;
+                        if (!has_frame<MODEL>(t)) continue;
+                        float2 d = dm[s][t];
+                        if (MODEL == KM_EXCH) {  // self exchange (a nonzero K diagonal)
+                            d.x += fr[t][t].x;
+                            d.y += fr[t][t].y;
+                        }
+                        float ix = fmaf(d.x, px[t], -d.y * py[t]);
+                        float iy = fmaf(d.x, py[t], d.y * px[t]);
 #pragma unroll
                         for (int p = 0; p < P; ++p) {
-                            const float f = fin[t][p];
-                            if (f == 0.f) continue;
-                            iz = fmaf(f, pz[p], iz);
-                            if (!bound && L.kind[p] == 0) {
-                                // m_p(prev) carried into t's frame after the step
-                                const float2 rel = cmul_conj(Pprev[p], Ph[s][t]);
-                                const float2 m = cmul(make_float2(px[p], py[p]), rel);
-                                ix = fmaf(f, m.x, ix);
-                                iy = fmaf(f, m.y, iy);
-                            }
+                            if (p == t || !has_frame<MODEL>(p)) continue;
+                            if (MODEL == KM_NORMAL || MODEL == KM_MT) continue;
+                            if (MODEL == KM_CEST && !((t == 0 && p >= 2) || (t >= 2 && p == 0))) continue;
+                            const float2 f = fr[t][p];
+                            ix = fmaf(f.x, px[p], fmaf(-f.y, py[p], ix));
+                            iy = fmaf(f.x, py[p], fmaf(f.y, px[p], iy));
                         }
-                        if (bound) {
-                            if (rf) z = fmaf(-one_minus_exp(w_sat[t] * dt), z, z);
-                        } else {
-                            x = fmaf(-y2[t], x, x);
-                            y = fmaf(-y2[t], y, y);
-                            x = fmaf(-yo[t], x, x) + ix;
-                            y = fmaf(-yo[t], y, y) + iy;
-                            X[s][t] = x;
-                            Y[s][t] = y;
-                        }
+                        X[s][t] = px[t] + ix;
+                        Y[s][t] = py[t] + iy;
+                    }
+                }
+                // ---- longitudinal (and the bound pools) -----------------------
+                if (MODEL == KM_NORMAL) {
+#pragma unroll
+                    for (int t = 0; t < P; ++t) Z[s][t] = fmaf(y1[t], rhoS[t] - Z[s][t], Z[s][t]);
+                } else if (MODEL == KM_EXCH) {
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        float iz = 0.f;
+#pragma unroll
+                        for (int p = 0; p < P; ++p) iz = fmaf(fin[t][p], pz[p], iz);
+                        float z = Z[s][t];
+                        if (!FREE && rf) z = fmaf(-sat[t], z, z);
                         z = fmaf(-y1[t], z, z);
                         Z[s][t] = fmaf(-yo[t], z, z) + iz + rhoS[t] * y1[t];
                     }
                 } else {  // MT / CEST
-                    float x = X[s][0], y = Y[s][0], z = Z[s][0];
                     const float zb0 = pz[1], z0 = pz[0];
-                    x = fmaf(-y2[0], x, x);
-                    y = fmaf(-y2[0], y, y);
+                    float z = Z[s][0];
                     if (MODEL == KM_MT) {
                         z = fmaf(-mt_y1k, z, z) + rhoS[0] * y1[0] + zb0 * mt_y21;
                     } else {
-                        float ix = 0.f, iy = 0.f, iz = 0.f;
+                        float iz = 0.f;
 #pragma unroll
-                        for (int t = 2; t < P; ++t) {
-                            const float f = fin[0][t];
-                            const float2 rel = cmul_conj(Pprev[t], Ph[s][0]);
-                            const float2 m = cmul(make_float2(px[t], py[t]), rel);
-                            ix = fmaf(f, m.x, ix);
-                            iy = fmaf(f, m.y, iy);
-                            iz = fmaf(f, pz[t], iz);
-                        }
-                        x = fmaf(-yo[0], x, x) + ix;
-                        y = fmaf(-yo[0], y, y) + iy;
+                        for (int t = 2; t < P; ++t) iz = fmaf(fin[0][t], pz[t], iz);
                         z = fmaf(-mt_y1k, z, z);
                         z = fmaf(-yo[0], z, z) + iz + zb0 * mt_y21 + rhoS[0] * y1[0];
 #pragma unroll
                         for (int t = 2; t < P; ++t) {
-                            float cx = X[s][t], cy = Y[s][t], cz = Z[s][t];
-                            cx = fmaf(-y2[t], cx, cx);
-                            cy = fmaf(-y2[t], cy, cy);
-                            cz = fmaf(-y1[t], cz, cz);
-                            const float f = fin[t][0];
-                            const float2 rel = cmul_conj(Pprev[0], Ph[s][t]);
-                            const float2 m = cmul(make_float2(px[0], py[0]), rel);
-                            X[s][t] = fmaf(-yo[t], cx, cx) + f * m.x;
-                            Y[s][t] = fmaf(-yo[t], cy, cy) + f * m.y;
-                            Z[s][t] = fmaf(-yo[t], cz, cz) + f * z0 + rhoS[t] * y1[t];
+                            const float cz = fmaf(-y1[t], Z[s][t], Z[s][t]);
+                            Z[s][t] = fmaf(-yo[t], cz, cz) + fin[t][0] * z0 + rhoS[t] * y1[t];
                         }
                     }
                     float bz = zb0;
-                    if (rf) bz = fmaf(-one_minus_exp(w_sat[1] * dt), bz, bz);
+                    if (rf) bz = fmaf(-sat[1], bz, bz);
                     Z[s][1] = fmaf(-mt_y1bk, bz, bz) + rhoS[1] * mt_y1b + z0 * mt_y12;
-                    X[s][0] = x;
-                    Y[s][0] = y;
                     Z[s][0] = z;
                 }
             }
@@ -773,7 +802,8 @@ __global__ void __launch_bounds__(kBlock) scan_fast_kernel(FastLaunch F) {
 #pragma unroll
             for (int t = 0; t < P; ++t) {
                 // back to the lab frame: m_lab = m_frame * P
-                const float2 m = entered ? cmul(make_float2(X[s][t], Y[s][t]), Ph[s][t]) : make_float2(X[s][t], Y[s][t]);
+                float2 m = make_float2(X[s][t], Y[s][t]);
+                if (entered && has_frame<MODEL>(t)) m = cmul(m, Pc[t]);
                 const long long i = ((long long)t * L.S + sp) * n + v;
                 L.mx[i] = m.x;
                 L.my[i] = m.y;

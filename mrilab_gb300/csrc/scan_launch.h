@@ -12,7 +12,13 @@ namespace mrl {
 
 // Spins handled per thread for a given SpinNum: all of them when S <= 4 and
 // S is 1, 2 or 4; otherwise one spin per thread.
-inline int spins_per_thread(int S) { return (S == 4 || S == 2) ? S : 1; }
+// Spins of one voxel a thread integrates: as many as divide S while a
+// thread holds at most 8 isochromat-pools (register budget).
+inline int spins_per_thread(int S, int P) {
+    for (int ns = 4; ns > 1; ns /= 2)
+        if (S % ns == 0 && ns * P <= 8) return ns;
+    return 1;
+}
 
 // Dynamic shared memory of one block.
 inline size_t scan_smem_bytes(int stride4, int nsamp) {
@@ -20,11 +26,20 @@ inline size_t scan_smem_bytes(int stride4, int nsamp) {
 }
 // ... of the accurate kernel: staged records, coil sensitivities of the
 // block's voxels and the per-warp receive tile.
-inline size_t scan_fast_smem_bytes(int stride4, int nsamp, int rx) {
-    (void)nsamp;
+// Receive partial sums per block and sample (both kernels reduce their
+// warps' sums in shared memory).
+inline int partial_slices(bool fast) {
+    (void)fast;
+    return 1;
+}
+
+inline size_t scan_fast_smem_bytes(int stride4, int rx, int P, int NS) {
     const size_t c4 = (size_t)((rx + 3) & ~3);
     const size_t row = kBlock + 2;
-    return 128 + (size_t)2 * kFastChunk * stride4 * 16 + 16 * row * 16 + c4 * row * 16 + (kBlock / 32) * 16 * 2 * c4 * 4;
+    return 128 + (size_t)2 * kFastChunk * stride4 * 16  // staged step records
+           + 16 * row * 8 + c4 * row * 8                 // receive tile, coil maps
+           + (kBlock / 32) * 16 * 2 * c4 * 4             // per-warp receive sums
+           + ((size_t)NS * P + 4) * kBlock * 4;          // dWRnd, low parts of omega
 }
 
 cudaError_t launch_scan_ref_normal(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);

@@ -231,3 +231,25 @@ def test_device_sincos_error_bounds(built):
     rel = err_s[small] / np.maximum(np.abs(np.sin(xd[small])), 1e-30)
     print(f"max relative sine error for |x| <= 0.8: {rel.max():.2e}")
     assert rel.max() <= 3e-7
+
+
+def test_tf32_rounding_matches_hardware_conversion(built):
+    """The receive contraction rounds its TF32 operands with integer
+    arithmetic; it must give the bits of cvt.rna.tf32.f32 for finite inputs."""
+    import ctypes
+
+    lib = engine.library()
+    fp = ctypes.POINTER(ctypes.c_float)
+    up = ctypes.POINTER(ctypes.c_uint32)
+    lib.mrl_selftest_tf32.argtypes = [fp, up, up, ctypes.c_int]
+    lib.mrl_selftest_tf32.restype = ctypes.c_int
+    rng = np.random.default_rng(5)
+    bits = rng.integers(0, 2**32, 400000, dtype=np.uint64).astype(np.uint32)
+    x = bits.view(np.float32)
+    x = x[np.isfinite(x) & (np.abs(x) < 1e38)]
+    x = np.concatenate([x, rng.standard_normal(100000).astype(np.float32), np.float32([0.0, -0.0, 1.0, 1e-40])])
+    x = np.ascontiguousarray(x)
+    rn = np.empty(x.size, np.uint32)
+    cvt = np.empty(x.size, np.uint32)
+    assert lib.mrl_selftest_tf32(x.ctypes.data_as(fp), rn.ctypes.data_as(up), cvt.ctypes.data_as(up), x.size) == 0
+    assert np.array_equal(rn, cvt), f"{np.count_nonzero(rn != cvt)} of {x.size} differ"
