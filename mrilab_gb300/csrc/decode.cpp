@@ -71,6 +71,9 @@ void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx, double gyro
     out.n_rf_steps = 0;
     out.adc_begin = s.signali;
     out.stopped_at_ext = false;
+    out.point_uts.clear();
+    out.point_step.clear();
+    out.point_dt.clear();
     if (s.pend_active) {
         finish_time_point(s, tx, s.pend_ext, s.pend_flag_sum, s.pend_dt);
         s.pend_active = false;
@@ -106,6 +109,9 @@ void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx, double gyro
         s.dt = q.uts[nxt] - q.uts[cur];
         s.utsi = nxt;
         const double dt = s.dt;
+        out.point_uts.push_back(cur);
+        out.point_step.push_back((int)out.n_steps);
+        out.point_dt.push_back(dt);
 
         if (flag[0] >= 1) {  // rf: one update per merged rf entry (:385-419)
             for (int j = 0; j < flag[0]; ++j) {

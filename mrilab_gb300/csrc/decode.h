@@ -54,6 +54,11 @@ struct DecodeChunk {
     int adc_begin = 0, adc_end = 0;  // sample indices acquired in this chunk
     int n_rf_steps = 0;              // steps with rf on
     bool stopped_at_ext = false;     // true: an Ext callback is due now
+    // every time point decoded (RunMode 1 history): its uts index, the
+    // number of dt > 0 steps of this chunk before it (the state at that
+    // time is the state after those steps) and its dt
+    std::vector<int> point_uts, point_step;
+    std::vector<double> point_dt;
 };
 
 void load_state(DecodeState &s, const mrl_state &v, int tx_num);

@@ -203,6 +203,38 @@ __global__ void scatter_state(const float *__restrict__ m, const int *__restrict
     }
 }
 
+// RunMode 1: out[c][j][ts][v] = component c of the state of isochromat-pool
+// ts of voxel v at time point j: snapshot snap[j] for an active voxel (inv
+// maps a voxel to its compact index), the voxel's unchanging state otherwise.
+__global__ void expand_history(const float *__restrict__ hist, long long stride, int n_act,
+                               const long long *__restrict__ snap, int npts, const int *__restrict__ inv,
+                               long long V, int PS, const float *rx, const float *ry, const float *rz,
+                               float *__restrict__ out) {
+    const long long total = (long long)npts * PS * V;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long v = e % V;
+        const long long r = e / V;
+        const int ts = (int)(r % PS);
+        const int j = (int)(r / PS);
+        const int iv = inv[v];
+        float x, y, z;
+        if (iv >= 0) {
+            const float *h = hist + snap[j] * 3 * stride + (long long)ts * n_act + iv;
+            x = h[0];
+            y = h[stride];
+            z = h[2 * stride];
+        } else {
+            x = rx[(long long)ts * V + v];
+            y = ry[(long long)ts * V + v];
+            z = rz[(long long)ts * V + v];
+        }
+        out[e] = x;
+        out[total + e] = y;
+        out[2 * total + e] = z;
+    }
+}
+
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
@@ -273,6 +305,14 @@ struct Scanner {
     // offsets into d_f
     size_t o_gx = 0, o_gy = 0, o_gz = 0, o_db0 = 0, o_txmg = 0, o_txpe = 0, o_rho = 0, o_t1 = 0, o_t2 = 0, o_k = 0,
            o_dwr = 0;
+    // RunMode 1 history: snapshots of the state before every dt > 0 step
+    bool hist_on = false;
+    DevBuf<float> d_hist;        // [step][Mx|My|Mz][P][S][n_act], then the final state
+    long long hist_steps = 0;    // steps of the chunks run so far
+    long long hist_cap = 0;      // dt > 0 steps the buffer holds
+    std::vector<int> pts_uts;    // every decoded time point: uts index
+    std::vector<long long> pts_snap;  // ... and the snapshot holding its state
+    std::vector<double> pts_dt;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_scan, ev_red;
     int launches = 0;
     double h2d_ms = 0, d2h_ms = 0, h2d_bytes = 0, d2h_bytes = 0;
@@ -329,7 +369,6 @@ struct Scanner {
             return set_err("empty sequence"), MRL_ERR_ARG;
         if (TX > 4) return set_err("TxCoilNum %d > 4 not supported", TX), MRL_ERR_UNSUPPORTED;
         if (P > kMaxPool) return set_err("TypeNum %d > %d not supported", P, kMaxPool), MRL_ERR_UNSUPPORTED;
-        if (a.ctl.run_mode == 1) return set_err("RunMode 1 (per-step history) is not supported yet"), MRL_ERR_UNSUPPORTED;
         switch (a.model) {
         case MRL_MODEL_NORMAL:
             if (P > 3) return set_err("normal model supports TypeNum <= 3"), MRL_ERR_UNSUPPORTED;
@@ -357,6 +396,11 @@ struct Scanner {
         fast = a.ctl.numerics == MRL_NUMERICS_ACCURATE;
         if (a.ctl.numerics != MRL_NUMERICS_ACCURATE && a.ctl.numerics != MRL_NUMERICS_REFERENCE)
             return set_err("unknown numerics %d", a.ctl.numerics), MRL_ERR_ARG;
+        hist_on = a.ctl.run_mode == 1;  // other values scan normally, as in the reference's switch
+        if (hist_on && !fast)
+            return set_err("RunMode 1 (per-step history) needs MRL_NUMERICS_ACCURATE"), MRL_ERR_UNSUPPORTED;
+        if (hist_on && (!a.sig.mxs || !a.sig.mys || !a.sig.mzs))
+            return set_err("RunMode 1 needs the history arrays VSig.Mx/My/Mz"), MRL_ERR_ARG;
         if (fast && TX > 1) {
             bool bound = mi.km == KM_MT || mi.km == KM_CEST;
             if (mi.gm)
@@ -661,6 +705,8 @@ struct Scanner {
             L.s0 = d.s0;
             L.s1 = d.s1;
             L.a_launch = d.a_count;
+            L.hist_stride = (long long)P * S * std::max(1, n_act);
+            L.hist = hist_on ? d_hist.p + (hist_steps + d.s0) * 3 * L.hist_stride : nullptr;
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (timed) {
                 cudaEventCreate(&e0);
@@ -725,10 +771,19 @@ struct Scanner {
         std::vector<LaunchDesc> ls;
         int rc = prepare_chunk(ch, ls);
         if (rc) return rc;
+        if (hist_on && hist_steps + ch.n_steps > hist_cap) return set_err("history buffer overrun"), MRL_ERR_ARG;
         if ((rc = enqueue(ls, rf_ref, st, true))) return rc;
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return fail_cuda(e, "scan kernels");
         phase("scan kernels");
+        if (hist_on) {
+            for (size_t j = 0; j < ch.point_uts.size(); ++j) {
+                pts_uts.push_back(ch.point_uts[j]);
+                pts_snap.push_back(hist_steps + ch.point_step[j]);
+                pts_dt.push_back(ch.point_dt[j]);
+            }
+            hist_steps += ch.n_steps;
+        }
         return MRL_OK;
     }
 
@@ -752,7 +807,83 @@ struct Scanner {
         cudaMemsetAsync(d_sx.p, 0, nsig * sizeof(double), st);
         cudaMemsetAsync(d_sy.p, 0, nsig * sizeof(double), st);
         phase("device setup");
-        return upload_object();
+        if ((rc = upload_object())) return rc;
+        return hist_on ? setup_history() : MRL_OK;
+    }
+
+    // RunMode 1: room for a snapshot before every dt > 0 step still to run
+    // and one for the final state.
+    int setup_history() {
+        const mrl_sequence &q = args->seq;
+        const int u0 = args->var.utsi ? *args->var.utsi : 0;
+        hist_cap = 0;
+        for (int i = std::max(0, u0); i + 1 < q.n_uts; ++i) hist_cap += q.uts[i + 1] - q.uts[i] > 0;
+        const double stride = (double)P * S * std::max(1, n_act);
+        const double bytes = (double)(hist_cap + 1) * 3 * stride * sizeof(float) +
+                             (double)std::max(0, q.n_uts - u0) * 3 * P * S * (double)V * sizeof(float);
+        if (bytes > 32.0 * (1ull << 30))
+            return set_err("RunMode 1 history needs %.1f GiB of device memory (limit 32 GiB)", bytes / (1ull << 30)),
+                   MRL_ERR_NOMEM;
+        cudaError_t e = d_hist.ensure((size_t)((hist_cap + 1) * 3 * (long long)stride));
+        if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(history)");
+        hist_steps = 0;
+        pts_uts.clear();
+        pts_snap.clear();
+        pts_dt.clear();
+        return MRL_OK;
+    }
+
+    // RunMode 1 output: VSig.Mx/My/Mz[slot] = state at uts[slot] for every
+    // decoded time point (the GPU engines' d_b_M* copies,
+    // DoGMScanAtGPU.cu:347-358,831-840), VSig.Muts accumulated like
+    // DoGMScanAtGPU.cu:437-446.
+    int write_history() {
+        mrl_scan_args &a = *args;
+        const size_t npts = pts_uts.size();
+        if (npts == 0) return MRL_OK;
+        for (size_t j = 1; j < npts; ++j)
+            if (pts_uts[j] != pts_uts[0] + (int)j) return set_err("history time points not contiguous"), MRL_ERR_ARG;
+        const long long stride = (long long)P * S * std::max(1, n_act);
+        cudaError_t e = cudaMemcpyAsync(d_hist.p + hist_steps * 3 * stride, d_m.p, 3 * stride * sizeof(float),
+                                        cudaMemcpyDeviceToDevice, st);  // the final state
+        std::vector<int> inv((size_t)V, -1);
+        for (int j = 0; j < n_act; ++j) inv[act[j]] = j;
+        DevBuf<int> d_inv;
+        DevBuf<long long> d_snap;
+        DevBuf<float> d_out;
+        const long long PSV = (long long)P * S * V;
+        if (e == cudaSuccess) e = d_inv.ensure(inv.size());
+        if (e == cudaSuccess) e = d_snap.ensure(npts);
+        if (e == cudaSuccess) e = d_out.ensure((size_t)(3 * (long long)npts * PSV));
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_inv.p, inv.data(), inv.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_snap.p, pts_snap.data(), npts * sizeof(long long), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return fail_cuda(e, "history setup");
+        const long long total = (long long)npts * PSV;
+        const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 32);
+        expand_history<<<blocks, 256, 0, st>>>(d_hist.p, stride, std::max(1, n_act), d_snap.p, (int)npts, d_inv.p, V,
+                                               P * S, raw.mx, raw.my, raw.mz, d_out.p);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "history launch");
+        launches++;
+        float *dst[3] = {a.sig.mxs, a.sig.mys, a.sig.mzs};
+        for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+            e = cudaMemcpyAsync(dst[c] + (long long)pts_uts[0] * PSV, d_out.p + c * total, total * sizeof(float),
+                                cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail_cuda(e, "history download");
+        d2h_bytes += 3.0 * total * sizeof(float);
+        if (a.sig.muts) {
+            const int nu = a.seq.n_uts;
+            for (size_t j = 0; j < npts; ++j) {
+                const int cur = pts_uts[j], nxt = cur + 1 < nu - 1 ? cur + 1 : nu - 1;
+                if (pts_dt[j] > 0)
+                    a.sig.muts[nxt] = a.sig.muts[cur] + pts_dt[j];
+                else if (pts_dt[j] < 0)
+                    a.sig.muts[nxt] = a.sig.muts[cur];
+            }
+        }
+        return MRL_OK;
     }
 
     int check_device_status() {
@@ -797,13 +928,20 @@ struct Scanner {
                     return MRL_ERR_EXT;
                 }
                 load_state(ds, args->var, TX);
-                if (fetch && (rc = upload_object())) return rc;
+                if (fetch) {
+                    const std::vector<int> act_before = act;
+                    if ((rc = upload_object())) return rc;
+                    if (hist_on && act != act_before)
+                        return set_err("RunMode 1: an Ext plugin changed which voxels are active"),
+                               MRL_ERR_UNSUPPORTED;
+                }
             }
         }
         if ((rc = download_signal(signal_synced, ds.signali))) return rc;
         phase("download signal");
         if ((rc = download_state())) return rc;
         phase("download state");
+        if (hist_on && (rc = write_history())) return rc;
         store_state(ds, args->var, TX);
         if ((rc = check_device_status())) return rc;
         (void)e;
@@ -922,6 +1060,10 @@ int mrl_plan_create(const mrl_scan_args *args, mrl_plan **out) {
         return MRL_ERR_ARG;
     }
     *out = nullptr;
+    if (args->ctl.run_mode == 1) {
+        mrl::set_err("plans do not record RunMode 1 history; use mrl_scan");
+        return MRL_ERR_UNSUPPORTED;
+    }
     mrl_plan *p = new mrl_plan();
     p->args = *args;
     mrl::Scanner &sc = p->sc;
@@ -1037,6 +1179,10 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
     if (rc) return rc;
     if (!sc.fast) {
         set_err("mrl_scan_noalloc runs the MRL_NUMERICS_ACCURATE integrator only");
+        return MRL_ERR_UNSUPPORTED;
+    }
+    if (sc.hist_on) {
+        set_err("mrl_scan_noalloc does not record RunMode 1 history");
         return MRL_ERR_UNSUPPORTED;
     }
     if (sc.TX != 1) {

@@ -161,6 +161,12 @@ bool bind(mrl_scan_args &a) {
     s.kx = ptr<double>("VSig", "Kx");
     const int *sn2 = ptr<int>("VSig", "SignalNum");
     s.signal_num = sn2 ? *sn2 : 0;
+    if (a.ctl.run_mode == 1) {  // history arrays (DoGMScanAtGPU.cu:218-221)
+        s.mxs = ptr<float>("VSig", "Mx");
+        s.mys = ptr<float>("VSig", "My");
+        s.mzs = ptr<float>("VSig", "Mz");
+        s.muts = ptr<double>("VSig", "Muts");
+    }
     return true;
 }
 

@@ -604,6 +604,20 @@ __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>()) scan_fast_ke
                 if (++a_fill == kTile) flush();
             }
             if (!active) continue;
+            if (L.hist != nullptr) {  // RunMode 1: the state at the start of the step, lab frame
+                float *h = L.hist + (long long)(k * kFastChunk + q) * 3 * L.hist_stride;
+#pragma unroll
+                for (int s = 0; s < NS; ++s)
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        float2 m = make_float2(X[s][t], Y[s][t]);
+                        if (has_frame<MODEL>(t)) m = cmul(m, Pc[t]);
+                        const long long i = ((long long)t * L.S + sg * NS + s) * n + v;
+                        h[i] = m.x;
+                        h[L.hist_stride + i] = m.y;
+                        h[2 * L.hist_stride + i] = Z[s][t];
+                    }
+            }
 
             const bool rf = (flags & kFlagRf) != 0;
             float2 Pprev[P];

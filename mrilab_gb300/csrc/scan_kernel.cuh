@@ -57,6 +57,8 @@ struct ScanLaunch {
     float2 *partial;  // [(block * a_launch + a) * npairs + pair]
     int a_launch;
     int *err;
+    float *hist;            // RunMode 1: [step][Mx|My|Mz][P][S][n_act] from the launch's first step, or null
+    long long hist_stride;  // P * S * n_act
     float cs2pi[kMaxPool];  // (float)(2*pi*(float)CS[t])
     int kind[kMaxPool];     // KM_EXCH: 0 free, 1 bound, other values: pool left untouched
 };

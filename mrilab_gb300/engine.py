@@ -111,7 +111,7 @@ def _flat(a, dtype, copy=True):
 
 
 # host arrays mrl_scan writes into
-_WRITTEN = frozenset({"mx", "my", "mz", "sx", "sy", "skz", "sky", "skx"})
+_WRITTEN = frozenset({"mx", "my", "mz", "sx", "sy", "skz", "sky", "skx", "hmx", "hmy", "hmz", "muts"})
 
 
 class HostScan:
@@ -180,12 +180,21 @@ class HostScan:
         sg.sx, sg.sy = p(f64("sx", sig["Sx"]), _d), p(f64("sy", sig["Sy"]), _d)
         sg.kz, sg.ky, sg.kx = p(f64("skz", sig["Kz"]), _d), p(f64("sky", sig["Ky"]), _d), p(f64("skx", sig["Kx"]), _d)
         sg.signal_num = int(sig["SignalNum"])
+        if ct.run_mode == 1:  # RunMode 1 history, written by the engine
+            sg.mxs, sg.mys, sg.mzs = (p(f32("hmx", sig["Mx"]), _f), p(f32("hmy", sig["My"]), _f),
+                                      p(f32("hmz", sig["Mz"]), _f))
+            sg.muts = p(f64("muts", sig["Muts"]), _d)
         self.args = a
 
     def outputs(self) -> Dict[str, np.ndarray]:
         K = self.keep
-        return dict(Sx=K["sx"], Sy=K["sy"], Kx=K["skx"], Ky=K["sky"], Kz=K["skz"], Mx=K["mx"], My=K["my"],
-                    Mz=K["mz"], TRCount=int(K["var_tr_count"][0]), utsi=int(K["var_utsi"][0]))
+        out = dict(Sx=K["sx"], Sy=K["sy"], Kx=K["skx"], Ky=K["sky"], Kz=K["skz"], Mx=K["mx"], My=K["my"],
+                   Mz=K["mz"], TRCount=int(K["var_tr_count"][0]), utsi=int(K["var_utsi"][0]))
+        if "hmx" in K:  # RunMode 1 history [len(uts)][P*S*V]
+            n = K["muts"].size
+            out.update(Mxs=K["hmx"].reshape(n, -1), Mys=K["hmy"].reshape(n, -1), Mzs=K["hmz"].reshape(n, -1),
+                       Muts=K["muts"])
+        return out
 
 
 def last_timing() -> Dict[str, float]:

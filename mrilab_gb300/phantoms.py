@@ -194,6 +194,22 @@ def assemble(rho, t1, t2, *, spin_num=1, t2star=None, db0_hz=None, res=(1e-3, 1e
                 info=dict(seed=seed))
 
 
+def with_history(sc: Scan) -> Scan:
+    """A copy of ``sc`` set up for RunMode 1 the way the spin watcher does
+    (DoSpinWatchExec.m:152-161): VSig.Mx/My/Mz [Y, X, Z, S, P, len(uts)]
+    single with slot 0 = the initial magnetisation, VSig.Muts zeros."""
+    out = sc.copy()
+    n = out.VSeq["utsLine"].size
+    for k in ("Mx", "My", "Mz"):
+        m = np.asarray(out.VObj[k], np.float32)
+        h = np.zeros(m.shape + (n,), np.float32, order="F")
+        h[..., 0] = m
+        out.VSig[k] = h
+    out.VSig["Muts"] = np.zeros((n, 1))
+    out.VCtl["RunMode"] = np.int32(1)
+    return out
+
+
 # ---------------------------------------------------------------------------
 # sequences
 # ---------------------------------------------------------------------------

@@ -65,6 +65,7 @@ class PortArgs(ctypes.Structure):
         ("signal_num", ctypes.c_int), ("threads", ctypes.c_int),
         ("max_steps", ctypes.c_longlong),
         ("ext_cb", _EXT_CB), ("ext_user", ctypes.c_void_p),
+        ("run_mode", ctypes.c_int), ("mxs", _f), ("mys", _f), ("mzs", _f), ("muts", _d),
     ]
 
 
@@ -165,6 +166,15 @@ def _call_with_args(scan, call, threads: int = 0, max_steps: int = -1, ext_cb=No
         cb = _EXT_CB(lambda user, val: int(ext_cb(val, out)))
         keep["cb"] = cb
         args.ext_cb = cb
+    args.run_mode = int(ctl["RunMode"])
+    if args.run_mode == 1:  # history [len(uts)][P][S][V], slot 0 = the initial state (DoSpinWatchExec.m:152-161)
+        for k in ("Mx", "My", "Mz"):
+            h = np.zeros((q["utsLine"].size, out[k].size), np.float32)
+            h[0] = out[k]
+            out[k + "s"] = h
+        out["Muts"] = np.zeros(q["utsLine"].size)
+        args.mxs, args.mys, args.mzs = _ptr(out["Mxs"], _f), _ptr(out["Mys"], _f), _ptr(out["Mzs"], _f)
+        args.muts = _ptr(out["Muts"], _d)
     rc = call(args)
     if rc != 0:
         raise RuntimeError(f"oracle returned {rc}")
@@ -187,6 +197,11 @@ def run_ref_cpu(scan, threads: int = 1) -> Dict[str, np.ndarray]:
     out = {k: ms.get("VSig", k).ravel(order="F").copy() for k in ("Sx", "Sy", "Kx", "Ky", "Kz")}
     for k in ("Mx", "My", "Mz"):
         out[k] = ms.get("VObj", k).ravel(order="F").copy()
+    if int(scan.VCtl["RunMode"]) == 1:  # history [len(uts)][P*S*V]
+        n = scan.VSeq["utsLine"].size
+        for k in ("Mx", "My", "Mz"):
+            out[k + "s"] = ms.get("VSig", k).ravel(order="F").reshape(n, -1).copy()
+        out["Muts"] = ms.get("VSig", "Muts").ravel(order="F").copy()
     return out
 
 

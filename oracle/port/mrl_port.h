@@ -59,6 +59,13 @@ typedef struct mrl_port_args {
     /* optional Ext callback: called with the state written back to mx/my/mz */
     int (*ext_cb)(void *user, double ext_value);
     void *ext_user;
+    /* RunMode 1 (DoScanAtCPU.cpp:431-436,544-552): after every dt > 0 step
+     * and at every TR boundary the state is copied into slot utsi of
+     * mxs/mys/mzs [len(uts)][P][S][V] and muts[utsi] advances by dt (held
+     * at a TR boundary); slot 0 is the caller's */
+    int run_mode;
+    float *mxs, *mys, *mzs;
+    double *muts;
 } mrl_port_args;
 
 /* Returns 0 on success, < 0 on bad arguments.  *steps_done (optional)

@@ -493,6 +493,14 @@ int PORT_FN(const mrl_port_args *a, long long *steps_done) {
             ADC = 0;
             Ext = 0;
         }
+        if (dt < 0 && a->run_mode == 1 && a->mxs) { /* TR boundary (DoScanAtCPU.cpp:431-436) */
+            for (long q = 0; q < N; ++q) {
+                a->mxs[(long)utsi * N + q] = (float)MX[q];
+                a->mys[(long)utsi * N + q] = (float)MY[q];
+                a->mzs[(long)utsi * N + q] = (float)MZ[q];
+            }
+            if (a->muts && utsi > 0) a->muts[utsi] = a->muts[utsi - 1];
+        }
         if (dt <= 0) continue; /* end of a time point, or TR boundary */
         if (a->max_steps >= 0 && done >= a->max_steps) break;
 
@@ -581,6 +589,14 @@ int PORT_FN(const mrl_port_args *a, long long *steps_done) {
         KzT += GzAmp * dt * (a->gyro / (2 * PI));
         KyT += GyAmp * dt * (a->gyro / (2 * PI));
         KxT += GxAmp * dt * (a->gyro / (2 * PI));
+        if (a->run_mode == 1 && a->mxs) { /* DoScanAtCPU.cpp:544-552 */
+            for (long q = 0; q < N; ++q) {
+                a->mxs[(long)utsi * N + q] = (float)MX[q];
+                a->mys[(long)utsi * N + q] = (float)MY[q];
+                a->mzs[(long)utsi * N + q] = (float)MZ[q];
+            }
+            if (a->muts && utsi > 0) a->muts[utsi] = a->muts[utsi - 1] + dt;
+        }
     }
     for (long q = 0; q < N; ++q) {
         a->mx[q] = (float)MX[q];

@@ -48,4 +48,6 @@ def load_golden(name):
     builder = str(z["builder"])
     kwargs = ast.literal_eval(str(z["kwargs"]))
     sc = getattr(phantoms, builder)(**kwargs)
+    if "history" in z.files and bool(z["history"]):
+        sc = phantoms.with_history(sc)
     return sc, {k: z[k] for k in z.files}

@@ -32,6 +32,11 @@ MULTIPOOL = {
     "mp_cest_p4_s2_c2": dict(model="cest", seed=3, pools=4, spins=2, coils=2, seq="sat"),
 }
 
+HISTORY = {
+    # RunMode 1: the reference CPU engine's per-time-point state history
+    "history_gre2d_n4_tr2_seed4": dict(seed=4, n=4, n_tr=2),
+}
+
 CASES = {
     # name: (builder kwargs)
     "gre2d_n16_tr4_seed1": dict(seed=1, n=16, n_tr=4),
@@ -58,6 +63,17 @@ def main():
         s_ref = ref["Sx"] + 1j * ref["Sy"]
         s64 = f64["Sx"] + 1j * f64["Sy"]
         print(name, "reference vs FP64 oracle: %.3e" % (np.linalg.norm(s_ref - s64) / np.linalg.norm(s64)))
+    for name, kw in HISTORY.items():
+        sc = phantoms.with_history(phantoms.config1_gre(**kw))
+        ref = oracle.run_ref_cpu(sc, threads=1)
+        f64 = oracle.run_port(sc, "f64")
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            builder=np.array("config1_gre"), kwargs=np.array(repr(kw)), history=np.array(True),
+            ref_Sx=ref["Sx"], ref_Sy=ref["Sy"], ref_Mxs=ref["Mxs"], ref_Mys=ref["Mys"], ref_Mzs=ref["Mzs"],
+            ref_Muts=ref["Muts"], f64_Mxs=f64["Mxs"], f64_Mys=f64["Mys"], f64_Mzs=f64["Mzs"],
+        )
+        print(name, "history: reference vs FP64 oracle max abs %.3e" % np.abs(ref["Mxs"] - f64["Mxs"]).max())
     for name, kw in MULTIPOOL.items():
         sc = phantoms.small_multipool(**kw)
         ref = oracle.run_ref_kernel(sc)

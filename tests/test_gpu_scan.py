@@ -253,3 +253,47 @@ def test_tf32_rounding_matches_hardware_conversion(built):
     cvt = np.empty(x.size, np.uint32)
     assert lib.mrl_selftest_tf32(x.ctypes.data_as(fp), rn.ctypes.data_as(up), cvt.ctypes.data_as(up), x.size) == 0
     assert np.array_equal(rn, cvt), f"{np.count_nonzero(rn != cvt)} of {x.size} differ"
+
+
+# RunMode 1 history (relative L2 over every time point of every isochromat)
+TOL_HIST = 1e-5
+
+
+def _history(out):
+    return np.stack([out["Mxs"], out["Mys"], out["Mzs"]])
+
+
+def test_runmode1_history_single_pool(built):
+    """VSig.Mx/My/Mz[slot] = state at uts[slot] and VSig.Muts, against the
+    FP64 oracle's history and the reference CPU engine's step times; the
+    history changes nothing else."""
+    sc, g = load_golden("history_gre2d_n4_tr2_seed4")
+    out = engine.scan(sc, numerics="accurate")
+    ref64 = np.stack([g["f64_Mxs"], g["f64_Mys"], g["f64_Mzs"]])
+    err = rel_l2(_history(out), ref64)
+    print(f"RunMode 1 history vs FP64 oracle: {err:.2e}")
+    assert err <= TOL_HIST
+    np.testing.assert_array_equal(out["Muts"].ravel(), g["ref_Muts"].ravel())
+    plain = sc.copy()
+    plain.VCtl["RunMode"] = np.int32(0)
+    out0 = engine.scan(plain, numerics="accurate")
+    np.testing.assert_array_equal(out["Mx"], out0["Mx"])
+    np.testing.assert_array_equal(signal(out), signal(out0))
+    np.testing.assert_array_equal(out["Mzs"][-1], out["Mz"])
+
+
+def test_runmode1_history_exchange_model(built):
+    sc = phantoms.with_history(phantoms.small_multipool("me", seed=11, n=3, pools=2, spins=2, coils=1, n_tr=1))
+    out = engine.scan(sc, numerics="accurate")
+    ref = oracle.run_port(sc, "f64")
+    err = rel_l2(_history(out), _history(ref))
+    print(f"ME RunMode 1 history vs FP64 oracle: {err:.2e}")
+    assert err <= TOL_HIST
+    np.testing.assert_array_equal(out["Muts"], ref["Muts"])
+
+
+def test_runmode1_needs_accurate_numerics(built):
+    sc, _ = load_golden("history_gre2d_n4_tr2_seed4")
+    with pytest.raises(engine.ScanError) as e:
+        engine.scan(sc, numerics="reference")
+    assert e.value.status == -6

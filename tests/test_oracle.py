@@ -85,3 +85,26 @@ def test_port_ext_callback_zeroes_transverse(built):
     assert len(calls) == 3
     base = oracle.run_port(sc, "f64")
     assert rel_l2(signal(out), signal(base)) > 1e-3  # the spoiler changed later echoes
+
+
+def test_port_history_matches_reference_cpu_engine_golden(built):
+    """RunMode 1: the port's per-time-point state history and step times
+    equal the reference CPU engine's (recorded from DoScanAtCPU)."""
+    sc, g = load_golden("history_gre2d_n4_tr2_seed4")
+    out = oracle.run_port(sc, "f32")
+    for k in ("Mxs", "Mys", "Mzs"):
+        np.testing.assert_allclose(out[k], g["ref_" + k], rtol=0, atol=1e-6)
+    np.testing.assert_array_equal(out["Muts"].ravel(), g["ref_Muts"].ravel())
+    f64 = oracle.run_port(sc, "f64")
+    for k in ("Mxs", "Mys", "Mzs"):
+        np.testing.assert_allclose(f64[k], g["f64_" + k], rtol=0, atol=1e-12)
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference tree not mounted")
+def test_port_history_matches_live_reference_cpu_engine(built):
+    sc = phantoms.with_history(phantoms.config1_gre(seed=9, n=4, n_tr=3))
+    ref = oracle.run_ref_cpu(sc)
+    out = oracle.run_port(sc, "f32")
+    for k in ("Mxs", "Mys", "Mzs"):
+        np.testing.assert_allclose(out[k], ref[k], rtol=0, atol=1e-6)
+    np.testing.assert_array_equal(out["Muts"], ref["Muts"])
