@@ -254,6 +254,25 @@ struct DevBuf {
     }
 };
 
+cudaError_t launch_fast(int km, int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
+                        const FastGrid &g) {
+    switch (km) {
+    case KM_NORMAL: return launch_scan_fast_normal(P, NS, all_free, grid, smem, st, g);
+    case KM_EXCH: return launch_scan_fast_exch(P, NS, all_free, grid, smem, st, g);
+    case KM_MT: return launch_scan_fast_mt(P, NS, all_free, grid, smem, st, g);
+    default: return launch_scan_fast_cest(P, NS, all_free, grid, smem, st, g);
+    }
+}
+
+int occupancy_fast(int km, int P, int NS, bool all_free, size_t smem) {
+    switch (km) {
+    case KM_NORMAL: return occupancy_scan_fast_normal(P, NS, all_free, smem);
+    case KM_EXCH: return occupancy_scan_fast_exch(P, NS, all_free, smem);
+    case KM_MT: return occupancy_scan_fast_mt(P, NS, all_free, smem);
+    default: return occupancy_scan_fast_cest(P, NS, all_free, smem);
+    }
+}
+
 struct ModelInfo {
     int km;        // KModel
     int nsamp;     // pools with a receive signal slot that can be nonzero
@@ -313,6 +332,10 @@ struct Scanner {
     std::vector<int> pts_uts;    // every decoded time point: uts index
     std::vector<long long> pts_snap;  // ... and the snapshot holding its state
     std::vector<double> pts_dt;
+    // accurate kernel: launch descriptors in device memory, one per launch
+    // of the current chunk, uploaded when they change
+    std::vector<FastLaunch> h_desc;
+    DevBuf<FastLaunch> d_desc;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_scan, ev_red;
     int launches = 0;
     double h2d_ms = 0, d2h_ms = 0, h2d_bytes = 0, d2h_bytes = 0;
@@ -692,21 +715,62 @@ struct Scanner {
     }
 
     // Enqueue the launches of a prepared chunk on `stream` (no host sync).
-    int enqueue(const std::vector<LaunchDesc> &ls, double rf_ref, cudaStream_t stream, bool timed) {
-        if (ls.empty()) return MRL_OK;
+    // Descriptor of the accurate kernel for launch fields L.
+    FastLaunch fast_launch(const ScanLaunch &L) const {
+        FastLaunch F{};
+        F.b = L;
+        F.omega = d_f2.p + o_om;
+        F.txc = d_f2.p + o_txc;
+        F.all_free = all_free();
+        for (int t = 0; t < kMaxPool; ++t) {  // 2 pi CS[t] as a (hi, lo) pair
+            const double w = (t < P && args->ctl.cs) ? 2 * kPiRef * args->ctl.cs[t] : 0.0;
+            F.cs_hi[t] = (float)w;
+            F.cs_lo[t] = (float)(w - (double)F.cs_hi[t]);
+        }
+        return F;
+    }
+
+    // Launch fields of launch d of the current chunk.
+    ScanLaunch launch_fields(const LaunchDesc &d, double rf_ref) {
         ScanLaunch L = make_launch(rf_ref);
         L.rec = d_rec.p;
         L.partial = d_part.p;
+        L.s0 = d.s0;
+        L.s1 = d.s1;
+        L.a_launch = d.a_count;
+        L.hist_stride = (long long)P * S * std::max(1, n_act);
+        L.hist = hist_on ? d_hist.p + (hist_steps + d.s0) * 3 * L.hist_stride : nullptr;
+        return L;
+    }
+
+    // Upload the accurate kernel's descriptors of launches ls (if changed).
+    int upload_descs(const std::vector<LaunchDesc> &ls, double rf_ref, cudaStream_t stream) {
+        std::vector<FastLaunch> h;
+        h.reserve(ls.size());
+        for (const LaunchDesc &d : ls) h.push_back(fast_launch(launch_fields(d, rf_ref)));
+        if (h.size() == h_desc.size() && std::memcmp(h.data(), h_desc.data(), h.size() * sizeof(FastLaunch)) == 0)
+            return MRL_OK;
+        cudaError_t e = d_desc.ensure(h.size());
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_desc.p, h.data(), h.size() * sizeof(FastLaunch), cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return fail_cuda(e, "upload launch descriptors");
+        h_desc.swap(h);
+        return MRL_OK;
+    }
+
+    int enqueue(const std::vector<LaunchDesc> &ls, double rf_ref, cudaStream_t stream, bool timed) {
+        if (ls.empty()) return MRL_OK;
         const int nblk = (int)n_blocks();
-        const size_t smem = fast ? scan_fast_smem_bytes(stride4, RX, P, NS) : scan_smem_bytes(stride4, mi.nsamp);
+        const size_t smem =
+            fast ? scan_fast_smem_bytes(stride4, RX, P, NS) : scan_smem_bytes(stride4, mi.nsamp);
         const double cr = std::cos(-rf_ref), sr = std::sin(-rf_ref);
         cudaError_t e;
-        for (const LaunchDesc &d : ls) {
-            L.s0 = d.s0;
-            L.s1 = d.s1;
-            L.a_launch = d.a_count;
-            L.hist_stride = (long long)P * S * std::max(1, n_act);
-            L.hist = hist_on ? d_hist.p + (hist_steps + d.s0) * 3 * L.hist_stride : nullptr;
+        int rc;
+        if (fast && n_act > 0 && (rc = upload_descs(ls, rf_ref, stream))) return rc;
+        for (size_t li = 0; li < ls.size(); ++li) {
+            const LaunchDesc &d = ls[li];
+            ScanLaunch L = launch_fields(d, rf_ref);
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (timed) {
                 cudaEventCreate(&e0);
@@ -717,24 +781,8 @@ struct Scanner {
             if (n_act > 0) {
                 dim3 grid(nblk);
                 if (fast) {
-                    FastLaunch F{};
-                    F.b = L;
-                    const size_t n = std::max(1, n_act);
-                    F.omega = d_f2.p + o_om;
-                    F.txc = d_f2.p + o_txc;
-                    F.all_free = all_free();
-                    for (int t = 0; t < kMaxPool; ++t) {  // 2 pi CS[t] as a (hi, lo) pair
-                        const double w = (t < P && args->ctl.cs) ? 2 * kPiRef * args->ctl.cs[t] : 0.0;
-                        F.cs_hi[t] = (float)w;
-                        F.cs_lo[t] = (float)(w - (double)F.cs_hi[t]);
-                    }
-                    (void)n;
-                    switch (mi.km) {
-                    case KM_NORMAL: e = launch_scan_fast_normal(P, NS, grid, smem, stream, F); break;
-                    case KM_EXCH: e = launch_scan_fast_exch(P, NS, grid, smem, stream, F); break;
-                    case KM_MT: e = launch_scan_fast_mt(P, NS, grid, smem, stream, F); break;
-                    default: e = launch_scan_fast_cest(P, NS, grid, smem, stream, F); break;
-                    }
+                    const FastGrid g{d_desc.p + li, nullptr, nblk, nullptr};
+                    e = launch_fast(mi.km, P, NS, all_free() != 0, grid, smem, stream, g);
                 } else {
                     switch (mi.km) {
                     case KM_NORMAL: e = launch_scan_ref_normal(P, NS, grid, smem, stream, L); break;
@@ -968,9 +1016,11 @@ struct Scanner {
 };
 
 // ---- allocation-free scans (mrl_scan_noalloc) -------------------------------
-// Scratch of mrl_scan_noalloc: [status word, padded to 256 B][ADC map of one
-// launch (int)][receive partial sums (float2)].  One array per process per
-// device, shared by every call.
+// Scratch of mrl_scan_noalloc: [status word, padded to 256 B][kernel
+// launch descriptor, padded to 256 B][ADC map of one launch (int)][receive
+// partial sums (float2)].  One array per process per device, shared by
+// every call.
+constexpr size_t kNoAllocDescBytes = (sizeof(FastLaunch) + 255) / 256 * 256;
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -1226,14 +1276,16 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
     const int npairs = sc.mi.nsamp * sc.RX;
     const long long nslices = nblk * partial_slices(true);
     const double per_sample = sizeof(int) + (double)nslices * npairs * sizeof(float2);
-    const long long a_cap = (long long)((kNoAllocScratchBytes - 256) / per_sample);
+    const long long a_cap = (long long)((kNoAllocScratchBytes - 256 - kNoAllocDescBytes) / per_sample);
     if (a_cap < 1) {
         set_err("object too large for the %zu-byte scratch: one ADC sample needs %.0f bytes", kNoAllocScratchBytes,
                 per_sample);
         return MRL_ERR_UNSUPPORTED;
     }
-    int *d_amap = reinterpret_cast<int *>(scratch + 256);
-    float2 *d_part = reinterpret_cast<float2 *>(scratch + 256 + ((a_cap * sizeof(int) + 255) / 256) * 256);
+    FastLaunch *d_desc = reinterpret_cast<FastLaunch *>(scratch + 256);
+    int *d_amap = reinterpret_cast<int *>(scratch + 256 + kNoAllocDescBytes);
+    float2 *d_part =
+        reinterpret_cast<float2 *>(scratch + 256 + kNoAllocDescBytes + ((a_cap * sizeof(int) + 255) / 256) * 256);
     if ((e = cudaMemsetAsync(d_status, 0, sizeof(int), st)) != cudaSuccess) return sc.fail_cuda(e, "status reset");
     if ((e = cudaMemcpyAsync(d_steps, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice, st)) !=
         cudaSuccess)
@@ -1299,12 +1351,10 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
             (le = cudaMemcpyAsync(d_amap, amap.data(), amap.size() * sizeof(int), cudaMemcpyHostToDevice, st)) !=
                 cudaSuccess)
             return sc.fail_cuda(le, "upload ADC map");
-        switch (sc.mi.km) {
-        case KM_NORMAL: le = launch_scan_fast_normal(sc.P, sc.NS, dim3((unsigned)nblk), smem, st, F); break;
-        case KM_EXCH: le = launch_scan_fast_exch(sc.P, sc.NS, dim3((unsigned)nblk), smem, st, F); break;
-        case KM_MT: le = launch_scan_fast_mt(sc.P, sc.NS, dim3((unsigned)nblk), smem, st, F); break;
-        default: le = launch_scan_fast_cest(sc.P, sc.NS, dim3((unsigned)nblk), smem, st, F); break;
-        }
+        if ((le = cudaMemcpyAsync(d_desc, &F, sizeof(F), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return sc.fail_cuda(le, "upload launch descriptor");
+        const FastGrid g{d_desc, nullptr, (int)nblk, nullptr};
+        le = launch_fast(sc.mi.km, sc.P, sc.NS, F.all_free != 0, dim3((unsigned)nblk), smem, st, g);
         if (le != cudaSuccess) return sc.fail_cuda(le, "scan kernel launch");
         if (!amap.empty()) {
             const int tot = (int)amap.size() * npairs;

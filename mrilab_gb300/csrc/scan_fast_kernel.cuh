@@ -48,6 +48,7 @@ struct FastLaunch {
     float gam_hi, gam_lo;     // gyromagnetic ratio split
     float cs_hi[kMaxPool], cs_lo[kMaxPool];  // 2 pi CS[t] split
 };
+static_assert(sizeof(FastLaunch) % 4 == 0, "FastLaunch is copied to shared memory as 32-bit words");
 
 // ---- double-float helpers ------------------------------------------------
 struct df {
@@ -213,13 +214,17 @@ constexpr int fast_min_blocks() {
     return (P <= 2 && P * NS <= 8) ? 4 : ((P <= 3 && P * NS <= 6) ? 3 : 2);
 }
 
+// One work item: tile `tile` (kBlock consecutive voxel-threads) of the scan
+// described by F, over F's step range.  kbase counts the record chunks this
+// block has staged before (it picks the buffer and mbarrier phase).
+// Returns false, block-uniformly, when a wait ran out (status word raised).
 template <int MODEL, int P, int NS, bool FREE>
-__global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>()) scan_fast_kernel(FastLaunch F) {
+__device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigned char *smem, uint32_t &kbase) {
     const ScanLaunch &L = F.b;
-    extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     float4 *rbuf = reinterpret_cast<float4 *>(smem + 128);
     const int rstride = L.stride4;
+    constexpr int chunk = kFastChunk;  // a runtime length costs registers (spills at P=2, 4 spins)
     constexpr bool kMTC = MODEL == KM_MT || MODEL == KM_CEST;
     // receive tile: one row per (sample, sampled pool), one column per thread
     // holding its lab-frame transverse magnetisation; the coil sensitivities
@@ -231,14 +236,14 @@ __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>()) scan_fast_ke
     constexpr int kTRow = kBlock + 2;                             // padded row (float2)
     constexpr int kWarps = kBlock / 32;
     const int C4 = (L.rx + 3) & ~3;
-    float2 *mtile = reinterpret_cast<float2 *>(rbuf + 2 * kFastChunk * rstride);  // [16][kTRow]
+    float2 *mtile = reinterpret_cast<float2 *>(rbuf + 2 * chunk * rstride);  // [16][kTRow]
     float2 *rsm = mtile + 16 * kTRow;                                              // [C4][kTRow]
     float *wstage = reinterpret_cast<float *>(rsm + C4 * kTRow);                   // [warp][16][2*C4]
     float *dwsm = wstage + kWarps * 16 * 2 * C4;                                   // [NS * P][kBlock]
     float *omlo = dwsm + NS * P * kBlock;                                        // [4][kBlock]
 
     const int tid = threadIdx.x;
-    const long long gt = (long long)blockIdx.x * kBlock + tid;
+    const long long gt = (long long)tile * kBlock + tid;
     const int v = (int)(gt / L.tpv);
     const int sg = (int)(gt % L.tpv);
     bool active = v < L.n_act;
@@ -371,20 +376,17 @@ __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>()) scan_fast_ke
     LineshapeCache lc;
     const float gyro = L.gyro;
 
-    if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
+    __syncthreads();  // the staged coil maps
     const long long nsteps = L.s1 - L.s0;
-    const int nchunks = (int)((nsteps + kFastChunk - 1) / kFastChunk);
+    const int nchunks = (int)((nsteps + chunk - 1) / chunk);
+    // chunk k of this item uses buffer and mbarrier (kbase + k) & 1, phase ((kbase + k) >> 1) & 1
     auto issue = [&](int k) {
-        const long long first = L.s0 + (long long)k * kFastChunk;
-        const long long cnt = min((long long)kFastChunk, L.s1 - first);
+        const long long first = L.s0 + (long long)k * chunk;
+        const long long cnt = min((long long)chunk, L.s1 - first);
         const uint32_t bytes = (uint32_t)(cnt * rstride * 16);
-        mbar_expect_tx(&bar[k & 1], bytes);
-        bulk_g2s(rbuf + (k & 1) * kFastChunk * rstride, L.rec + first * rstride, bytes, &bar[k & 1]);
+        const uint32_t b = (kbase + k) & 1;
+        mbar_expect_tx(&bar[b], bytes);
+        bulk_g2s(rbuf + b * chunk * rstride, L.rec + first * rstride, bytes, &bar[b]);
     };
     if (tid == 0 && nchunks > 0) issue(0);
 
@@ -458,24 +460,29 @@ __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>()) scan_fast_ke
                 sx += red[(w * 16 + row) * (2 * C4) + 2 * c];
                 sy += red[(w * 16 + row) * (2 * C4) + 2 * c + 1];
             }
-            L.partial[((long long)blockIdx.x * L.a_launch + a_base + a) * L.npairs + t * L.rx + c] = make_float2(sx, sy);
+            L.partial[((long long)tile * L.a_launch + a_base + a) * L.npairs + t * L.rx + c] = make_float2(sx, sy);
         }
         a_base += a_fill;
         a_fill = 0;
         __syncthreads();
     };
 
-    bool ok = true;
-    for (int k = 0; k < nchunks && ok; ++k) {
+    for (int k = 0; k < nchunks; ++k) {
         if (tid == 0 && k + 1 < nchunks) issue(k + 1);
-        ok = mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, L.err);
+        const uint32_t kk = kbase + k;
+        bool ok = mbar_wait_bounded(&bar[kk & 1], (kk >> 1) & 1, L.err);
         ok = __syncthreads_and(ok) != 0;
         if (!ok) {
-            if (tid == 0) mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, L.err);
-            break;
+            // wait (bounded) for the copies still in flight: this chunk and the next
+            if (tid == 0) {
+                mbar_wait_bounded(&bar[kk & 1], (kk >> 1) & 1, L.err);
+                if (k + 1 < nchunks) mbar_wait_bounded(&bar[(kk + 1) & 1], ((kk + 1) >> 1) & 1, L.err);
+            }
+            __syncthreads();
+            return false;
         }
-        const float4 *cb = rbuf + (k & 1) * kFastChunk * rstride;
-        const int cnt = (int)min((long long)kFastChunk, nsteps - (long long)k * kFastChunk);
+        const float4 *cb = rbuf + (kk & 1) * chunk * rstride;
+        const int cnt = (int)min((long long)chunk, nsteps - (long long)k * chunk);
         for (int q = 0; q < cnt; ++q) {
             const float4 r0 = cb[q * rstride];
             const float4 r1 = cb[q * rstride + 1];
@@ -605,7 +612,7 @@ __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>()) scan_fast_ke
             }
             if (!active) continue;
             if (L.hist != nullptr) {  // RunMode 1: the state at the start of the step, lab frame
-                float *h = L.hist + (long long)(k * kFastChunk + q) * 3 * L.hist_stride;
+                float *h = L.hist + ((long long)k * chunk + q) * 3 * L.hist_stride;
 #pragma unroll
                 for (int s = 0; s < NS; ++s)
 #pragma unroll
@@ -824,6 +831,42 @@ __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>()) scan_fast_ke
                 L.mz[i] = Z[s][t];
             }
         }
+    }
+    kbase += (uint32_t)nchunks;
+    return true;
+}
+
+// The accurate scan kernel.  A block works through items (instance, tile):
+// with counter == nullptr it runs item blockIdx.x alone (one scan, one
+// block per tile); otherwise it is persistent and, after item blockIdx.x,
+// takes items gridDim.x, gridDim.x + 1, ... from *counter (the batched
+// form: the tiles of many scans, ordered longest first).  Each item's
+// descriptor is copied from descs into shared memory.
+template <int MODEL, int P, int NS, bool FREE>
+__global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>())
+    scan_fast_kernel(const FastLaunch *__restrict__ descs, const int2 *__restrict__ items, int n_items, int *counter) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ FastLaunch fs;
+    __shared__ int next_item;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    uint32_t kbase = 0;
+    for (int it = blockIdx.x; it < n_items;) {
+        const int2 item = items ? items[it] : make_int2(0, it);
+        const int *src = reinterpret_cast<const int *>(descs + item.x);
+        int *dst = reinterpret_cast<int *>(&fs);
+        for (int w = threadIdx.x; w < (int)(sizeof(FastLaunch) / 4); w += blockDim.x) dst[w] = src[w];
+        __syncthreads();
+        if (!scan_item<MODEL, P, NS, FREE>(fs, item.y, smem, kbase)) return;
+        if (counter == nullptr) break;
+        __syncthreads();  // every thread is done with fs and the item's shared memory
+        if (threadIdx.x == 0) next_item = atomicAdd(counter, 1) + (int)gridDim.x;
+        __syncthreads();
+        it = next_item;
     }
 }
 

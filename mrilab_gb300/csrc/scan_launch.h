@@ -37,19 +37,40 @@ inline size_t scan_fast_smem_bytes(int stride4, int rx, int P, int NS) {
     const size_t c4 = (size_t)((rx + 3) & ~3);
     const size_t row = kBlock + 2;
     return 128 + (size_t)2 * kFastChunk * stride4 * 16  // staged step records
-           + 16 * row * 8 + c4 * row * 8                 // receive tile, coil maps
-           + (kBlock / 32) * 16 * 2 * c4 * 4             // per-warp receive sums
-           + ((size_t)NS * P + 4) * kBlock * 4;          // dWRnd, low parts of omega
+           + 16 * row * 8 + c4 * row * 8            // receive tile, coil maps
+           + (kBlock / 32) * 16 * 2 * c4 * 4        // per-warp receive sums
+           + ((size_t)NS * P + 4) * kBlock * 4;     // dWRnd, low parts of omega
 }
+
+// One launch of the accurate kernel: n_items work items (instance, tile)
+// of the scans described by descs (device memory).  items == nullptr: a
+// single scan, item i = tile i, one block per item.  counter != nullptr
+// (device int, zero at launch): a persistent grid that takes further items
+// from the counter.
+struct FastGrid {
+    const FastLaunch *descs;
+    const int2 *items;
+    int n_items;
+    int *counter;
+};
 
 cudaError_t launch_scan_ref_normal(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
 cudaError_t launch_scan_ref_exch(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
 cudaError_t launch_scan_ref_mt(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
 cudaError_t launch_scan_ref_cest(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const ScanLaunch &L);
 
-cudaError_t launch_scan_fast_normal(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastLaunch &F);
-cudaError_t launch_scan_fast_exch(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastLaunch &F);
-cudaError_t launch_scan_fast_mt(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastLaunch &F);
-cudaError_t launch_scan_fast_cest(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastLaunch &F);
+cudaError_t launch_scan_fast_normal(int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
+                                    const FastGrid &g);
+cudaError_t launch_scan_fast_exch(int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
+                                  const FastGrid &g);
+cudaError_t launch_scan_fast_mt(int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
+                                const FastGrid &g);
+cudaError_t launch_scan_fast_cest(int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
+                                  const FastGrid &g);
+// resident blocks per SM of an instantiation at `smem` bytes (0 if none)
+int occupancy_scan_fast_normal(int P, int NS, bool all_free, size_t smem);
+int occupancy_scan_fast_exch(int P, int NS, bool all_free, size_t smem);
+int occupancy_scan_fast_mt(int P, int NS, bool all_free, size_t smem);
+int occupancy_scan_fast_cest(int P, int NS, bool all_free, size_t smem);
 
 }  // namespace mrl
