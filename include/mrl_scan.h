@@ -177,6 +177,41 @@ int mrl_plan_download(mrl_plan *plan, mrl_scan_args *args);
 int mrl_plan_work(const mrl_plan *plan, long long out[5]);
 void mrl_plan_destroy(mrl_plan *plan);
 
+/* Batched scans: many independent scans (phantoms, sequences, coils of any
+ * size) prepared together and run together on one GPU.  MRiLab's batch
+ * mode calls the engine once per instance (Src/Main/BatchSim.m:160); here
+ * the instances' tiles of 128 voxel-threads share one persistent launch
+ * per kernel instantiation (tissue model, pools, spins per thread),
+ * ordered longest first, and the receive sums of every instance are
+ * reduced by one kernel.
+ *
+ * mrl_batch_create takes n scan descriptions (MRL_NUMERICS_ACCURATE,
+ * RunMode 0, no Ext events; host pointers as for mrl_scan), uploads them
+ * and decodes every sequence once.  mrl_batch_execute runs every scan from
+ * its initial magnetisation, asynchronously on `stream`:
+ *   MRL_BATCH_PERSISTENT  the batched form; captured into a CUDA graph on
+ *                         its first use and replayed afterwards;
+ *   MRL_BATCH_PLAIN       one launch (and one reduction) per instance, in
+ *                         turn -- the per-instance form, for comparison.
+ * mrl_batch_tune times candidate spins-per-thread and resident-blocks-per-SM
+ * settings of every instantiation on a prefix of the steps and keeps the
+ * fastest (it changes no result beyond float rounding).
+ * mrl_batch_download writes Sx/Sy, Kx/Ky/Kz and the final Mx/My/Mz of
+ * instance i into the host arrays named by args[i].
+ * mrl_batch_work: [0] isochromat-pool-steps, [1] dt>0 steps, [2] acquired
+ * samples, summed over the instances, [3] kernel launches of one batched
+ * execution, [4] of one plain execution.
+ * mrl_scan_batched: create, execute (batched), download, destroy. */
+enum { MRL_BATCH_PERSISTENT = 0, MRL_BATCH_PLAIN = 1 };
+typedef struct mrl_batch mrl_batch;
+int mrl_batch_create(mrl_scan_args *const *args, int n, mrl_batch **out);
+int mrl_batch_tune(mrl_batch *batch, void *stream);
+int mrl_batch_execute(mrl_batch *batch, int mode, void *stream);
+int mrl_batch_download(mrl_batch *batch, mrl_scan_args *const *args, int n);
+int mrl_batch_work(const mrl_batch *batch, long long out[5]);
+void mrl_batch_destroy(mrl_batch *batch);
+int mrl_scan_batched(mrl_scan_args *const *args, int n);
+
 /* Scan without allocating device memory.
  *
  * For callers that cannot call cudaMalloc themselves -- code running inside

@@ -22,7 +22,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -53,12 +55,12 @@ void set_err(const char *fmt, ...) {
 // split the scan blocks (warp w sums blocks w, w + 8, ...; 256-byte loads)
 // and their sums are added in a fixed order, so results are reproducible.
 constexpr int kRedWarps = 8;
-__global__ void __launch_bounds__(32 * kRedWarps)
-    reduce_partials(const float2 *__restrict__ partial, int nblk, int a_launch, int npairs, int rx,
-                    const int *__restrict__ amap, int A, double *sx, double *sy, double cr, double sr) {
+__device__ __forceinline__ void reduce_block(int bx, const float2 *__restrict__ partial, int nblk, int a_launch,
+                                             int npairs, int rx, const int *__restrict__ amap, int A, double *sx,
+                                             double *sy, double cr, double sr) {
     __shared__ double2 red[kRedWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int o = blockIdx.x * 32 + lane;
+    const int o = bx * 32 + lane;
     const int tot = a_launch * npairs;
     double x = 0.0, y = 0.0;
     if (o < tot) {
@@ -101,6 +103,28 @@ __global__ void __launch_bounds__(32 * kRedWarps)
     const long long idx = ((long long)t * rx + c) * A + sig;
     sx[idx] = cr * x - sr * y;
     sy[idx] = sr * x + cr * y;
+}
+
+__global__ void __launch_bounds__(32 * kRedWarps)
+    reduce_partials(const float2 *__restrict__ partial, int nblk, int a_launch, int npairs, int rx,
+                    const int *__restrict__ amap, int A, double *sx, double *sy, double cr, double sr) {
+    reduce_block(blockIdx.x, partial, nblk, a_launch, npairs, rx, amap, A, sx, sy, cr, sr);
+}
+
+// The receive reduction of many scans in one launch: blockIdx.y picks the
+// scan, blockIdx.x its block of 32 outputs.
+struct RedDesc {
+    const float2 *partial;
+    const int *amap;
+    double *sx, *sy;
+    double cr, sr;
+    int nblk, a_launch, npairs, rx, A;
+};
+
+__global__ void __launch_bounds__(32 * kRedWarps) reduce_partials_batched(const RedDesc *__restrict__ descs) {
+    const RedDesc &d = descs[blockIdx.y];
+    if ((int)blockIdx.x * 32 >= d.a_launch * d.npairs) return;  // block-uniform
+    reduce_block(blockIdx.x, d.partial, d.nblk, d.a_launch, d.npairs, d.rx, d.amap, d.A, d.sx, d.sy, d.cr, d.sr);
 }
 
 // ---- object staging on the device -------------------------------------------
@@ -339,11 +363,13 @@ struct Scanner {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_scan, ev_red;
     int launches = 0;
     double h2d_ms = 0, d2h_ms = 0, h2d_bytes = 0, d2h_bytes = 0;
+    bool own_st = true;          // false: st belongs to the caller (batched scans)
+    double partial_budget = 0;   // bytes of receive partials per launch; 0: MRL_PARTIAL_MB or 4 GiB
 
     ~Scanner() {
         for (auto &e : ev_scan) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
         for (auto &e : ev_red) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
-        if (st) cudaStreamDestroy(st);
+        if (st && own_st) cudaStreamDestroy(st);
     }
 
     // every pool of an exchange model is a free pool (ME, or GM without bound pools)
@@ -668,7 +694,7 @@ struct Scanner {
         if (ch.n_steps == 0) return MRL_OK;
         const int npairs = mi.nsamp * RX;
         const char *env = getenv("MRL_PARTIAL_MB");
-        const double budget = (env ? atof(env) : 4096.0) * 1048576.0;
+        const double budget = partial_budget > 0 ? partial_budget : (env ? atof(env) : 4096.0) * 1048576.0;
         const long long a_max =
             std::max(1LL, (long long)(budget / ((double)n_slices() * npairs * sizeof(float2))));
         long long s0 = 0;
@@ -845,7 +871,7 @@ struct Scanner {
             set_err("cudaSetDevice(%d): %s", dev, cudaGetErrorString(e));
             return e == cudaErrorNoDevice || e == cudaErrorInvalidDevice ? MRL_ERR_NO_DEVICE : MRL_ERR_CUDA;
         }
-        if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess)
+        if (!st && (e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess)
             return fail_cuda(e, "cudaStreamCreate");
         if ((e = d_err.ensure(1)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(err)");
         cudaMemsetAsync(d_err.p, 0, sizeof(int), st);
@@ -932,6 +958,22 @@ struct Scanner {
             }
         }
         return MRL_OK;
+    }
+
+    // Active isochromat-pools (the work of one step).
+    long long iso_pools() const {
+        const mrl_scan_args &a = *args;
+        long long n = 0;
+        for (int i = 0; i < n_act; ++i) {
+            const long long v = act[i];
+            if (mi.km == KM_MT || mi.km == KM_CEST) {
+                n += P;
+            } else {
+                for (int t = 0; t < P; ++t)
+                    n += a.obj.t1[t * V + v] != 0.f && a.obj.t2[t * V + v] != 0.f && a.obj.rho[t * V + v] != 0.f;
+            }
+        }
+        return n * S;
     }
 
     int check_device_status() {
@@ -1078,6 +1120,206 @@ struct mrl_plan {
     long long work[5] = {0, 0, 0, 0, 0};
 };
 
+// Batched scans: one Scanner per instance (sharing the batch's stream), the
+// instances grouped by kernel instantiation, one persistent launch per group.
+struct mrl_batch {
+    struct Inst {
+        std::unique_ptr<mrl::Scanner> sc;
+        mrl_scan_args args{};
+        mrl::DevBuf<float> d_m0;                     // initial magnetisation
+        std::vector<mrl::Scanner::LaunchDesc> ls;    // exactly one launch
+        std::vector<double> kx, ky, kz;
+        double rf_ref = 0;
+        long long steps = 0, rf_steps = 0, units = 0, samples = 0;
+        int group = -1, slot = -1;                   // group and descriptor slot in it
+    };
+    struct Group {
+        int km = 0, P = 0, NS = 1;
+        bool free = false;
+        int cap = 0;                                 // resident blocks per SM (0: occupancy)
+        std::vector<int> inst;
+        size_t smem = 0;
+        int grid = 0, n_items = 0;
+        mrl::DevBuf<mrl::FastLaunch> descs;
+        mrl::DevBuf<int2> items;
+        mrl::DevBuf<int> counter;
+        cudaStream_t st = nullptr;
+        cudaEvent_t done = nullptr;
+    };
+    std::vector<Inst> in;
+    std::vector<Group> groups;
+    mrl::DevBuf<int> d_err;
+    mrl::DevBuf<mrl::RedDesc> d_red;
+    int red_x = 0, device = 0, sms = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+    void drop_groups() {
+        for (Group &g : groups) {
+            if (g.st) cudaStreamDestroy(g.st);
+            if (g.done) cudaEventDestroy(g.done);
+        }
+        groups.clear();
+    }
+    ~mrl_batch() {
+        drop_graph();
+        drop_groups();
+        in.clear();  // Scanners before the stream they use
+        if (fork) cudaEventDestroy(fork);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+namespace mrl {
+namespace {
+
+// Descriptor of instance `it` for a run over at most `max_steps` steps.
+FastLaunch batch_desc(mrl_batch &b, mrl_batch::Inst &it, long long max_steps) {
+    Scanner &sc = *it.sc;
+    ScanLaunch L = sc.launch_fields(it.ls[0], it.rf_ref);
+    if (max_steps >= 0) L.s1 = std::min(L.s1, L.s0 + max_steps);
+    L.err = b.d_err.p;
+    return sc.fast_launch(L);
+}
+
+// (Re)build the groups from every instance's current spins per thread:
+// descriptors, the item list ordered longest first, the persistent grid.
+int batch_build(mrl_batch &b, long long max_steps) {
+    std::vector<int> caps;
+    for (auto &g : b.groups) caps.push_back(g.cap);
+    std::vector<std::tuple<int, int, int, bool, int>> keys;
+    for (auto &g : b.groups) keys.emplace_back(g.km, g.P, g.NS, g.free, g.cap);
+    b.drop_groups();
+    for (size_t i = 0; i < b.in.size(); ++i) {
+        Scanner &sc = *b.in[i].sc;
+        const bool fr = sc.all_free() != 0;
+        int gi = -1;
+        for (size_t k = 0; k < b.groups.size(); ++k) {
+            const auto &g = b.groups[k];
+            if (g.km == sc.mi.km && g.P == sc.P && g.NS == sc.NS && g.free == fr) gi = (int)k;
+        }
+        if (gi < 0) {
+            mrl_batch::Group g;
+            g.km = sc.mi.km;
+            g.P = sc.P;
+            g.NS = sc.NS;
+            g.free = fr;
+            for (auto &k : keys)  // keep a tuned resident-block cap
+                if (std::get<0>(k) == g.km && std::get<1>(k) == g.P && std::get<2>(k) == g.NS &&
+                    std::get<3>(k) == g.free)
+                    g.cap = std::get<4>(k);
+            b.groups.push_back(std::move(g));
+            gi = (int)b.groups.size() - 1;
+        }
+        b.in[i].group = gi;
+        b.in[i].slot = (int)b.groups[gi].inst.size();
+        b.groups[gi].inst.push_back((int)i);
+    }
+    for (auto &g : b.groups) {
+        std::vector<FastLaunch> h;
+        std::vector<std::pair<long long, int2>> items;  // (cost, item)
+        g.smem = 0;
+        for (int i : g.inst) {
+            mrl_batch::Inst &it = b.in[i];
+            Scanner &sc = *it.sc;
+            h.push_back(batch_desc(b, it, max_steps));
+            g.smem = std::max(g.smem, scan_fast_smem_bytes(sc.stride4, sc.RX, sc.P, sc.NS));
+            const long long steps = max_steps >= 0 ? std::min(it.steps, max_steps) : it.steps;
+            const long long cost = steps + 3 * std::min(it.rf_steps, steps);  // an rf step costs ~4 free steps
+            const int nblk = sc.n_act > 0 ? (int)sc.n_blocks() : 0;
+            for (int t = 0; t < nblk; ++t) items.push_back({cost, make_int2(it.slot, t)});
+        }
+        std::stable_sort(items.begin(), items.end(),
+                         [](const std::pair<long long, int2> &x, const std::pair<long long, int2> &y) {
+                             return x.first > y.first;
+                         });
+        std::vector<int2> hi;
+        for (auto &x : items) hi.push_back(x.second);
+        g.n_items = (int)hi.size();
+        cudaError_t e = g.descs.ensure(h.size());
+        if (e == cudaSuccess) e = g.items.ensure(std::max<size_t>(1, hi.size()));
+        if (e == cudaSuccess) e = g.counter.ensure(1);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(g.descs.p, h.data(), h.size() * sizeof(FastLaunch), cudaMemcpyHostToDevice, b.st);
+        if (e == cudaSuccess && !hi.empty())
+            e = cudaMemcpyAsync(g.items.p, hi.data(), hi.size() * sizeof(int2), cudaMemcpyHostToDevice, b.st);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b.st);
+        if (e != cudaSuccess) return set_err("batch setup: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+        const int occ = occupancy_fast(g.km, g.P, g.NS, g.free, g.smem);
+        if (occ < 1) return set_err("batch: kernel does not fit (%zu bytes of shared memory)", g.smem), MRL_ERR_UNSUPPORTED;
+        const int per_sm = g.cap > 0 ? std::min(g.cap, occ) : occ;
+        g.grid = std::max(1, std::min(g.n_items, per_sm * b.sms));
+    }
+    // receive reduction of every instance (block counts follow the spins per thread)
+    std::vector<RedDesc> rd;
+    b.red_x = 0;
+    for (auto &it : b.in) {
+        Scanner &sc = *it.sc;
+        const Scanner::LaunchDesc &d = it.ls[0];
+        RedDesc r{};
+        r.partial = sc.d_part.p;
+        r.amap = sc.d_amap.p + d.a_off;
+        r.sx = sc.d_sx.p;
+        r.sy = sc.d_sy.p;
+        r.cr = std::cos(-it.rf_ref);
+        r.sr = std::sin(-it.rf_ref);
+        r.nblk = (int)sc.n_slices();
+        r.a_launch = sc.n_act > 0 ? d.a_count : 0;
+        r.npairs = sc.mi.nsamp * sc.RX;
+        r.rx = sc.RX;
+        r.A = sc.A;
+        rd.push_back(r);
+        b.red_x = std::max(b.red_x, (r.a_launch * r.npairs + 31) / 32);
+    }
+    cudaError_t e = b.d_red.ensure(rd.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b.d_red.p, rd.data(), rd.size() * sizeof(RedDesc), cudaMemcpyHostToDevice, b.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b.st);
+    if (e != cudaSuccess) return set_err("batch setup: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+    return MRL_OK;
+}
+
+// Enqueue one batched execution on s: reset, one persistent launch per
+// group on the groups' streams (forked from and joined back into s), then
+// the receive reduction of every instance.
+int batch_record(mrl_batch &b, cudaStream_t s, bool reduce) {
+    cudaError_t e = cudaMemsetAsync(b.d_err.p, 0, sizeof(int), s);
+    for (auto &it : b.in)
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(it.sc->d_m.p, it.d_m0.p, it.d_m0.n * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    for (auto &g : b.groups)
+        if (e == cudaSuccess) e = cudaMemsetAsync(g.counter.p, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaEventRecord(b.fork, s);
+    for (auto &g : b.groups) {
+        if (e != cudaSuccess) break;
+        e = cudaStreamWaitEvent(g.st, b.fork, 0);
+        if (e == cudaSuccess && g.n_items > 0)
+            e = launch_fast(g.km, g.P, g.NS, g.free, dim3(g.grid), g.smem, g.st,
+                            FastGrid{g.descs.p, g.items.p, g.n_items, g.counter.p});
+        if (e == cudaSuccess) e = cudaEventRecord(g.done, g.st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g.done, 0);
+    }
+    if (e == cudaSuccess && reduce && b.red_x > 0) {
+        reduce_partials_batched<<<dim3(b.red_x, (unsigned)b.in.size()), 32 * kRedWarps, 0, s>>>(b.d_red.p);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return set_err("batch launch: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+    return MRL_OK;
+}
+
+}  // namespace
+}  // namespace mrl
+
 extern "C" {
 
 int mrl_scan(mrl_scan_args *args, mrl_ext_fn ext, void *user) {
@@ -1158,21 +1400,9 @@ int mrl_plan_create(const mrl_scan_args *args, mrl_plan **out) {
         delete p;
         return MRL_ERR_CUDA;
     }
-    // work units: active isochromat-pools x dt>0 steps
-    long long iso_pools = 0;
-    for (int i = 0; i < sc.n_act; ++i) {
-        const long long v = sc.act[i];
-        if (sc.mi.km == mrl::KM_MT || sc.mi.km == mrl::KM_CEST) {
-            iso_pools += sc.P;
-        } else {
-            for (int t = 0; t < sc.P; ++t)
-                iso_pools += args->obj.t1[t * sc.V + v] != 0.f && args->obj.t2[t * sc.V + v] != 0.f &&
-                             args->obj.rho[t * sc.V + v] != 0.f;
-        }
-    }
     long long launches = 0;
     for (auto &d : p->ls) launches += 1 + (d.a_count > 0 ? 1 : 0);
-    p->work[0] = iso_pools * sc.S * ch.n_steps;
+    p->work[0] = sc.iso_pools() * ch.n_steps;  // active isochromat-pools x dt>0 steps
     p->work[1] = ch.n_steps;
     p->work[2] = ch.n_rf_steps;
     p->work[3] = ch.adc_end - ch.adc_begin;
@@ -1215,6 +1445,281 @@ int mrl_plan_work(const mrl_plan *p, long long out[5]) {
 }
 
 void mrl_plan_destroy(mrl_plan *p) { delete p; }
+
+int mrl_batch_create(mrl_scan_args *const *args, int n, mrl_batch **out) {
+    using namespace mrl;
+    g_err.clear();
+    if (!args || n < 1 || !out) {
+        set_err("mrl_batch_create: NULL argument or n < 1");
+        return MRL_ERR_ARG;
+    }
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        if (!args[i]) return set_err("instance %d: NULL", i), MRL_ERR_ARG;
+        if (args[i]->ctl.gpu_index != args[0]->ctl.gpu_index)
+            return set_err("instance %d: every instance of a batch runs on one GPU", i), MRL_ERR_ARG;
+        if (args[i]->ctl.run_mode == 1)
+            return set_err("instance %d: batches do not record RunMode 1 history", i), MRL_ERR_UNSUPPORTED;
+        if (args[i]->ctl.numerics != MRL_NUMERICS_ACCURATE)
+            return set_err("instance %d: batches run MRL_NUMERICS_ACCURATE", i), MRL_ERR_UNSUPPORTED;
+    }
+    std::unique_ptr<mrl_batch> b(new mrl_batch());
+    b->device = args[0]->ctl.gpu_index;
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) {
+        set_err("cudaSetDevice(%d): %s", b->device, cudaGetErrorString(e));
+        return e == cudaErrorNoDevice || e == cudaErrorInvalidDevice ? MRL_ERR_NO_DEVICE : MRL_ERR_CUDA;
+    }
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = b->d_err.ensure(1);
+    if (e != cudaSuccess) return set_err("batch setup: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+    b->in.resize(n);
+    for (int i = 0; i < n; ++i) {
+        mrl_batch::Inst &it = b->in[i];
+        it.args = *args[i];
+        it.sc.reset(new Scanner());
+        Scanner &sc = *it.sc;
+        sc.args = &it.args;
+        sc.st = b->st;
+        sc.own_st = false;
+        sc.partial_budget = 1e18;  // one launch per instance
+        int rc = sc.setup();
+        if (rc) {
+            const std::string why = g_err;
+            set_err("instance %d: %s", i, why.c_str());
+            return rc;
+        }
+        it.kx.assign(std::max(sc.A, 1), 0.0);
+        it.ky.assign(std::max(sc.A, 1), 0.0);
+        it.kz.assign(std::max(sc.A, 1), 0.0);
+        mrl_signal sig = it.args.sig;
+        sig.kx = it.kx.data();
+        sig.ky = it.ky.data();
+        sig.kz = it.kz.data();
+        DecodeState ds;
+        mrl_state none{};
+        load_state(ds, none, sc.TX);
+        DecodeChunk ch;
+        decode_until_ext(ds, it.args.seq, sc.TX, it.args.obj.gyro, sig, ch);
+        if (ch.stopped_at_ext) return set_err("instance %d: the sequence has Ext events", i), MRL_ERR_UNSUPPORTED;
+        if ((rc = sc.prepare_chunk(ch, it.ls))) return rc;
+        if (it.ls.size() != 1) return set_err("instance %d: receive partials do not fit one launch", i), MRL_ERR_NOMEM;
+        // room for the partials of one spin per thread, the most blocks the tuner may pick
+        const long long nblk1 = std::max(1LL, ((long long)sc.n_act * sc.S + kBlock - 1) / kBlock);
+        if ((e = sc.d_part.ensure((size_t)nblk1 * std::max(1, it.ls[0].a_count) * sc.mi.nsamp * sc.RX)) !=
+            cudaSuccess)
+            return sc.fail_cuda(e, "cudaMalloc(partials)");
+        it.rf_ref = it.args.var.rf_ref ? *it.args.var.rf_ref : 0.0;
+        if ((e = it.d_m0.ensure(sc.d_m.n)) == cudaSuccess)
+            e = cudaMemcpyAsync(it.d_m0.p, sc.d_m.p, sc.d_m.n * sizeof(float), cudaMemcpyDeviceToDevice, b->st);
+        if (e != cudaSuccess) return sc.fail_cuda(e, "batch state copy");
+        it.steps = ch.n_steps;
+        it.rf_steps = ch.n_rf_steps;
+        it.units = sc.iso_pools() * ch.n_steps;
+        it.samples = ch.adc_end - ch.adc_begin;
+    }
+    int rc = batch_build(*b, -1);
+    if (rc) return rc;
+    *out = b.release();
+    return MRL_OK;
+}
+
+int mrl_batch_execute(mrl_batch *b, int mode, void *stream) {
+    using namespace mrl;
+    if (!b || (mode != MRL_BATCH_PERSISTENT && mode != MRL_BATCH_PLAIN)) return MRL_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return set_err("cudaSetDevice: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+    if (mode == MRL_BATCH_PERSISTENT) {
+        if (!b->exec) {  // capture once, replay after
+            if ((e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+                return set_err("graph capture: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+            const int rc = batch_record(*b, b->st, true);
+            cudaGraph_t g = nullptr;
+            e = cudaStreamEndCapture(b->st, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
+            b->graph = g;
+            if (e != cudaSuccess) {
+                b->drop_graph();
+                return set_err("graph instantiate: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+            }
+        }
+        if ((e = cudaGraphLaunch(b->exec, s)) != cudaSuccess)
+            return set_err("graph launch: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+        return MRL_OK;
+    }
+    // plain: each instance in turn, its own launch and reduction
+    e = cudaMemsetAsync(b->d_err.p, 0, sizeof(int), s);
+    for (auto &it : b->in) {
+        Scanner &sc = *it.sc;
+        const mrl_batch::Group &g = b->groups[it.group];
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(sc.d_m.p, it.d_m0.p, it.d_m0.n * sizeof(float), cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess || sc.n_act == 0) continue;
+        const int nblk = (int)sc.n_blocks();
+        e = launch_fast(g.km, g.P, g.NS, g.free, dim3(nblk), scan_fast_smem_bytes(sc.stride4, sc.RX, sc.P, sc.NS), s,
+                        FastGrid{g.descs.p + it.slot, nullptr, nblk, nullptr});
+        const mrl::Scanner::LaunchDesc &d = it.ls[0];
+        if (e == cudaSuccess && d.a_count > 0) {
+            const int npairs = sc.mi.nsamp * sc.RX;
+            const int tot = d.a_count * npairs;
+            reduce_partials<<<(tot + 31) / 32, 32 * kRedWarps, 0, s>>>(
+                sc.d_part.p, (int)sc.n_slices(), d.a_count, npairs, sc.RX, sc.d_amap.p + d.a_off, sc.A, sc.d_sx.p,
+                sc.d_sy.p, std::cos(-it.rf_ref), std::sin(-it.rf_ref));
+            e = cudaGetLastError();
+        }
+    }
+    if (e != cudaSuccess) return set_err("batch launch: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+    return MRL_OK;
+}
+
+int mrl_batch_tune(mrl_batch *b, void *stream) {
+    using namespace mrl;
+    if (!b) return MRL_ERR_ARG;
+    (void)stream;  // trials run on the batch's own stream
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return set_err("cudaSetDevice: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+    constexpr long long kTrialSteps = 256;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = MRL_OK;
+    const std::vector<std::vector<int>> sets = [&] {
+        std::vector<std::vector<int>> v;
+        for (auto &g : b->groups) v.push_back(g.inst);
+        return v;
+    }();
+    for (const std::vector<int> &set : sets) {
+        if (rc) break;
+        double best = 1e300;
+        int best_ns = b->in[set[0]].sc->NS, best_cap = 0;
+        long long units = 0;
+        for (int i : set) units += b->in[i].units / std::max(1LL, b->in[i].steps) * std::min(b->in[i].steps, kTrialSteps);
+        for (int ns : {1, 2, 4}) {
+            bool ok = true;
+            for (int i : set) ok &= b->in[i].sc->S % ns == 0 && b->in[i].sc->P * ns <= 8;
+            if (!ok) continue;
+            for (int i : set) {
+                b->in[i].sc->NS = ns;
+                b->in[i].sc->tpv = b->in[i].sc->S / ns;
+            }
+            if ((rc = batch_build(*b, kTrialSteps))) break;
+            mrl_batch::Group &g = b->groups[b->in[set[0]].group];
+            const int occ = occupancy_fast(g.km, g.P, g.NS, g.free, g.smem);
+            for (int cap : {occ, occ - 1}) {
+                if (cap < 1 || g.n_items == 0) continue;
+                const int grid = std::max(1, std::min(g.n_items, cap * b->sms));
+                float ms = 0, run_best = 1e30f;
+                for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+                    for (int i : set)
+                        if (e == cudaSuccess)
+                            e = cudaMemcpyAsync(b->in[i].sc->d_m.p, b->in[i].d_m0.p, b->in[i].d_m0.n * sizeof(float),
+                                                cudaMemcpyDeviceToDevice, b->st);
+                    if (e == cudaSuccess) e = cudaMemsetAsync(g.counter.p, 0, sizeof(int), b->st);
+                    if (e == cudaSuccess) e = cudaEventRecord(e0, b->st);
+                    if (e == cudaSuccess)
+                        e = launch_fast(g.km, g.P, g.NS, g.free, dim3(grid), g.smem, b->st,
+                                        FastGrid{g.descs.p, g.items.p, g.n_items, g.counter.p});
+                    if (e == cudaSuccess) e = cudaEventRecord(e1, b->st);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                    if (rep > 0) run_best = std::min(run_best, ms);  // the first run warms up
+                }
+                if (e != cudaSuccess) break;
+                const double per_unit = run_best / std::max(1LL, units);
+                if (per_unit < best) {
+                    best = per_unit;
+                    best_ns = ns;
+                    best_cap = cap;
+                }
+            }
+            if (e != cudaSuccess) break;
+        }
+        if (e != cudaSuccess) {
+            rc = MRL_ERR_CUDA;
+            set_err("batch tune: %s", cudaGetErrorString(e));
+            break;
+        }
+        for (int i : set) {
+            b->in[i].sc->NS = best_ns;
+            b->in[i].sc->tpv = b->in[i].sc->S / best_ns;
+        }
+        if ((rc = batch_build(*b, -1))) break;
+        b->groups[b->in[set[0]].group].cap = best_cap;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!rc) rc = batch_build(*b, -1);  // final grids with the chosen caps
+    if (!rc) {
+        for (auto &it : b->in)
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(it.sc->d_m.p, it.d_m0.p, it.d_m0.n * sizeof(float), cudaMemcpyDeviceToDevice, b->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+        if (e != cudaSuccess) rc = MRL_ERR_CUDA;
+    }
+    b->drop_graph();  // the next persistent execution captures the tuned launches
+    return rc;
+}
+
+int mrl_batch_download(mrl_batch *b, mrl_scan_args *const *args, int n) {
+    using namespace mrl;
+    if (!b || !args || n != (int)b->in.size()) return MRL_ERR_ARG;
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return set_err("batch sync: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+    int herr = 0;
+    if ((e = cudaMemcpy(&herr, b->d_err.p, sizeof(int), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return set_err("batch status: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
+    if (herr) return set_err("a device wait timed out (status bits %d)", herr), MRL_ERR_TIMEOUT;
+    for (int i = 0; i < n; ++i) {
+        if (!args[i]) return MRL_ERR_ARG;
+        mrl_batch::Inst &it = b->in[i];
+        Scanner &sc = *it.sc;
+        mrl_scan_args *keep = sc.args;
+        sc.args = args[i];
+        int rc = sc.download_signal(0, sc.A);
+        if (!rc) rc = sc.download_state();
+        sc.args = keep;
+        if (rc) return rc;
+        for (int a = 0; a < sc.A; ++a) {
+            if (args[i]->sig.kx) args[i]->sig.kx[a] = it.kx[a];
+            if (args[i]->sig.ky) args[i]->sig.ky[a] = it.ky[a];
+            if (args[i]->sig.kz) args[i]->sig.kz[a] = it.kz[a];
+        }
+    }
+    return MRL_OK;
+}
+
+int mrl_batch_work(const mrl_batch *b, long long out[5]) {
+    if (!b || !out) return MRL_ERR_ARG;
+    for (int k = 0; k < 5; ++k) out[k] = 0;
+    for (const auto &it : b->in) {
+        out[0] += it.units;
+        out[1] += it.steps;
+        out[2] += it.samples;
+        out[4] += (it.sc->n_act > 0) + (it.ls[0].a_count > 0);
+    }
+    for (const auto &g : b->groups) out[3] += g.n_items > 0;
+    out[3] += b->red_x > 0;
+    return MRL_OK;
+}
+
+void mrl_batch_destroy(mrl_batch *b) { delete b; }
+
+int mrl_scan_batched(mrl_scan_args *const *args, int n) {
+    mrl_batch *b = nullptr;
+    int rc = mrl_batch_create(args, n, &b);
+    if (!rc) rc = mrl_batch_execute(b, MRL_BATCH_PERSISTENT, nullptr);
+    if (!rc) rc = mrl_batch_download(b, args, n);
+    mrl_batch_destroy(b);
+    return rc;
+}
 
 int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, void *stream) {
     using namespace mrl;

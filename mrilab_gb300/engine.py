@@ -265,3 +265,72 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+BATCH_MODES = {"persistent": 0, "plain": 1}
+
+
+class Batch:
+    """Many independent scans prepared together (``mrl_batch``): one
+    persistent launch per kernel instantiation runs them all
+    (``execute("persistent")``, captured into a CUDA graph on first use), or
+    one launch per instance in turn (``execute("plain")``)."""
+
+    def __init__(self, scans, numerics: str = "accurate", gpu_index: int = 0):
+        lib = library()
+        vp = ctypes.c_void_p
+        lib.mrl_batch_create.argtypes = [ctypes.POINTER(ctypes.POINTER(ScanArgs)), ctypes.c_int, ctypes.POINTER(vp)]
+        lib.mrl_batch_tune.argtypes = [vp, vp]
+        lib.mrl_batch_execute.argtypes = [vp, ctypes.c_int, vp]
+        lib.mrl_batch_download.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(ScanArgs)), ctypes.c_int]
+        lib.mrl_batch_work.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        lib.mrl_batch_destroy.argtypes = [vp]
+        self.lib = lib
+        self.hosts = [HostScan(sc, numerics=numerics, gpu_index=gpu_index) for sc in scans]
+        n = len(self.hosts)
+        self._arr = (ctypes.POINTER(ScanArgs) * n)(*[ctypes.pointer(h.args) for h in self.hosts])
+        self.ptr = vp()
+        self._check(lib.mrl_batch_create(self._arr, n, ctypes.byref(self.ptr)))
+
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            raise ScanError(rc, self.lib.mrl_last_error().decode())
+
+    def tune(self) -> None:
+        self._check(self.lib.mrl_batch_tune(self.ptr, None))
+
+    def execute(self, mode: str = "persistent", stream: int = 0) -> None:
+        self._check(self.lib.mrl_batch_execute(self.ptr, BATCH_MODES[mode], ctypes.c_void_p(stream)))
+
+    def download(self):
+        self._check(self.lib.mrl_batch_download(self.ptr, self._arr, len(self.hosts)))
+        return [h.outputs() for h in self.hosts]
+
+    def work(self) -> Dict[str, int]:
+        buf = (ctypes.c_longlong * 5)()
+        self.lib.mrl_batch_work(self.ptr, buf)
+        return dict(units=buf[0], steps=buf[1], samples=buf[2], launches=buf[3], plain_launches=buf[4])
+
+    def close(self) -> None:
+        if self.ptr:
+            self.lib.mrl_batch_destroy(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def scan_batched(scans, numerics: str = "accurate", gpu_index: int = 0):
+    """``mrl_scan_batched``: every scan of ``scans`` in one batched pass;
+    returns their outputs like ``scan``."""
+    lib = library()
+    lib.mrl_scan_batched.argtypes = [ctypes.POINTER(ctypes.POINTER(ScanArgs)), ctypes.c_int]
+    hosts = [HostScan(sc, numerics=numerics, gpu_index=gpu_index) for sc in scans]
+    arr = (ctypes.POINTER(ScanArgs) * len(hosts))(*[ctypes.pointer(h.args) for h in hosts])
+    rc = lib.mrl_scan_batched(arr, len(hosts))
+    if rc != 0:
+        raise ScanError(rc, lib.mrl_last_error().decode())
+    return [h.outputs() for h in hosts]

@@ -103,3 +103,14 @@ def test_no_cpu_fallback_without_gpu(built):
     with pytest.raises(engine.ScanError) as e:
         engine.run(hs)
     assert e.value.status in (-7, -2)
+
+
+def test_batch_argument_errors_are_status_codes(built):
+    lib = engine.library()
+    ptr = ctypes.c_void_p()
+    lib.mrl_batch_create.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    assert lib.mrl_batch_create(None, 0, ctypes.byref(ptr)) == -1
+    hs = engine.HostScan(phantoms.config1_gre(seed=0, n=8, n_tr=1), numerics="reference")
+    arr = (ctypes.POINTER(engine.ScanArgs) * 1)(ctypes.pointer(hs.args))
+    assert lib.mrl_batch_create(ctypes.cast(arr, ctypes.c_void_p), 1, ctypes.byref(ptr)) == -6
+    assert b"ACCURATE" in lib.mrl_last_error()
