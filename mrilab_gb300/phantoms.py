@@ -465,3 +465,88 @@ def small_multipool(model: str, seed=0, n=8, nz=1, pools=2, spins=1, coils=1, n_
     t2s = np.maximum(t2 * 0.5, 1e-6) if spins > 1 else None
     return assemble(rho, t1, t2, spin_num=spins, t2star=t2s, db0_hz=db0, res=res, cs_hz=cs, model=model,
                     rates=rates, type_flag=type_flag, rx=rx, seqlines=lines, tr_num=ntr, seed=seed)
+
+
+# ---------------------------------------------------------------------------
+# batched CEST Z-spectra (many independent instances)
+# ---------------------------------------------------------------------------
+
+PPM_3T_HZ = GAMMA / (2 * np.pi) * 3.0 * 1e-6  # Hz per ppm of the 1H resonance at 3 T
+CEST_POOLS_PPM = (3.5, 2.0, -3.5)             # amide, amine, NOE
+
+
+def zspec_lines(*, offset_hz, sat_ms, b1_ut, raster_us=10.0, flip=90.0, gamma=GAMMA):
+    """One Z-spectrum point: continuous-wave saturation at ``offset_hz`` and
+    ``b1_ut`` for ``sat_ms`` on a ``raster_us`` raster, then a hard
+    excitation and one sample of the FID."""
+    raster = int(round(raster_us * 1e3))
+    sat_ns = int(round(sat_ms * 1e6)) // raster * raster
+    t_ex = sat_ns + 200_000
+    tr_ns = t_ex + 1_000_000
+    tr = S.TR(tr_ns)
+    t = np.arange(sat_ns // raster + 1, dtype=np.int64) * raster
+    amp = np.full(t.size, b1_ut * 1e-6)
+    amp[0] = amp[-1] = 0.0
+    tr.rf(t, amp, 0.0, offset_hz)
+    t_hr, a_hr = S.hard_rf(t_ex, 100_000, flip, gamma)
+    tr.rf(t_hr, a_hr)
+    tr.adc_t += [0]
+    tr.adc_v += [0.0]
+    tr.adc([t_ex + 300_000])
+    tr.adc_t += [tr_ns]
+    tr.adc_v += [0.0]
+    return S.concat([tr]), 1
+
+
+def cest_instance(seed, n_vox, pools, offset_ppm, b1_ut, sat_ms) -> Scan:
+    """One instance of the batched CEST workload: ``n_vox`` voxels of water,
+    a semisolid MT pool and ``pools - 2`` CEST pools (amide, amine, NOE),
+    fractions U(0.001, 0.1), exchange rates U(10, 5000) /s (pool -> water;
+    water -> pool by detailed balance), dB0 N(0, 10 Hz), 3 T."""
+    rng = np.random.default_rng(seed)
+    P = pools
+    shape = (n_vox, 1, 1)
+    frac = rng.uniform(0.001, 0.1, shape + (P,))
+    frac[..., 0] = 1.0
+    rho = frac.astype(np.float32)
+    t1 = np.empty(shape + (P,), np.float32)
+    t2 = np.empty(shape + (P,), np.float32)
+    t1[..., 0] = rng.uniform(0.8, 1.6, shape)
+    t2[..., 0] = rng.uniform(0.04, 0.1, shape)
+    t1[..., 1] = 1.0
+    t2[..., 1] = 10e-6  # semisolid (super-Lorentzian lineshape)
+    for p in range(2, P):
+        t1[..., p] = 1.0
+        t2[..., p] = rng.uniform(0.005, 0.02, shape)
+    rates = np.zeros(shape + (P, P), np.float32)
+    for p in range(1, P):
+        k = rng.uniform(10, 5000, shape)
+        rates[..., p, 0] = k
+        rates[..., 0, p] = k * rho[..., p] / rho[..., 0]
+    cs = np.zeros(P)
+    cs[2:] = np.array(CEST_POOLS_PPM[:P - 2]) * PPM_3T_HZ
+    lines, ntr = zspec_lines(offset_hz=offset_ppm * PPM_3T_HZ, sat_ms=sat_ms, b1_ut=b1_ut)
+    return assemble(rho, t1, t2, db0_hz=rng.normal(0.0, 10.0, shape), res=(1e-3, 1e-3, 1e-3), cs_hz=cs,
+                    model="cest", rates=rates, seqlines=lines, tr_num=ntr, seed=seed)
+
+
+def config3_batch(seed=0, n_inst=256, vox_range=(1000, 262144), sat_s=(1.0, 4.0), sat_scale=1.0 / 40,
+                  n_offsets=51, vox_scale=1.0):
+    """The batched CEST workload: ``n_inst`` instances with log-uniform voxel
+    counts in ``vox_range`` (times ``vox_scale``), 3-5 pools, one of
+    ``n_offsets`` offsets in +-6 ppm, B1 U(0.5, 3) uT and a saturation of
+    U(``sat_s``) seconds times ``sat_scale`` (the timed subset of the 1-4 s
+    trains).  Returns the list of scans and their description."""
+    rng = np.random.default_rng(seed)
+    offsets = np.linspace(-6.0, 6.0, n_offsets)
+    scans, meta = [], []
+    for i in range(n_inst):
+        nv = int(round(np.exp(rng.uniform(np.log(vox_range[0]), np.log(vox_range[1]))) * vox_scale))
+        nv = max(nv, 1)
+        pools = int(rng.integers(3, 6))
+        off = float(offsets[rng.integers(0, n_offsets)])
+        b1 = float(rng.uniform(0.5, 3.0))
+        sat_ms = float(rng.uniform(*sat_s)) * sat_scale * 1e3
+        scans.append(cest_instance(seed * 100003 + i, nv, pools, off, b1, sat_ms))
+        meta.append(dict(voxels=nv, pools=pools, offset_ppm=off, b1_ut=b1, sat_ms=sat_ms))
+    return scans, meta
