@@ -241,11 +241,15 @@ void pack_fast_records(const DecodeChunk &ch, int tx, FrameMoments &fm, std::vec
         const bool new_state = new_dt || si.gx != fm.last_gx || si.gy != fm.last_gy || si.gz != fm.last_gz;
         if (new_dt) flags |= kFlagDt;
         if (new_state) flags |= kFlagState;
-        if (new_state || rf || fm.since_anchor >= every) {
+        // anchor the frames at every change of (dt, G), at the first step of
+        // an rf block and after `every` free steps; within an rf block the
+        // frames hold still, so their phasors stay exact without anchors
+        if (new_state || (rf && !fm.last_rf) || (!rf && fm.since_anchor >= every)) {
             flags |= kFlagAnchor;
             fm.since_anchor = 0;
         }
-        fm.since_anchor++;
+        if (!rf) fm.since_anchor++;
+        fm.last_rf = rf;
         fm.last_dt = si.dt;
         fm.last_gx = si.gx;
         fm.last_gy = si.gy;

@@ -70,7 +70,8 @@ void store_state(const DecodeState &s, mrl_state &v, int tx_num);
 struct FrameMoments {
     double t = 0, kx = 0, ky = 0, kz = 0;
     double last_dt = -1, last_gx = 0, last_gy = 0, last_gz = 0;
-    int since_anchor = 1 << 30;
+    int since_anchor = 1 << 30;  // free steps since the last anchor
+    bool last_rf = false;
 };
 
 // Step record of the MRL_NUMERICS_ACCURATE integrator (16 floats + 4 per

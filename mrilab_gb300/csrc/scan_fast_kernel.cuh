@@ -11,8 +11,9 @@
 // Between anchors P_t advances by a factor (1 + d_t), d_t = exp(-i theta) - 1
 // evaluated once per change of (dt, G); P_t is recomputed exactly from the
 // moments (double-float arithmetic, Cody-Waite reduction) at every change
-// of (dt, G), every rf step and at least every kAnchorEvery steps, so the
-// large gradient and off-resonance phases never accumulate rounding.  In
+// of (dt, G), the first step of every rf block (the frames hold still
+// during rf) and at least every kAnchorEvery free steps, so the large
+// gradient and off-resonance phases never accumulate rounding.  In
 // its pool's frame an isochromat only sees its own small residual
 // frequency dWRnd, relaxation and exchange: a free step is the increment
 //   m += dm m + sum_p f_tp (P_p,before / P_t,after) m_p,
@@ -166,6 +167,29 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// Super-Lorentzian lineshape of a bound pool by the reference's rule
+// (BlochKernelMT.cuh:348-358): G = sum over u = p / 1000, p < 1000, of
+// sqrt(2 / pi) T2b / |3u^2 - 1| exp(-2 x^2) / 1000, x = w T2b / (3u^2 - 1),
+// w = 2 pi rf_freq + gamma dB0.  In single precision with an exact u and a
+// compensated (Kahan) sum: the reference-order kernel keeps the
+// reference's double-precision arithmetic, which on this GPU's FP64 pipe
+// costs more than the rf steps it feeds.
+static __device__ __noinline__ float lineshape_f32(float rf_freq, float db0, float gyro, float t2b) {
+    const float a = fmaf((float)(2 * kPiRef), rf_freq, db0 * gyro) * t2b;
+    float g = 0.f, comp = 0.f;
+    for (int p = 0; p < 1000; ++p) {
+        const float u = (float)p * 0.001f;
+        const float den = fmaf(3.f * u, u, -1.f);
+        const float inv = 1.f / den;
+        const float x = a * inv;
+        const float term = fabsf(inv) * __expf(-2.f * x * x) - comp;
+        const float sum = g + term;
+        comp = (sum - g) - term;
+        g = sum;
+    }
+    return g * (0.79788456080286536f * 0.001f) * t2b;  // sqrt(2 / pi) / 1000
+}
+
 // y = 1 - exp(-x)
 __device__ __forceinline__ float one_minus_exp(float x) { return -expm1f(-x); }
 
@@ -211,7 +235,7 @@ __device__ __forceinline__ constexpr bool has_frame(int t) {
 // while a thread's isochromat state is small.
 template <int P, int NS>
 constexpr int fast_min_blocks() {
-    return (P <= 2 && P * NS <= 8) ? 4 : ((P <= 3 && P * NS <= 6) ? 3 : 2);
+    return (P <= 2 && P * NS <= 8) ? 4 : (((P <= 3 && P * NS <= 6) || P * NS <= 5) ? 3 : 2);
 }
 
 // One work item: tile `tile` (kBlock consecutive voxel-threads) of the scan
@@ -689,9 +713,10 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                         if (lc.t2b != t2v[t] || lc.freq != freq) {
                             lc.freq = freq;
                             lc.t2b = t2v[t];
-                            lc.g = lineshape(freq, db0, gyro, t2v[t]);
+                            lc.g = lineshape_f32(freq, db0, gyro, t2v[t]);
                         }
-                        const float w = (float)(kPiRef * (double)((b1 * gyro) * (b1 * gyro)) * (double)lc.g);
+                        const float bg = b1 * gyro;
+                        const float w = (float)kPiRef * bg * bg * lc.g;
                         sat[t] = one_minus_exp(w * dt);
                     }
                 }
