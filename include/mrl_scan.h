@@ -212,6 +212,38 @@ int mrl_batch_work(const mrl_batch *batch, long long out[5]);
 void mrl_batch_destroy(mrl_batch *batch);
 int mrl_scan_batched(mrl_scan_args *const *args, int n);
 
+/* Adjoint scan: the gradient of a loss L of the signal with respect to the
+ * tissue parameters, the initial magnetisation and the rf waveform, given
+ * dL/dSx and dL/dSy (for example 2 (S - target) for an L2 loss).  The
+ * reference has no gradients; this runs the discrete map the integrator
+ * applies (rotation, relaxation, split exchange) backwards, with the state
+ * checkpointed every few steps and recomputed in between.
+ * Scope: free-pool models (normal; ME, or GM without bound pools), one Tx
+ * coil, RunMode 0, no Ext events, TypeNum <= 3; rfRef is taken as 0.
+ * Host arrays (NULL: not wanted), V voxels, layouts as in mrl_scan_args:
+ *   grad_sx, grad_sy  [P][Rx][A]   inputs
+ *   g_t1, g_t2, g_rho [P][V]       dL/dT1, dL/dT2, dL/dRho (the recovery
+ *                                  term; the initial state's share is in g_mz0)
+ *   g_db0             [V]          dL/d dB0
+ *   g_k               [nK][V]      dL/dK, the model's exchange channels
+ *   g_mx0, g_my0, g_mz0 [P][S][V]  dL/d(initial Mx, My, Mz)
+ *   g_rf              [rf_capacity][2] dL/dRe A, dL/dIm A of every rf-on
+ *                                  step in sequence order (A = rfAmp e^{i rfPhase})
+ *   rf_a              [rf_capacity][2] Re A, Im A of each of those steps
+ *   rf_step_uts       [rf_capacity] the uts index of each of those steps
+ * n_rf_steps receives the number of rf-on steps (g_rf, rf_a and rf_step_uts
+ * are filled only if they fit rf_capacity). */
+typedef struct {
+    const double *grad_sx, *grad_sy;
+    float *g_t1, *g_t2, *g_rho, *g_db0, *g_k;
+    float *g_mx0, *g_my0, *g_mz0;
+    double *g_rf, *rf_a;
+    int *rf_step_uts;
+    int rf_capacity;
+    int n_rf_steps;
+} mrl_adjoint_args;
+int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj);
+
 /* Scan without allocating device memory.
  *
  * For callers that cannot call cudaMalloc themselves -- code running inside

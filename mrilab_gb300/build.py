@@ -47,6 +47,7 @@ UNITS = {
     "scan_fast_exch.cu": [],
     "scan_fast_mt.cu": [],
     "scan_fast_cest.cu": [],
+    "adjoint.cu": [],
     "decode.cpp": None,  # host C++
 }
 

@@ -1,0 +1,483 @@
+// Adjoint of the scan: gradients of a loss of the signal with respect to the
+// tissue parameters, the initial magnetisation and the rf waveform.
+//
+// The map differentiated is the integrator's discrete step (free-pool
+// models: the normal model and exchange among free pools, as
+// BlochKernel.cuh:241-276 and BlochKernelME.cuh:225-343 define it), for
+// isochromat-pool t of one spin:
+//   rotation   m_r = exp([v]x) m,  v = -dt (gamma Bx, gamma By, w_t)
+//              (B = TxCoil * A the complex rf field, w_t the off-resonance
+//              gamma (dB0 + G.r) + dWRnd + 2 pi CS_t + 2 pi f_rf)
+//   relaxation and split exchange, with the inflow taken from the
+//              magnetisation before the step:
+//              x' = d2_t x_r + sum_p f_tp x_p,  y' likewise,
+//              z' = d1_t z_r + sum_p f_tp z_p + c_t,
+//              d2 = (1 - yo)(1 - y2), d1 = (1 - yo)(1 - y1), c = rho / S y1,
+//              y1,2 = 1 - exp(-dt / T1,2), yo = 1 - exp(-dt sum_p k_tp),
+//              f_tp = 1 - exp(-dt k_pt)
+// and the receive sums S_{t,c,a} = sum over isochromats of (x + i y)_t
+// conj(R_c) at ADC steps, before the step.  Given G = dL/dSx + i dL/dSy the
+// adjoint lambda_j = dL/dm_j runs backwards:
+//   lambda_j = F_j^T lambda_{j+1} + sum_c G_{t,c,a} R_c  (ADC step j),
+// and every step adds lambda_{j+1}^T dF_j/dtheta to the gradient of each
+// parameter theta.  The rotation's derivative uses the left Jacobian of
+// SO(3) exponential coordinates: lambda^T d(exp([v]x) m) = dv . J_l(v)^T
+// (m_r x lambda_r), J_l(v)^T u = u - c1 v x u + c2 v x (v x u),
+// c1 = (1 - cos a) / a^2, c2 = (a - sin a) / a^3, a = |v|.
+//
+// One thread owns one isochromat (a voxel's spin, all its pools).  A
+// forward sweep stores the state every kAdjWin steps (checkpoints, in
+// HBM); the backward sweep takes the windows last to first, recomputes the
+// window's states from its checkpoint into shared memory and walks them in
+// reverse.  The rf gradient of a step is summed over the block (warp
+// shuffles, then the warps) and added to its FP64 slot.
+#include "scan_launch.h"
+
+namespace mrl {
+
+namespace {
+
+constexpr int kAdjMaxRx = 8;
+
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+
+// exp([v]x) m with a = |v| > 0: m + sin a (n x m) + (1 - cos a)((n.m) n - m)
+__device__ __forceinline__ float3 rodrigues(float3 v, float3 m, float sa, float omc, float inv_a) {
+    const float3 n = make_float3(v.x * inv_a, v.y * inv_a, v.z * inv_a);
+    const float3 c = cross3(n, m);
+    const float k = dot3(n, m);
+    return make_float3(m.x + fmaf(omc, fmaf(k, n.x, -m.x), sa * c.x), m.y + fmaf(omc, fmaf(k, n.y, -m.y), sa * c.y),
+                       m.z + fmaf(omc, fmaf(k, n.z, -m.z), sa * c.z));
+}
+
+struct Rot {  // exp([v]x) of one step for one pool
+    float3 v;
+    float sa, omc, inv_a, c1, c2;
+    bool id;
+};
+
+__device__ __forceinline__ Rot make_rot(float3 v) {
+    Rot r;
+    r.v = v;
+    const float a2 = dot3(v, v);
+    r.id = a2 == 0.f;
+    const float a = sqrtf(a2);
+    float sh, ch;
+    sincos_cw(0.5f * a, sh, ch);
+    r.sa = 2.f * sh * ch;
+    r.omc = 2.f * sh * sh;
+    r.inv_a = r.id ? 0.f : 1.f / a;
+    if (a < 0.05f) {  // Taylor forms, error below 1e-10
+        r.c1 = 0.5f - a2 * (1.f / 24.f);
+        r.c2 = 1.f / 6.f - a2 * (1.f / 120.f);
+    } else {
+        r.c1 = r.omc / a2;
+        r.c2 = (a - r.sa) / (a2 * a);
+    }
+    return r;
+}
+
+__device__ __forceinline__ float3 rot_apply(const Rot &r, float3 m) {
+    return r.id ? m : rodrigues(r.v, m, r.sa, r.omc, r.inv_a);
+}
+__device__ __forceinline__ float3 rot_apply_t(const Rot &r, float3 m) {  // exp(-[v]x) m
+    return r.id ? m : rodrigues(make_float3(-r.v.x, -r.v.y, -r.v.z), m, r.sa, r.omc, r.inv_a);
+}
+// J_l(v)^T u
+__device__ __forceinline__ float3 jl_t(const Rot &r, float3 u) {
+    const float3 vu = cross3(r.v, u);
+    const float3 vvu = cross3(r.v, vu);
+    return make_float3(u.x - r.c1 * vu.x + r.c2 * vvu.x, u.y - r.c1 * vu.y + r.c2 * vvu.y,
+                       u.z - r.c1 * vu.z + r.c2 * vvu.z);
+}
+
+// compensated running sum (window sums added to a float total)
+struct KSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+template <int P>
+__global__ void __launch_bounds__(kAdjBlock) adjoint_kernel(AdjLaunch L) {
+    extern __shared__ __align__(16) float adj_sm[];
+    float *win = adj_sm;                                            // [kAdjWin][3P][kAdjBlock]
+    float *rfp = adj_sm + kAdjWin * 3 * P * kAdjBlock;              // [kAdjWin][warp][2]
+    constexpr int kWarps = kAdjBlock / 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long iso = (long long)blockIdx.x * kAdjBlock + tid;
+    const bool active = iso < L.n_iso;
+    const int n = L.n_act;
+    const int v = active ? (int)(iso % n) : 0;
+    const int s = active ? (int)(iso / n) : 0;
+
+    // ---- per-isochromat constants ------------------------------------------
+    float om[4] = {0.f, 0.f, 0.f, 0.f}, wres[P], rhoS[P], t1[P], t2[P];
+    float kc[P * P];
+    float2 txc = make_float2(0.f, 0.f), rc[kAdjMaxRx];
+    float3 m[P];
+#pragma unroll
+    for (int c = 0; c < kAdjMaxRx; ++c) rc[c] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < P * P; ++i) kc[i] = 0.f;
+#pragma unroll
+    for (int t = 0; t < P; ++t) {
+        wres[t] = rhoS[t] = t1[t] = t2[t] = 0.f;
+        m[t] = make_float3(0.f, 0.f, 0.f);
+    }
+    if (active) {
+        om[0] = L.gyro * L.db0[v];
+        om[1] = L.gyro * L.gxg[v];
+        om[2] = L.gyro * L.gyg[v];
+        om[3] = L.gyro * L.gzg[v];
+        txc = L.txc[v];
+#pragma unroll
+        for (int c = 0; c < kAdjMaxRx; ++c)
+            if (c < L.rx) rc[c] = L.rxc ? L.rxc[(long long)c * n + v] : make_float2(1.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+            const long long i = ((long long)t * L.S + s) * n + v;
+            wres[t] = L.dwrnd[i] + L.cs2pi[t];
+            rhoS[t] = L.rho[(long long)t * n + v] / (float)L.S;
+            t1[t] = L.t1[(long long)t * n + v];
+            t2[t] = L.t2[(long long)t * n + v];
+            m[t] = make_float3(L.m0[i], L.m0[L.m0_stride + i], L.m0[2 * L.m0_stride + i]);
+        }
+        if (L.kch)
+#pragma unroll
+            for (int i = 0; i < P * P; ++i) kc[i] = L.kch[(long long)i * n + v];
+    }
+    // a pool with T1, T2 or Rho zero is left alone (BlochKernel.cuh:103)
+    bool on[P];
+#pragma unroll
+    for (int t = 0; t < P; ++t) on[t] = active && t1[t] != 0.f && t2[t] != 0.f && rhoS[t] != 0.f;
+
+    // ---- per-dt coefficients ------------------------------------------------
+    float d1[P], d2[P], cc[P], y1[P], y2[P], yo[P], fin[P][P], fT1[P], fT2[P], fyo[P], ffin[P][P];
+    auto set_dt = [&](float dt) {
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+            y1[t] = on[t] ? -expm1f(-dt / t1[t]) : 0.f;
+            y2[t] = on[t] ? -expm1f(-dt / t2[t]) : 0.f;
+            float ksum = 0.f;
+#pragma unroll
+            for (int p = 0; p < P; ++p) {
+                fin[t][p] = 0.f;
+                if (L.exch_gm && p == t) continue;
+                const float kgo = L.exch_gm ? kc[p * P + t] : kc[t * P + p];
+                const float kin = L.exch_gm ? kc[t * P + p] : kc[p * P + t];
+                ksum += kgo;
+                if (on[t] && kin != 0.f) fin[t][p] = -expm1f(-dt * kin);
+                ffin[t][p] = on[t] ? (1.f - fin[t][p]) * dt : 0.f;
+            }
+            yo[t] = on[t] ? -expm1f(-dt * ksum) : 0.f;
+            d1[t] = (1.f - yo[t]) * (1.f - y1[t]);
+            d2[t] = (1.f - yo[t]) * (1.f - y2[t]);
+            cc[t] = rhoS[t] * y1[t];
+            fT1[t] = on[t] ? -(1.f - y1[t]) * dt / (t1[t] * t1[t]) : 0.f;
+            fT2[t] = on[t] ? -(1.f - y2[t]) * dt / (t2[t] * t2[t]) : 0.f;
+            fyo[t] = (1.f - yo[t]) * dt;
+        }
+    };
+    // ---- per-state rotation of free steps -----------------------------------
+    float cth[P], sth[P];
+    auto set_state = [&](float dt, float4 r0) {
+        const float wc = fmaf(om[3], r0.y, fmaf(om[2], r0.z, fmaf(om[1], r0.w, om[0])));
+#pragma unroll
+        for (int t = 0; t < P; ++t) sincos_cw((wc + wres[t]) * dt, sth[t], cth[t]);
+    };
+    auto rot_of = [&](int t, float dt, float4 r0, float4 r1, float2 B) -> Rot {
+        const float wc = fmaf(om[3], r0.y, fmaf(om[2], r0.z, fmaf(om[1], r0.w, om[0])));
+        return make_rot(make_float3(-dt * L.gyro * B.x, -dt * L.gyro * B.y, -dt * (wc + wres[t] + r1.z)));
+    };
+    // one forward step, m -> F(m)
+    auto fwd = [&](float dt, float4 r0, float4 r1, bool rf) {
+        float3 mr[P];
+        const float2 B = make_float2(txc.x * r1.x - txc.y * r1.y, txc.x * r1.y + txc.y * r1.x);
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+            if (rf) {
+                mr[t] = on[t] ? rot_apply(rot_of(t, dt, r0, r1, B), m[t]) : m[t];
+            } else {
+                mr[t] = on[t] ? make_float3(fmaf(m[t].x, cth[t], m[t].y * sth[t]), fmaf(-m[t].x, sth[t], m[t].y * cth[t]),
+                                            m[t].z)
+                              : m[t];
+            }
+        }
+        float3 nm[P];
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+            if (!on[t]) {
+                nm[t] = m[t];
+                continue;
+            }
+            float3 a = make_float3(d2[t] * mr[t].x, d2[t] * mr[t].y, fmaf(d1[t], mr[t].z, cc[t]));
+#pragma unroll
+            for (int p = 0; p < P; ++p) {
+                a.x = fmaf(fin[t][p], m[p].x, a.x);
+                a.y = fmaf(fin[t][p], m[p].y, a.y);
+                a.z = fmaf(fin[t][p], m[p].z, a.z);
+            }
+            nm[t] = a;
+        }
+#pragma unroll
+        for (int t = 0; t < P; ++t) m[t] = nm[t];
+    };
+    auto rec = [&](long long k, int i) { return __ldg(L.rec + k * 3 + i); };
+
+    // ---- forward sweep with checkpoints -------------------------------------
+    const long long N = L.n_steps;
+    const long long nwin = (N + kAdjWin - 1) / kAdjWin;
+    const long long cs = (long long)3 * P;  // checkpoint components
+    for (long long k = 0; k < N; ++k) {
+        const float4 r0 = rec(k, 0), r1 = rec(k, 1);
+        const int flags = __float_as_int(r1.w);
+        const float dt = r0.x;
+        if (k % kAdjWin == 0 && active) {
+            float *cp = L.ckpt + (k / kAdjWin) * cs * L.n_iso + iso;
+#pragma unroll
+            for (int t = 0; t < P; ++t) {
+                cp[(3 * t + 0) * L.n_iso] = m[t].x;
+                cp[(3 * t + 1) * L.n_iso] = m[t].y;
+                cp[(3 * t + 2) * L.n_iso] = m[t].z;
+            }
+        }
+        if (k == 0 || (flags & kFlagDt)) set_dt(dt);
+        if (k == 0 || (flags & kFlagState)) set_state(dt, r0);
+        fwd(dt, r0, r1, (flags & kFlagRf) != 0);
+    }
+
+    // ---- backward sweep -----------------------------------------------------
+    float3 lam[P];
+#pragma unroll
+    for (int t = 0; t < P; ++t) lam[t] = make_float3(0.f, 0.f, 0.f);
+    KSum gT1[P], gT2[P], grho[P], gw[P], gk[P * P];
+    for (long long w = nwin - 1; w >= 0; --w) {
+        const long long k0 = w * kAdjWin, k1 = min(N, k0 + kAdjWin);
+        // recompute the window's states (before each step) into shared memory
+        if (active) {
+            const float *cp = L.ckpt + w * cs * L.n_iso + iso;
+#pragma unroll
+            for (int t = 0; t < P; ++t)
+                m[t] = make_float3(cp[(3 * t + 0) * L.n_iso], cp[(3 * t + 1) * L.n_iso], cp[(3 * t + 2) * L.n_iso]);
+        }
+        for (long long k = k0; k < k1; ++k) {
+            const float4 r0 = rec(k, 0), r1 = rec(k, 1);
+            const int flags = __float_as_int(r1.w);
+            const float dt = r0.x;
+            float *ws = win + (k - k0) * 3 * P * kAdjBlock + tid;
+#pragma unroll
+            for (int t = 0; t < P; ++t) {
+                ws[(3 * t + 0) * kAdjBlock] = m[t].x;
+                ws[(3 * t + 1) * kAdjBlock] = m[t].y;
+                ws[(3 * t + 2) * kAdjBlock] = m[t].z;
+            }
+            if (k == k0 || (flags & kFlagDt)) set_dt(dt);
+            if (k == k0 || (flags & kFlagState)) set_state(dt, r0);
+            if (k + 1 < k1) fwd(dt, r0, r1, (flags & kFlagRf) != 0);
+        }
+        // window partial sums of the parameter gradients
+        float wT1[P], wT2[P], wrho[P], ww[P], wk[P * P];
+#pragma unroll
+        for (int t = 0; t < P; ++t) wT1[t] = wT2[t] = wrho[t] = ww[t] = 0.f;
+#pragma unroll
+        for (int i = 0; i < P * P; ++i) wk[i] = 0.f;
+        // the coefficients in registers are those of step k1 - 1
+        for (long long k = k1 - 1; k >= k0; --k) {
+            const float4 r0 = rec(k, 0), r1 = rec(k, 1), r2 = rec(k, 2);
+            const int flags = __float_as_int(r1.w);
+            const float dt = r0.x;
+            if (k < k1 - 1) {  // coefficients of step k, if step k + 1 changed them
+                const int fn = __float_as_int(rec(k + 1, 1).w);
+                if (fn & kFlagDt) set_dt(dt);
+                if (fn & kFlagState) set_state(dt, r0);
+            }
+            const bool rf = (flags & kFlagRf) != 0;
+            const float *ws = win + (k - k0) * 3 * P * kAdjBlock + tid;
+            float3 mk[P];
+#pragma unroll
+            for (int t = 0; t < P; ++t)
+                mk[t] = make_float3(ws[(3 * t + 0) * kAdjBlock], ws[(3 * t + 1) * kAdjBlock], ws[(3 * t + 2) * kAdjBlock]);
+            const float2 B = make_float2(txc.x * r1.x - txc.y * r1.y, txc.x * r1.y + txc.y * r1.x);
+            float3 nl[P];
+#pragma unroll
+            for (int t = 0; t < P; ++t) nl[t] = make_float3(0.f, 0.f, 0.f);
+            float2 gB = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int t = 0; t < P; ++t) {
+                if (!on[t]) {
+                    nl[t].x += lam[t].x;
+                    nl[t].y += lam[t].y;
+                    nl[t].z += lam[t].z;
+                    continue;
+                }
+                // rotation of this step
+                Rot R;
+                float3 mr;
+                if (rf) {
+                    R = rot_of(t, dt, r0, r1, B);
+                    mr = rot_apply(R, mk[t]);
+                } else {
+                    mr = make_float3(fmaf(mk[t].x, cth[t], mk[t].y * sth[t]), fmaf(-mk[t].x, sth[t], mk[t].y * cth[t]),
+                                     mk[t].z);
+                }
+                const float3 l = lam[t];
+                // relaxation / recovery parameters
+                const float gd2 = fmaf(l.x, mr.x, l.y * mr.y), gd1 = l.z * mr.z;
+                const float gyo = -(gd2 * (1.f - y2[t]) + gd1 * (1.f - y1[t]));
+                wT1[t] = fmaf((-(1.f - yo[t]) * gd1 + rhoS[t] * l.z), fT1[t], wT1[t]);
+                wT2[t] = fmaf(-(1.f - yo[t]) * gd2, fT2[t], wT2[t]);
+                wrho[t] = fmaf(l.z, y1[t] / (float)L.S, wrho[t]);
+                // exchange rates: yo_t (outflow) and the inflow f_tp
+#pragma unroll
+                for (int p = 0; p < P; ++p) {
+                    if (L.exch_gm && p == t) continue;
+                    const int go = L.exch_gm ? p * P + t : t * P + p;  // channel of rate t -> p
+                    const int gi = L.exch_gm ? t * P + p : p * P + t;  // channel of rate p -> t
+                    wk[go] = fmaf(gyo, fyo[t], wk[go]);
+                    wk[gi] = fmaf(dot3(l, mk[p]), ffin[t][p], wk[gi]);
+                    // inflow to t from p's magnetisation before the step
+                    nl[p].x = fmaf(fin[t][p], l.x, nl[p].x);
+                    nl[p].y = fmaf(fin[t][p], l.y, nl[p].y);
+                    nl[p].z = fmaf(fin[t][p], l.z, nl[p].z);
+                }
+                // adjoint with respect to the rotated magnetisation
+                const float3 lr = make_float3(d2[t] * l.x, d2[t] * l.y, d1[t] * l.z);
+                const float3 u = cross3(mr, lr);
+                if (rf) {
+                    const float3 g = jl_t(R, u);
+                    ww[t] = fmaf(-dt, g.z, ww[t]);
+                    gB.x = fmaf(-dt * L.gyro, g.x, gB.x);
+                    gB.y = fmaf(-dt * L.gyro, g.y, gB.y);
+                    const float3 b = rot_apply_t(R, lr);
+                    nl[t].x += b.x;
+                    nl[t].y += b.y;
+                    nl[t].z += b.z;
+                } else {
+                    ww[t] = fmaf(-dt, u.z, ww[t]);
+                    nl[t].x += fmaf(cth[t], lr.x, -sth[t] * lr.y);
+                    nl[t].y += fmaf(sth[t], lr.x, cth[t] * lr.y);
+                    nl[t].z += lr.z;
+                }
+            }
+            // receive before the step: lambda += sum_c G R_c
+            const int a = __float_as_int(r2.x);
+            if (a >= 0 && active) {
+#pragma unroll
+                for (int t = 0; t < P; ++t) {
+                    float2 src = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int c = 0; c < kAdjMaxRx; ++c) {
+                        if (c >= L.rx) break;
+                        const float2 g = __ldg(L.gsig + ((long long)t * L.rx + c) * L.A + a);
+                        src.x = fmaf(g.x, rc[c].x, fmaf(-g.y, rc[c].y, src.x));
+                        src.y = fmaf(g.x, rc[c].y, fmaf(g.y, rc[c].x, src.y));
+                    }
+                    nl[t].x += src.x;
+                    nl[t].y += src.y;
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < P; ++t) lam[t] = active ? nl[t] : make_float3(0.f, 0.f, 0.f);
+            // rf gradient of this step: dL/dA = conj(TxCoil) dL/dB, summed over the warp
+            if (rf) {
+                float2 gA = make_float2(txc.x * gB.x + txc.y * gB.y, txc.x * gB.y - txc.y * gB.x);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    gA.x += __shfl_xor_sync(0xffffffffu, gA.x, o);
+                    gA.y += __shfl_xor_sync(0xffffffffu, gA.y, o);
+                }
+                if (lane == 0) {
+                    rfp[((k - k0) * kWarps + warp) * 2 + 0] = gA.x;
+                    rfp[((k - k0) * kWarps + warp) * 2 + 1] = gA.y;
+                }
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+            gT1[t].add(wT1[t]);
+            gT2[t].add(wT2[t]);
+            grho[t].add(wrho[t]);
+            gw[t].add(ww[t]);
+        }
+#pragma unroll
+        for (int i = 0; i < P * P; ++i) gk[i].add(wk[i]);
+        // the window's rf gradients, summed over the block, into their FP64 slots
+        __syncthreads();
+        if (tid < (int)(k1 - k0)) {
+            const long long k = k0 + tid;
+            const int ri = __float_as_int(rec(k, 2).y);
+            if (ri >= 0 && (__float_as_int(rec(k, 1).w) & kFlagRf)) {
+                float gx = 0.f, gy = 0.f;
+#pragma unroll
+                for (int q = 0; q < kWarps; ++q) {
+                    gx += rfp[(tid * kWarps + q) * 2 + 0];
+                    gy += rfp[(tid * kWarps + q) * 2 + 1];
+                }
+                atomicAdd(&L.grf[2 * ri], (double)gx);
+                atomicAdd(&L.grf[2 * ri + 1], (double)gy);
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- per-isochromat outputs -------------------------------------------
+    if (!active) return;
+    float *g = L.giso + iso;
+    const long long st = L.n_iso;
+    int f = 0;
+#pragma unroll
+    for (int t = 0; t < P; ++t) g[(f + t) * st] = gT1[t].s;
+    f += P;
+#pragma unroll
+    for (int t = 0; t < P; ++t) g[(f + t) * st] = gT2[t].s;
+    f += P;
+#pragma unroll
+    for (int t = 0; t < P; ++t) g[(f + t) * st] = grho[t].s;
+    f += P;
+    float gdb0 = 0.f;
+#pragma unroll
+    for (int t = 0; t < P; ++t) gdb0 = fmaf(L.gyro, gw[t].s, gdb0);
+    g[f * st] = gdb0;
+    f += 1;
+#pragma unroll
+    for (int i = 0; i < P * P; ++i) g[(f + i) * st] = gk[i].s;
+    f += P * P;
+#pragma unroll
+    for (int t = 0; t < P; ++t) {  // dL/d(initial Mx, My, Mz)
+        g[(f + t) * st] = lam[t].x;
+        g[(f + P + t) * st] = lam[t].y;
+        g[(f + 2 * P + t) * st] = lam[t].z;
+    }
+}
+
+template <int P>
+cudaError_t go(const AdjLaunch &L, cudaStream_t st) {
+    const size_t smem = adjoint_smem_bytes(P);
+    auto k = adjoint_kernel<P>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const long long blocks = (L.n_iso + kAdjBlock - 1) / kAdjBlock;
+    k<<<(unsigned)blocks, kAdjBlock, smem, st>>>(L);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_adjoint(int P, const AdjLaunch &L, cudaStream_t st) {
+    switch (P) {
+    case 1: return go<1>(L, st);
+    case 2: return go<2>(L, st);
+    case 3: return go<3>(L, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace mrl

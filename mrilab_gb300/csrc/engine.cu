@@ -1721,6 +1721,170 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n) {
     return rc;
 }
 
+int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
+    using namespace mrl;
+    g_err.clear();
+    if (!args || !adj) return set_err("NULL argument"), MRL_ERR_ARG;
+    if (args->ctl.run_mode == 1) return set_err("the adjoint runs RunMode 0 scans"), MRL_ERR_UNSUPPORTED;
+    Scanner sc;
+    sc.args = args;
+    int rc = sc.setup();
+    if (rc) return rc;
+    if (!(sc.mi.km == KM_NORMAL || (sc.mi.km == KM_EXCH && sc.all_free())))
+        return set_err("the adjoint covers free-pool models (normal; ME, or GM without bound pools)"),
+               MRL_ERR_UNSUPPORTED;
+    if (sc.TX != 1) return set_err("the adjoint supports one Tx coil"), MRL_ERR_UNSUPPORTED;
+    if (sc.P > 3) return set_err("the adjoint supports TypeNum <= 3"), MRL_ERR_UNSUPPORTED;
+    if (sc.RX > 8) return set_err("the adjoint supports up to 8 Rx coils"), MRL_ERR_UNSUPPORTED;
+    const int P = sc.P, S = sc.S, RX = sc.RX, A = sc.A;
+    const long long V = sc.V;
+    // the whole sequence, decoded once
+    std::vector<double> kx(std::max(A, 1)), ky(std::max(A, 1)), kz(std::max(A, 1));
+    mrl_signal sig = args->sig;
+    sig.kx = kx.data();
+    sig.ky = ky.data();
+    sig.kz = kz.data();
+    DecodeState ds;
+    mrl_state none{};
+    load_state(ds, none, sc.TX);
+    DecodeChunk ch;
+    decode_until_ext(ds, args->seq, sc.TX, args->obj.gyro, sig, ch);
+    if (ch.stopped_at_ext) return set_err("the adjoint runs sequences without Ext events"), MRL_ERR_UNSUPPORTED;
+    // step records
+    const long long N = ch.n_steps;
+    std::vector<float4> rec((size_t)std::max<long long>(1, N) * 3);
+    std::vector<int> step_uts((size_t)std::max<long long>(1, N), -1);
+    for (size_t j = 0; j < ch.point_uts.size(); ++j)
+        if (ch.point_dt[j] > 0) step_uts[ch.point_step[j]] = ch.point_uts[j];
+    int n_rf = 0;
+    double last_dt = -1, lgx = 0, lgy = 0, lgz = 0;
+    std::vector<int> rf_uts;
+    std::vector<double> rf_a;
+    for (long long q = 0; q < N; ++q) {
+        const StepInfo &si = ch.steps[q];
+        const bool rf = (float)si.amp[0] != 0.f;
+        int flags = rf ? kFlagRf : 0;
+        if (si.dt != last_dt) flags |= kFlagDt;
+        if (si.dt != last_dt || si.gx != lgx || si.gy != lgy || si.gz != lgz) flags |= kFlagState;
+        last_dt = si.dt, lgx = si.gx, lgy = si.gy, lgz = si.gz;
+        float4 r1;
+        r1.x = (float)(si.amp[0] * std::cos(si.phase[0]));
+        r1.y = (float)(si.amp[0] * std::sin(si.phase[0]));
+        r1.z = (float)(2 * kPiRef * si.freq[0]);
+        std::memcpy(&r1.w, &flags, sizeof(int));
+        const int ri = rf ? n_rf++ : -1;
+        if (rf) {
+            rf_uts.push_back(step_uts[q]);
+            rf_a.push_back(si.amp[0] * std::cos(si.phase[0]));
+            rf_a.push_back(si.amp[0] * std::sin(si.phase[0]));
+        }
+        float4 r2 = make_float4(0.f, 0.f, 0.f, 0.f);
+        std::memcpy(&r2.x, &si.adc, sizeof(int));
+        std::memcpy(&r2.y, &ri, sizeof(int));
+        rec[q * 3 + 0] = make_float4((float)si.dt, (float)si.gz, (float)si.gy, (float)si.gx);
+        rec[q * 3 + 1] = r1;
+        rec[q * 3 + 2] = r2;
+    }
+    adj->n_rf_steps = n_rf;
+    const int n = std::max(1, sc.n_act);
+    const long long n_iso = (long long)sc.n_act * S;
+    const long long nwin = (N + kAdjWin - 1) / kAdjWin;
+    const double ck_bytes = (double)nwin * 3 * P * std::max(1LL, n_iso) * sizeof(float);
+    if (ck_bytes > 96.0 * (1ull << 30))
+        return set_err("adjoint checkpoints need %.1f GiB (limit 96 GiB)", ck_bytes / (1ull << 30)), MRL_ERR_NOMEM;
+    const int nf = adjoint_fields(P);
+    DevBuf<float4> d_rec;
+    DevBuf<float> d_ck, d_g;
+    DevBuf<float2> d_gs;
+    DevBuf<double> d_rf;
+    cudaError_t e = d_rec.ensure(rec.size());
+    if (e == cudaSuccess) e = d_ck.ensure((size_t)std::max(1LL, nwin * 3 * P * n_iso));
+    if (e == cudaSuccess) e = d_g.ensure((size_t)nf * std::max(1LL, n_iso));
+    if (e == cudaSuccess) e = d_gs.ensure((size_t)P * RX * std::max(A, 1));
+    if (e == cudaSuccess) e = d_rf.ensure((size_t)2 * std::max(1, n_rf));
+    if (e != cudaSuccess) return sc.fail_cuda(e, "cudaMalloc(adjoint)");
+    std::vector<float2> gs((size_t)P * RX * std::max(A, 1), make_float2(0.f, 0.f));
+    for (size_t i = 0; i < (size_t)P * RX * A; ++i)
+        gs[i] = make_float2(adj->grad_sx ? (float)adj->grad_sx[i] : 0.f, adj->grad_sy ? (float)adj->grad_sy[i] : 0.f);
+    cudaStream_t st = sc.st;
+    if ((e = cudaMemcpyAsync(d_rec.p, rec.data(), rec.size() * sizeof(float4), cudaMemcpyHostToDevice, st)) ==
+        cudaSuccess)
+        e = cudaMemcpyAsync(d_gs.p, gs.data(), gs.size() * sizeof(float2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_rf.p, 0, d_rf.n * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_g.p, 0, d_g.n * sizeof(float), st);
+    if (e != cudaSuccess) return sc.fail_cuda(e, "adjoint upload");
+    if (n_iso > 0 && N > 0) {
+        AdjLaunch L{};
+        L.n_act = sc.n_act;
+        L.S = S;
+        L.rx = RX;
+        L.A = std::max(A, 1);
+        L.exch_gm = sc.mi.gm ? 1 : 0;
+        L.n_iso = n_iso;
+        L.gyro = (float)args->obj.gyro;
+        L.gxg = sc.d_f.p + sc.o_gx;
+        L.gyg = sc.d_f.p + sc.o_gy;
+        L.gzg = sc.d_f.p + sc.o_gz;
+        L.db0 = sc.d_f.p + sc.o_db0;
+        L.rho = sc.d_f.p + sc.o_rho;
+        L.t1 = sc.d_f.p + sc.o_t1;
+        L.t2 = sc.d_f.p + sc.o_t2;
+        L.kch = sc.mi.nk > 0 ? sc.d_f.p + sc.o_k : nullptr;
+        L.dwrnd = sc.d_f.p + sc.o_dwr;
+        L.m0 = sc.d_m.p;
+        L.m0_stride = (long long)P * S * n;
+        L.rxc = args->coil.rx_default == 0 ? sc.d_rx.p : nullptr;
+        L.txc = sc.d_f2.p + sc.o_txc;
+        for (int t = 0; t < kMaxPool; ++t)
+            L.cs2pi[t] = (t < P && args->ctl.cs) ? (float)(2 * kPiRef * args->ctl.cs[t]) : 0.f;
+        L.rec = d_rec.p;
+        L.n_steps = N;
+        L.ckpt = d_ck.p;
+        L.gsig = d_gs.p;
+        L.giso = d_g.p;
+        L.grf = d_rf.p;
+        if ((e = launch_adjoint(P, L, st)) != cudaSuccess) return sc.fail_cuda(e, "adjoint launch");
+    }
+    std::vector<float> g((size_t)nf * std::max(1LL, n_iso));
+    std::vector<double> grf(d_rf.n);
+    if ((e = cudaMemcpyAsync(g.data(), d_g.p, g.size() * sizeof(float), cudaMemcpyDeviceToHost, st)) == cudaSuccess)
+        e = cudaMemcpyAsync(grf.data(), d_rf.p, grf.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return sc.fail_cuda(e, "adjoint download");
+    // per voxel: sums over the voxel's spins; per isochromat: the initial state
+    auto field = [&](int f, int s2, int j) { return g[(size_t)f * n_iso + (size_t)s2 * sc.n_act + j]; };
+    const int F_T1 = 0, F_T2 = P, F_RHO = 2 * P, F_DB0 = 3 * P, F_K = 3 * P + 1, F_M0 = 3 * P + 1 + P * P;
+    for (float *o : {adj->g_t1, adj->g_t2, adj->g_rho})
+        if (o) std::fill(o, o + (size_t)P * V, 0.f);
+    if (adj->g_db0) std::fill(adj->g_db0, adj->g_db0 + V, 0.f);
+    if (adj->g_k && sc.mi.nk > 0) std::fill(adj->g_k, adj->g_k + (size_t)args->obj.k_channels * V, 0.f);
+    for (float *o : {adj->g_mx0, adj->g_my0, adj->g_mz0})
+        if (o) std::fill(o, o + (size_t)P * S * V, 0.f);
+    for (int j = 0; j < sc.n_act; ++j) {
+        const long long v = sc.act[j];
+        for (int s2 = 0; s2 < S; ++s2) {
+            for (int t = 0; t < P; ++t) {
+                if (adj->g_t1) adj->g_t1[t * V + v] += field(F_T1 + t, s2, j);
+                if (adj->g_t2) adj->g_t2[t * V + v] += field(F_T2 + t, s2, j);
+                if (adj->g_rho) adj->g_rho[t * V + v] += field(F_RHO + t, s2, j);
+                const long long i = ((long long)t * S + s2) * V + v;
+                if (adj->g_mx0) adj->g_mx0[i] = field(F_M0 + t, s2, j);
+                if (adj->g_my0) adj->g_my0[i] = field(F_M0 + P + t, s2, j);
+                if (adj->g_mz0) adj->g_mz0[i] = field(F_M0 + 2 * P + t, s2, j);
+            }
+            if (adj->g_db0) adj->g_db0[v] += field(F_DB0, s2, j);
+            if (adj->g_k && sc.mi.nk > 0)
+                for (int k = 0; k < P * P; ++k) adj->g_k[k * V + v] += field(F_K + k, s2, j);
+        }
+    }
+    if (n_rf <= adj->rf_capacity) {
+        if (adj->g_rf) std::copy(grf.begin(), grf.begin() + 2 * n_rf, adj->g_rf);
+        if (adj->rf_step_uts) std::copy(rf_uts.begin(), rf_uts.end(), adj->rf_step_uts);
+        if (adj->rf_a) std::copy(rf_a.begin(), rf_a.end(), adj->rf_a);
+    }
+    return sc.check_device_status();
+}
+
 int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, void *stream) {
     using namespace mrl;
     g_err.clear();

@@ -67,6 +67,39 @@ cudaError_t launch_scan_fast_mt(int P, int NS, bool all_free, dim3 grid, size_t 
                                 const FastGrid &g);
 cudaError_t launch_scan_fast_cest(int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
                                   const FastGrid &g);
+// ---- adjoint (adjoint.cu) ----------------------------------------------------
+constexpr int kAdjBlock = 128;  // threads (isochromats) per block
+constexpr int kAdjWin = 16;     // steps between checkpoints, recomputed into shared memory
+
+// Step record of the adjoint: {dt, Gz, Gy, Gx}, {Re A, Im A, 2 pi f_rf,
+// flags (kFlagRf, kFlagState, kFlagDt)}, {ADC sample (int bits) or -1, rf
+// step index (int bits) or -1, 0, 0}.
+struct AdjLaunch {
+    int n_act, S, rx, A, exch_gm;
+    long long n_iso;  // n_act * S; isochromat i = spin (i / n_act) of voxel (i % n_act)
+    float gyro;
+    const float *gxg, *gyg, *gzg, *db0;  // [n_act]
+    const float *rho, *t1, *t2;          // [P][n_act]
+    const float *kch;                    // [P*P][n_act] exchange channels, or null
+    const float *dwrnd;                  // [P][S][n_act]
+    const float *m0;                     // initial Mx | My | Mz, each [P][S][n_act]
+    long long m0_stride;                 // P * S * n_act
+    const float2 *rxc;                   // [rx][n_act], null: the default coil
+    const float2 *txc;                   // [n_act] TxCoilmg exp(i TxCoilpe)
+    float cs2pi[kMaxPool];
+    const float4 *rec;                   // [n_steps][3]
+    long long n_steps;
+    float *ckpt;                         // [window][3P][n_iso]
+    const float2 *gsig;                  // [P][rx][A] dL/dSx + i dL/dSy
+    float *giso;                         // [fields][n_iso]: T1[P] T2[P] Rho[P] dB0 K[P*P] Mx0[P] My0[P] Mz0[P]
+    double *grf;                         // [n_rf][2]
+};
+inline size_t adjoint_smem_bytes(int P) {
+    return (size_t)kAdjWin * 3 * P * kAdjBlock * 4 + (size_t)kAdjWin * (kAdjBlock / 32) * 2 * 4;
+}
+inline int adjoint_fields(int P) { return 3 * P + 1 + P * P + 3 * P; }
+cudaError_t launch_adjoint(int P, const AdjLaunch &L, cudaStream_t st);
+
 // resident blocks per SM of an instantiation at `smem` bytes (0 if none)
 int occupancy_scan_fast_normal(int P, int NS, bool all_free, size_t smem);
 int occupancy_scan_fast_exch(int P, int NS, bool all_free, size_t smem);

@@ -334,3 +334,51 @@ def scan_batched(scans, numerics: str = "accurate", gpu_index: int = 0):
     if rc != 0:
         raise ScanError(rc, lib.mrl_last_error().decode())
     return [h.outputs() for h in hosts]
+
+
+class AdjointArgs(ctypes.Structure):
+    _fields_ = [("grad_sx", _d), ("grad_sy", _d), ("g_t1", _f), ("g_t2", _f), ("g_rho", _f), ("g_db0", _f),
+                ("g_k", _f), ("g_mx0", _f), ("g_my0", _f), ("g_mz0", _f), ("g_rf", _d), ("rf_a", _d),
+                ("rf_step_uts", ctypes.POINTER(ctypes.c_int)), ("rf_capacity", ctypes.c_int),
+                ("n_rf_steps", ctypes.c_int)]
+
+
+def adjoint(sc, grad_sx, grad_sy, gpu_index: int = 0, rf_capacity: Optional[int] = None) -> Dict[str, np.ndarray]:
+    """``mrl_adjoint``: gradients of a loss L of the signal of ``sc`` given
+    dL/dSx, dL/dSy (flat [P][Rx][A]).  Returns T1, T2, Rho ([P*V]), dB0
+    ([V]), K ([nK*V], exchange models), Mx0/My0/Mz0 ([P*S*V]), rf ([n_rf, 2]:
+    dL/dRe A, dL/dIm A per rf-on step), rf_a (their A) and rf_uts (their uts
+    indices)."""
+    lib = library()
+    lib.mrl_adjoint.argtypes = [ctypes.POINTER(ScanArgs), ctypes.POINTER(AdjointArgs)]
+    lib.mrl_adjoint.restype = ctypes.c_int
+    hs = HostScan(sc, numerics="accurate", gpu_index=gpu_index)
+    o = sc.VObj
+    V = o["Rho"].size // int(o["TypeNum"])
+    P, S = int(o["TypeNum"]), int(o["SpinNum"])
+    gsx = np.ascontiguousarray(np.asarray(grad_sx, np.float64).ravel())
+    gsy = np.ascontiguousarray(np.asarray(grad_sy, np.float64).ravel())
+    if rf_capacity is None:
+        rf_capacity = int(np.count_nonzero(np.diff(sc.VSeq["utsLine"]) > 0))
+    out = dict(T1=np.zeros(P * V, np.float32), T2=np.zeros(P * V, np.float32), Rho=np.zeros(P * V, np.float32),
+               dB0=np.zeros(V, np.float32), Mx0=np.zeros(P * S * V, np.float32),
+               My0=np.zeros(P * S * V, np.float32), Mz0=np.zeros(P * S * V, np.float32),
+               rf=np.zeros((max(rf_capacity, 1), 2)), rf_a=np.zeros((max(rf_capacity, 1), 2)),
+               rf_uts=np.zeros(max(rf_capacity, 1), np.int32))
+    if "K" in o:
+        out["K"] = np.zeros(o["K"].size, np.float32)
+    a = AdjointArgs()
+    a.grad_sx, a.grad_sy = gsx.ctypes.data_as(_d), gsy.ctypes.data_as(_d)
+    f = lambda k: out[k].ctypes.data_as(_f) if k in out else ctypes.cast(None, _f)
+    a.g_t1, a.g_t2, a.g_rho, a.g_db0, a.g_k = f("T1"), f("T2"), f("Rho"), f("dB0"), f("K")
+    a.g_mx0, a.g_my0, a.g_mz0 = f("Mx0"), f("My0"), f("Mz0")
+    a.g_rf = out["rf"].ctypes.data_as(_d)
+    a.rf_a = out["rf_a"].ctypes.data_as(_d)
+    a.rf_step_uts = out["rf_uts"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    a.rf_capacity = rf_capacity
+    rc = lib.mrl_adjoint(ctypes.byref(hs.args), ctypes.byref(a))
+    if rc != 0:
+        raise ScanError(rc, lib.mrl_last_error().decode())
+    n = a.n_rf_steps
+    out["rf"], out["rf_a"], out["rf_uts"] = out["rf"][:n], out["rf_a"][:n], out["rf_uts"][:n]
+    return out
