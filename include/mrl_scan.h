@@ -231,6 +231,13 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n);
  *                                  step in sequence order (A = rfAmp e^{i rfPhase})
  *   rf_a              [rf_capacity][2] Re A, Im A of each of those steps
  *   rf_step_uts       [rf_capacity] the uts index of each of those steps
+ *   g_rf_amp_line, g_rf_phase_line [n_rf of the sequence] dL/d VSeq.rfAmpLine
+ *                                  and dL/d VSeq.rfPhaseLine: each step holds
+ *                                  the smaller-magnitude end of its rf
+ *                                  interval (separately for amplitude and
+ *                                  phase), so each step's share goes to the
+ *                                  entry it held (entries at a tie of
+ *                                  magnitudes have a one-sided derivative)
  * n_rf_steps receives the number of rf-on steps (g_rf, rf_a and rf_step_uts
  * are filled only if they fit rf_capacity). */
 typedef struct {
@@ -241,6 +248,7 @@ typedef struct {
     int *rf_step_uts;
     int rf_capacity;
     int n_rf_steps;
+    double *g_rf_amp_line, *g_rf_phase_line;
 } mrl_adjoint_args;
 int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj);
 

@@ -31,6 +31,7 @@ void load_state(DecodeState &s, const mrl_state &v, int tx) {
         if (v.rf_amp) s.rf_amp[c] = v.rf_amp[c];
         if (v.rf_phase) s.rf_phase[c] = v.rf_phase[c];
         if (v.rf_freq) s.rf_freq[c] = v.rf_freq[c];
+        s.rf_amp_src[c] = s.rf_phase_src[c] = -1;
     }
 }
 
@@ -52,7 +53,10 @@ namespace {
 void finish_time_point(DecodeState &s, int tx, bool ext_flag, double flag_sum, double dt) {
     if (ext_flag) s.exti++;
     if (flag_sum == 0) {  // no channel fired: reset the pulse packet (:463-472)
-        for (int c = 0; c < tx; ++c) s.rf_amp[c] = s.rf_phase[c] = s.rf_freq[c] = 0;
+        for (int c = 0; c < tx; ++c) {
+            s.rf_amp[c] = s.rf_phase[c] = s.rf_freq[c] = 0;
+            s.rf_amp_src[c] = s.rf_phase_src[c] = -1;
+        }
         s.gz = s.gy = s.gx = 0;
         s.adc = 0;
         s.ext = 0;
@@ -122,9 +126,12 @@ void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx, double gyro
                     if (s.rf_coil == q.rf_coil[k]) {
                         if (txi >= 1 && txi <= tx) {
                             const int a = s.rfi;
-                            s.rf_amp[txi - 1] = std::fabs(q.rf_amp[a]) <= std::fabs(q.rf_amp[k]) ? q.rf_amp[a] : q.rf_amp[k];
-                            s.rf_phase[txi - 1] =
-                                std::fabs(q.rf_phase[a]) <= std::fabs(q.rf_phase[k]) ? q.rf_phase[a] : q.rf_phase[k];
+                            const int ja = std::fabs(q.rf_amp[a]) <= std::fabs(q.rf_amp[k]) ? a : k;
+                            const int jp = std::fabs(q.rf_phase[a]) <= std::fabs(q.rf_phase[k]) ? a : k;
+                            s.rf_amp[txi - 1] = q.rf_amp[ja];
+                            s.rf_phase[txi - 1] = q.rf_phase[jp];
+                            s.rf_amp_src[txi - 1] = ja;
+                            s.rf_phase_src[txi - 1] = jp;
                             s.rf_freq[txi - 1] = std::fabs(q.rf_freq[a]) <= std::fabs(q.rf_freq[k]) ? q.rf_freq[a] : q.rf_freq[k];
                         }
                         break;
@@ -174,6 +181,8 @@ void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx, double gyro
                 si.freq[c] = c < tx ? s.rf_freq[c] : 0.0;
             }
             si.adc = s.adc == 1 ? s.signali : -1;
+            si.amp_src = s.rf_amp_src[0];
+            si.phase_src = s.rf_phase_src[0];
             out.steps.push_back(si);
             bool rf_on = false;
             for (int c = 0; c < tx; ++c) rf_on |= (float)s.rf_amp[c] != 0.f;

@@ -29,6 +29,10 @@ struct DecodeState {
     double t = 0, dt = 0, rf_coil = 0, rf_ref = 0;
     double rf_amp[kMaxTx] = {0}, rf_phase[kMaxTx] = {0}, rf_freq[kMaxTx] = {0};
     double gz = 0, gy = 0, gx = 0, adc = 0, ext = 0, kz = 0, ky = 0, kx = 0, gpu_fetch = 0;
+    // the rfAmpLine / rfPhaseLine entries the held rf values came from (-1:
+    // none, the value is a reset or was loaded from VVar)
+    int rf_amp_src[kMaxTx] = {-1, -1, -1, -1, -1, -1, -1, -1};
+    int rf_phase_src[kMaxTx] = {-1, -1, -1, -1, -1, -1, -1, -1};
     int utsi = 0, rfi = 0, gzi = 0, gyi = 0, gxi = 0, adci = 0, exti = 0, tr_count = 0;
     // decoder position
     int i = 0;        // tsLine cursor
@@ -44,6 +48,7 @@ struct StepInfo {
     double dt, gz, gy, gx;
     double amp[kMaxTx], phase[kMaxTx], freq[kMaxTx];
     int adc;  // ADC sample index, or -1
+    int amp_src, phase_src;  // Tx coil 1: source entries of amp and phase (-1: none)
 };
 
 struct DecodeChunk {

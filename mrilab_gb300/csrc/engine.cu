@@ -1758,7 +1758,7 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
         if (ch.point_dt[j] > 0) step_uts[ch.point_step[j]] = ch.point_uts[j];
     int n_rf = 0;
     double last_dt = -1, lgx = 0, lgy = 0, lgz = 0;
-    std::vector<int> rf_uts;
+    std::vector<int> rf_uts, rf_src;
     std::vector<double> rf_a;
     for (long long q = 0; q < N; ++q) {
         const StepInfo &si = ch.steps[q];
@@ -1777,6 +1777,8 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
             rf_uts.push_back(step_uts[q]);
             rf_a.push_back(si.amp[0] * std::cos(si.phase[0]));
             rf_a.push_back(si.amp[0] * std::sin(si.phase[0]));
+            rf_src.push_back(si.amp_src);
+            rf_src.push_back(si.phase_src);
         }
         float4 r2 = make_float4(0.f, 0.f, 0.f, 0.f);
         std::memcpy(&r2.x, &si.adc, sizeof(int));
@@ -1881,6 +1883,20 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
         if (adj->g_rf) std::copy(grf.begin(), grf.begin() + 2 * n_rf, adj->g_rf);
         if (adj->rf_step_uts) std::copy(rf_uts.begin(), rf_uts.end(), adj->rf_step_uts);
         if (adj->rf_a) std::copy(rf_a.begin(), rf_a.end(), adj->rf_a);
+    }
+    // onto the waveform lines: A = a e^{i phi} with a = rfAmpLine[ja] (a
+    // negative a is the same A as |a| at phi + pi), phi = rfPhaseLine[jp]
+    const int n_line = args->seq.n_rf;
+    if (adj->g_rf_amp_line) std::fill(adj->g_rf_amp_line, adj->g_rf_amp_line + n_line, 0.0);
+    if (adj->g_rf_phase_line) std::fill(adj->g_rf_phase_line, adj->g_rf_phase_line + n_line, 0.0);
+    for (int i = 0; i < n_rf; ++i) {
+        const double gx = grf[2 * i], gy = grf[2 * i + 1], ax = rf_a[2 * i], ay = rf_a[2 * i + 1];
+        const int ja = rf_src[2 * i], jp = rf_src[2 * i + 1];
+        if (adj->g_rf_amp_line && ja >= 0 && ja < n_line) {
+            const double a = args->seq.rf_amp[ja];
+            if (a != 0) adj->g_rf_amp_line[ja] += (gx * ax + gy * ay) / a;
+        }
+        if (adj->g_rf_phase_line && jp >= 0 && jp < n_line) adj->g_rf_phase_line[jp] += gy * ax - gx * ay;
     }
     return sc.check_device_status();
 }

@@ -340,15 +340,16 @@ class AdjointArgs(ctypes.Structure):
     _fields_ = [("grad_sx", _d), ("grad_sy", _d), ("g_t1", _f), ("g_t2", _f), ("g_rho", _f), ("g_db0", _f),
                 ("g_k", _f), ("g_mx0", _f), ("g_my0", _f), ("g_mz0", _f), ("g_rf", _d), ("rf_a", _d),
                 ("rf_step_uts", ctypes.POINTER(ctypes.c_int)), ("rf_capacity", ctypes.c_int),
-                ("n_rf_steps", ctypes.c_int)]
+                ("n_rf_steps", ctypes.c_int), ("g_rf_amp_line", _d), ("g_rf_phase_line", _d)]
 
 
 def adjoint(sc, grad_sx, grad_sy, gpu_index: int = 0, rf_capacity: Optional[int] = None) -> Dict[str, np.ndarray]:
     """``mrl_adjoint``: gradients of a loss L of the signal of ``sc`` given
     dL/dSx, dL/dSy (flat [P][Rx][A]).  Returns T1, T2, Rho ([P*V]), dB0
     ([V]), K ([nK*V], exchange models), Mx0/My0/Mz0 ([P*S*V]), rf ([n_rf, 2]:
-    dL/dRe A, dL/dIm A per rf-on step), rf_a (their A) and rf_uts (their uts
-    indices)."""
+    dL/dRe A, dL/dIm A per rf-on step), rf_a (their A), rf_uts (their uts
+    indices) and rf_amp_line, rf_phase_line (dL/d VSeq.rfAmpLine and
+    dL/d VSeq.rfPhaseLine)."""
     lib = library()
     lib.mrl_adjoint.argtypes = [ctypes.POINTER(ScanArgs), ctypes.POINTER(AdjointArgs)]
     lib.mrl_adjoint.restype = ctypes.c_int
@@ -364,7 +365,9 @@ def adjoint(sc, grad_sx, grad_sy, gpu_index: int = 0, rf_capacity: Optional[int]
                dB0=np.zeros(V, np.float32), Mx0=np.zeros(P * S * V, np.float32),
                My0=np.zeros(P * S * V, np.float32), Mz0=np.zeros(P * S * V, np.float32),
                rf=np.zeros((max(rf_capacity, 1), 2)), rf_a=np.zeros((max(rf_capacity, 1), 2)),
-               rf_uts=np.zeros(max(rf_capacity, 1), np.int32))
+               rf_uts=np.zeros(max(rf_capacity, 1), np.int32),
+               rf_amp_line=np.zeros(max(int(np.size(sc.VSeq["rfAmpLine"])), 1)),
+               rf_phase_line=np.zeros(max(int(np.size(sc.VSeq["rfAmpLine"])), 1)))
     if "K" in o:
         out["K"] = np.zeros(o["K"].size, np.float32)
     a = AdjointArgs()
@@ -376,6 +379,8 @@ def adjoint(sc, grad_sx, grad_sy, gpu_index: int = 0, rf_capacity: Optional[int]
     a.rf_a = out["rf_a"].ctypes.data_as(_d)
     a.rf_step_uts = out["rf_uts"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
     a.rf_capacity = rf_capacity
+    a.g_rf_amp_line = out["rf_amp_line"].ctypes.data_as(_d)
+    a.g_rf_phase_line = out["rf_phase_line"].ctypes.data_as(_d)
     rc = lib.mrl_adjoint(ctypes.byref(hs.args), ctypes.byref(a))
     if rc != 0:
         raise ScanError(rc, lib.mrl_last_error().decode())

@@ -69,7 +69,30 @@ def _target(sc):
     return out["Sx"], out["Sy"]
 
 
+def _phase_modulated(sc, seed):
+    """sc with random rf phases on the rf-on entries: without ties between
+    neighbouring |phase| values every entry's phase derivative is two-sided.
+    The phases are all positive, so shifting every phase by +-h keeps the
+    order of the magnitudes and with it the entries the steps hold."""
+    out = sc.copy()
+    amp = np.asarray(out.VSeq["rfAmpLine"], np.float64)
+    ph = np.asarray(out.VSeq["rfPhaseLine"], np.float64).copy()
+    on = amp != 0
+    ph[on] = np.random.default_rng(seed).uniform(0.05, 0.45, int(on.sum()))
+    out.VSeq["rfPhaseLine"] = ph
+    return out
+
+
+def _untied(v, tol):
+    """Entries j of a line whose magnitude differs from both neighbours' by
+    more than tol[j] (the held value cannot switch under a step of tol / 4)."""
+    a = np.abs(v)
+    j = np.arange(1, v.size - 1)
+    return j[(np.abs(a[j] - a[j - 1]) > tol[j]) & (np.abs(a[j] - a[j + 1]) > tol[j])]
+
+
 def _run(sc):
+    sc = _phase_modulated(sc, 5)
     target = _target(sc)
     _, gsx, gsy = _loss(sc, target)
     g = engine.adjoint(sc, gsx, gsy)
@@ -105,6 +128,19 @@ def _run(sc):
     adj = float(np.sum(-grf[:, 0] * a[:, 1] + grf[:, 1] * a[:, 0]))
     print(f"rf phase: adjoint {adj:.6e}, finite difference {fd:.6e}")
     assert abs(adj - fd) <= TOL * abs(fd)
+    # single waveform entries (VSeq.rfAmpLine / rfPhaseLine)
+    rng = np.random.default_rng(11)
+    cand = _untied(amp, 4 * H * np.abs(amp))
+    cand = cand[amp[cand] != 0]
+    pick = np.sort(rng.choice(cand, min(24, cand.size), replace=False))
+    _check("rfAmpLine", g["rf_amp_line"][pick],
+           _fd_gradient(sc, target, "VSeq", "rfAmpLine", pick, H * np.abs(amp[pick])))
+    ph = np.asarray(sc.VSeq["rfPhaseLine"], np.float64).ravel()
+    cand = _untied(ph, np.full(ph.size, 4 * H))
+    cand = cand[(np.abs(ph[cand]) > 4 * H) & (g["rf_phase_line"][cand] != 0)]
+    pick = np.sort(rng.choice(cand, min(24, cand.size), replace=False))
+    _check("rfPhaseLine", g["rf_phase_line"][pick],
+           _fd_gradient(sc, target, "VSeq", "rfPhaseLine", pick, np.full(pick.size, H)))
     return g
 
 
@@ -125,3 +161,36 @@ def test_adjoint_rejects_bound_pools(built):
     with pytest.raises(engine.ScanError) as e:
         engine.adjoint(sc, np.zeros(1), np.zeros(1))
     assert e.value.status == -6
+
+
+def test_autograd_bridge(built):
+    """The torch.autograd bridge: loss.backward() gives mrl_adjoint's
+    gradients, in the parameters' shapes, and they match FP64 differences."""
+    torch = pytest.importorskip("torch")
+    from mrilab_gb300 import autograd
+
+    sc = _phase_modulated(phantoms.small_multipool("me", seed=35, n=6, pools=2, spins=2, coils=2, n_tr=2), 6)
+    tx, ty = _target(sc)
+    params = autograd.parameters(sc, names=("T1", "T2", "Rho", "dB0", "K", "rfAmp"))
+    sx, sy = autograd.scan(sc, **params)
+    loss = ((sx - torch.from_numpy(tx)) ** 2 + (sy - torch.from_numpy(ty)) ** 2).sum()
+    loss.backward()
+    out = engine.scan(sc)
+    g = engine.adjoint(sc, 2 * (out["Sx"] - tx), 2 * (out["Sy"] - ty))
+    for name, key in (("T1", "T1"), ("T2", "T2"), ("Rho", "Rho"), ("dB0", "dB0"), ("K", "K"),
+                      ("rfAmp", "rf_amp_line")):
+        t = params[name]
+        assert t.grad is not None and t.grad.shape == t.shape
+        flat = t.grad.numpy().ravel(order="F")
+        np.testing.assert_allclose(flat, g[key][: flat.size], rtol=1e-6, atol=1e-12 * np.abs(g[key]).max())
+    # one direction of T2 against differences of the FP64 oracle
+    t2 = np.asarray(sc.VObj["T2"], np.float64)
+    d = np.random.default_rng(3).uniform(-1, 1, t2.shape) * t2
+    lp, _, _ = _loss(_with(sc, "VObj", "T2", (t2 + H * d).ravel(order="F")), (tx, ty))
+    lm, _, _ = _loss(_with(sc, "VObj", "T2", (t2 - H * d).ravel(order="F")), (tx, ty))
+    plus = (t2 + H * d).astype(np.float32).astype(np.float64)
+    minus = (t2 - H * d).astype(np.float32).astype(np.float64)
+    fd = (lp - lm) / (2 * H)
+    adj = float(np.sum(params["T2"].grad.numpy() * (plus - minus) / (2 * H)))
+    print(f"autograd T2 direction: {adj:.6e}, finite difference {fd:.6e}")
+    assert abs(adj - fd) <= TOL * abs(fd)
