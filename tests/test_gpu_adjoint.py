@@ -131,7 +131,8 @@ def _run(sc):
     # single waveform entries (VSeq.rfAmpLine / rfPhaseLine)
     rng = np.random.default_rng(11)
     cand = _untied(amp, 4 * H * np.abs(amp))
-    cand = cand[amp[cand] != 0]
+    # not the sinc's zero crossings: a relative step there leaves L unchanged
+    cand = cand[np.abs(amp[cand]) > 1e-3 * np.abs(amp).max()]
     pick = np.sort(rng.choice(cand, min(24, cand.size), replace=False))
     _check("rfAmpLine", g["rf_amp_line"][pick],
            _fd_gradient(sc, target, "VSeq", "rfAmpLine", pick, H * np.abs(amp[pick])))
