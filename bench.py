@@ -212,6 +212,89 @@ def run_config3(args):
     print(json.dumps(line))
 
 
+def run_config4(args):
+    """fwd+adjoint on the bSSFP adjoint workload (96 x 96 x 16 voxels, 2
+    spins, free + short-T2 water exchanging, 4 Rx, 200 TRs with a
+    512-sample complex rf waveform): one iteration = the forward scan, the
+    L2 loss gradient against a perturbed-parameter target (T1, T2 x 1.05) and
+    the adjoint, which returns the gradients of every per-voxel parameter
+    and of every rf waveform entry."""
+    import torch
+    from mrilab_gb300 import engine, phantoms
+
+    torch.cuda.set_device(0)
+    sc = phantoms.config4_adjoint(seed=0, n_tr=args.n_tr or 200)
+    tgt = sc.copy()
+    for k in ("T1", "T2"):
+        tgt.VObj[k] = np.asfortranarray(tgt.VObj[k] * np.float32(1.05))
+    target = engine.scan(tgt)
+    tx, ty = target["Sx"], target["Sy"]
+    # device time of the forward scan (prepared, inputs resident, L2 flushed)
+    plan = engine.Plan(sc)
+    work = plan.work()
+    stream = torch.cuda.Stream()
+    flush = torch.empty(int(256 * 2**20), dtype=torch.uint8, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        plan.execute(stream.cuda_stream)
+    fwd = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.execute(stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        fwd.append(e0.elapsed_time(e1))
+    plan.close()
+    # iterations through the public calls (mrl_scan, then mrl_adjoint), host buffers
+    wall, adj, h2d, d2h = [], [], 0, 0
+    with ClockSampler(0) as clk:
+        for i in range(max(3, args.warmup) + args.steps):
+            t0 = time.perf_counter()
+            out = engine.scan(sc)
+            tf = engine.last_timing()
+            g = engine.adjoint(sc, 2 * (out["Sx"] - tx), 2 * (out["Sy"] - ty))
+            ta = engine.last_timing()
+            t1 = time.perf_counter()
+            if i >= max(3, args.warmup):
+                wall.append((t1 - t0) * 1e3)
+                adj.append(ta["scan_ms"])
+                h2d = tf["h2d_bytes"] + ta["h2d_bytes"]
+                d2h = tf["d2h_bytes"] + ta["d2h_bytes"]
+    fwd_ms, adj_ms = float(np.mean(fwd)), float(np.mean(adj))
+    units = work["units"]
+    fp32_tf, mufu_g = peaks()
+    desc = dict(model="me", pools=2, rx=4)
+    flops, mufu = op_counts(work, desc)
+    line = {
+        "metric": "fwd+adjoint ms/iter", "value": fwd_ms + adj_ms, "unit": "ms", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": fwd_ms + adj_ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "adjoint bSSFP: 96x96x16 voxels, 4-class phantom, 2 spins, free + short-T2 "
+                               "water exchanging, 4 Rx, %d TRs of 5 ms, flip 40, 512-sample complex rf"
+                               % int(sc.VCtl["TRNum"]),
+                   "units_per_iter": units, "steps": work["steps"], "rf_steps": work["rf_steps"],
+                   "samples": work["samples"], "checkpoint_every_steps": 16,
+                   "l2": "flushed between timed forward scans (256 MiB write); the adjoint streams its "
+                         "checkpoints (tens of GB) through HBM"},
+        "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
+        "forward_rate": units / (fwd_ms * 1e-3), "adjoint_rate": units / (adj_ms * 1e-3),
+        "e2e": {"value": float(np.mean(wall)), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "api": "mrl_scan then mrl_adjoint with host buffers (decode, uploads, downloads, host "
+                       "reductions included)"},
+        "gpu_launches": (work["launches"] + 1) * args.steps,
+        "roofline": {"bound": "fp32", "kernel": "forward scan kernel (op table)",
+                     "achieved": flops / (fwd_ms * 1e-3) / 1e12, "peak": fp32_tf, "unit": "TFLOP/s",
+                     "frac": flops / (fwd_ms * 1e-3) / 1e12 / fp32_tf, "traffic": None,
+                     "mufu": {"achieved": mufu / (fwd_ms * 1e-3) / 1e9, "peak": mufu_g, "unit": "Gop/s",
+                              "frac": mufu / (fwd_ms * 1e-3) / 1e9 / mufu_g}},
+        "clocks": clk.summary(),
+        "check": float(np.abs(g["T2"]).sum()),
+    }
+    print(json.dumps(line))
+
+
 def cpu_baseline(sc, target_s=12.0):
     """The reference scan algorithm on the host cores (single-precision
     oracle port, all threads) on the first steps of the same workload."""
@@ -240,7 +323,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=["config2", "config1", "config3"])
+    ap.add_argument("--workload", default="config2", choices=["config2", "config1", "config3", "config4"])
     ap.add_argument("--vox-scale", type=float, default=1.0, help="config3: scale of the instance voxel counts")
     ap.add_argument("--n-tr", type=int, default=None, help="TRs of the workload (default: all)")
     ap.add_argument("--numerics", default="accurate", choices=["accurate", "reference"])
@@ -249,6 +332,9 @@ def main():
 
     if args.workload == "config3" and args.impl == "ours":
         run_config3(args)
+        return
+    if args.workload == "config4" and args.impl == "ours":
+        run_config4(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -1726,6 +1726,8 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
     g_err.clear();
     if (!args || !adj) return set_err("NULL argument"), MRL_ERR_ARG;
     if (args->ctl.run_mode == 1) return set_err("the adjoint runs RunMode 0 scans"), MRL_ERR_UNSUPPORTED;
+    const auto t_start = std::chrono::steady_clock::now();
+    for (double &x : g_timing) x = 0;
     Scanner sc;
     sc.args = args;
     int rc = sc.setup();
@@ -1845,7 +1847,18 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
         L.gsig = d_gs.p;
         L.giso = d_g.p;
         L.grf = d_rf.p;
-        if ((e = launch_adjoint(P, L, st)) != cudaSuccess) return sc.fail_cuda(e, "adjoint launch");
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+        if ((e = cudaEventCreate(&ev0)) == cudaSuccess && (e = cudaEventCreate(&ev1)) == cudaSuccess &&
+            (e = cudaEventRecord(ev0, st)) == cudaSuccess && (e = launch_adjoint(P, L, st)) == cudaSuccess)
+            e = cudaEventRecord(ev1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (e != cudaSuccess) return sc.fail_cuda(e, "adjoint launch");
+        g_timing[1] = ms;
+        g_timing[5] = 1;
     }
     std::vector<float> g((size_t)nf * std::max(1LL, n_iso));
     std::vector<double> grf(d_rf.n);
@@ -1898,6 +1911,9 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
         }
         if (adj->g_rf_phase_line && jp >= 0 && jp < n_line) adj->g_rf_phase_line[jp] += gy * ax - gx * ay;
     }
+    g_timing[6] = (double)(rec.size() * sizeof(float4) + gs.size() * sizeof(float2));
+    g_timing[7] = (double)(g.size() * sizeof(float) + grf.size() * sizeof(double));
+    g_timing[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
     return sc.check_device_status();
 }
 

@@ -375,6 +375,64 @@ def config2_me_gre(seed=0, nx=128, ny=128, nz=32, n_pe=32, n_par=8, n_read=128, 
                     tr_num=ntr, seed=seed)
 
 
+def bssfp_lines(*, n_read=96, n_pe=96, n_par=16, fov=(0.24, 0.24, 0.04), tr_ms=5.0, te_ms=2.0, flip=40.0,
+                rf_samples=512, rf_raster_us=2.0, tbw=4.0, bw_hz=125000.0, n_tr=200, gamma=GAMMA):
+    """Balanced SSFP, 3D Cartesian: every TR plays the same complex rf
+    waveform of ``rf_samples`` samples (a windowed sinc with a slow phase
+    modulation) with the phase cycled by pi every other TR, a slab gradient
+    under it, phase / partition / readout prephasers, a readout of
+    ``n_read`` samples centred ``te_ms`` after the rf centre, and rewinders
+    that null every gradient axis's area over the TR.  The areas are those
+    the engine's sample-and-hold integrates (trapezoid flats; the ramps hold
+    their zero end).  Phase and partition encodes cycle over ``n_tr`` TRs."""
+    raster = int(round(rf_raster_us * 1e3))
+    rf_ns = (rf_samples - 1) * raster
+    dwell = int(round(1e9 / bw_hz))
+    ro_ns = n_read * dwell
+    tr_ns = int(round(tr_ms * 1e6))
+    ramp = 100_000
+    rf_center = rf_ns // 2
+    ro_start = rf_center + int(round(te_ms * 1e6)) - ro_ns // 2
+    enc0, enc1 = rf_ns + 20_000, ro_start - ramp - 20_000
+    rw0 = ro_start + ro_ns + ramp + 20_000
+    rw1 = rw0 + (enc1 - enc0)
+    if enc1 - enc0 < 3 * ramp or rw1 + 20_000 > tr_ns:
+        raise ValueError("TR / TE too short for the balanced lobes")
+    flat = lambda t0, t1: (t1 - t0 - 2 * ramp) * S.NS  # seconds of flat top
+    gread = 2 * np.pi / (gamma * fov[0] * dwell * S.NS)
+    slab_area = 2 * np.pi / (gamma * fov[2] * 4 * raster * S.NS) * 0.05 * (rf_ns - 2 * raster) * S.NS
+    gslab = slab_area / ((rf_ns - 2 * raster) * S.NS)
+    t_rf, a_rf = S.sinc_rf(0, rf_ns, raster, flip, tbw)
+    assert t_rf.size == rf_samples
+    j = np.arange(rf_samples)
+    ph_rf = 0.25 + 0.1 * np.sin(2 * np.pi * j / (rf_samples - 1))
+    trs = []
+    for i in range(n_tr):
+        ipe, ipar = i % n_pe, (i // n_pe) % n_par
+        tr = S.TR(tr_ns)
+        tr.rf(t_rf, a_rf, ph_rf + np.pi * (i % 2))
+        tr.trap("z", 0, rf_ns, gslab, ramp_ns=raster)
+        ky = (ipe - n_pe // 2) / fov[1]
+        kz = (ipar - n_par // 2) / fov[2]
+        a_y = 2 * np.pi * ky / gamma
+        a_z = -slab_area / 2 + 2 * np.pi * kz / gamma
+        a_x = -gread * (n_read // 2) * dwell * S.NS
+        tr.trap("y", enc0, enc1, a_y / flat(enc0, enc1), ramp_ns=ramp)
+        tr.trap("z", enc0, enc1, a_z / flat(enc0, enc1), ramp_ns=ramp)
+        tr.trap("x", enc0, enc1, a_x / flat(enc0, enc1), ramp_ns=ramp)
+        tr.trap("x", ro_start - ramp, ro_start + ro_ns + ramp, gread, ramp_ns=ramp)
+        tr.adc_t += [0]
+        tr.adc_v += [0.0]
+        tr.adc(ro_start + dwell * np.arange(n_read))
+        tr.adc_t += [tr_ns]
+        tr.adc_v += [0.0]
+        tr.trap("y", rw0, rw1, -a_y / flat(rw0, rw1), ramp_ns=ramp)
+        tr.trap("z", rw0, rw1, -(slab_area + a_z) / flat(rw0, rw1), ramp_ns=ramp)
+        tr.trap("x", rw0, rw1, -(a_x + gread * ro_ns * S.NS) / flat(rw0, rw1), ramp_ns=ramp)
+        trs.append(tr)
+    return S.concat(trs), n_tr
+
+
 def sat_gre_lines(*, n_read=16, n_pe=4, fov=0.2, tr_ms=30.0, sat_offsets_hz=(1500.0,), sat_ms=4.0,
                   sat_b1_ut=2.0, sat_raster_us=20.0, flip=15.0, bw_hz=32000.0, gamma=GAMMA):
     """Saturation-prepared GRE: per TR a block of Gaussian saturation pulses
@@ -550,3 +608,45 @@ def config3_batch(seed=0, n_inst=256, vox_range=(1000, 262144), sat_s=(1.0, 4.0)
         scans.append(cest_instance(seed * 100003 + i, nv, pools, off, b1, sat_ms))
         meta.append(dict(voxels=nv, pools=pools, offset_ppm=off, b1_ut=b1, sat_ms=sat_ms))
     return scans, meta
+
+
+# the four tissue classes of the adjoint workload: T1 (s), T2 (s), M0 and
+# the fraction of the second (short-T2, exchanging) water pool
+CONFIG4_CLASSES = ((0.83, 0.080, 0.70, 0.15), (1.33, 0.110, 0.80, 0.05), (4.00, 2.000, 1.00, 0.01),
+                   (1.40, 0.050, 0.90, 0.10))
+
+
+def config4_adjoint(seed=0, nx=96, ny=96, nz=16, spins=2, n_tr=200, n_coils=4, rf_samples=512) -> Scan:
+    """The adjoint workload: ``ny x nx x nz`` voxels of a seeded 4-class
+    phantom (classes ``CONFIG4_CLASSES``, per-voxel values jittered by
+    U(0.95, 1.05)), each voxel a free pool and a short-T2 pool (T1 400 ms,
+    T2 12 ms) exchanging at k ~ U(2, 20) /s (detailed balance sets the
+    reverse rate), dB0 ~ N(0, 15 Hz), ``spins`` spins per voxel with
+    intravoxel dephasing (T2* = 0.7 T2), ``n_coils`` Rx coils on a cylinder;
+    balanced SSFP with ``n_tr`` TRs of 5 ms, flip 40 degrees and a
+    ``rf_samples``-sample complex rf waveform."""
+    rng = np.random.default_rng(seed)
+    Y, X, Z = ny, nx, nz
+    # blocky class map: argmax of four coarse random fields, upsampled
+    coarse = rng.normal(size=(max(Y // 8, 1), max(X // 8, 1), max(Z // 4, 1), 4))
+    iy = np.minimum(np.arange(Y) * coarse.shape[0] // Y, coarse.shape[0] - 1)
+    ix = np.minimum(np.arange(X) * coarse.shape[1] // X, coarse.shape[1] - 1)
+    iz = np.minimum(np.arange(Z) * coarse.shape[2] // Z, coarse.shape[2] - 1)
+    label = np.argmax(coarse[iy][:, ix][:, :, iz], axis=-1)
+    tab = np.asarray(CONFIG4_CLASSES)
+    jit = lambda: rng.uniform(0.95, 1.05, (Y, X, Z))
+    T1, T2, M0, f2 = (tab[label, c] * jit() for c in range(4))
+    rho = np.stack([M0 * (1 - f2), M0 * f2], -1).astype(np.float32)
+    t1 = np.stack([T1, np.full_like(T1, 0.4)], -1).astype(np.float32)
+    t2 = np.stack([T2, np.full_like(T2, 0.012)], -1).astype(np.float32)
+    k = rng.uniform(2.0, 20.0, (Y, X, Z))
+    rates = np.zeros((Y, X, Z, 2, 2), np.float32)
+    rates[..., 1, 0] = k
+    rates[..., 0, 1] = k * f2 / (1 - f2)
+    db0 = rng.normal(0.0, 15.0, (Y, X, Z))
+    fov = (0.24, 0.24 * Y / X, 0.24 * Z / X)
+    res = (fov[0] / X, fov[1] / Y, fov[2] / Z)
+    rxx, rxy = _cylinder_coils((Y, X, Z), res, n_coils, rng)
+    lines, ntr = bssfp_lines(n_read=X, n_pe=Y, n_par=Z, fov=fov, n_tr=n_tr, rf_samples=rf_samples)
+    return assemble(rho, t1, t2, spin_num=spins, t2star=0.7 * t2, db0_hz=db0, res=res, model="me",
+                    rates=rates, rx=(rxx, rxy), seqlines=lines, tr_num=ntr, seed=seed)
