@@ -44,54 +44,40 @@ __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
 }
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
 
-// exp([v]x) m with a = |v| > 0: m + sin a (n x m) + (1 - cos a)((n.m) n - m)
-__device__ __forceinline__ float3 rodrigues(float3 v, float3 m, float sa, float omc, float inv_a) {
-    const float3 n = make_float3(v.x * inv_a, v.y * inv_a, v.z * inv_a);
-    const float3 c = cross3(n, m);
-    const float k = dot3(n, m);
-    return make_float3(m.x + fmaf(omc, fmaf(k, n.x, -m.x), sa * c.x), m.y + fmaf(omc, fmaf(k, n.y, -m.y), sa * c.y),
-                       m.z + fmaf(omc, fmaf(k, n.z, -m.z), sa * c.z));
-}
-
-struct Rot {  // exp([v]x) of one step for one pool
+struct Rot {  // exp([v]x) of one step for one pool: s = (sin a / a, (1 - cos a) / a^2)
     float3 v;
-    float sa, omc, inv_a, c1, c2;
-    bool id;
+    float2 s;
 };
 
 __device__ __forceinline__ Rot make_rot(float3 v) {
     Rot r;
     r.v = v;
-    const float a2 = dot3(v, v);
-    r.id = a2 == 0.f;
-    const float a = sqrtf(a2);
-    float sh, ch;
-    sincos_cw(0.5f * a, sh, ch);
-    r.sa = 2.f * sh * ch;
-    r.omc = 2.f * sh * sh;
-    r.inv_a = r.id ? 0.f : 1.f / a;
-    if (a < 0.05f) {  // Taylor forms, error below 1e-10
-        r.c1 = 0.5f - a2 * (1.f / 24.f);
-        r.c2 = 1.f / 6.f - a2 * (1.f / 120.f);
-    } else {
-        r.c1 = r.omc / a2;
-        r.c2 = (a - r.sa) / (a2 * a);
-    }
+    r.s = rot_coeffs(dot3(v, v));
     return r;
 }
 
 __device__ __forceinline__ float3 rot_apply(const Rot &r, float3 m) {
-    return r.id ? m : rodrigues(r.v, m, r.sa, r.omc, r.inv_a);
+    rot_exp(m.x, m.y, m.z, r.v.x, r.v.y, r.v.z, r.s);
+    return m;
 }
 __device__ __forceinline__ float3 rot_apply_t(const Rot &r, float3 m) {  // exp(-[v]x) m
-    return r.id ? m : rodrigues(make_float3(-r.v.x, -r.v.y, -r.v.z), m, r.sa, r.omc, r.inv_a);
+    rot_exp(m.x, m.y, m.z, -r.v.x, -r.v.y, -r.v.z, r.s);
+    return m;
 }
-// J_l(v)^T u
+// (a - sin a) / a^3 = (1 - s1) / a^2: Taylor series in a^2 through a^6 below
+// a = 0.25 (truncation below 1e-12), the quotient above
+__device__ __forceinline__ float jl_c2(float a2, float s1) {
+    if (a2 < 0.0625f)
+        return fmaf(fmaf(fmaf(a2, -1.f / 362880.f, 1.f / 5040.f), a2, -1.f / 120.f), a2, 1.f / 6.f);
+    return (1.f - s1) / a2;
+}
+// J_l(v)^T u = u - c1 v x u + c2 v x (v x u), c1 = (1 - cos a) / a^2
 __device__ __forceinline__ float3 jl_t(const Rot &r, float3 u) {
+    const float c2 = jl_c2(dot3(r.v, r.v), r.s.x);
     const float3 vu = cross3(r.v, u);
     const float3 vvu = cross3(r.v, vu);
-    return make_float3(u.x - r.c1 * vu.x + r.c2 * vvu.x, u.y - r.c1 * vu.y + r.c2 * vvu.y,
-                       u.z - r.c1 * vu.z + r.c2 * vvu.z);
+    return make_float3(u.x - r.s.y * vu.x + c2 * vvu.x, u.y - r.s.y * vu.y + c2 * vvu.y,
+                       u.z - r.s.y * vu.z + c2 * vvu.z);
 }
 
 // compensated running sum (window sums added to a float total)
@@ -106,7 +92,7 @@ struct KSum {
 };
 
 template <int P>
-__global__ void __launch_bounds__(kAdjBlock) adjoint_kernel(AdjLaunch L) {
+__global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjLaunch L) {
     extern __shared__ __align__(16) float adj_sm[];
     float *win = adj_sm;                                            // [kAdjWin][3P][kAdjBlock]
     float *rfp = adj_sm + kAdjWin * 3 * P * kAdjBlock;              // [kAdjWin][warp][2]
@@ -121,10 +107,8 @@ __global__ void __launch_bounds__(kAdjBlock) adjoint_kernel(AdjLaunch L) {
     // ---- per-isochromat constants ------------------------------------------
     float om[4] = {0.f, 0.f, 0.f, 0.f}, wres[P], rhoS[P], t1[P], t2[P];
     float kc[P * P];
-    float2 txc = make_float2(0.f, 0.f), rc[kAdjMaxRx];
+    float2 txc = make_float2(0.f, 0.f);
     float3 m[P];
-#pragma unroll
-    for (int c = 0; c < kAdjMaxRx; ++c) rc[c] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int i = 0; i < P * P; ++i) kc[i] = 0.f;
 #pragma unroll
@@ -138,9 +122,6 @@ __global__ void __launch_bounds__(kAdjBlock) adjoint_kernel(AdjLaunch L) {
         om[2] = L.gyro * L.gyg[v];
         om[3] = L.gyro * L.gzg[v];
         txc = L.txc[v];
-#pragma unroll
-        for (int c = 0; c < kAdjMaxRx; ++c)
-            if (c < L.rx) rc[c] = L.rxc ? L.rxc[(long long)c * n + v] : make_float2(1.f, 0.f);
 #pragma unroll
         for (int t = 0; t < P; ++t) {
             const long long i = ((long long)t * L.S + s) * n + v;
@@ -377,8 +358,9 @@ __global__ void __launch_bounds__(kAdjBlock) adjoint_kernel(AdjLaunch L) {
                     for (int c = 0; c < kAdjMaxRx; ++c) {
                         if (c >= L.rx) break;
                         const float2 g = __ldg(L.gsig + ((long long)t * L.rx + c) * L.A + a);
-                        src.x = fmaf(g.x, rc[c].x, fmaf(-g.y, rc[c].y, src.x));
-                        src.y = fmaf(g.x, rc[c].y, fmaf(g.y, rc[c].x, src.y));
+                        const float2 rc = L.rxc ? __ldg(L.rxc + (long long)c * n + v) : make_float2(1.f, 0.f);
+                        src.x = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src.x));
+                        src.y = fmaf(g.x, rc.y, fmaf(g.y, rc.x, src.y));
                     }
                     nl[t].x += src.x;
                     nl[t].y += src.y;

@@ -193,33 +193,35 @@ static __device__ __noinline__ float lineshape_f32(float rf_freq, float db0, flo
 // y = 1 - exp(-x)
 __device__ __forceinline__ float one_minus_exp(float x) { return -expm1f(-x); }
 
-// Rotation of the frame magnetisation by an rf step: angle alpha about
-// n = (cb cos PHI, -cb sin PHI, sb) in the sense of the reference's closed
-// form (verified identity: R = cos a I - sin a [n]x + (1 - cos a) n n^T).
-__device__ __forceinline__ void rf_rotate(float &x, float &y, float &z, float dW, float b, float2 uphi, float dt) {
-    const float q = fmaf(dW, dW, b * b);
-    if (q == 0.f) return;
-    const float rn = rsqrtf(q);
-    const float Bm = q * rn;
-    const float cb = fabsf(b) * rn;
-    const float sb = copysignf(1.f, b) * dW * rn;
+// Rotation of the magnetisation by an rf step, written with its rotation
+// vector v (angle a = |v|): exp([v]x) m = m + s1 (v x m) + s2 (v x (v x m)),
+// s1 = sin a / a, s2 = (1 - cos a) / a^2 (Rodrigues' formula), the
+// increment added to m with one rounding.  An rf step of the reference's
+// closed form (angle alpha = dt sqrt(b^2 + dW^2) about n = (cb cos PHI,
+// -cb sin PHI, sb), R = cos a I - sin a [n]x + (1 - cos a) n n^T) is
+// v = -alpha n = -dt (gamma Re(conj(B) P), -gamma Im(conj(B) P), dW) with B
+// the complex rf field and P the frame phasor: no normalisation needed.
+// Below a = 0.25 (rf steps of practical sequences turn by a few mrad) s1
+// and s2 are their Taylor series in a^2 through a^6, truncated below 1e-10;
+// larger angles take sin and cos.
+static __device__ __noinline__ float2 rot_coeffs_large(float a2) {
+    const float a = sqrtf(a2);
     float sh, ch;
-    sincos_cw(0.5f * Bm * dt, sh, ch);
-    const float sa = 2.f * sh * ch;
-    const float omc = 2.f * sh * sh;  // 1 - cos(alpha)
-    const float ca = 1.f - omc;
-    const float nx = cb * uphi.x, ny = -cb * uphi.y, nz = sb;
-    const float cx = ny * z - nz * y, cy = nz * x - nx * z, cz = nx * y - ny * x;
-    const float k = fmaf(nx, x, fmaf(ny, y, nz * z));
-    // increment form R M = M + (1 - cos a)((n.M) n - M) - sin a (n x M): the
-    // small increment is added to M with a single rounding
-    (void)ca;
-    const float x2 = x + fmaf(omc, fmaf(k, nx, -x), -sa * cx);
-    const float y2 = y + fmaf(omc, fmaf(k, ny, -y), -sa * cy);
-    const float z2 = z + fmaf(omc, fmaf(k, nz, -z), -sa * cz);
-    x = x2;
-    y = y2;
-    z = z2;
+    sincos_cw(0.5f * a, sh, ch);
+    return make_float2(2.f * sh * ch / a, 2.f * sh * sh / a2);
+}
+__device__ __forceinline__ float2 rot_coeffs(float a2) {
+    if (a2 < 0.0625f)
+        return make_float2(fmaf(fmaf(fmaf(a2, -1.f / 5040.f, 1.f / 120.f), a2, -1.f / 6.f), a2, 1.f),
+                           fmaf(fmaf(fmaf(a2, -1.f / 40320.f, 1.f / 720.f), a2, -1.f / 24.f), a2, 0.5f));
+    return rot_coeffs_large(a2);
+}
+__device__ __forceinline__ void rot_exp(float &x, float &y, float &z, float vx, float vy, float vz, float2 s) {
+    const float cx = fmaf(vy, z, -vz * y), cy = fmaf(vz, x, -vx * z), cz = fmaf(vx, y, -vy * x);
+    const float dx = fmaf(vy, cz, -vz * cy), dy = fmaf(vz, cx, -vx * cz), dz = fmaf(vx, cy, -vy * cx);
+    x += fmaf(s.x, cx, s.y * dx);
+    y += fmaf(s.x, cy, s.y * dy);
+    z += fmaf(s.x, cz, s.y * dz);
 }
 
 // Pools with a frame: every pool but the bound pool (pool 1) of MT / CEST,
@@ -684,11 +686,10 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 }
             }
 
-            float b = 0.f;
-            float2 u0 = make_float2(1.f, 0.f);  // exp(i PHI) before the frame shift
             float sat[P];                        // bound-pool saturation of the rf step
 #pragma unroll
             for (int t = 0; t < P; ++t) sat[t] = 0.f;
+            float2 vt[P];
             if (rf) {
                 // complex B1 = sum_c TxCoilmg_c exp(i pe_c) * amp_c exp(i phase_c)
                 float2 B = cmul(tx0, make_float2(r1.x, r1.y));
@@ -698,9 +699,13 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     B.x += t2.x;
                     B.y += t2.y;
                 }
-                const float Bm = sqrtf(fmaf(B.x, B.x, B.y * B.y));
-                b = Bm * gyro;
-                if (Bm > 0.f) u0 = make_float2(B.x / Bm, -B.y / Bm);  // conj(B)/|B|
+                // transverse part of the rotation vector, per pool (the frames hold still)
+                const float sc = -dt * gyro;
+#pragma unroll
+                for (int t = 0; t < P; ++t) {
+                    const float wx = fmaf(B.x, Pc[t].x, B.y * Pc[t].y), wy = fmaf(B.x, Pc[t].y, -B.y * Pc[t].x);
+                    vt[t] = make_float2(sc * wx, -sc * wy);
+                }
                 if (MODEL != KM_NORMAL && !(MODEL == KM_EXCH && FREE)) {
                     // bound pools: W = pi (gamma TxCoilmg |amp|)^2 G(rf offset, T2b) with the
                     // reference's lineshape rule (single transmit coil)
@@ -722,9 +727,6 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 }
             }
             const float wrf = r1.z;  // 2 pi sum of active rf frequencies
-            float2 uphi[P];
-#pragma unroll
-            for (int t = 0; t < P; ++t) uphi[t] = rf ? cmul(u0, Pc[t]) : make_float2(1.f, 0.f);
 
 #pragma unroll
             for (int s = 0; s < NS; ++s) {
@@ -742,7 +744,8 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                         if (!has_frame<MODEL>(t)) continue;
                         float x = px[t], y = py[t], z = pz[t];
                         const float dW = wc + dwsm[(s * P + t) * kBlock + tid] + F.cs_hi[t] + wrf;
-                        rf_rotate(x, y, z, dW, b, uphi[t], dt);
+                        const float vz = -dt * dW;
+                        rot_exp(x, y, z, vt[t].x, vt[t].y, vz, rot_coeffs(fmaf(vz, vz, fmaf(vt[t].x, vt[t].x, vt[t].y * vt[t].y))));
                         const bool on = tvo >> t & 1u;
                         X[s][t] = on ? x : px[t];
                         Y[s][t] = on ? y : py[t];
