@@ -229,39 +229,51 @@ def run_config4(args):
         tgt.VObj[k] = np.asfortranarray(tgt.VObj[k] * np.float32(1.05))
     target = engine.scan(tgt)
     tx, ty = target["Sx"], target["Sy"]
-    # device time of the forward scan (prepared, inputs resident, L2 flushed)
-    plan = engine.Plan(sc)
+    plan = engine.AdjointPlan(sc)
     work = plan.work()
     stream = torch.cuda.Stream()
     flush = torch.empty(int(256 * 2**20), dtype=torch.uint8, device="cuda")
-    for _ in range(max(3, args.warmup)):
-        plan.execute(stream.cuda_stream)
-    fwd = []
-    for _ in range(args.steps):
+
+    def event_pair():
+        return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    # device time: the forward scan (writing the checkpoints) and the adjoint
+    # kernel, each bracketed by CUDA events on the launching stream, L2 flushed
+    fwd, adj = [], []
+    for i in range(max(3, args.warmup) + args.steps):
         flush.fill_(1)
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        plan.execute(stream.cuda_stream)
-        e1.record(stream)
-        e1.synchronize()
-        fwd.append(e0.elapsed_time(e1))
-    plan.close()
-    # iterations through the public calls (mrl_scan, then mrl_adjoint), host buffers
-    wall, adj, h2d, d2h = [], [], 0, 0
+        (f0, f1), (b0, b1) = event_pair(), event_pair()
+        f0.record(stream)
+        plan.forward(stream.cuda_stream)
+        f1.record(stream)
+        stream.synchronize()
+        out = plan.signal()
+        gx, gy = 2 * (out["Sx"] - tx), 2 * (out["Sy"] - ty)
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        b0.record(stream)
+        plan.backward(gx, gy, stream.cuda_stream)
+        b1.record(stream)
+        b1.synchronize()
+        if i >= max(3, args.warmup):
+            fwd.append(f0.elapsed_time(f1))
+            adj.append(b0.elapsed_time(b1))
+    g = plan.gradients()
+    # iterations through the public calls with host buffers: forward, signal
+    # download, dL/dS on the host, backward, gradient download and reductions
+    wall = []
     with ClockSampler(0) as clk:
-        for i in range(max(3, args.warmup) + args.steps):
+        for i in range(args.steps):
             t0 = time.perf_counter()
-            out = engine.scan(sc)
-            tf = engine.last_timing()
-            g = engine.adjoint(sc, 2 * (out["Sx"] - tx), 2 * (out["Sy"] - ty))
-            ta = engine.last_timing()
-            t1 = time.perf_counter()
-            if i >= max(3, args.warmup):
-                wall.append((t1 - t0) * 1e3)
-                adj.append(ta["scan_ms"])
-                h2d = tf["h2d_bytes"] + ta["h2d_bytes"]
-                d2h = tf["d2h_bytes"] + ta["d2h_bytes"]
+            plan.forward()
+            out = plan.signal()
+            plan.backward(2 * (out["Sx"] - tx), 2 * (out["Sy"] - ty))
+            g = plan.gradients()
+            wall.append((time.perf_counter() - t0) * 1e3)
+    plan.close()
+    h2d = 2 * out["Sx"].size * 8
+    d2h = 2 * out["Sx"].size * 8 + sum(int(v.nbytes) for v in g.values())
     fwd_ms, adj_ms = float(np.mean(fwd)), float(np.mean(adj))
     units = work["units"]
     fp32_tf, mufu_g = peaks()
@@ -275,14 +287,15 @@ def run_config4(args):
                                "water exchanging, 4 Rx, %d TRs of 5 ms, flip 40, 512-sample complex rf"
                                % int(sc.VCtl["TRNum"]),
                    "units_per_iter": units, "steps": work["steps"], "rf_steps": work["rf_steps"],
-                   "samples": work["samples"], "checkpoint_every_steps": 16,
-                   "l2": "flushed between timed forward scans (256 MiB write); the adjoint streams its "
-                         "checkpoints (tens of GB) through HBM"},
+                   "samples": work["samples"], "rf_entries": int(np.size(sc.VSeq["rfAmpLine"])),
+                   "checkpoint_every_steps": 16,
+                   "l2": "flushed before each timed forward scan and adjoint (256 MiB write); the checkpoints "
+                         "(tens of GB) stream through HBM"},
         "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
         "forward_rate": units / (fwd_ms * 1e-3), "adjoint_rate": units / (adj_ms * 1e-3),
         "e2e": {"value": float(np.mean(wall)), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "api": "mrl_scan then mrl_adjoint with host buffers (decode, uploads, downloads, host "
-                       "reductions included)"},
+                "api": "mrl_adjoint_plan forward, download, backward, gradients with host buffers (signal "
+                       "download, dL/dS upload, gradient download and per-voxel reductions included)"},
         "gpu_launches": (work["launches"] + 1) * args.steps,
         "roofline": {"bound": "fp32", "kernel": "forward scan kernel (op table)",
                      "achieved": flops / (fwd_ms * 1e-3) / 1e12, "peak": fp32_tf, "unit": "TFLOP/s",

@@ -219,7 +219,7 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n);
  * applies (rotation, relaxation, split exchange) backwards, with the state
  * checkpointed every few steps and recomputed in between.
  * Scope: free-pool models (normal; ME, or GM without bound pools), one Tx
- * coil, RunMode 0, no Ext events, TypeNum <= 3; rfRef is taken as 0.
+ * coil, RunMode 0, no Ext events, TypeNum <= 3, up to 8 Rx coils.
  * Host arrays (NULL: not wanted), V voxels, layouts as in mrl_scan_args:
  *   grad_sx, grad_sy  [P][Rx][A]   inputs
  *   g_t1, g_t2, g_rho [P][V]       dL/dT1, dL/dT2, dL/dRho (the recovery
@@ -251,6 +251,33 @@ typedef struct {
     double *g_rf_amp_line, *g_rf_phase_line;
 } mrl_adjoint_args;
 int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj);
+
+/* Adjoint plans, for fitting loops: the forward scan (the accurate
+ * integrator, which writes a lab-frame checkpoint of every isochromat every
+ * 16 steps into device memory) and the adjoint kernel's inputs stay on the
+ * device between iterations.  mrl_adjoint is create, forward, backward,
+ * gradients, destroy.  args must outlive the plan (its host arrays are
+ * read at create and written by download).
+ *   create     decodes the sequence once, uploads the object and sizes the
+ *              checkpoints (MRL_ERR_NOMEM if they do not fit the free
+ *              device memory); same scope as mrl_adjoint
+ *   forward    runs the scan from the initial magnetisation on `stream`
+ *              (NULL: the default stream), writing the checkpoints
+ *   download   signal and final magnetisation of the last forward pass
+ *              into args' host arrays, like mrl_plan_download
+ *   backward   dL/dSx, dL/dSy (host, [P][Rx][A]) of the last forward pass:
+ *              enqueues the adjoint kernel on `stream`
+ *   gradients  waits for the device and fills adj's outputs (its grad_sx,
+ *              grad_sy are not read)
+ *   work       out[0..4] as mrl_plan_work, out[5] = rf-on steps */
+typedef struct mrl_adjoint_plan mrl_adjoint_plan;
+int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out);
+int mrl_adjoint_plan_forward(mrl_adjoint_plan *plan, void *stream);
+int mrl_adjoint_plan_download(mrl_adjoint_plan *plan, mrl_scan_args *args);
+int mrl_adjoint_plan_backward(mrl_adjoint_plan *plan, const double *grad_sx, const double *grad_sy, void *stream);
+int mrl_adjoint_plan_gradients(mrl_adjoint_plan *plan, mrl_adjoint_args *adj);
+int mrl_adjoint_plan_work(const mrl_adjoint_plan *plan, long long out[6]);
+void mrl_adjoint_plan_destroy(mrl_adjoint_plan *plan);
 
 /* Scan without allocating device memory.
  *

@@ -1,7 +1,9 @@
 """``torch.autograd`` bridge over the scan engine, for test harnesses and
-parameter fitting: the forward pass runs ``mrl_scan`` (the accurate
-integrator) and the backward pass ``mrl_adjoint``, both through the C ABI
-on the GPU.  There is no CPU path: without the CUDA library both raise.
+parameter fitting, through an adjoint plan (``mrl_adjoint_plan``): the
+forward pass runs the accurate integrator, which leaves a checkpoint of
+every isochromat every 16 steps on the device, and the backward pass runs
+the adjoint kernel from those checkpoints; both through the C ABI on the
+GPU.  There is no CPU path: without the CUDA library both raise.
 
     sx, sy = autograd.scan(sc, T1=t1, T2=t2, Rho=rho, dB0=db0)
     loss = ((sx - tx) ** 2 + (sy - ty) ** 2).sum()
@@ -60,8 +62,10 @@ class _Scan(torch.autograd.Function):
     @staticmethod
     def forward(ctx, sc, gpu_index, names, *tensors):
         s = _with_values(sc, dict(zip(names, tensors)))
-        out = engine.scan(s, numerics="accurate", gpu_index=gpu_index)
-        ctx.sc, ctx.gpu_index, ctx.names = s, gpu_index, names
+        plan = engine.AdjointPlan(s, gpu_index=gpu_index)
+        plan.forward()
+        out = plan.signal()
+        ctx.plan, ctx.sc, ctx.names = plan, s, names
         ctx.shapes = [t.shape for t in tensors]
         ctx.dtypes = [t.dtype for t in tensors]
         return torch.from_numpy(out["Sx"].copy()), torch.from_numpy(out["Sy"].copy())
@@ -72,7 +76,10 @@ class _Scan(torch.autograd.Function):
                                 int(ctx.sc.VCoi["RxCoilNum"]))
         gx = gsx.detach().cpu().numpy() if gsx is not None else zero()
         gy = gsy.detach().cpu().numpy() if gsy is not None else zero()
-        g = engine.adjoint(ctx.sc, gx, gy, gpu_index=ctx.gpu_index)
+        plan = ctx.plan
+        plan.backward(gx, gy)
+        g = plan.gradients()
+        plan.close()  # the checkpoints are released with the graph's one backward pass
         outs = []
         key_of = {name: out for name, _, _, out in _PARAMS}
         for name, shape, dtype in zip(ctx.names, ctx.shapes, ctx.dtypes):

@@ -25,11 +25,12 @@
 // (m_r x lambda_r), J_l(v)^T u = u - c1 v x u + c2 v x (v x u),
 // c1 = (1 - cos a) / a^2, c2 = (a - sin a) / a^3, a = |v|.
 //
-// One thread owns one isochromat (a voxel's spin, all its pools).  A
-// forward sweep stores the state every kAdjWin steps (checkpoints, in
-// HBM); the backward sweep takes the windows last to first, recomputes the
-// window's states from its checkpoint into shared memory and walks them in
-// reverse.  The rf gradient of a step is summed over the block (warp
+// One thread owns one isochromat (a voxel's spin, all its pools).  The
+// forward scan (the accurate integrator, whose frames are anchored to FP64
+// phase moments) stores the lab-frame state every kAdjWin steps
+// (checkpoints, in HBM); this kernel takes the windows last to first,
+// recomputes each window's states from its checkpoint into shared memory
+// with the map above and walks them in reverse.  The rf gradient of a step is summed over the block (warp
 // shuffles, then the warps) and added to its FP64 slot.
 #include "scan_launch.h"
 
@@ -129,7 +130,6 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
             rhoS[t] = L.rho[(long long)t * n + v] / (float)L.S;
             t1[t] = L.t1[(long long)t * n + v];
             t2[t] = L.t2[(long long)t * n + v];
-            m[t] = make_float3(L.m0[i], L.m0[L.m0_stride + i], L.m0[2 * L.m0_stride + i]);
         }
         if (L.kch)
 #pragma unroll
@@ -213,27 +213,11 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
     };
     auto rec = [&](long long k, int i) { return __ldg(L.rec + k * 3 + i); };
 
-    // ---- forward sweep with checkpoints -------------------------------------
     const long long N = L.n_steps;
     const long long nwin = (N + kAdjWin - 1) / kAdjWin;
     const long long cs = (long long)3 * P;  // checkpoint components
-    for (long long k = 0; k < N; ++k) {
-        const float4 r0 = rec(k, 0), r1 = rec(k, 1);
-        const int flags = __float_as_int(r1.w);
-        const float dt = r0.x;
-        if (k % kAdjWin == 0 && active) {
-            float *cp = L.ckpt + (k / kAdjWin) * cs * L.n_iso + iso;
-#pragma unroll
-            for (int t = 0; t < P; ++t) {
-                cp[(3 * t + 0) * L.n_iso] = m[t].x;
-                cp[(3 * t + 1) * L.n_iso] = m[t].y;
-                cp[(3 * t + 2) * L.n_iso] = m[t].z;
-            }
-        }
-        if (k == 0 || (flags & kFlagDt)) set_dt(dt);
-        if (k == 0 || (flags & kFlagState)) set_state(dt, r0);
-        fwd(dt, r0, r1, (flags & kFlagRf) != 0);
-    }
+    // (dt, Gz, Gy, Gx) of the coefficients in registers
+    float4 cur = make_float4(-1.f, 0.f, 0.f, 0.f);
 
     // ---- backward sweep -----------------------------------------------------
     float3 lam[P];
@@ -260,8 +244,15 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
                 ws[(3 * t + 1) * kAdjBlock] = m[t].y;
                 ws[(3 * t + 2) * kAdjBlock] = m[t].z;
             }
-            if (k == k0 || (flags & kFlagDt)) set_dt(dt);
-            if (k == k0 || (flags & kFlagState)) set_state(dt, r0);
+            if (k == k0) {  // the coefficients of the window's first step, if not in registers
+                if (dt != cur.x) set_dt(dt);
+                if (dt != cur.x || r0.y != cur.y || r0.z != cur.z || r0.w != cur.w) set_state(dt, r0);
+                cur = r0;
+            } else if (flags & (kFlagDt | kFlagState)) {
+                if (flags & kFlagDt) set_dt(dt);
+                if (flags & kFlagState) set_state(dt, r0);
+                cur = r0;
+            }
             if (k + 1 < k1) fwd(dt, r0, r1, (flags & kFlagRf) != 0);
         }
         // window partial sums of the parameter gradients
@@ -279,6 +270,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
                 const int fn = __float_as_int(rec(k + 1, 1).w);
                 if (fn & kFlagDt) set_dt(dt);
                 if (fn & kFlagState) set_state(dt, r0);
+                if (fn & (kFlagDt | kFlagState)) cur = r0;
             }
             const bool rf = (flags & kFlagRf) != 0;
             const float *ws = win + (k - k0) * 3 * P * kAdjBlock + tid;

@@ -227,7 +227,7 @@ inline void split(double v, float &hi, float &lo) {
 }
 }  // namespace
 
-void pack_fast_records(const DecodeChunk &ch, int tx, FrameMoments &fm, std::vector<float> &out) {
+void pack_fast_records(const DecodeChunk &ch, int tx, FrameMoments &fm, std::vector<float> &out, int ckpt_every) {
     const int stride = fast_stride_f4(tx) * 4;
     int every = kAnchorEvery;
     if (const char *e = std::getenv("MRL_ANCHOR_EVERY")) every = std::max(1, std::atoi(e));
@@ -250,6 +250,7 @@ void pack_fast_records(const DecodeChunk &ch, int tx, FrameMoments &fm, std::vec
         const bool new_state = new_dt || si.gx != fm.last_gx || si.gy != fm.last_gy || si.gz != fm.last_gz;
         if (new_dt) flags |= kFlagDt;
         if (new_state) flags |= kFlagState;
+        if (ckpt_every > 0 && q % ckpt_every == 0) flags |= kFlagCkpt;
         // anchor the frames at every change of (dt, G), at the first step of
         // an rf block and after `every` free steps; within an rf block the
         // frames hold still, so their phasors stay exact without anchors

@@ -88,11 +88,15 @@ struct FrameMoments {
 //   {Re Ac, Im Ac, freq c, |Ac|} for every coil c >= 1
 // with Ac = amp_c * exp(i phase_c) the complex rf amplitude, and flag bits
 // kFlagAdc, kFlagRf, kFlagAnchor (recompute the frame phasors exactly),
-// kFlagState (dt or gradient changed), kFlagDt (dt changed).
-enum : int { kFlagAdc = 1, kFlagRf = 2, kFlagAnchor = 4, kFlagState = 8, kFlagDt = 16 };
+// kFlagState (dt or gradient changed), kFlagDt (dt changed), kFlagCkpt
+// (write the lab-frame state before this step to its checkpoint slot).
+enum : int { kFlagAdc = 1, kFlagRf = 2, kFlagAnchor = 4, kFlagState = 8, kFlagDt = 16, kFlagCkpt = 32 };
 constexpr int kAnchorEvery = 8;
+constexpr int kAdjWin = 16;  // steps between adjoint checkpoints (recomputed into shared memory)
 inline int fast_stride_f4(int tx_num) { return 4 + (tx_num - 1); }
-void pack_fast_records(const DecodeChunk &ch, int tx_num, FrameMoments &fm, std::vector<float> &out);
+// ckpt_every > 0 flags every ckpt_every-th step of the chunk with kFlagCkpt
+void pack_fast_records(const DecodeChunk &ch, int tx_num, FrameMoments &fm, std::vector<float> &out,
+                       int ckpt_every = 0);
 
 // Decode until the next nonzero Ext sample or the end of the sequence.
 // K-space positions of acquired samples are accumulated into sig.kx/ky/kz.

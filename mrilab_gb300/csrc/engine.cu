@@ -350,6 +350,10 @@ struct Scanner {
            o_dwr = 0;
     // RunMode 1 history: snapshots of the state before every dt > 0 step
     bool hist_on = false;
+    // adjoint checkpoints (single-chunk scans): every ckpt_every-th step's
+    // lab-frame state into ckpt (kFlagCkpt), 0 = off
+    float *ckpt = nullptr;
+    int ckpt_every = 0;
     DevBuf<float> d_hist;        // [step][Mx|My|Mz][P][S][n_act], then the final state
     long long hist_steps = 0;    // steps of the chunks run so far
     long long hist_cap = 0;      // dt > 0 steps the buffer holds
@@ -715,7 +719,7 @@ struct Scanner {
         a_peak = std::max(a_peak, a_cnt);
         const std::vector<float> *recs = &ch.records;
         if (fast) {
-            pack_fast_records(ch, TX, fmom, frec);
+            pack_fast_records(ch, TX, fmom, frec, ckpt_every);
             recs = &frec;
         }
         phase("pack records");
@@ -766,6 +770,8 @@ struct Scanner {
         L.a_launch = d.a_count;
         L.hist_stride = (long long)P * S * std::max(1, n_act);
         L.hist = hist_on ? d_hist.p + (hist_steps + d.s0) * 3 * L.hist_stride : nullptr;
+        L.ckpt = ckpt;
+        L.ckpt_step0 = d.s0;
         return L;
     }
 
@@ -1345,7 +1351,12 @@ int mrl_scan(mrl_scan_args *args, mrl_ext_fn ext, void *user) {
     return rc;
 }
 
-int mrl_plan_create(const mrl_scan_args *args, mrl_plan **out) {
+}  // extern "C"
+
+namespace {
+// A prepared scan.  ckpt_every > 0 flags every ckpt_every-th step for an
+// adjoint checkpoint; `keep` (optional) receives the decoded sequence.
+int plan_create_impl(const mrl_scan_args *args, mrl_plan **out, int ckpt_every, mrl::DecodeChunk *keep) {
     mrl::g_err.clear();
     if (!args || !out) {
         mrl::set_err("NULL argument");
@@ -1367,6 +1378,7 @@ int mrl_plan_create(const mrl_scan_args *args, mrl_plan **out) {
         delete p;
         return rc;
     }
+    sc.ckpt_every = ckpt_every;
     const int A = sc.A;
     p->kx.assign(std::max(A, 1), 0.0);
     p->ky.assign(std::max(A, 1), 0.0);
@@ -1407,9 +1419,15 @@ int mrl_plan_create(const mrl_scan_args *args, mrl_plan **out) {
     p->work[2] = ch.n_rf_steps;
     p->work[3] = ch.adc_end - ch.adc_begin;
     p->work[4] = launches;
+    if (keep) *keep = std::move(ch);
     *out = p;
     return MRL_OK;
 }
+}  // namespace
+
+extern "C" {
+
+int mrl_plan_create(const mrl_scan_args *args, mrl_plan **out) { return plan_create_impl(args, out, 0, nullptr); }
 
 int mrl_plan_execute(mrl_plan *p, void *stream) {
     if (!p) return MRL_ERR_ARG;
@@ -1721,17 +1739,43 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n) {
     return rc;
 }
 
-int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
+}  // extern "C"
+
+// An adjoint plan: the forward scan, prepared with a checkpoint every
+// kAdjWin steps, and the adjoint kernel's inputs and outputs, resident.
+struct mrl_adjoint_plan {
+    mrl_plan *fwd = nullptr;
+    mrl::DevBuf<float4> d_rec;
+    mrl::DevBuf<float> d_ck, d_g;
+    mrl::DevBuf<float2> d_gs;
+    mrl::DevBuf<double> d_rf;
+    mrl::AdjLaunch L{};
+    std::vector<int> rf_uts, rf_src;  // per rf step: uts index; rfAmpLine, rfPhaseLine entries held
+    std::vector<double> rf_a;         // per rf step: Re A, Im A
+    int P = 0, S = 0, RX = 0, A = 0, n_rf = 0;
+    long long V = 0, n_iso = 0, N = 0;
+    double rf_ref = 0;
+    bool forward_done = false, backward_done = false;
+    ~mrl_adjoint_plan() {
+        if (fwd) mrl_plan_destroy(fwd);
+    }
+};
+
+extern "C" {
+
+int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     using namespace mrl;
     g_err.clear();
-    if (!args || !adj) return set_err("NULL argument"), MRL_ERR_ARG;
+    if (!args || !out) return set_err("NULL argument"), MRL_ERR_ARG;
+    *out = nullptr;
     if (args->ctl.run_mode == 1) return set_err("the adjoint runs RunMode 0 scans"), MRL_ERR_UNSUPPORTED;
-    const auto t_start = std::chrono::steady_clock::now();
-    for (double &x : g_timing) x = 0;
-    Scanner sc;
-    sc.args = args;
-    int rc = sc.setup();
+    std::unique_ptr<mrl_adjoint_plan> p(new mrl_adjoint_plan());
+    mrl_scan_args a = *args;
+    a.ctl.numerics = MRL_NUMERICS_ACCURATE;  // the checkpoints come from the accurate integrator
+    DecodeChunk ch;
+    int rc = plan_create_impl(&a, &p->fwd, kAdjWin, &ch);
     if (rc) return rc;
+    Scanner &sc = p->fwd->sc;
     if (!(sc.mi.km == KM_NORMAL || (sc.mi.km == KM_EXCH && sc.all_free())))
         return set_err("the adjoint covers free-pool models (normal; ME, or GM without bound pools)"),
                MRL_ERR_UNSUPPORTED;
@@ -1739,29 +1783,16 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
     if (sc.P > 3) return set_err("the adjoint supports TypeNum <= 3"), MRL_ERR_UNSUPPORTED;
     if (sc.RX > 8) return set_err("the adjoint supports up to 8 Rx coils"), MRL_ERR_UNSUPPORTED;
     const int P = sc.P, S = sc.S, RX = sc.RX, A = sc.A;
-    const long long V = sc.V;
-    // the whole sequence, decoded once
-    std::vector<double> kx(std::max(A, 1)), ky(std::max(A, 1)), kz(std::max(A, 1));
-    mrl_signal sig = args->sig;
-    sig.kx = kx.data();
-    sig.ky = ky.data();
-    sig.kz = kz.data();
-    DecodeState ds;
-    mrl_state none{};
-    load_state(ds, none, sc.TX);
-    DecodeChunk ch;
-    decode_until_ext(ds, args->seq, sc.TX, args->obj.gyro, sig, ch);
-    if (ch.stopped_at_ext) return set_err("the adjoint runs sequences without Ext events"), MRL_ERR_UNSUPPORTED;
-    // step records
+    p->P = P, p->S = S, p->RX = RX, p->A = A, p->V = sc.V;
+    p->rf_ref = args->var.rf_ref ? *args->var.rf_ref : 0.0;
+    // step records of the adjoint
     const long long N = ch.n_steps;
+    p->N = N;
     std::vector<float4> rec((size_t)std::max<long long>(1, N) * 3);
     std::vector<int> step_uts((size_t)std::max<long long>(1, N), -1);
     for (size_t j = 0; j < ch.point_uts.size(); ++j)
         if (ch.point_dt[j] > 0) step_uts[ch.point_step[j]] = ch.point_uts[j];
-    int n_rf = 0;
     double last_dt = -1, lgx = 0, lgy = 0, lgz = 0;
-    std::vector<int> rf_uts, rf_src;
-    std::vector<double> rf_a;
     for (long long q = 0; q < N; ++q) {
         const StepInfo &si = ch.steps[q];
         const bool rf = (float)si.amp[0] != 0.f;
@@ -1774,13 +1805,13 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
         r1.y = (float)(si.amp[0] * std::sin(si.phase[0]));
         r1.z = (float)(2 * kPiRef * si.freq[0]);
         std::memcpy(&r1.w, &flags, sizeof(int));
-        const int ri = rf ? n_rf++ : -1;
+        const int ri = rf ? p->n_rf++ : -1;
         if (rf) {
-            rf_uts.push_back(step_uts[q]);
-            rf_a.push_back(si.amp[0] * std::cos(si.phase[0]));
-            rf_a.push_back(si.amp[0] * std::sin(si.phase[0]));
-            rf_src.push_back(si.amp_src);
-            rf_src.push_back(si.phase_src);
+            p->rf_uts.push_back(step_uts[q]);
+            p->rf_a.push_back(si.amp[0] * std::cos(si.phase[0]));
+            p->rf_a.push_back(si.amp[0] * std::sin(si.phase[0]));
+            p->rf_src.push_back(si.amp_src);
+            p->rf_src.push_back(si.phase_src);
         }
         float4 r2 = make_float4(0.f, 0.f, 0.f, 0.f);
         std::memcpy(&r2.x, &si.adc, sizeof(int));
@@ -1789,83 +1820,113 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
         rec[q * 3 + 1] = r1;
         rec[q * 3 + 2] = r2;
     }
-    adj->n_rf_steps = n_rf;
     const int n = std::max(1, sc.n_act);
     const long long n_iso = (long long)sc.n_act * S;
+    p->n_iso = n_iso;
     const long long nwin = (N + kAdjWin - 1) / kAdjWin;
     const double ck_bytes = (double)nwin * 3 * P * std::max(1LL, n_iso) * sizeof(float);
-    if (ck_bytes > 96.0 * (1ull << 30))
-        return set_err("adjoint checkpoints need %.1f GiB (limit 96 GiB)", ck_bytes / (1ull << 30)), MRL_ERR_NOMEM;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    if (ck_bytes > 0.85 * (double)free_b)
+        return set_err("adjoint checkpoints need %.1f GiB, %.1f GiB free", ck_bytes / (1ull << 30),
+                       (double)free_b / (1ull << 30)),
+               MRL_ERR_NOMEM;
     const int nf = adjoint_fields(P);
-    DevBuf<float4> d_rec;
-    DevBuf<float> d_ck, d_g;
-    DevBuf<float2> d_gs;
-    DevBuf<double> d_rf;
-    cudaError_t e = d_rec.ensure(rec.size());
-    if (e == cudaSuccess) e = d_ck.ensure((size_t)std::max(1LL, nwin * 3 * P * n_iso));
-    if (e == cudaSuccess) e = d_g.ensure((size_t)nf * std::max(1LL, n_iso));
-    if (e == cudaSuccess) e = d_gs.ensure((size_t)P * RX * std::max(A, 1));
-    if (e == cudaSuccess) e = d_rf.ensure((size_t)2 * std::max(1, n_rf));
-    if (e != cudaSuccess) return sc.fail_cuda(e, "cudaMalloc(adjoint)");
-    std::vector<float2> gs((size_t)P * RX * std::max(A, 1), make_float2(0.f, 0.f));
-    for (size_t i = 0; i < (size_t)P * RX * A; ++i)
-        gs[i] = make_float2(adj->grad_sx ? (float)adj->grad_sx[i] : 0.f, adj->grad_sy ? (float)adj->grad_sy[i] : 0.f);
-    cudaStream_t st = sc.st;
-    if ((e = cudaMemcpyAsync(d_rec.p, rec.data(), rec.size() * sizeof(float4), cudaMemcpyHostToDevice, st)) ==
-        cudaSuccess)
-        e = cudaMemcpyAsync(d_gs.p, gs.data(), gs.size() * sizeof(float2), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_rf.p, 0, d_rf.n * sizeof(double), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_g.p, 0, d_g.n * sizeof(float), st);
-    if (e != cudaSuccess) return sc.fail_cuda(e, "adjoint upload");
-    if (n_iso > 0 && N > 0) {
-        AdjLaunch L{};
-        L.n_act = sc.n_act;
-        L.S = S;
-        L.rx = RX;
-        L.A = std::max(A, 1);
-        L.exch_gm = sc.mi.gm ? 1 : 0;
-        L.n_iso = n_iso;
-        L.gyro = (float)args->obj.gyro;
-        L.gxg = sc.d_f.p + sc.o_gx;
-        L.gyg = sc.d_f.p + sc.o_gy;
-        L.gzg = sc.d_f.p + sc.o_gz;
-        L.db0 = sc.d_f.p + sc.o_db0;
-        L.rho = sc.d_f.p + sc.o_rho;
-        L.t1 = sc.d_f.p + sc.o_t1;
-        L.t2 = sc.d_f.p + sc.o_t2;
-        L.kch = sc.mi.nk > 0 ? sc.d_f.p + sc.o_k : nullptr;
-        L.dwrnd = sc.d_f.p + sc.o_dwr;
-        L.m0 = sc.d_m.p;
-        L.m0_stride = (long long)P * S * n;
-        L.rxc = args->coil.rx_default == 0 ? sc.d_rx.p : nullptr;
-        L.txc = sc.d_f2.p + sc.o_txc;
-        for (int t = 0; t < kMaxPool; ++t)
-            L.cs2pi[t] = (t < P && args->ctl.cs) ? (float)(2 * kPiRef * args->ctl.cs[t]) : 0.f;
-        L.rec = d_rec.p;
-        L.n_steps = N;
-        L.ckpt = d_ck.p;
-        L.gsig = d_gs.p;
-        L.giso = d_g.p;
-        L.grf = d_rf.p;
-        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-        if ((e = cudaEventCreate(&ev0)) == cudaSuccess && (e = cudaEventCreate(&ev1)) == cudaSuccess &&
-            (e = cudaEventRecord(ev0, st)) == cudaSuccess && (e = launch_adjoint(P, L, st)) == cudaSuccess)
-            e = cudaEventRecord(ev1, st);
-        if (e == cudaSuccess) e = cudaEventSynchronize(ev1);
-        float ms = 0.f;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);
-        if (ev0) cudaEventDestroy(ev0);
-        if (ev1) cudaEventDestroy(ev1);
-        if (e != cudaSuccess) return sc.fail_cuda(e, "adjoint launch");
-        g_timing[1] = ms;
-        g_timing[5] = 1;
+    cudaError_t e = p->d_rec.ensure(rec.size());
+    if (e == cudaSuccess) e = p->d_ck.ensure((size_t)std::max(1LL, nwin * 3 * P * n_iso));
+    if (e == cudaSuccess) e = p->d_g.ensure((size_t)nf * std::max(1LL, n_iso));
+    if (e == cudaSuccess) e = p->d_gs.ensure((size_t)P * RX * std::max(A, 1));
+    if (e == cudaSuccess) e = p->d_rf.ensure((size_t)2 * std::max(1, p->n_rf));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p->d_rec.p, rec.data(), rec.size() * sizeof(float4), cudaMemcpyHostToDevice, sc.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sc.st);
+    if (e != cudaSuccess) return sc.fail_cuda(e, "adjoint buffers");
+    sc.ckpt = p->d_ck.p;
+    AdjLaunch &L = p->L;
+    L.n_act = sc.n_act;
+    L.S = S;
+    L.rx = RX;
+    L.A = std::max(A, 1);
+    L.exch_gm = sc.mi.gm ? 1 : 0;
+    L.n_iso = n_iso;
+    L.gyro = (float)args->obj.gyro;
+    L.gxg = sc.d_f.p + sc.o_gx;
+    L.gyg = sc.d_f.p + sc.o_gy;
+    L.gzg = sc.d_f.p + sc.o_gz;
+    L.db0 = sc.d_f.p + sc.o_db0;
+    L.rho = sc.d_f.p + sc.o_rho;
+    L.t1 = sc.d_f.p + sc.o_t1;
+    L.t2 = sc.d_f.p + sc.o_t2;
+    L.kch = sc.mi.nk > 0 ? sc.d_f.p + sc.o_k : nullptr;
+    L.dwrnd = sc.d_f.p + sc.o_dwr;
+    L.rxc = args->coil.rx_default == 0 ? sc.d_rx.p : nullptr;
+    L.txc = sc.d_f2.p + sc.o_txc;
+    for (int t = 0; t < kMaxPool; ++t)
+        L.cs2pi[t] = (t < P && args->ctl.cs) ? (float)(2 * kPiRef * args->ctl.cs[t]) : 0.f;
+    L.rec = p->d_rec.p;
+    L.n_steps = N;
+    L.ckpt = p->d_ck.p;
+    L.gsig = p->d_gs.p;
+    L.giso = p->d_g.p;
+    L.grf = p->d_rf.p;
+    (void)n;
+    *out = p.release();
+    return MRL_OK;
+}
+
+int mrl_adjoint_plan_forward(mrl_adjoint_plan *p, void *stream) {
+    if (!p) return MRL_ERR_ARG;
+    int rc = mrl_plan_execute(p->fwd, stream);
+    p->forward_done = rc == MRL_OK;
+    return rc;
+}
+
+int mrl_adjoint_plan_download(mrl_adjoint_plan *p, mrl_scan_args *args) {
+    if (!p || !args) return MRL_ERR_ARG;
+    return mrl_plan_download(p->fwd, args);
+}
+
+int mrl_adjoint_plan_backward(mrl_adjoint_plan *p, const double *grad_sx, const double *grad_sy, void *stream) {
+    using namespace mrl;
+    g_err.clear();
+    if (!p) return set_err("NULL plan"), MRL_ERR_ARG;
+    if (!p->forward_done) return set_err("mrl_adjoint_plan_backward needs a forward pass first"), MRL_ERR_ARG;
+    Scanner &sc = p->fwd->sc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the signal is the receive sum rotated by exp(-i rfRef): dL/dS before
+    // the rotation = exp(+i rfRef) dL/dS after it
+    const double cr = std::cos(p->rf_ref), sr = std::sin(p->rf_ref);
+    std::vector<float2> gs((size_t)p->P * p->RX * std::max(p->A, 1), make_float2(0.f, 0.f));
+    for (size_t i = 0; i < (size_t)p->P * p->RX * p->A; ++i) {
+        const double gx = grad_sx ? grad_sx[i] : 0.0, gy = grad_sy ? grad_sy[i] : 0.0;
+        gs[i] = make_float2((float)(gx * cr - gy * sr), (float)(gx * sr + gy * cr));
     }
-    std::vector<float> g((size_t)nf * std::max(1LL, n_iso));
-    std::vector<double> grf(d_rf.n);
-    if ((e = cudaMemcpyAsync(g.data(), d_g.p, g.size() * sizeof(float), cudaMemcpyDeviceToHost, st)) == cudaSuccess)
-        e = cudaMemcpyAsync(grf.data(), d_rf.p, grf.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaError_t e = cudaMemcpyAsync(p->d_gs.p, gs.data(), gs.size() * sizeof(float2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p->d_rf.p, 0, p->d_rf.n * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p->d_g.p, 0, p->d_g.n * sizeof(float), st);
+    if (e == cudaSuccess && p->n_iso > 0 && p->N > 0) e = launch_adjoint(p->P, p->L, st);
+    if (e != cudaSuccess) return sc.fail_cuda(e, "adjoint launch");
+    p->backward_done = true;
+    return MRL_OK;
+}
+
+int mrl_adjoint_plan_gradients(mrl_adjoint_plan *p, mrl_adjoint_args *adj) {
+    using namespace mrl;
+    g_err.clear();
+    if (!p || !adj) return set_err("NULL argument"), MRL_ERR_ARG;
+    if (!p->backward_done) return set_err("mrl_adjoint_plan_gradients needs a backward pass first"), MRL_ERR_ARG;
+    Scanner &sc = p->fwd->sc;
+    const mrl_scan_args *args = &p->fwd->args;
+    const int P = p->P, S = p->S;
+    const long long V = p->V, n_iso = p->n_iso;
+    const int n_rf = p->n_rf;
+    cudaError_t e = cudaDeviceSynchronize();
+    std::vector<float> g(p->d_g.n);
+    std::vector<double> grf(p->d_rf.n);
+    if (e == cudaSuccess) e = cudaMemcpy(g.data(), p->d_g.p, g.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(grf.data(), p->d_rf.p, grf.size() * sizeof(double), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return sc.fail_cuda(e, "adjoint download");
+    adj->n_rf_steps = n_rf;
     // per voxel: sums over the voxel's spins; per isochromat: the initial state
     auto field = [&](int f, int s2, int j) { return g[(size_t)f * n_iso + (size_t)s2 * sc.n_act + j]; };
     const int F_T1 = 0, F_T2 = P, F_RHO = 2 * P, F_DB0 = 3 * P, F_K = 3 * P + 1, F_M0 = 3 * P + 1 + P * P;
@@ -1894,8 +1955,8 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
     }
     if (n_rf <= adj->rf_capacity) {
         if (adj->g_rf) std::copy(grf.begin(), grf.begin() + 2 * n_rf, adj->g_rf);
-        if (adj->rf_step_uts) std::copy(rf_uts.begin(), rf_uts.end(), adj->rf_step_uts);
-        if (adj->rf_a) std::copy(rf_a.begin(), rf_a.end(), adj->rf_a);
+        if (adj->rf_step_uts) std::copy(p->rf_uts.begin(), p->rf_uts.end(), adj->rf_step_uts);
+        if (adj->rf_a) std::copy(p->rf_a.begin(), p->rf_a.end(), adj->rf_a);
     }
     // onto the waveform lines: A = a e^{i phi} with a = rfAmpLine[ja] (a
     // negative a is the same A as |a| at phi + pi), phi = rfPhaseLine[jp]
@@ -1903,18 +1964,52 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
     if (adj->g_rf_amp_line) std::fill(adj->g_rf_amp_line, adj->g_rf_amp_line + n_line, 0.0);
     if (adj->g_rf_phase_line) std::fill(adj->g_rf_phase_line, adj->g_rf_phase_line + n_line, 0.0);
     for (int i = 0; i < n_rf; ++i) {
-        const double gx = grf[2 * i], gy = grf[2 * i + 1], ax = rf_a[2 * i], ay = rf_a[2 * i + 1];
-        const int ja = rf_src[2 * i], jp = rf_src[2 * i + 1];
+        const double gx = grf[2 * i], gy = grf[2 * i + 1], ax = p->rf_a[2 * i], ay = p->rf_a[2 * i + 1];
+        const int ja = p->rf_src[2 * i], jp = p->rf_src[2 * i + 1];
         if (adj->g_rf_amp_line && ja >= 0 && ja < n_line) {
             const double a = args->seq.rf_amp[ja];
             if (a != 0) adj->g_rf_amp_line[ja] += (gx * ax + gy * ay) / a;
         }
         if (adj->g_rf_phase_line && jp >= 0 && jp < n_line) adj->g_rf_phase_line[jp] += gy * ax - gx * ay;
     }
-    g_timing[6] = (double)(rec.size() * sizeof(float4) + gs.size() * sizeof(float2));
-    g_timing[7] = (double)(g.size() * sizeof(float) + grf.size() * sizeof(double));
-    g_timing[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
     return sc.check_device_status();
+}
+
+int mrl_adjoint_plan_work(const mrl_adjoint_plan *p, long long out[6]) {
+    if (!p || !out) return MRL_ERR_ARG;
+    for (int i = 0; i < 5; ++i) out[i] = p->fwd->work[i];
+    out[5] = p->n_rf;
+    return MRL_OK;
+}
+
+void mrl_adjoint_plan_destroy(mrl_adjoint_plan *p) { delete p; }
+
+int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
+    using namespace mrl;
+    if (!args || !adj) return g_err.clear(), set_err("NULL argument"), MRL_ERR_ARG;
+    const auto t_start = std::chrono::steady_clock::now();
+    for (double &x : g_timing) x = 0;
+    mrl_adjoint_plan *p = nullptr;
+    int rc = mrl_adjoint_plan_create(args, &p);
+    if (rc) return rc;
+    std::unique_ptr<mrl_adjoint_plan> keep(p);
+    cudaStream_t st = p->fwd->sc.st;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    rc = mrl_adjoint_plan_forward(p, st);
+    if (!rc) cudaEventRecord(ev0, st);
+    if (!rc) rc = mrl_adjoint_plan_backward(p, adj->grad_sx, adj->grad_sy, st);
+    if (!rc) cudaEventRecord(ev1, st);
+    float ms = 0.f;
+    if (!rc && cudaEventSynchronize(ev1) == cudaSuccess) cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    if (!rc) rc = mrl_adjoint_plan_gradients(p, adj);
+    g_timing[1] = ms;  // the adjoint kernel (after the forward scan that writes the checkpoints)
+    g_timing[5] = (double)p->fwd->work[4] + 1;
+    g_timing[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    return rc;
 }
 
 int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, void *stream) {

@@ -637,6 +637,22 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 if (++a_fill == kTile) flush();
             }
             if (!active) continue;
+            if (flags & kFlagCkpt) {  // adjoint checkpoint: the state at the start of the step, lab frame
+                const long long g = L.ckpt_step0 + (long long)k * chunk + q;
+                const long long niso = (long long)L.S * n;
+                float *c = L.ckpt + (g / kAdjWin) * 3 * P * niso;
+#pragma unroll
+                for (int s = 0; s < NS; ++s)
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        float2 m = make_float2(X[s][t], Y[s][t]);
+                        if (has_frame<MODEL>(t)) m = cmul(m, Pc[t]);
+                        const long long i = (long long)(sg * NS + s) * n + v;
+                        c[(3 * t + 0) * niso + i] = m.x;
+                        c[(3 * t + 1) * niso + i] = m.y;
+                        c[(3 * t + 2) * niso + i] = Z[s][t];
+                    }
+            }
             if (L.hist != nullptr) {  // RunMode 1: the state at the start of the step, lab frame
                 float *h = L.hist + ((long long)k * chunk + q) * 3 * L.hist_stride;
 #pragma unroll

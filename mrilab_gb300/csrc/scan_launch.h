@@ -69,7 +69,6 @@ cudaError_t launch_scan_fast_cest(int P, int NS, bool all_free, dim3 grid, size_
                                   const FastGrid &g);
 // ---- adjoint (adjoint.cu) ----------------------------------------------------
 constexpr int kAdjBlock = 128;  // threads (isochromats) per block
-constexpr int kAdjWin = 16;     // steps between checkpoints, recomputed into shared memory
 
 // Step record of the adjoint: {dt, Gz, Gy, Gx}, {Re A, Im A, 2 pi f_rf,
 // flags (kFlagRf, kFlagState, kFlagDt)}, {ADC sample (int bits) or -1, rf
@@ -82,14 +81,12 @@ struct AdjLaunch {
     const float *rho, *t1, *t2;          // [P][n_act]
     const float *kch;                    // [P*P][n_act] exchange channels, or null
     const float *dwrnd;                  // [P][S][n_act]
-    const float *m0;                     // initial Mx | My | Mz, each [P][S][n_act]
-    long long m0_stride;                 // P * S * n_act
     const float2 *rxc;                   // [rx][n_act], null: the default coil
     const float2 *txc;                   // [n_act] TxCoilmg exp(i TxCoilpe)
     float cs2pi[kMaxPool];
     const float4 *rec;                   // [n_steps][3]
     long long n_steps;
-    float *ckpt;                         // [window][3P][n_iso]
+    const float *ckpt;                   // [window][3P][n_iso], written by the forward scan
     const float2 *gsig;                  // [P][rx][A] dL/dSx + i dL/dSy
     float *giso;                         // [fields][n_iso]: T1[P] T2[P] Rho[P] dB0 K[P*P] Mx0[P] My0[P] Mz0[P]
     double *grf;                         // [n_rf][2]

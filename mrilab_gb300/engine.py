@@ -343,6 +343,40 @@ class AdjointArgs(ctypes.Structure):
                 ("n_rf_steps", ctypes.c_int), ("g_rf_amp_line", _d), ("g_rf_phase_line", _d)]
 
 
+def _adjoint_outputs(sc, rf_capacity: Optional[int]):
+    """Host arrays for the gradients of ``sc`` and the AdjointArgs pointing at them."""
+    o = sc.VObj
+    V = o["Rho"].size // int(o["TypeNum"])
+    P, S = int(o["TypeNum"]), int(o["SpinNum"])
+    if rf_capacity is None:
+        rf_capacity = int(np.count_nonzero(np.diff(sc.VSeq["utsLine"]) > 0))
+    n_line = max(int(np.size(sc.VSeq["rfAmpLine"])), 1)
+    out = dict(T1=np.zeros(P * V, np.float32), T2=np.zeros(P * V, np.float32), Rho=np.zeros(P * V, np.float32),
+               dB0=np.zeros(V, np.float32), Mx0=np.zeros(P * S * V, np.float32),
+               My0=np.zeros(P * S * V, np.float32), Mz0=np.zeros(P * S * V, np.float32),
+               rf=np.zeros((max(rf_capacity, 1), 2)), rf_a=np.zeros((max(rf_capacity, 1), 2)),
+               rf_uts=np.zeros(max(rf_capacity, 1), np.int32),
+               rf_amp_line=np.zeros(n_line), rf_phase_line=np.zeros(n_line))
+    if "K" in o:
+        out["K"] = np.zeros(o["K"].size, np.float32)
+    a = AdjointArgs()
+    f = lambda k: out[k].ctypes.data_as(_f) if k in out else ctypes.cast(None, _f)
+    a.g_t1, a.g_t2, a.g_rho, a.g_db0, a.g_k = f("T1"), f("T2"), f("Rho"), f("dB0"), f("K")
+    a.g_mx0, a.g_my0, a.g_mz0 = f("Mx0"), f("My0"), f("Mz0")
+    a.g_rf = out["rf"].ctypes.data_as(_d)
+    a.rf_a = out["rf_a"].ctypes.data_as(_d)
+    a.rf_step_uts = out["rf_uts"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    a.rf_capacity = rf_capacity
+    a.g_rf_amp_line = out["rf_amp_line"].ctypes.data_as(_d)
+    a.g_rf_phase_line = out["rf_phase_line"].ctypes.data_as(_d)
+    return out, a
+
+
+def _trim_rf(out, n):
+    out["rf"], out["rf_a"], out["rf_uts"] = out["rf"][:n], out["rf_a"][:n], out["rf_uts"][:n]
+    return out
+
+
 def adjoint(sc, grad_sx, grad_sy, gpu_index: int = 0, rf_capacity: Optional[int] = None) -> Dict[str, np.ndarray]:
     """``mrl_adjoint``: gradients of a loss L of the signal of ``sc`` given
     dL/dSx, dL/dSy (flat [P][Rx][A]).  Returns T1, T2, Rho ([P*V]), dB0
@@ -354,36 +388,74 @@ def adjoint(sc, grad_sx, grad_sy, gpu_index: int = 0, rf_capacity: Optional[int]
     lib.mrl_adjoint.argtypes = [ctypes.POINTER(ScanArgs), ctypes.POINTER(AdjointArgs)]
     lib.mrl_adjoint.restype = ctypes.c_int
     hs = HostScan(sc, numerics="accurate", gpu_index=gpu_index)
-    o = sc.VObj
-    V = o["Rho"].size // int(o["TypeNum"])
-    P, S = int(o["TypeNum"]), int(o["SpinNum"])
     gsx = np.ascontiguousarray(np.asarray(grad_sx, np.float64).ravel())
     gsy = np.ascontiguousarray(np.asarray(grad_sy, np.float64).ravel())
-    if rf_capacity is None:
-        rf_capacity = int(np.count_nonzero(np.diff(sc.VSeq["utsLine"]) > 0))
-    out = dict(T1=np.zeros(P * V, np.float32), T2=np.zeros(P * V, np.float32), Rho=np.zeros(P * V, np.float32),
-               dB0=np.zeros(V, np.float32), Mx0=np.zeros(P * S * V, np.float32),
-               My0=np.zeros(P * S * V, np.float32), Mz0=np.zeros(P * S * V, np.float32),
-               rf=np.zeros((max(rf_capacity, 1), 2)), rf_a=np.zeros((max(rf_capacity, 1), 2)),
-               rf_uts=np.zeros(max(rf_capacity, 1), np.int32),
-               rf_amp_line=np.zeros(max(int(np.size(sc.VSeq["rfAmpLine"])), 1)),
-               rf_phase_line=np.zeros(max(int(np.size(sc.VSeq["rfAmpLine"])), 1)))
-    if "K" in o:
-        out["K"] = np.zeros(o["K"].size, np.float32)
-    a = AdjointArgs()
+    out, a = _adjoint_outputs(sc, rf_capacity)
     a.grad_sx, a.grad_sy = gsx.ctypes.data_as(_d), gsy.ctypes.data_as(_d)
-    f = lambda k: out[k].ctypes.data_as(_f) if k in out else ctypes.cast(None, _f)
-    a.g_t1, a.g_t2, a.g_rho, a.g_db0, a.g_k = f("T1"), f("T2"), f("Rho"), f("dB0"), f("K")
-    a.g_mx0, a.g_my0, a.g_mz0 = f("Mx0"), f("My0"), f("Mz0")
-    a.g_rf = out["rf"].ctypes.data_as(_d)
-    a.rf_a = out["rf_a"].ctypes.data_as(_d)
-    a.rf_step_uts = out["rf_uts"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
-    a.rf_capacity = rf_capacity
-    a.g_rf_amp_line = out["rf_amp_line"].ctypes.data_as(_d)
-    a.g_rf_phase_line = out["rf_phase_line"].ctypes.data_as(_d)
     rc = lib.mrl_adjoint(ctypes.byref(hs.args), ctypes.byref(a))
     if rc != 0:
         raise ScanError(rc, lib.mrl_last_error().decode())
-    n = a.n_rf_steps
-    out["rf"], out["rf_a"], out["rf_uts"] = out["rf"][:n], out["rf_a"][:n], out["rf_uts"][:n]
-    return out
+    return _trim_rf(out, a.n_rf_steps)
+
+
+class AdjointPlan:
+    """``mrl_adjoint_plan``: the forward scan (writing checkpoints) and the
+    adjoint of one scan, resident on the device for repeated iterations:
+    ``forward(stream)``, ``signal()``, ``backward(gx, gy, stream)``,
+    ``gradients()``."""
+
+    def __init__(self, sc, gpu_index: int = 0):
+        lib = library()
+        lib.mrl_adjoint_plan_create.argtypes = [ctypes.POINTER(ScanArgs), ctypes.POINTER(ctypes.c_void_p)]
+        lib.mrl_adjoint_plan_forward.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        lib.mrl_adjoint_plan_download.argtypes = [ctypes.c_void_p, ctypes.POINTER(ScanArgs)]
+        lib.mrl_adjoint_plan_backward.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_void_p]
+        lib.mrl_adjoint_plan_gradients.argtypes = [ctypes.c_void_p, ctypes.POINTER(AdjointArgs)]
+        lib.mrl_adjoint_plan_work.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
+        lib.mrl_adjoint_plan_destroy.argtypes = [ctypes.c_void_p]
+        self.lib = lib
+        self.sc = sc
+        self.host = HostScan(sc, numerics="accurate", gpu_index=gpu_index)
+        self.ptr = ctypes.c_void_p()
+        rc = lib.mrl_adjoint_plan_create(ctypes.byref(self.host.args), ctypes.byref(self.ptr))
+        if rc != 0:
+            raise ScanError(rc, lib.mrl_last_error().decode())
+        self._out, self._args = _adjoint_outputs(sc, None)
+
+    def _check(self, rc):
+        if rc != 0:
+            raise ScanError(rc, self.lib.mrl_last_error().decode())
+
+    def work(self) -> Dict[str, int]:
+        buf = (ctypes.c_longlong * 6)()
+        self.lib.mrl_adjoint_plan_work(self.ptr, buf)
+        return dict(units=buf[0], steps=buf[1], rf_steps=buf[2], samples=buf[3], launches=buf[4], n_rf=buf[5])
+
+    def forward(self, stream: Optional[int] = None) -> None:
+        self._check(self.lib.mrl_adjoint_plan_forward(self.ptr, ctypes.c_void_p(stream or 0)))
+
+    def signal(self) -> Dict[str, np.ndarray]:
+        """Signal and final magnetisation of the last forward pass."""
+        self._check(self.lib.mrl_adjoint_plan_download(self.ptr, ctypes.byref(self.host.args)))
+        return self.host.outputs()
+
+    def backward(self, grad_sx, grad_sy, stream: Optional[int] = None) -> None:
+        self._gx = np.ascontiguousarray(np.asarray(grad_sx, np.float64).ravel())
+        self._gy = np.ascontiguousarray(np.asarray(grad_sy, np.float64).ravel())
+        self._check(self.lib.mrl_adjoint_plan_backward(self.ptr, self._gx.ctypes.data_as(_d),
+                                                       self._gy.ctypes.data_as(_d), ctypes.c_void_p(stream or 0)))
+
+    def gradients(self) -> Dict[str, np.ndarray]:
+        self._check(self.lib.mrl_adjoint_plan_gradients(self.ptr, ctypes.byref(self._args)))
+        return _trim_rf({k: v.copy() for k, v in self._out.items()}, self._args.n_rf_steps)
+
+    def close(self) -> None:
+        if self.ptr:
+            self.lib.mrl_adjoint_plan_destroy(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -195,3 +195,76 @@ def test_autograd_bridge(built):
     adj = float(np.sum(params["T2"].grad.numpy() * (plus - minus) / (2 * H)))
     print(f"autograd T2 direction: {adj:.6e}, finite difference {fd:.6e}")
     assert abs(adj - fd) <= TOL * abs(fd)
+
+
+def test_adjoint_plan_iterations(built):
+    """An adjoint plan run twice gives the one-shot call's gradients, and its
+    forward pass the signal of mrl_scan."""
+    sc = _phase_modulated(phantoms.small_multipool("me", seed=36, n=6, pools=2, spins=2, coils=2, n_tr=2), 7)
+    tx, ty = _target(sc)
+    ref = engine.scan(sc)
+    gx, gy = 2 * (ref["Sx"] - tx), 2 * (ref["Sy"] - ty)
+    one = engine.adjoint(sc, gx, gy)
+    plan = engine.AdjointPlan(sc)
+    try:
+        for _ in range(2):
+            plan.forward()
+            out = plan.signal()
+            np.testing.assert_array_equal(out["Sx"], ref["Sx"])
+            np.testing.assert_array_equal(out["Sy"], ref["Sy"])
+            plan.backward(gx, gy)
+            g = plan.gradients()
+            for k in ("T1", "T2", "Rho", "dB0", "K", "Mz0", "rf", "rf_amp_line", "rf_phase_line"):
+                np.testing.assert_array_equal(g[k], one[k])
+        w = plan.work()
+        assert w["n_rf"] == len(one["rf"]) and w["steps"] > 0
+    finally:
+        plan.close()
+
+
+def test_adjoint_long_train(built):
+    """200 TRs of balanced SSFP (123,800 steps) on a small phantom: the
+    gradients keep their accuracy over a long train (the checkpoints come
+    from the anchored forward integrator; the backward sweep runs the whole
+    train in single precision)."""
+    sc = _phase_modulated(phantoms.config4_adjoint(seed=3, nx=4, ny=4, nz=2, n_tr=200), 8)
+    target = _target(sc)
+    _, gsx, gsy = _loss(sc, target)
+    g = engine.adjoint(sc, gsx, gsy)
+    o = sc.VObj
+    rng = np.random.default_rng(12)
+    act = ((o["Rho"] != 0) & (o["T1"] != 0) & (o["T2"] != 0)).ravel(order="F")
+    # 8 elements per family: one oracle run of the train takes about a second
+    idx = np.sort(rng.choice(np.flatnonzero(act), 8, replace=False))
+    for key in ("T1", "T2"):
+        p = np.asarray(o[key], np.float64).ravel(order="F")
+        _check(key + " (200 TRs)", g[key][idx], _fd_gradient(sc, target, "VObj", key, idx, H * np.abs(p[idx])))
+    vidx = np.sort(rng.choice(np.flatnonzero(act.reshape(-1, 2, order="F").any(axis=1)), 8, replace=False))
+    _check("dB0 (200 TRs)", g["dB0"][vidx],
+           _fd_gradient(sc, target, "VMag", "dB0", vidx, np.full(vidx.size, DB0_STEP)))
+    a, grf = g["rf_a"], g["rf"]
+    amp = np.asarray(sc.VSeq["rfAmpLine"], np.float64).ravel()
+    lp, _, _ = _loss(_with(sc, "VSeq", "rfAmpLine", amp * (1 + H)), target)
+    lm, _, _ = _loss(_with(sc, "VSeq", "rfAmpLine", amp * (1 - H)), target)
+    fd = (lp - lm) / (2 * H)
+    adj = float(np.sum(grf[:, 0] * a[:, 0] + grf[:, 1] * a[:, 1]))
+    print(f"rf amplitude (200 TRs): adjoint {adj:.6e}, finite difference {fd:.6e}")
+    assert abs(adj - fd) <= TOL * abs(fd)
+
+
+def test_adjoint_receiver_phase(built):
+    """A nonzero receiver reference phase (VVar.rfRef) rotates the signal;
+    the adjoint rotates dL/dS back."""
+    sc = _phase_modulated(phantoms.config1_gre(seed=37, n=6, n_tr=2), 9)
+    sc.VVar["rfRef"] = np.float64(0.7)
+    target = _target(sc)
+    _, gsx, gsy = _loss(sc, target)
+    g = engine.adjoint(sc, gsx, gsy)
+    o = sc.VObj
+    act = ((o["Rho"] != 0) & (o["T1"] != 0) & (o["T2"] != 0)).ravel(order="F")
+    idx = np.flatnonzero(act)
+    p = np.asarray(o["T2"], np.float64).ravel(order="F")
+    _check("T2 (rfRef 0.7)", g["T2"][idx], _fd_gradient(sc, target, "VObj", "T2", idx, H * np.abs(p[idx])))
+    vidx = np.flatnonzero(act)
+    _check("dB0 (rfRef 0.7)", g["dB0"][vidx],
+           _fd_gradient(sc, target, "VMag", "dB0", vidx, np.full(vidx.size, DB0_STEP)))
