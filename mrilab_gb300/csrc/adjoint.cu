@@ -92,11 +92,12 @@ struct KSum {
     }
 };
 
-template <int P>
+template <int P, bool GM>
 __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjLaunch L) {
     extern __shared__ __align__(16) float adj_sm[];
     float *win = adj_sm;                                            // [kAdjWin][3P][kAdjBlock]
     float *rfp = adj_sm + kAdjWin * 3 * P * kAdjBlock;              // [kAdjWin][warp][2]
+    float4 *wrec = reinterpret_cast<float4 *>(rfp + kAdjWin * (kAdjBlock / 32) * 2);  // [kAdjWin][3]
     constexpr int kWarps = kAdjBlock / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long iso = (long long)blockIdx.x * kAdjBlock + tid;
@@ -104,6 +105,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
     const int n = L.n_act;
     const int v = active ? (int)(iso % n) : 0;
     const int s = active ? (int)(iso / n) : 0;
+    // exchange channel of the rate from pool a to pool b (ME: a*P+b, GM: b*P+a)
+    auto ch = [](int a, int b) { return GM ? b * P + a : a * P + b; };
 
     // ---- per-isochromat constants ------------------------------------------
     float om[4] = {0.f, 0.f, 0.f, 0.f}, wres[P], rhoS[P], t1[P], t2[P];
@@ -141,77 +144,81 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
     for (int t = 0; t < P; ++t) on[t] = active && t1[t] != 0.f && t2[t] != 0.f && rhoS[t] != 0.f;
 
     // ---- per-dt coefficients ------------------------------------------------
-    float d1[P], d2[P], cc[P], y1[P], y2[P], yo[P], fin[P][P], fT1[P], fT2[P], fyo[P], ffin[P][P];
+    // map: d2, d1, cc, fin; gradient: hT1 (of l.z mr.z), hR (of l.z), hT2 (of
+    // l.xy mr.xy), e2, e1 (outflow rates, of l.xy mr.xy and l.z mr.z), ffin
+    float d1[P], d2[P], y1[P], fin[P][P], hT1[P], hR[P], hT2[P], e1[P], e2[P];
+    float dtc = 0.f;  // dt of these coefficients
     auto set_dt = [&](float dt) {
 #pragma unroll
         for (int t = 0; t < P; ++t) {
-            y1[t] = on[t] ? -expm1f(-dt / t1[t]) : 0.f;
-            y2[t] = on[t] ? -expm1f(-dt / t2[t]) : 0.f;
+            const float y1t = on[t] ? -expm1f(-dt / t1[t]) : 0.f;
+            const float y2t = on[t] ? -expm1f(-dt / t2[t]) : 0.f;
             float ksum = 0.f;
 #pragma unroll
             for (int p = 0; p < P; ++p) {
                 fin[t][p] = 0.f;
-                if (L.exch_gm && p == t) continue;
-                const float kgo = L.exch_gm ? kc[p * P + t] : kc[t * P + p];
-                const float kin = L.exch_gm ? kc[t * P + p] : kc[p * P + t];
+                if (GM && p == t) continue;
+                const float kgo = kc[ch(t, p)], kin = kc[ch(p, t)];
                 ksum += kgo;
                 if (on[t] && kin != 0.f) fin[t][p] = -expm1f(-dt * kin);
-                ffin[t][p] = on[t] ? (1.f - fin[t][p]) * dt : 0.f;
             }
-            yo[t] = on[t] ? -expm1f(-dt * ksum) : 0.f;
-            d1[t] = (1.f - yo[t]) * (1.f - y1[t]);
-            d2[t] = (1.f - yo[t]) * (1.f - y2[t]);
-            cc[t] = rhoS[t] * y1[t];
-            fT1[t] = on[t] ? -(1.f - y1[t]) * dt / (t1[t] * t1[t]) : 0.f;
-            fT2[t] = on[t] ? -(1.f - y2[t]) * dt / (t2[t] * t2[t]) : 0.f;
-            fyo[t] = (1.f - yo[t]) * dt;
+            const float yot = on[t] ? -expm1f(-dt * ksum) : 0.f;
+            y1[t] = y1t;
+            d1[t] = (1.f - yot) * (1.f - y1t);
+            d2[t] = (1.f - yot) * (1.f - y2t);
+            // dy1/dT1 = -(1 - y1) dt / T1^2, dyo/dk = (1 - yo) dt
+            const float fT1 = on[t] ? -(1.f - y1t) * dt / (t1[t] * t1[t]) : 0.f;
+            const float fT2 = on[t] ? -(1.f - y2t) * dt / (t2[t] * t2[t]) : 0.f;
+            const float fyo = (1.f - yot) * dt;
+            hT1[t] = -(1.f - yot) * fT1;
+            hR[t] = rhoS[t] * fT1;
+            hT2[t] = -(1.f - yot) * fT2;
+            e2[t] = -(1.f - y2t) * fyo;
+            e1[t] = -(1.f - y1t) * fyo;
         }
+        dtc = dt;
     };
     // ---- per-state rotation of free steps -----------------------------------
     float cth[P], sth[P];
+    auto wcom = [&](float4 r0) { return fmaf(om[3], r0.y, fmaf(om[2], r0.z, fmaf(om[1], r0.w, om[0]))); };
     auto set_state = [&](float dt, float4 r0) {
-        const float wc = fmaf(om[3], r0.y, fmaf(om[2], r0.z, fmaf(om[1], r0.w, om[0])));
+        const float wc = wcom(r0);
 #pragma unroll
         for (int t = 0; t < P; ++t) sincos_cw((wc + wres[t]) * dt, sth[t], cth[t]);
     };
-    auto rot_of = [&](int t, float dt, float4 r0, float4 r1, float2 B) -> Rot {
-        const float wc = fmaf(om[3], r0.y, fmaf(om[2], r0.z, fmaf(om[1], r0.w, om[0])));
-        return make_rot(make_float3(-dt * L.gyro * B.x, -dt * L.gyro * B.y, -dt * (wc + wres[t] + r1.z)));
+    // rotation vector of an rf step: -dt (gamma Bx, gamma By, w_t)
+    auto rf_vxy = [&](float dt, float4 r1) {
+        const float sc = -dt * L.gyro;
+        return make_float2(sc * (txc.x * r1.x - txc.y * r1.y), sc * (txc.x * r1.y + txc.y * r1.x));
     };
     // one forward step, m -> F(m)
     auto fwd = [&](float dt, float4 r0, float4 r1, bool rf) {
         float3 mr[P];
-        const float2 B = make_float2(txc.x * r1.x - txc.y * r1.y, txc.x * r1.y + txc.y * r1.x);
+        if (rf) {
+            const float2 vxy = rf_vxy(dt, r1);
+            const float wz = wcom(r0) + r1.z;
 #pragma unroll
-        for (int t = 0; t < P; ++t) {
-            if (rf) {
-                mr[t] = on[t] ? rot_apply(rot_of(t, dt, r0, r1, B), m[t]) : m[t];
-            } else {
-                mr[t] = on[t] ? make_float3(fmaf(m[t].x, cth[t], m[t].y * sth[t]), fmaf(-m[t].x, sth[t], m[t].y * cth[t]),
-                                            m[t].z)
-                              : m[t];
-            }
+            for (int t = 0; t < P; ++t) mr[t] = rot_apply(make_rot(make_float3(vxy.x, vxy.y, -dt * (wz + wres[t]))), m[t]);
+        } else {
+#pragma unroll
+            for (int t = 0; t < P; ++t)
+                mr[t] = make_float3(fmaf(m[t].x, cth[t], m[t].y * sth[t]), fmaf(-m[t].x, sth[t], m[t].y * cth[t]), m[t].z);
         }
         float3 nm[P];
 #pragma unroll
         for (int t = 0; t < P; ++t) {
-            if (!on[t]) {
-                nm[t] = m[t];
-                continue;
-            }
-            float3 a = make_float3(d2[t] * mr[t].x, d2[t] * mr[t].y, fmaf(d1[t], mr[t].z, cc[t]));
+            float3 a = make_float3(d2[t] * mr[t].x, d2[t] * mr[t].y, fmaf(d1[t], mr[t].z, rhoS[t] * y1[t]));
 #pragma unroll
             for (int p = 0; p < P; ++p) {
                 a.x = fmaf(fin[t][p], m[p].x, a.x);
                 a.y = fmaf(fin[t][p], m[p].y, a.y);
                 a.z = fmaf(fin[t][p], m[p].z, a.z);
             }
-            nm[t] = a;
+            nm[t] = on[t] ? a : m[t];
         }
 #pragma unroll
         for (int t = 0; t < P; ++t) m[t] = nm[t];
     };
-    auto rec = [&](long long k, int i) { return __ldg(L.rec + k * 3 + i); };
 
     const long long N = L.n_steps;
     const long long nwin = (N + kAdjWin - 1) / kAdjWin;
@@ -225,7 +232,11 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
     for (int t = 0; t < P; ++t) lam[t] = make_float3(0.f, 0.f, 0.f);
     KSum gT1[P], gT2[P], grho[P], gw[P], gk[P * P];
     for (long long w = nwin - 1; w >= 0; --w) {
-        const long long k0 = w * kAdjWin, k1 = min(N, k0 + kAdjWin);
+        const long long k0 = w * kAdjWin;
+        const int nk = (int)min((long long)kAdjWin, N - k0);
+        // the window's step records, staged in shared memory
+        if (tid < 3 * nk) wrec[tid] = __ldg(L.rec + k0 * 3 + tid);
+        __syncthreads();
         // recompute the window's states (before each step) into shared memory
         if (active) {
             const float *cp = L.ckpt + w * cs * L.n_iso + iso;
@@ -233,18 +244,18 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
             for (int t = 0; t < P; ++t)
                 m[t] = make_float3(cp[(3 * t + 0) * L.n_iso], cp[(3 * t + 1) * L.n_iso], cp[(3 * t + 2) * L.n_iso]);
         }
-        for (long long k = k0; k < k1; ++k) {
-            const float4 r0 = rec(k, 0), r1 = rec(k, 1);
+        for (int j = 0; j < nk; ++j) {
+            const float4 r0 = wrec[3 * j], r1 = wrec[3 * j + 1];
             const int flags = __float_as_int(r1.w);
             const float dt = r0.x;
-            float *ws = win + (k - k0) * 3 * P * kAdjBlock + tid;
+            float *ws = win + j * 3 * P * kAdjBlock + tid;
 #pragma unroll
             for (int t = 0; t < P; ++t) {
                 ws[(3 * t + 0) * kAdjBlock] = m[t].x;
                 ws[(3 * t + 1) * kAdjBlock] = m[t].y;
                 ws[(3 * t + 2) * kAdjBlock] = m[t].z;
             }
-            if (k == k0) {  // the coefficients of the window's first step, if not in registers
+            if (j == 0) {  // the coefficients of the window's first step, if not in registers
                 if (dt != cur.x) set_dt(dt);
                 if (dt != cur.x || r0.y != cur.y || r0.z != cur.z || r0.w != cur.w) set_state(dt, r0);
                 cur = r0;
@@ -253,7 +264,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
                 if (flags & kFlagState) set_state(dt, r0);
                 cur = r0;
             }
-            if (k + 1 < k1) fwd(dt, r0, r1, (flags & kFlagRf) != 0);
+            if (j + 1 < nk) fwd(dt, r0, r1, (flags & kFlagRf) != 0);
         }
         // window partial sums of the parameter gradients
         float wT1[P], wT2[P], wrho[P], ww[P], wk[P * P];
@@ -261,28 +272,33 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
         for (int t = 0; t < P; ++t) wT1[t] = wT2[t] = wrho[t] = ww[t] = 0.f;
 #pragma unroll
         for (int i = 0; i < P * P; ++i) wk[i] = 0.f;
-        // the coefficients in registers are those of step k1 - 1
-        for (long long k = k1 - 1; k >= k0; --k) {
-            const float4 r0 = rec(k, 0), r1 = rec(k, 1), r2 = rec(k, 2);
+        // the coefficients in registers are those of the window's last step
+        for (int j = nk - 1; j >= 0; --j) {
+            const float4 r0 = wrec[3 * j], r1 = wrec[3 * j + 1], r2 = wrec[3 * j + 2];
             const int flags = __float_as_int(r1.w);
             const float dt = r0.x;
-            if (k < k1 - 1) {  // coefficients of step k, if step k + 1 changed them
-                const int fn = __float_as_int(rec(k + 1, 1).w);
+            if (j < nk - 1) {  // coefficients of step j, if step j + 1 changed them
+                const int fn = __float_as_int(wrec[3 * j + 4].w);
                 if (fn & kFlagDt) set_dt(dt);
                 if (fn & kFlagState) set_state(dt, r0);
                 if (fn & (kFlagDt | kFlagState)) cur = r0;
             }
             const bool rf = (flags & kFlagRf) != 0;
-            const float *ws = win + (k - k0) * 3 * P * kAdjBlock + tid;
+            const float *ws = win + j * 3 * P * kAdjBlock + tid;
             float3 mk[P];
 #pragma unroll
             for (int t = 0; t < P; ++t)
                 mk[t] = make_float3(ws[(3 * t + 0) * kAdjBlock], ws[(3 * t + 1) * kAdjBlock], ws[(3 * t + 2) * kAdjBlock]);
-            const float2 B = make_float2(txc.x * r1.x - txc.y * r1.y, txc.x * r1.y + txc.y * r1.x);
+            float2 vxy = make_float2(0.f, 0.f);
+            float wz = 0.f;
+            if (rf) {
+                vxy = rf_vxy(dt, r1);
+                wz = wcom(r0) + r1.z;
+            }
             float3 nl[P];
 #pragma unroll
             for (int t = 0; t < P; ++t) nl[t] = make_float3(0.f, 0.f, 0.f);
-            float2 gB = make_float2(0.f, 0.f);
+            float2 gv = make_float2(0.f, 0.f);  // dL/d(vx, vy) of the step, summed over the pools
 #pragma unroll
             for (int t = 0; t < P; ++t) {
                 if (!on[t]) {
@@ -295,7 +311,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
                 Rot R;
                 float3 mr;
                 if (rf) {
-                    R = rot_of(t, dt, r0, r1, B);
+                    R = make_rot(make_float3(vxy.x, vxy.y, -dt * (wz + wres[t])));
                     mr = rot_apply(R, mk[t]);
                 } else {
                     mr = make_float3(fmaf(mk[t].x, cth[t], mk[t].y * sth[t]), fmaf(-mk[t].x, sth[t], mk[t].y * cth[t]),
@@ -304,18 +320,17 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
                 const float3 l = lam[t];
                 // relaxation / recovery parameters
                 const float gd2 = fmaf(l.x, mr.x, l.y * mr.y), gd1 = l.z * mr.z;
-                const float gyo = -(gd2 * (1.f - y2[t]) + gd1 * (1.f - y1[t]));
-                wT1[t] = fmaf((-(1.f - yo[t]) * gd1 + rhoS[t] * l.z), fT1[t], wT1[t]);
-                wT2[t] = fmaf(-(1.f - yo[t]) * gd2, fT2[t], wT2[t]);
-                wrho[t] = fmaf(l.z, y1[t] / (float)L.S, wrho[t]);
-                // exchange rates: yo_t (outflow) and the inflow f_tp
+                wT1[t] = fmaf(gd1, hT1[t], fmaf(l.z, hR[t], wT1[t]));
+                wT2[t] = fmaf(gd2, hT2[t], wT2[t]);
+                wrho[t] = fmaf(l.z, y1[t], wrho[t]);
+                // exchange rates: the outflow of t (yo_t) and the inflow to t (f_tp)
+                const float go_g = fmaf(gd2, e2[t], gd1 * e1[t]);
 #pragma unroll
                 for (int p = 0; p < P; ++p) {
-                    if (L.exch_gm && p == t) continue;
-                    const int go = L.exch_gm ? p * P + t : t * P + p;  // channel of rate t -> p
-                    const int gi = L.exch_gm ? t * P + p : p * P + t;  // channel of rate p -> t
-                    wk[go] = fmaf(gyo, fyo[t], wk[go]);
-                    wk[gi] = fmaf(dot3(l, mk[p]), ffin[t][p], wk[gi]);
+                    if (GM && p == t) continue;
+                    wk[ch(t, p)] += go_g;
+                    // df_tp/dk_pt = (1 - f_tp) dt
+                    wk[ch(p, t)] = fmaf(dot3(l, mk[p]), (1.f - fin[t][p]) * dtc, wk[ch(p, t)]);
                     // inflow to t from p's magnetisation before the step
                     nl[p].x = fmaf(fin[t][p], l.x, nl[p].x);
                     nl[p].y = fmaf(fin[t][p], l.y, nl[p].y);
@@ -327,8 +342,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
                 if (rf) {
                     const float3 g = jl_t(R, u);
                     ww[t] = fmaf(-dt, g.z, ww[t]);
-                    gB.x = fmaf(-dt * L.gyro, g.x, gB.x);
-                    gB.y = fmaf(-dt * L.gyro, g.y, gB.y);
+                    gv.x += g.x;
+                    gv.y += g.y;
                     const float3 b = rot_apply_t(R, lr);
                     nl[t].x += b.x;
                     nl[t].y += b.y;
@@ -360,17 +375,19 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
             }
 #pragma unroll
             for (int t = 0; t < P; ++t) lam[t] = active ? nl[t] : make_float3(0.f, 0.f, 0.f);
-            // rf gradient of this step: dL/dA = conj(TxCoil) dL/dB, summed over the warp
+            // rf gradient of this step: dB/dA = TxCoil, dv/dB = -dt gamma, so
+            // dL/dA = -dt gamma conj(TxCoil) (gvx + i gvy), summed over the warp
             if (rf) {
-                float2 gA = make_float2(txc.x * gB.x + txc.y * gB.y, txc.x * gB.y - txc.y * gB.x);
+                const float sc = -dt * L.gyro;
+                float2 gA = make_float2(sc * (txc.x * gv.x + txc.y * gv.y), sc * (txc.x * gv.y - txc.y * gv.x));
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     gA.x += __shfl_xor_sync(0xffffffffu, gA.x, o);
                     gA.y += __shfl_xor_sync(0xffffffffu, gA.y, o);
                 }
                 if (lane == 0) {
-                    rfp[((k - k0) * kWarps + warp) * 2 + 0] = gA.x;
-                    rfp[((k - k0) * kWarps + warp) * 2 + 1] = gA.y;
+                    rfp[(j * kWarps + warp) * 2 + 0] = gA.x;
+                    rfp[(j * kWarps + warp) * 2 + 1] = gA.y;
                 }
             }
         }
@@ -385,10 +402,9 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
         for (int i = 0; i < P * P; ++i) gk[i].add(wk[i]);
         // the window's rf gradients, summed over the block, into their FP64 slots
         __syncthreads();
-        if (tid < (int)(k1 - k0)) {
-            const long long k = k0 + tid;
-            const int ri = __float_as_int(rec(k, 2).y);
-            if (ri >= 0 && (__float_as_int(rec(k, 1).w) & kFlagRf)) {
+        if (tid < nk) {
+            const int ri = __float_as_int(wrec[3 * tid + 2].y);
+            if (ri >= 0 && (__float_as_int(wrec[3 * tid + 1].w) & kFlagRf)) {
                 float gx = 0.f, gy = 0.f;
 #pragma unroll
                 for (int q = 0; q < kWarps; ++q) {
@@ -414,7 +430,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
     for (int t = 0; t < P; ++t) g[(f + t) * st] = gT2[t].s;
     f += P;
 #pragma unroll
-    for (int t = 0; t < P; ++t) g[(f + t) * st] = grho[t].s;
+    for (int t = 0; t < P; ++t) g[(f + t) * st] = grho[t].s / (float)L.S;  // dc/dRho = y1 / S
     f += P;
     float gdb0 = 0.f;
 #pragma unroll
@@ -432,10 +448,10 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
     }
 }
 
-template <int P>
+template <int P, bool GM>
 cudaError_t go(const AdjLaunch &L, cudaStream_t st) {
     const size_t smem = adjoint_smem_bytes(P);
-    auto k = adjoint_kernel<P>;
+    auto k = adjoint_kernel<P, GM>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const long long blocks = (L.n_iso + kAdjBlock - 1) / kAdjBlock;
@@ -446,10 +462,11 @@ cudaError_t go(const AdjLaunch &L, cudaStream_t st) {
 }  // namespace
 
 cudaError_t launch_adjoint(int P, const AdjLaunch &L, cudaStream_t st) {
+    const bool gm = L.exch_gm != 0;
     switch (P) {
-    case 1: return go<1>(L, st);
-    case 2: return go<2>(L, st);
-    case 3: return go<3>(L, st);
+    case 1: return go<1, false>(L, st);
+    case 2: return gm ? go<2, true>(L, st) : go<2, false>(L, st);
+    case 3: return gm ? go<3, true>(L, st) : go<3, false>(L, st);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -91,8 +91,9 @@ struct AdjLaunch {
     float *giso;                         // [fields][n_iso]: T1[P] T2[P] Rho[P] dB0 K[P*P] Mx0[P] My0[P] Mz0[P]
     double *grf;                         // [n_rf][2]
 };
-inline size_t adjoint_smem_bytes(int P) {
-    return (size_t)kAdjWin * 3 * P * kAdjBlock * 4 + (size_t)kAdjWin * (kAdjBlock / 32) * 2 * 4;
+inline size_t adjoint_smem_bytes(int P) {  // window states, rf partials, window records
+    return (size_t)kAdjWin * 3 * P * kAdjBlock * 4 + (size_t)kAdjWin * (kAdjBlock / 32) * 2 * 4 +
+           (size_t)kAdjWin * 3 * 16;
 }
 inline int adjoint_fields(int P) { return 3 * P + 1 + P * P + 3 * P; }
 cudaError_t launch_adjoint(int P, const AdjLaunch &L, cudaStream_t st);
