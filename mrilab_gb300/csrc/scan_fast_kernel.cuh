@@ -400,6 +400,8 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     }
     float mt_y1k = 0.f, mt_y21 = 0.f, mt_y1bk = 0.f, mt_y1b = 0.f, mt_y12 = 0.f;
     LineshapeCache lc;
+    float4 satk = make_float4(0.f, 0.f, 0.f, -1.f);  // (Re A, Im A, 2 pi f, dt) of satv
+    float satv = 0.f;
     const float gyro = L.gyro;
 
     __syncthreads();  // the staged coil maps
@@ -722,14 +724,32 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     const float wx = fmaf(B.x, Pc[t].x, B.y * Pc[t].y), wy = fmaf(B.x, Pc[t].y, -B.y * Pc[t].x);
                     vt[t] = make_float2(sc * wx, -sc * wy);
                 }
-                if (MODEL != KM_NORMAL && !(MODEL == KM_EXCH && FREE)) {
+                if (MODEL == KM_MT || MODEL == KM_CEST) {
+                    // the bound pool (pool 1): saturation 1 - exp(-W dt), W = pi (gamma
+                    // TxCoilmg |amp|)^2 G(rf offset, T2b) with the reference's lineshape rule
+                    // (single transmit coil); kept while the step's (A, f, dt) repeat, as
+                    // they do through a continuous-wave saturation
+                    if (r1.x != satk.x || r1.y != satk.y || r1.z != satk.z || dt != satk.w) {
+                        const float b1 = sqrtf(fmaf(r1.x, r1.x, r1.y * r1.y)) * sqrtf(fmaf(tx0.x, tx0.x, tx0.y * tx0.y));
+                        const float freq = r1.z * 0.15915494309189535f;
+                        if (lc.t2b != t2v[1] || lc.freq != freq) {
+                            lc.freq = freq;
+                            lc.t2b = t2v[1];
+                            lc.g = lineshape_f32(freq, db0, gyro, t2v[1]);
+                        }
+                        const float bg = b1 * gyro;
+                        satv = one_minus_exp((float)kPiRef * bg * bg * lc.g * dt);
+                        satk = make_float4(r1.x, r1.y, r1.z, dt);
+                    }
+                    sat[1] = satv;
+                } else if (MODEL == KM_EXCH && !FREE) {
                     // bound pools: W = pi (gamma TxCoilmg |amp|)^2 G(rf offset, T2b) with the
                     // reference's lineshape rule (single transmit coil)
                     const float b1 = sqrtf(fmaf(r1.x, r1.x, r1.y * r1.y)) * sqrtf(fmaf(tx0.x, tx0.x, tx0.y * tx0.y));
                     const float freq = r1.z * 0.15915494309189535f;
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
-                        const bool bound = (MODEL == KM_EXCH) ? ((evo >> t & 1u) && L.kind[t] == 1) : (t == 1);
+                        const bool bound = (evo >> t & 1u) && L.kind[t] == 1;
                         if (!bound) continue;
                         if (lc.t2b != t2v[t] || lc.freq != freq) {
                             lc.freq = freq;
