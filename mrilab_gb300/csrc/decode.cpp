@@ -246,8 +246,9 @@ void pack_fast_records(const DecodeChunk &ch, int tx, FrameMoments &fm, std::vec
         int flags = 0;
         if (si.adc >= 0) flags |= kFlagAdc;
         if (rf) flags |= kFlagRf;
-        const bool new_dt = si.dt != fm.last_dt;
-        const bool new_state = new_dt || si.gx != fm.last_gx || si.gy != fm.last_gy || si.gz != fm.last_gz;
+        const float fdt = (float)si.dt, fgx = (float)si.gx, fgy = (float)si.gy, fgz = (float)si.gz;
+        const bool new_dt = fdt != fm.last_dt;
+        const bool new_state = new_dt || fgx != fm.last_gx || fgy != fm.last_gy || fgz != fm.last_gz;
         if (new_dt) flags |= kFlagDt;
         if (new_state) flags |= kFlagState;
         if (ckpt_every > 0 && q % ckpt_every == 0) flags |= kFlagCkpt;
@@ -260,10 +261,10 @@ void pack_fast_records(const DecodeChunk &ch, int tx, FrameMoments &fm, std::vec
         }
         if (!rf) fm.since_anchor++;
         fm.last_rf = rf;
-        fm.last_dt = si.dt;
-        fm.last_gx = si.gx;
-        fm.last_gy = si.gy;
-        fm.last_gz = si.gz;
+        fm.last_dt = fdt;
+        fm.last_gx = fgx;
+        fm.last_gy = fgy;
+        fm.last_gz = fgz;
         r[0] = (float)si.dt;
         r[1] = (float)si.gz;
         r[2] = (float)si.gy;

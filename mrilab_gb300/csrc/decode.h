@@ -74,7 +74,10 @@ void store_state(const DecodeState &s, mrl_state &v, int tx_num);
 // areas, in double precision, carried across chunks.
 struct FrameMoments {
     double t = 0, kx = 0, ky = 0, kz = 0;
-    double last_dt = -1, last_gx = 0, last_gy = 0, last_gz = 0;
+    // the previous step's dt and gradients as the kernels see them (float):
+    // consecutive dt of a uniform raster differ in the last bits of their
+    // double differences, so the change flags compare the float values
+    float last_dt = -1.f, last_gx = 0.f, last_gy = 0.f, last_gz = 0.f;
     int since_anchor = 1 << 30;  // free steps since the last anchor
     bool last_rf = false;
 };

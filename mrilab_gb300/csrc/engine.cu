@@ -1792,14 +1792,16 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     std::vector<int> step_uts((size_t)std::max<long long>(1, N), -1);
     for (size_t j = 0; j < ch.point_uts.size(); ++j)
         if (ch.point_dt[j] > 0) step_uts[ch.point_step[j]] = ch.point_uts[j];
-    double last_dt = -1, lgx = 0, lgy = 0, lgz = 0;
+    // change flags on the float values the kernel uses (see FrameMoments)
+    float last_dt = -1.f, lgx = 0.f, lgy = 0.f, lgz = 0.f;
     for (long long q = 0; q < N; ++q) {
         const StepInfo &si = ch.steps[q];
         const bool rf = (float)si.amp[0] != 0.f;
         int flags = rf ? kFlagRf : 0;
-        if (si.dt != last_dt) flags |= kFlagDt;
-        if (si.dt != last_dt || si.gx != lgx || si.gy != lgy || si.gz != lgz) flags |= kFlagState;
-        last_dt = si.dt, lgx = si.gx, lgy = si.gy, lgz = si.gz;
+        const float fdt = (float)si.dt, fgx = (float)si.gx, fgy = (float)si.gy, fgz = (float)si.gz;
+        if (fdt != last_dt) flags |= kFlagDt;
+        if (fdt != last_dt || fgx != lgx || fgy != lgy || fgz != lgz) flags |= kFlagState;
+        last_dt = fdt, lgx = fgx, lgy = fgy, lgz = fgz;
         float4 r1;
         r1.x = (float)(si.amp[0] * std::cos(si.phase[0]));
         r1.y = (float)(si.amp[0] * std::sin(si.phase[0]));
