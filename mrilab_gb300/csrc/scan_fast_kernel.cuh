@@ -263,8 +263,9 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     constexpr int kWarps = kBlock / 32;
     const int C4 = (L.rx + 3) & ~3;
     float2 *mtile = reinterpret_cast<float2 *>(rbuf + 2 * chunk * rstride);  // [16][kTRow]
-    float2 *rsm = mtile + 16 * kTRow;                                              // [C4][kTRow]
-    float *wstage = reinterpret_cast<float *>(rsm + C4 * kTRow);                   // [warp][16][2*C4]
+    // coil sensitivities as TF32 (big, small) pairs: [C4][kTRow][rx, ry]
+    uint2 *rsq = reinterpret_cast<uint2 *>(mtile + 16 * kTRow);
+    float *wstage = reinterpret_cast<float *>(rsq + 2 * C4 * kTRow);               // [warp][16][2*C4]
     float *dwsm = wstage + kWarps * 16 * 2 * C4;                                   // [NS * P][kBlock]
     float *omlo = dwsm + NS * P * kBlock;                                        // [4][kBlock]
 
@@ -386,7 +387,9 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
             else
                 r = L.rxc[(long long)c * n + v];
         }
-        rsm[c * kTRow + tid] = r;
+        const uint32_t bx = tf32_rn(r.x), by = tf32_rn(r.y);
+        rsq[2 * (c * kTRow + tid) + 0] = make_uint2(bx, tf32_rn(r.x - __uint_as_float(bx)));
+        rsq[2 * (c * kTRow + tid) + 1] = make_uint2(by, tf32_rn(r.y - __uint_as_float(by)));
     }
     // the isochromats enter their frames at the first step: m_frame = m_lab / P_t
     bool entered = false;
@@ -434,7 +437,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         const int bcomp = (ri == cmp) ? 0 : 1;                 // rx, else ry
         const uint32_t sgn = (cmp && !ri) ? 0x80000000u : 0u;  // -ry
         const float *mt1 = reinterpret_cast<const float *>(mtile) + ri;
-        const float *rs1 = reinterpret_cast<const float *>(rsm) + bcomp;
+        const uint2 *rs1 = rsq + bcomp;
         const int nt_all = C4 / 4;
         float *rw = wstage + warp * 16 * (2 * C4);
         for (int nt = 0; nt < nt_all; ++nt) {
@@ -449,18 +452,14 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 const int j0 = warp * 32 + ks * 4 + (tig >> 1), j1 = j0 + 2;
                 const float a[4] = {mt1[2 * (g * kTRow + j0)], mt1[2 * ((g + 8) * kTRow + j0)],
                                     mt1[2 * (g * kTRow + j1)], mt1[2 * ((g + 8) * kTRow + j1)]};
-                const float b[2] = {__uint_as_float(__float_as_uint(rs1[2 * (c * kTRow + j0)]) ^ sgn),
-                                    __uint_as_float(__float_as_uint(rs1[2 * (c * kTRow + j1)]) ^ sgn)};
-                uint32_t ab[4], as[4], bb[2], bs[2];
+                // the coil operand was split once per launch; -ry flips the signs
+                const uint2 q0 = rs1[2 * (c * kTRow + j0)], q1 = rs1[2 * (c * kTRow + j1)];
+                const uint32_t bb[2] = {q0.x ^ sgn, q1.x ^ sgn}, bs[2] = {q0.y ^ sgn, q1.y ^ sgn};
+                uint32_t ab[4], as[4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
                     ab[i] = tf32_rn(a[i]);
                     as[i] = tf32_rn(a[i] - __uint_as_float(ab[i]));
-                }
-#pragma unroll
-                for (int i = 0; i < 2; ++i) {
-                    bb[i] = tf32_rn(b[i]);
-                    bs[i] = tf32_rn(b[i] - __uint_as_float(bb[i]));
                 }
                 mma_tf32(acc[0], as, bb);
                 mma_tf32(acc[1], ab, bs);
@@ -599,6 +598,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 }
             }
             if (active && (flags & kFlagState)) {
+                const bool new_dt = (flags & kFlagDt) != 0;  // kFlagDt implies kFlagState
 #pragma unroll
                 for (int t = 0; t < P; ++t)
                     if (has_frame<MODEL>(t)) Dc[t] = phase_step((wc + F.cs_hi[t]) * dt);
@@ -611,8 +611,11 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 #pragma unroll
                     for (int s = 0; s < NS; ++s) {
                         if (tvo >> t & 1u) {
-                            const float2 p = phase_step(dwsm[(s * P + t) * kBlock + tid] * dt);
-                            dm[s][t] = make_float2(fmaf(p.x, 1.f - a, -a), p.y * (1.f - a));
+                            // the isochromat's own step in its pool's frame: a function of dt alone
+                            if (new_dt) {
+                                const float2 p = phase_step(dwsm[(s * P + t) * kBlock + tid] * dt);
+                                dm[s][t] = make_float2(fmaf(p.x, 1.f - a, -a), p.y * (1.f - a));
+                            }
                         } else {
                             // constant in the lab: m_frame turns back by the frame's step
                             dm[s][t] = make_float2(Dc[t].x, -Dc[t].y);
