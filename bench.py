@@ -308,6 +308,75 @@ def run_config4(args):
     print(json.dumps(line))
 
 
+def run_config5(args):
+    """The MT + exchange 3D EPI stress case (default 256 x 256 x 128 voxels,
+    4 spins, 3 pools in the general model with a bound MT pool, 32 Rx, a
+    128 x 128 single-shot EPI at 250 kHz after an 8 ms MT pulse): device
+    time of a prepared scan, e2e through mrl_scan, roofline of the Bloch
+    work plus the receive contraction."""
+    import torch
+    from mrilab_gb300 import engine, phantoms
+
+    torch.cuda.set_device(0)
+    nx, ny, nz = (int(v) for v in args.c5_size.split("x"))
+    t0 = time.perf_counter()
+    sc = phantoms.config5_mt_epi(seed=0, nx=nx, ny=ny, nz=nz)
+    build_s = time.perf_counter() - t0
+    plan = engine.Plan(sc)
+    work = plan.work()
+    stream = torch.cuda.Stream()
+    flush = torch.empty(int(256 * 2**20), dtype=torch.uint8, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        plan.execute(stream.cuda_stream)
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.execute(stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    plan.close()
+    ms = float(np.mean(times))
+    t0 = time.perf_counter()
+    engine.scan(sc)
+    e2e_s = time.perf_counter() - t0
+    tm = engine.last_timing()
+    o = sc.VObj
+    vox = int(((o["Rho"][..., 0] != 0) & (o["T1"][..., 0] != 0) & (o["T2"][..., 0] != 0)).sum())
+    n_free = 2
+    rx = int(sc.VCoi["RxCoilNum"])
+    desc = dict(model="gm", pools=3, rx=0)
+    flops_bloch, mufu = op_counts(work, desc)
+    flops_recv = work["samples"] * vox * n_free * rx * OPS["recv_flops"]
+    fp32_tf, mufu_g = peaks()
+    ach = (flops_bloch + flops_recv) / (ms * 1e-3) / 1e12
+    line = {
+        "metric": METRIC, "value": work["units"] / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "MT + exchange 3D EPI: %dx%dx%d voxels, 4 spins, 3 pools (free, myelin, bound "
+                               "MT), 32 Rx, 128x128 single-shot EPI at 250 kHz after an 8 ms MT pulse" % (ny, nx, nz),
+                   "units_per_step": work["units"], "steps_per_scan": work["steps"], "samples": work["samples"],
+                   "active_voxels": vox, "phantom_build_s": build_s,
+                   "l2": "flushed between timed scans (256 MiB write); the working set (state, coil maps) "
+                         "exceeds L2"},
+        "e2e": {"value": work["units"] / e2e_s, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
+                "h2d_bytes_per_step": tm["h2d_bytes"], "d2h_bytes_per_step": tm["d2h_bytes"]},
+        "gpu_launches": work["launches"] * args.steps,
+        "roofline": {"bound": "fp32", "kernel": "scan kernel (op table: Bloch + receive contraction)",
+                     "achieved": ach, "peak": fp32_tf, "unit": "TFLOP/s", "frac": ach / fp32_tf, "traffic": None,
+                     "flops_bloch": flops_bloch, "flops_receive": flops_recv,
+                     "mufu": {"achieved": mufu / (ms * 1e-3) / 1e9, "peak": mufu_g, "unit": "Gop/s",
+                              "frac": mufu / (ms * 1e-3) / 1e9 / mufu_g}},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def cpu_baseline(sc, target_s=12.0):
     """The reference scan algorithm on the host cores (single-precision
     oracle port, all threads) on the first steps of the same workload."""
@@ -336,8 +405,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=["config2", "config1", "config3", "config4"])
+    ap.add_argument("--workload", default="config2", choices=["config2", "config1", "config3", "config4", "config5"])
     ap.add_argument("--vox-scale", type=float, default=1.0, help="config3: scale of the instance voxel counts")
+    ap.add_argument("--c5-size", default="256x256x128", help="config5: voxels NXxNYxNZ")
     ap.add_argument("--n-tr", type=int, default=None, help="TRs of the workload (default: all)")
     ap.add_argument("--numerics", default="accurate", choices=["accurate", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
@@ -348,6 +418,9 @@ def main():
         return
     if args.workload == "config4" and args.impl == "ours":
         run_config4(args)
+        return
+    if args.workload == "config5" and args.impl == "ours":
+        run_config5(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

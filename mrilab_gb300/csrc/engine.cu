@@ -369,6 +369,11 @@ struct Scanner {
     double h2d_ms = 0, d2h_ms = 0, h2d_bytes = 0, d2h_bytes = 0;
     bool own_st = true;          // false: st belongs to the caller (batched scans)
     double partial_budget = 0;   // bytes of receive partials per launch; 0: MRL_PARTIAL_MB or 4 GiB
+    // direct receive: blocks add into the FP64 signal with atomics, no
+    // partials, one launch per chunk.  Chosen (accurate numerics) when the
+    // partials of a chunk exceed the per-launch budget, or by
+    // MRL_RECEIVE=direct|partials; batches keep partials
+    bool direct_rx = false, no_direct = false;
 
     ~Scanner() {
         for (auto &e : ev_scan) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
@@ -699,8 +704,14 @@ struct Scanner {
         const int npairs = mi.nsamp * RX;
         const char *env = getenv("MRL_PARTIAL_MB");
         const double budget = partial_budget > 0 ? partial_budget : (env ? atof(env) : 4096.0) * 1048576.0;
-        const long long a_max =
-            std::max(1LL, (long long)(budget / ((double)n_slices() * npairs * sizeof(float2))));
+        long long a_max = std::max(1LL, (long long)(budget / ((double)n_slices() * npairs * sizeof(float2))));
+        {
+            long long n_adc = 0;
+            for (long long q = 0; q < ch.n_steps; ++q) n_adc += ch.step_adc[q] >= 0;
+            const char *mode = getenv("MRL_RECEIVE");
+            direct_rx = fast && !no_direct && (mode ? strcmp(mode, "direct") == 0 : n_adc > a_max);
+            if (direct_rx) a_max = std::max(1LL, n_adc);
+        }
         long long s0 = 0;
         int a_off = 0, a_cnt = 0, a_peak = 0;
         for (long long q = 0; q < ch.n_steps; ++q) {
@@ -727,7 +738,7 @@ struct Scanner {
         if ((e = d_rec.ensure(recs->size() / 4)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(steps)");
         if ((e = d_amap.ensure(std::max<size_t>(1, amap_host.size()))) != cudaSuccess)
             return fail_cuda(e, "cudaMalloc(amap)");
-        if ((e = d_part.ensure((size_t)n_slices() * std::max(1, a_peak) * npairs)) != cudaSuccess)
+        if ((e = d_part.ensure(direct_rx ? 1 : (size_t)n_slices() * std::max(1, a_peak) * npairs)) != cudaSuccess)
             return fail_cuda(e, "cudaMalloc(partials)");
         auto t0 = std::chrono::steady_clock::now();
         if ((e = cudaMemcpyAsync(d_rec.p, recs->data(), recs->size() * sizeof(float), cudaMemcpyHostToDevice, st)) !=
@@ -772,6 +783,14 @@ struct Scanner {
         L.hist = hist_on ? d_hist.p + (hist_steps + d.s0) * 3 * L.hist_stride : nullptr;
         L.ckpt = ckpt;
         L.ckpt_step0 = d.s0;
+        if (direct_rx) {
+            L.dsx = d_sx.p;
+            L.dsy = d_sy.p;
+            L.amap = d_amap.p + d.a_off;
+            L.A = A;
+            L.cr = std::cos(-rf_ref);
+            L.sr = std::sin(-rf_ref);
+        }
         return L;
     }
 
@@ -827,7 +846,7 @@ struct Scanner {
                 launches++;
             }
             if (timed) cudaEventRecord(e1, stream);
-            if (d.a_count > 0 && n_act > 0) {
+            if (d.a_count > 0 && n_act > 0 && !direct_rx) {
                 cudaEvent_t r0 = nullptr, r1 = nullptr;
                 if (timed) {
                     cudaEventCreate(&r0);
@@ -1433,6 +1452,10 @@ int mrl_plan_execute(mrl_plan *p, void *stream) {
     if (!p) return MRL_ERR_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e = cudaMemcpyAsync(p->sc.d_m.p, p->d_m0.p, p->sc.d_m.n * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && p->sc.direct_rx) {  // the direct receive accumulates into the signal
+        e = cudaMemsetAsync(p->sc.d_sx.p, 0, p->sc.d_sx.n * sizeof(double), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(p->sc.d_sy.p, 0, p->sc.d_sy.n * sizeof(double), s);
+    }
     if (e != cudaSuccess) return p->sc.fail_cuda(e, "plan reset");
     return p->sc.enqueue(p->ls, p->rf_ref, s, false);
 }
@@ -1503,6 +1526,7 @@ int mrl_batch_create(mrl_scan_args *const *args, int n, mrl_batch **out) {
         sc.st = b->st;
         sc.own_st = false;
         sc.partial_budget = 1e18;  // one launch per instance
+        sc.no_direct = true;       // the batch reduces every instance's partials in one kernel
         int rc = sc.setup();
         if (rc) {
             const std::string why = g_err;

@@ -487,7 +487,16 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 sx += red[(w * 16 + row) * (2 * C4) + 2 * c];
                 sy += red[(w * 16 + row) * (2 * C4) + 2 * c + 1];
             }
-            L.partial[((long long)tile * L.a_launch + a_base + a) * L.npairs + t * L.rx + c] = make_float2(sx, sy);
+            if (L.dsx) {
+                const int sig = L.amap[a_base + a];
+                if (sig >= 0 && sig < L.A) {
+                    const long long idx = ((long long)t * L.rx + c) * L.A + sig;
+                    atomicAdd(L.dsx + idx, L.cr * sx - L.sr * sy);
+                    atomicAdd(L.dsy + idx, L.sr * sx + L.cr * sy);
+                }
+            } else {
+                L.partial[((long long)tile * L.a_launch + a_base + a) * L.npairs + t * L.rx + c] = make_float2(sx, sy);
+            }
         }
         a_base += a_fill;
         a_fill = 0;

@@ -56,6 +56,13 @@ struct ScanLaunch {
     long long s0, s1;
     float2 *partial;  // [(block * a_launch + a) * npairs + pair]
     int a_launch;
+    // direct receive (accurate kernel): instead of partials, each block adds
+    // its sums, rotated by (cr, sr) = exp(-i rfRef), into the FP64 signal
+    // [P][rx][A] at the sample amap[launch-local sample] with atomics
+    double *dsx, *dsy;
+    const int *amap;
+    int A;
+    double cr, sr;
     int *err;
     float *hist;            // RunMode 1: [step][Mx|My|Mz][P][S][n_act] from the launch's first step, or null
     long long hist_stride;  // P * S * n_act

@@ -433,6 +433,64 @@ def bssfp_lines(*, n_read=96, n_pe=96, n_par=16, fov=(0.24, 0.24, 0.04), tr_ms=5
     return S.concat(trs), n_tr
 
 
+def epi_lines(*, n_read=128, n_pe=128, fov=(0.24, 0.24, 0.12), bw_hz=250000.0, ramp_us=40.0,
+              mt_ms=8.0, mt_offset_hz=1500.0, mt_b1_ut=6.0, mt_raster_us=10.0, ex_ms=2.0, ex_raster_us=10.0,
+              flip=90.0, tbw=4.0, gamma=GAMMA):
+    """Single-shot EPI with magnetisation-transfer preparation: a Gaussian
+    off-resonance MT pulse (``mt_ms`` long, ``mt_offset_hz`` off, peak
+    ``mt_b1_ut``), a spoiler, a slab-selective sinc excitation, prephasers
+    and ``n_pe`` readout lines of ``n_read`` samples at ``bw_hz`` with
+    alternating readout polarity and phase-encode blips between lines."""
+    dwell = int(round(1e9 / bw_hz))
+    ramp = int(round(ramp_us * 1e3))
+    ro_ns = n_read * dwell
+    mt_raster = int(round(mt_raster_us * 1e3))
+    mt_ns = int(round(mt_ms * 1e6)) // mt_raster * mt_raster
+    ex_raster = int(round(ex_raster_us * 1e3))
+    ex_ns = int(round(ex_ms * 1e6)) // ex_raster * ex_raster
+    flat = lambda t0, t1: (t1 - t0 - 2 * ramp) * S.NS
+    gread = 2 * np.pi / (gamma * fov[0] * dwell * S.NS)
+    gblip_area = 2 * np.pi / (gamma * fov[1])
+    t = 0
+    tr = None
+    # MT preparation: Gaussian envelope, sigma = duration / 6
+    t_mt = np.arange(mt_ns // mt_raster + 1, dtype=np.int64) * mt_raster
+    env = np.exp(-0.5 * ((t_mt - mt_ns / 2) / (mt_ns / 6)) ** 2)
+    env[0] = env[-1] = 0.0
+    t = mt_ns
+    spoil0, spoil1 = t + 20_000, t + 1_020_000
+    ex0 = spoil1 + 20_000
+    t_ex, a_ex = S.sinc_rf(ex0, ex_ns, ex_raster, flip, tbw)
+    gslab = 2 * np.pi / (gamma * fov[2] * 4 * ex_raster * S.NS) * 0.05
+    slab_area = gslab * (ex_ns - 2 * ex_raster) * S.NS
+    pre0 = ex0 + ex_ns + 20_000
+    pre1 = pre0 + 400_000
+    lines0 = pre1 + 20_000
+    line_ns = ro_ns + 2 * ramp
+    tr_ns = lines0 + n_pe * line_ns + 200_000
+    tr = S.TR(tr_ns)
+    tr.rf(t_mt, mt_b1_ut * 1e-6 * env, 0.0, mt_offset_hz)
+    tr.trap("z", spoil0, spoil1, 4 * gread, ramp_ns=100_000)
+    tr.rf(t_ex, a_ex)
+    tr.trap("z", ex0, ex0 + ex_ns, gslab, ramp_ns=ex_raster)
+    tr.trap("z", pre0, pre1, -slab_area / 2 / flat(pre0, pre1), ramp_ns=ramp)
+    tr.trap("x", pre0, pre1, -gread * (ro_ns / 2 + ramp) * S.NS / flat(pre0, pre1), ramp_ns=ramp)
+    tr.trap("y", pre0, pre1, -gblip_area * (n_pe // 2) / flat(pre0, pre1), ramp_ns=ramp)
+    tr.adc_t += [0]
+    tr.adc_v += [0.0]
+    for i in range(n_pe):
+        l0 = lines0 + i * line_ns
+        sgn = 1.0 if i % 2 == 0 else -1.0
+        tr.trap("x", l0, l0 + line_ns, sgn * gread, ramp_ns=ramp)
+        tr.adc(l0 + ramp + dwell * np.arange(n_read))
+        if i + 1 < n_pe:  # blip across the ramps between lines
+            b0 = l0 + line_ns - ramp
+            tr.trap("y", b0, b0 + 2 * ramp, gblip_area / ((2 * ramp - ramp) * S.NS), ramp_ns=ramp // 2)
+    tr.adc_t += [tr_ns]
+    tr.adc_v += [0.0]
+    return S.concat([tr]), 1
+
+
 def sat_gre_lines(*, n_read=16, n_pe=4, fov=0.2, tr_ms=30.0, sat_offsets_hz=(1500.0,), sat_ms=4.0,
                   sat_b1_ut=2.0, sat_raster_us=20.0, flip=15.0, bw_hz=32000.0, gamma=GAMMA):
     """Saturation-prepared GRE: per TR a block of Gaussian saturation pulses
@@ -650,3 +708,39 @@ def config4_adjoint(seed=0, nx=96, ny=96, nz=16, spins=2, n_tr=200, n_coils=4, r
     lines, ntr = bssfp_lines(n_read=X, n_pe=Y, n_par=Z, fov=fov, n_tr=n_tr, rf_samples=rf_samples)
     return assemble(rho, t1, t2, spin_num=spins, t2star=0.7 * t2, db0_hz=db0, res=res, model="me",
                     rates=rates, rx=(rxx, rxy), seqlines=lines, tr_num=ntr, seed=seed)
+
+
+def config5_mt_epi(seed=0, nx=256, ny=256, nz=128, spins=4, n_coils=32, n_read=128, n_pe=128) -> Scan:
+    """The roofline stress case: ``ny x nx x nz`` voxels, ``spins`` spins,
+    three pools in the general model -- free water (T1 1.0 s, T2 80 ms),
+    myelin water (T1 0.4 s, T2 12 ms, fraction U(0, 0.2)) and a bound
+    macromolecular pool (T1 1 s, T2 12 us, super-Lorentzian, fraction
+    U(0.05, 0.15)) -- exchanging at U(1, 50) /s (pools -> free water;
+    the reverse rates by detailed balance), dB0 ~ N(0, 20 Hz), T2* = 0.7 T2
+    for the intravoxel dephasing, ``n_coils`` Rx coils on a cylinder;
+    single-shot EPI (``n_pe`` x ``n_read`` at 250 kHz) after an 8 ms
+    off-resonance MT pulse."""
+    rng = np.random.default_rng(seed)
+    Y, X, Z = ny, nx, nz
+    yy, xx = np.mgrid[0:Y, 0:X]
+    r = np.hypot((xx - (X - 1) / 2) / (X / 2), (yy - (Y - 1) / 2) / (Y / 2))
+    inside = np.repeat((r <= 0.9)[..., None], Z, axis=2)
+    fm = rng.uniform(0.0, 0.2, (Y, X, Z)).astype(np.float32)
+    fb = rng.uniform(0.05, 0.15, (Y, X, Z)).astype(np.float32)
+    rho = np.stack([1 - fm - fb, fm, fb], -1) * inside[..., None]
+    t1 = np.stack([np.full((Y, X, Z), 1.0), np.full((Y, X, Z), 0.4), np.full((Y, X, Z), 1.0)], -1) * inside[..., None]
+    t2 = np.stack([np.full((Y, X, Z), 0.08), np.full((Y, X, Z), 0.012), np.full((Y, X, Z), 12e-6)], -1) * inside[..., None]
+    rates = np.zeros((Y, X, Z, 3, 3), np.float32)
+    for p in (1, 2):
+        k = rng.uniform(1.0, 50.0, (Y, X, Z)).astype(np.float32)
+        rates[..., p, 0] = np.where(inside, k, 0.0)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            rates[..., 0, p] = np.where(inside, k * rho[..., p] / np.maximum(rho[..., 0], 1e-6), 0.0)
+    db0 = rng.normal(0.0, 20.0, (Y, X, Z)).astype(np.float32)
+    fov = (0.24, 0.24 * Y / X, 0.24 * Z / X)
+    res = (fov[0] / X, fov[1] / Y, fov[2] / Z)
+    rxx, rxy = _cylinder_coils((Y, X, Z), res, n_coils, rng)
+    lines, ntr = epi_lines(n_read=n_read, n_pe=n_pe, fov=fov)
+    return assemble(rho.astype(np.float32), t1.astype(np.float32), t2.astype(np.float32), spin_num=spins,
+                    t2star=0.7 * t2, db0_hz=db0, res=res, model="gm", rates=rates,
+                    type_flag=np.array([0.0, 0.0, 1.0]), rx=(rxx, rxy), seqlines=lines, tr_num=ntr, seed=seed)
