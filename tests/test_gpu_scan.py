@@ -332,7 +332,11 @@ def test_direct_receive_matches_partials(built, monkeypatch, rf_ref):
 @pytest.mark.gpu
 def test_mt_epi_matches_fp64_oracle(built):
     """The 3-pool MT + exchange EPI (general model, bound pool, 32-coil
-    class receive on a shrunken phantom) against the all-FP64 oracle."""
+    class receive on a shrunken phantom) against the all-FP64 oracle.  The
+    EPI's k-space encoding cancels most of each sample's sum, so FP32
+    arithmetic shows more here: the reference algorithm in single precision
+    is 2.7e-5 from FP64 on this case, the accurate kernel 1.4e-5 (the same
+    with anchors at every step, without the MT pulse 1.0e-5); bound 2e-5."""
     from mrilab_gb300 import engine, phantoms
     import oracle
 
@@ -340,5 +344,6 @@ def test_mt_epi_matches_fp64_oracle(built):
     ref = oracle.run_port(sc, "f64")
     out = engine.scan(sc)
     err = rel_l2(signal(out), signal(ref))
-    print(f"MT EPI shrunk: relative L2 {err:.2e}")
-    assert err <= 1e-5
+    port32 = rel_l2(signal(oracle.run_port(sc, "f32")), signal(ref))
+    print(f"MT EPI shrunk: relative L2 {err:.2e} (reference algorithm in FP32: {port32:.2e})")
+    assert err <= 2e-5 and err < port32
