@@ -224,6 +224,17 @@ __device__ __forceinline__ void rot_exp(float &x, float &y, float &z, float vx, 
     z += fmaf(s.x, cz, s.y * dz);
 }
 
+// Direct receive: the block's sum of launch-local sample `a`, pool t, coil
+// c, rotated by exp(-i rfRef), added into the FP64 signal (out of line: the
+// partial-sum path is the usual one)
+static __device__ __noinline__ void direct_add(const ScanLaunch &L, int a, int t, int c, float sx, float sy) {
+    const int sig = L.amap[a];
+    if (sig < 0 || sig >= L.A) return;
+    const long long idx = ((long long)t * L.rx + c) * L.A + sig;
+    atomicAdd(L.dsx + idx, L.cr * sx - L.sr * sy);
+    atomicAdd(L.dsy + idx, L.sr * sx + L.cr * sy);
+}
+
 // Pools with a frame: every pool but the bound pool (pool 1) of MT / CEST,
 // which has no transverse magnetisation.
 template <int MODEL>
@@ -236,7 +247,7 @@ __device__ __forceinline__ constexpr bool has_frame(int t) {
 // Resident blocks per SM the register allocation aims at: four (16 warps)
 // while a thread's isochromat state is small.
 template <int P, int NS>
-constexpr int fast_min_blocks() {
+__host__ __device__ constexpr int fast_min_blocks() {
     return (P <= 2 && P * NS <= 8) ? 4 : (((P <= 3 && P * NS <= 6) || P * NS <= 5) ? 3 : 2);
 }
 
@@ -440,39 +451,48 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         const uint2 *rs1 = rsq + bcomp;
         const int nt_all = C4 / 4;
         float *rw = wstage + warp * 16 * (2 * C4);
-        for (int nt = 0; nt < nt_all; ++nt) {
-            float acc[3][4];
+        // n-tiles (4 coils each) in groups of kNG: the magnetisation operand
+        // is loaded and split once per k-step for the whole group; per n-tile
+        // two accumulator chains, big*big and the two correction products
+        constexpr int kNG = 2;
+        for (int nt0 = 0; nt0 < nt_all; nt0 += kNG) {
+            float accb[kNG][4], accs[kNG][4];
 #pragma unroll
-            for (int u = 0; u < 3; ++u)
+            for (int u = 0; u < kNG; ++u)
 #pragma unroll
-                for (int i = 0; i < 4; ++i) acc[u][i] = 0.f;
-            const int c = nt * 4 + (g >> 1);
-#pragma unroll
+                for (int i = 0; i < 4; ++i) accb[u][i] = accs[u][i] = 0.f;
+#pragma unroll 2
             for (int ks = 0; ks < 8; ++ks) {
                 const int j0 = warp * 32 + ks * 4 + (tig >> 1), j1 = j0 + 2;
                 const float a[4] = {mt1[2 * (g * kTRow + j0)], mt1[2 * ((g + 8) * kTRow + j0)],
                                     mt1[2 * (g * kTRow + j1)], mt1[2 * ((g + 8) * kTRow + j1)]};
-                // the coil operand was split once per launch; -ry flips the signs
-                const uint2 q0 = rs1[2 * (c * kTRow + j0)], q1 = rs1[2 * (c * kTRow + j1)];
-                const uint32_t bb[2] = {q0.x ^ sgn, q1.x ^ sgn}, bs[2] = {q0.y ^ sgn, q1.y ^ sgn};
                 uint32_t ab[4], as[4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
                     ab[i] = tf32_rn(a[i]);
                     as[i] = tf32_rn(a[i] - __uint_as_float(ab[i]));
                 }
-                mma_tf32(acc[0], as, bb);
-                mma_tf32(acc[1], ab, bs);
-                mma_tf32(acc[2], ab, bb);
-            }
-            float d[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) d[i] = (acc[0][i] + acc[1][i]) + acc[2][i];
-            const int col = nt * 8 + 2 * tig;
-            rw[g * (2 * C4) + col] = d[0];
-            rw[g * (2 * C4) + col + 1] = d[1];
-            rw[(g + 8) * (2 * C4) + col] = d[2];
-            rw[(g + 8) * (2 * C4) + col + 1] = d[3];
+                for (int u = 0; u < kNG; ++u) {
+                    if (nt0 + u >= nt_all) break;
+                    const int c = (nt0 + u) * 4 + (g >> 1);
+                    // the coil operand was split once per launch; -ry flips the signs
+                    const uint2 q0 = rs1[2 * (c * kTRow + j0)], q1 = rs1[2 * (c * kTRow + j1)];
+                    const uint32_t bb[2] = {q0.x ^ sgn, q1.x ^ sgn}, bs[2] = {q0.y ^ sgn, q1.y ^ sgn};
+                    mma_tf32(accs[u], as, bb);
+                    mma_tf32(accs[u], ab, bs);
+                    mma_tf32(accb[u], ab, bb);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kNG; ++u) {
+                if (nt0 + u >= nt_all) break;
+                const int col = (nt0 + u) * 8 + 2 * tig;
+                rw[g * (2 * C4) + col] = accs[u][0] + accb[u][0];
+                rw[g * (2 * C4) + col + 1] = accs[u][1] + accb[u][1];
+                rw[(g + 8) * (2 * C4) + col] = accs[u][2] + accb[u][2];
+                rw[(g + 8) * (2 * C4) + col + 1] = accs[u][3] + accb[u][3];
+            }
         }
         __syncthreads();
         const float *red = wstage;
@@ -488,12 +508,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 sy += red[(w * 16 + row) * (2 * C4) + 2 * c + 1];
             }
             if (L.dsx) {
-                const int sig = L.amap[a_base + a];
-                if (sig >= 0 && sig < L.A) {
-                    const long long idx = ((long long)t * L.rx + c) * L.A + sig;
-                    atomicAdd(L.dsx + idx, L.cr * sx - L.sr * sy);
-                    atomicAdd(L.dsy + idx, L.sr * sx + L.cr * sy);
-                }
+                direct_add(L, a_base + a, t, c, sx, sy);
             } else {
                 L.partial[((long long)tile * L.a_launch + a_base + a) * L.npairs + t * L.rx + c] = make_float2(sx, sy);
             }
