@@ -461,7 +461,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
             for (int u = 0; u < kNG; ++u)
 #pragma unroll
                 for (int i = 0; i < 4; ++i) accb[u][i] = accs[u][i] = 0.f;
-#pragma unroll 2
+#pragma unroll
             for (int ks = 0; ks < 8; ++ks) {
                 const int j0 = warp * 32 + ks * 4 + (tig >> 1), j1 = j0 + 2;
                 const float a[4] = {mt1[2 * (g * kTRow + j0)], mt1[2 * ((g + 8) * kTRow + j0)],
