@@ -151,8 +151,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
     auto set_dt = [&](float dt) {
 #pragma unroll
         for (int t = 0; t < P; ++t) {
-            const float y1t = on[t] ? -expm1f(-dt / t1[t]) : 0.f;
-            const float y2t = on[t] ? -expm1f(-dt / t2[t]) : 0.f;
+            const float y1t = on[t] ? one_minus_exp(dt / t1[t]) : 0.f;
+            const float y2t = on[t] ? one_minus_exp(dt / t2[t]) : 0.f;
             float ksum = 0.f;
 #pragma unroll
             for (int p = 0; p < P; ++p) {
@@ -160,9 +160,9 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
                 if (GM && p == t) continue;
                 const float kgo = kc[ch(t, p)], kin = kc[ch(p, t)];
                 ksum += kgo;
-                if (on[t] && kin != 0.f) fin[t][p] = -expm1f(-dt * kin);
+                if (on[t] && kin != 0.f) fin[t][p] = one_minus_exp(dt * kin);
             }
-            const float yot = on[t] ? -expm1f(-dt * ksum) : 0.f;
+            const float yot = on[t] ? one_minus_exp(dt * ksum) : 0.f;
             y1[t] = y1t;
             d1[t] = (1.f - yot) * (1.f - y1t);
             d2[t] = (1.f - yot) * (1.f - y2t);

@@ -94,7 +94,7 @@ struct FrameMoments {
 // kFlagState (dt or gradient changed), kFlagDt (dt changed), kFlagCkpt
 // (write the lab-frame state before this step to its checkpoint slot).
 enum : int { kFlagAdc = 1, kFlagRf = 2, kFlagAnchor = 4, kFlagState = 8, kFlagDt = 16, kFlagCkpt = 32 };
-constexpr int kAnchorEvery = 8;
+constexpr int kAnchorEvery = 16;
 constexpr int kAdjWin = 16;  // steps between adjoint checkpoints (recomputed into shared memory)
 inline int fast_stride_f4(int tx_num) { return 4 + (tx_num - 1); }
 // ckpt_every > 0 flags every ckpt_every-th step of the chunk with kFlagCkpt

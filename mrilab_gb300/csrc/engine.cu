@@ -1138,6 +1138,16 @@ __global__ void sincos_probe(const float *x, float *sn, float *cs, int n) {
     }
 }
 
+// 1 - exp(-x) of the accurate kernel and CUDA's -expm1f(-x) on caller-given
+// arguments: the hook of its accuracy test.
+__global__ void one_minus_exp_probe(const float *x, float *ours, float *lib, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        ours[i] = one_minus_exp(x[i]);
+        lib[i] = -expm1f(-x[i]);
+    }
+}
+
 }  // namespace
 }  // namespace mrl
 
@@ -2247,6 +2257,28 @@ int mrl_selftest_sincos(const float *x, float *sn, float *cs, int n) {
     if (e == cudaSuccess) e = cudaMemcpy(cs, d.p + 2 * n, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {
         set_err("selftest sincos: %s", cudaGetErrorString(e));
+        return MRL_ERR_CUDA;
+    }
+    return MRL_OK;
+}
+
+// Test hook (not declared in mrl_scan.h): 1 - exp(-x) of n host floats as
+// the accurate kernel computes it, and as CUDA's expm1f does.
+int mrl_selftest_one_minus_exp(const float *x, float *ours, float *lib, int n) {
+    using namespace mrl;
+    if (!x || !ours || !lib || n < 0) return MRL_ERR_ARG;
+    if (n == 0) return MRL_OK;
+    DevBuf<float> d;
+    cudaError_t e = d.ensure((size_t)3 * n);
+    if (e == cudaSuccess) e = cudaMemcpy(d.p, x, (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        one_minus_exp_probe<<<(n + 255) / 256, 256>>>(d.p, d.p + n, d.p + 2 * n, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(ours, d.p + n, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(lib, d.p + 2 * n, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_err("selftest one_minus_exp: %s", cudaGetErrorString(e));
         return MRL_ERR_CUDA;
     }
     return MRL_OK;

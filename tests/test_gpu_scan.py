@@ -233,6 +233,34 @@ def test_device_sincos_error_bounds(built):
     assert rel.max() <= 3e-7
 
 
+def test_device_one_minus_exp_error_bounds(built):
+    """The accurate kernel's 1 - exp(-x) (Taylor series below |x| = 1/16,
+    expm1f above) against FP64 and against CUDA's expm1f on the same float
+    arguments: relative error within 2e-7 (about 3 ulp) everywhere."""
+    import ctypes
+
+    lib = engine.library()
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.mrl_selftest_one_minus_exp.argtypes = [fp, fp, fp, ctypes.c_int]
+    lib.mrl_selftest_one_minus_exp.restype = ctypes.c_int
+    rng = np.random.default_rng(4)
+    x = np.concatenate([np.geomspace(1e-12, 0.0625, 100000), -np.geomspace(1e-12, 0.0625, 20000),
+                        rng.uniform(-0.0625, 0.0625, 100000), rng.uniform(0.0, 20.0, 50000),
+                        [0.0, 0.0625, np.nextafter(np.float32(0.0625), np.float32(0))]]).astype(np.float32)
+    ours = np.empty_like(x)
+    lib_v = np.empty_like(x)
+    rc = lib.mrl_selftest_one_minus_exp(x.ctypes.data_as(fp), ours.ctypes.data_as(fp), lib_v.ctypes.data_as(fp),
+                                        x.size)
+    assert rc == 0
+    ref = -np.expm1(-x.astype(np.float64))
+    nz = ref != 0
+    rel = np.abs(ours[nz] - ref[nz]) / np.abs(ref[nz])
+    rel_lib = np.abs(lib_v[nz] - ref[nz]) / np.abs(ref[nz])
+    print(f"max relative error: ours {rel.max():.2e}, expm1f {rel_lib.max():.2e}")
+    assert rel.max() <= 2e-7
+    assert ours[x == 0].max() == 0.0
+
+
 def test_tf32_rounding_matches_hardware_conversion(built):
     """The receive contraction rounds its TF32 operands with integer
     arithmetic; it must give the bits of cvt.rna.tf32.f32 for finite inputs."""
