@@ -66,6 +66,7 @@ class PortArgs(ctypes.Structure):
         ("max_steps", ctypes.c_longlong),
         ("ext_cb", _EXT_CB), ("ext_user", ctypes.c_void_p),
         ("run_mode", ctypes.c_int), ("mxs", _f), ("mys", _f), ("mzs", _f), ("muts", _d),
+        ("exact", ctypes.c_int),
     ]
 
 
@@ -98,21 +99,24 @@ def _f64(a):
 
 
 def run_port(scan, precision: str = "f32", threads: int = 0, max_steps: int = -1,
-             ext_cb=None) -> Dict[str, np.ndarray]:
+             ext_cb=None, exact: bool = False) -> Dict[str, np.ndarray]:
     """Run the C oracle on a ``phantoms.Scan``; returns Sx, Sy, Kx, Ky, Kz,
-    final Mx, My, Mz (flattened column-major) and ``steps``."""
+    final Mx, My, Mz (flattened column-major) and ``steps``.  ``exact``: the
+    exact relaxation-exchange propagator instead of the reference's split
+    exchange (ME, and GM without bound pools)."""
     lib = ctypes.CDLL(PORT_SO)
     fn = lib.mrl_port_scan_f32 if precision == "f32" else lib.mrl_port_scan_f64
     fn.argtypes = [ctypes.POINTER(PortArgs), ctypes.POINTER(ctypes.c_longlong)]
     fn.restype = ctypes.c_int
     steps = ctypes.c_longlong(0)
     out = _call_with_args(scan, lambda args: fn(ctypes.byref(args), ctypes.byref(steps)), threads, max_steps,
-                          ext_cb)
+                          ext_cb, exact)
     out["steps"] = int(steps.value)
     return out
 
 
-def _call_with_args(scan, call, threads: int = 0, max_steps: int = -1, ext_cb=None) -> Dict[str, np.ndarray]:
+def _call_with_args(scan, call, threads: int = 0, max_steps: int = -1, ext_cb=None,
+                    exact: bool = False) -> Dict[str, np.ndarray]:
     o, m, c, ctl, q, sig = scan.VObj, scan.VMag, scan.VCoi, scan.VCtl, scan.VSeq, scan.VSig
     Y, X, Z = o["Rho"].shape[:3]
     keep = {}
@@ -166,6 +170,7 @@ def _call_with_args(scan, call, threads: int = 0, max_steps: int = -1, ext_cb=No
         cb = _EXT_CB(lambda user, val: int(ext_cb(val, out)))
         keep["cb"] = cb
         args.ext_cb = cb
+    args.exact = int(bool(exact))
     args.run_mode = int(ctl["RunMode"])
     if args.run_mode == 1:  # history [len(uts)][P][S][V], slot 0 = the initial state (DoSpinWatchExec.m:152-161)
         for k in ("Mx", "My", "Mz"):

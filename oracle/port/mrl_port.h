@@ -66,6 +66,12 @@ typedef struct mrl_port_args {
     int run_mode;
     float *mxs, *mys, *mzs;
     double *muts;
+    /* exact relaxation-exchange propagator (ME, and GM without bound pools):
+     * each step rotates every pool, then applies x' = E_T x, y' = E_T y,
+     * z' = E_L z + dt phi1(A_L dt) b with E = exp(A dt) of the relaxation-
+     * exchange generator (Bloch-McConnell equations without the rotation);
+     * not in the reference, which splits the exchange (first order) */
+    int exact;
 } mrl_port_args;
 
 /* Returns 0 on success, < 0 on bad arguments.  *steps_done (optional)

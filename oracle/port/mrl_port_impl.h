@@ -231,6 +231,56 @@ static void PORT_T(update)(const mrl_port_args *a, REAL *MX, REAL *MY, REAL *MZ,
         return;
     }
 
+    if ((a->model == MRL_PORT_ME || a->model == MRL_PORT_GM) && a->exact) {
+        /* exact relaxation-exchange propagator after the rotation of every pool */
+        REAL rx[MRL_PORT_MAX_POOL], ry[MRL_PORT_MAX_POOL], rz[MRL_PORT_MAX_POOL];
+        double At[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL] = {0}, Al[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL] = {0};
+        double Ft[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL], Fl[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL];
+        double Xt[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL], Xl[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL];
+        double b[MRL_PORT_MAX_POOL] = {0};
+        int on[MRL_PORT_MAX_POOL];
+        for (int t = 0; t < P; ++t) {
+            REAL T1 = a->t1[PIDX(t)], T2 = a->t2[PIDX(t)], rho = a->rho[PIDX(t)];
+            on[t] = !(T2 == 0 || T1 == 0 || rho == 0);
+            rx[t] = MX[IDX(t)];
+            ry[t] = MY[IDX(t)];
+            rz[t] = MZ[IDX(t)];
+            if (!on[t]) continue;
+            PORT_T(rotate)(&rx[t], &ry[t], &rz[t], DW(t), st, tx, gyro, mg, pe, rf_sum);
+            At[t * P + t] = -1.0 / (double)T2;
+            Al[t * P + t] = -1.0 / (double)T1;
+            b[t] = (double)rho / ((double)S * (double)T1);
+            for (int p = 0; p < P; ++p) {
+                if (p == t) continue; /* a self rate moves nothing */
+                const double kgo = a->model == MRL_PORT_ME ? a->k[(long)(t * P + p) * V + v] : a->k[(long)(p * P + t) * V + v];
+                const double kin = a->model == MRL_PORT_ME ? a->k[(long)(p * P + t) * V + v] : a->k[(long)(t * P + p) * V + v];
+                At[t * P + t] -= kgo;
+                Al[t * P + t] -= kgo;
+                At[t * P + p] += kin;
+                Al[t * P + p] += kin;
+            }
+        }
+        for (int i = 0; i < P * P; ++i) {
+            At[i] *= (double)dt;
+            Al[i] *= (double)dt;
+        }
+        port_expm1_phi1(P, At, Ft, Xt);
+        port_expm1_phi1(P, Al, Fl, Xl);
+        for (int t = 0; t < P; ++t) {
+            if (!on[t]) continue;
+            double x = rx[t], y = ry[t], z = rz[t];
+            for (int p = 0; p < P; ++p) {
+                x += Ft[t * P + p] * (double)rx[p];
+                y += Ft[t * P + p] * (double)ry[p];
+                z += Fl[t * P + p] * (double)rz[p] + (double)dt * Xl[t * P + p] * b[p];
+            }
+            MX[IDX(t)] = (REAL)x;
+            MY[IDX(t)] = (REAL)y;
+            MZ[IDX(t)] = (REAL)z;
+        }
+        return;
+    }
+
     if (a->model == MRL_PORT_ME || a->model == MRL_PORT_GM) {
         REAL px[MRL_PORT_MAX_POOL], py[MRL_PORT_MAX_POOL], pz[MRL_PORT_MAX_POOL];
         for (int t = 0; t < P; ++t) {
@@ -390,6 +440,11 @@ int PORT_FN(const mrl_port_args *a, long long *steps_done) {
         return -1;
     if ((a->model == MRL_PORT_MT && a->type_num != 2) || (a->model == MRL_PORT_CEST && a->type_num < 2))
         return -1;
+    if (a->exact) { /* free pools exchanging: ME, or GM without bound pools */
+        if (a->model != MRL_PORT_ME && a->model != MRL_PORT_GM) return -1;
+        for (int t = 0; a->model == MRL_PORT_GM && t < a->type_num; ++t)
+            if ((int)a->type_flag[t] != 0) return -1;
+    }
     const long V = (long)a->ny * a->nx * a->nz;
     const int P = a->type_num, S = a->spin_num, TX = a->tx_num, RX = a->rx_num, A = a->signal_num;
     const long N = (long)P * S * V;

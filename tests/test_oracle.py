@@ -108,3 +108,58 @@ def test_port_history_matches_live_reference_cpu_engine(built):
     for k in ("Mxs", "Mys", "Mzs"):
         np.testing.assert_allclose(out[k], ref[k], rtol=0, atol=1e-6)
     np.testing.assert_array_equal(out["Muts"], ref["Muts"])
+
+
+@pytest.mark.parametrize("model", ["me", "gm"])
+def test_exact_oracle_matches_bloch_mcconnell_expm(built, model):
+    """The oracle's exact propagator (rotate every pool, then exp of the
+    relaxation-exchange generator) equals the exponential of the whole
+    Bloch-McConnell generator when every pool precesses at the same
+    frequency (rotation about z then commutes with relaxation and exchange):
+    one voxel, three pools with stiff exchange, free precession at dB0, the
+    state read after the last of several uneven steps."""
+    scipy_linalg = pytest.importorskip("scipy.linalg")
+    from mrilab_gb300 import seq as S
+
+    P = 3
+    rho = np.array([[[[0.7, 0.2, 0.1]]]], np.float32)
+    t1 = np.array([[[[1.1, 0.45, 0.8]]]], np.float32)
+    t2 = np.array([[[[0.07, 0.015, 0.03]]]], np.float32)
+    rates = np.zeros((1, 1, 1, P, P), np.float32)
+    rates[..., 1, 0], rates[..., 2, 0], rates[..., 1, 2] = 300.0, 120.0, 40.0
+    rates[..., 0, 1] = rates[..., 1, 0] * rho[..., 1] / rho[..., 0]
+    rates[..., 0, 2] = rates[..., 2, 0] * rho[..., 2] / rho[..., 0]
+    rates[..., 2, 1] = rates[..., 1, 2] * rho[..., 1] / rho[..., 2]
+    tr = S.TR(30_000_000)
+    times = [0, 1_500_000, 1_700_000, 6_000_000, 6_010_000, 18_000_000, 30_000_000]
+    tr.adc(times[1:-1])
+    lines = S.concat([tr])
+    tf = np.zeros(P) if model == "gm" else None
+    sc = phantoms.assemble(rho, t1, t2, db0_hz=np.full((1, 1, 1), 37.0), model=model, rates=rates,
+                           type_flag=tf, seqlines=lines)
+    m0 = np.array([[0.3, -0.2, 0.4], [0.05, 0.1, 0.02], [-0.03, 0.04, 0.05]])  # [pool][x, y, z]
+    for k, comp in (("Mx", 0), ("My", 1), ("Mz", 2)):
+        sc.VObj[k] = np.asfortranarray(m0[:, comp].reshape(1, 1, 1, 1, P).astype(np.float32))
+    out = oracle.run_port(sc, "f64", exact=True)
+    # the generator on (x_0..x_P-1, y.., z.., 1)
+    w = float(sc.VObj["Gyro"]) * float(sc.VMag["dB0"].ravel()[0])
+    n = 3 * P + 1
+    G = np.zeros((n, n))
+    for t in range(P):
+        kout = sum(rates[0, 0, 0, t, p] for p in range(P) if p != t)
+        for c, r in ((0, 1 / t2[0, 0, 0, t]), (1, 1 / t2[0, 0, 0, t]), (2, 1 / t1[0, 0, 0, t])):
+            G[c * P + t, c * P + t] = -r - kout
+            for p in range(P):
+                if p != t:
+                    G[c * P + t, c * P + p] = rates[0, 0, 0, p, t]
+        G[0 * P + t, 1 * P + t] += w   # dx/dt = w y
+        G[1 * P + t, 0 * P + t] -= w   # dy/dt = -w x
+        G[2 * P + t, n - 1] = rho[0, 0, 0, t] / t1[0, 0, 0, t]
+    state = np.concatenate([m0[:, 0], m0[:, 1], m0[:, 2], [1.0]])
+    # the integrated time: every dt > 0 step of the decoded sequence
+    uts = sc.VSeq["utsLine"]
+    total = float(np.sum(np.diff(uts)[np.diff(uts) > 0]))
+    ref = scipy_linalg.expm(G * total) @ state
+    got = np.concatenate([out["Mx"], out["My"], out["Mz"]])
+    # the oracle's FP64 state is returned in the single-precision state arrays
+    assert np.abs(got - ref[:-1]).max() <= 2e-7 * np.abs(ref[:-1]).max()
