@@ -50,7 +50,15 @@ typedef enum {
      * (BlochKernel.h for one pool, BlochKernel*.cuh otherwise), evaluated
      * without fused multiply-add and with correctly rounded FP32 math, for
      * bit-level parity studies against the reference CPU engine. */
-    MRL_NUMERICS_REFERENCE = 1
+    MRL_NUMERICS_REFERENCE = 1,
+    /* The accurate integrator with the exact relaxation-exchange propagator
+     * in place of the reference's first-order split exchange: after each
+     * step's rotation, x' = E_T x, y' = E_T y, z' = E_L z + dt phi1(A_L dt) b,
+     * E = exp(A dt) of the relaxation-exchange generator, computed in FP64 per
+     * voxel and distinct dt.  Free pools exchanging (ME; GM without bound
+     * pools), TypeNum <= 3; the normal model runs as MRL_NUMERICS_ACCURATE
+     * (its relaxation is exact already).  No reference counterpart. */
+    MRL_NUMERICS_EXACT = 2
 } mrl_numerics;
 
 typedef enum {

@@ -48,6 +48,7 @@ UNITS = {
     "scan_fast_mt.cu": [],
     "scan_fast_cest.cu": [],
     "adjoint.cu": [],
+    "scan_fast_exact.cu": [],
     "decode.cpp": None,  # host C++
 }
 

@@ -22,6 +22,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <tuple>
@@ -374,6 +375,12 @@ struct Scanner {
     // objects whose partials do not fit the device; otherwise partials are
     // faster (atomics: 631 ms, partials: 580 ms on a 128x128x32 32-coil EPI)
     bool direct_rx = false, no_direct = false;
+    // exact relaxation-exchange propagator: its coefficient table per
+    // (distinct float dt, voxel) and the dt values so far (index = position)
+    bool exact = false;
+    std::map<uint32_t, int> xdt_index;
+    std::vector<float> xdts;
+    DevBuf<float> d_xdts, d_xtab;
 
     ~Scanner() {
         for (auto &e : ev_scan) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
@@ -451,9 +458,19 @@ struct Scanner {
         }
         if (mi.nk > 0 && (!a.obj.k || a.obj.k_channels < mi.nk))
             return set_err("K needs %d channels, got %d", mi.nk, a.obj.k ? a.obj.k_channels : 0), MRL_ERR_ARG;
-        fast = a.ctl.numerics == MRL_NUMERICS_ACCURATE;
-        if (a.ctl.numerics != MRL_NUMERICS_ACCURATE && a.ctl.numerics != MRL_NUMERICS_REFERENCE)
+        fast = a.ctl.numerics == MRL_NUMERICS_ACCURATE || a.ctl.numerics == MRL_NUMERICS_EXACT;
+        if (a.ctl.numerics != MRL_NUMERICS_ACCURATE && a.ctl.numerics != MRL_NUMERICS_REFERENCE &&
+            a.ctl.numerics != MRL_NUMERICS_EXACT)
             return set_err("unknown numerics %d", a.ctl.numerics), MRL_ERR_ARG;
+        exact = a.ctl.numerics == MRL_NUMERICS_EXACT && mi.km != KM_NORMAL;
+        if (exact) {
+            bool free_pools = mi.km == KM_EXCH;
+            for (int t = 0; free_pools && mi.gm && t < P; ++t) free_pools = (int)a.obj.type_flag[t] == 0;
+            if (!free_pools)
+                return set_err("MRL_NUMERICS_EXACT covers free pools exchanging (ME, GM without bound pools)"),
+                       MRL_ERR_UNSUPPORTED;
+            if (P > 3) return set_err("MRL_NUMERICS_EXACT supports TypeNum <= 3"), MRL_ERR_UNSUPPORTED;
+        }
         hist_on = a.ctl.run_mode == 1;  // other values scan normally, as in the reference's switch
         if (hist_on && !fast)
             return set_err("RunMode 1 (per-step history) needs MRL_NUMERICS_ACCURATE"), MRL_ERR_UNSUPPORTED;
@@ -697,6 +714,44 @@ struct Scanner {
     // Split a decoded chunk into launches whose receive partials fit the
     // budget (MRL_PARTIAL_MB, default 16 GiB or a quarter of the free memory), upload its step records and
     // ADC map, and size the partial buffer.
+    // Exact propagator: the index of every step's float dt in its flags (bits
+    // 8 and up), and the coefficient table of every dt value so far (FP64
+    // exponentials, one thread per (dt, voxel)).
+    int exact_coefficients(std::vector<float> &rec) {
+        const int stride = fast_stride_f4(TX) * 4;
+        const size_t n_before = xdts.size();
+        for (size_t q = 0; q < rec.size() / stride; ++q) {
+            float *r = &rec[q * stride];
+            uint32_t key;
+            std::memcpy(&key, &r[0], sizeof(key));
+            auto it = xdt_index.find(key);
+            int idx;
+            if (it == xdt_index.end()) {
+                idx = (int)xdts.size();
+                if (idx >= (1 << 22)) return set_err("more than 2^22 distinct step lengths"), MRL_ERR_UNSUPPORTED;
+                xdt_index.emplace(key, idx);
+                xdts.push_back(r[0]);
+            } else {
+                idx = it->second;
+            }
+            int flags;
+            std::memcpy(&flags, &r[7], sizeof(int));
+            flags |= idx << 8;
+            std::memcpy(&r[7], &flags, sizeof(int));
+        }
+        if (n_act == 0 || (xdts.size() == n_before && d_xtab.p)) return MRL_OK;
+        cudaError_t e = d_xdts.ensure(xdts.size());
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_xdts.p, xdts.data(), xdts.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = d_xtab.ensure(xdts.size() * (size_t)exact_fields(P) * n_act);
+        if (e == cudaSuccess)
+            e = launch_exact_table(P, d_xdts.p, (int)xdts.size(), n_act, S, mi.gm ? 1 : 0, d_f.p + o_rho,
+                                   d_f.p + o_t1, d_f.p + o_t2, mi.nk > 0 ? d_f.p + o_k : nullptr, d_xtab.p, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail_cuda(e, "exact propagator table");
+        return MRL_OK;
+    }
+
     int prepare_chunk(const DecodeChunk &ch, std::vector<LaunchDesc> &out) {
         out.clear();
         amap_host.clear();
@@ -738,6 +793,10 @@ struct Scanner {
         if (fast) {
             pack_fast_records(ch, TX, fmom, frec, ckpt_every);
             recs = &frec;
+            if (exact) {
+                const int rc = exact_coefficients(frec);
+                if (rc) return rc;
+            }
         }
         phase("pack records");
         cudaError_t e;
@@ -789,6 +848,8 @@ struct Scanner {
         L.hist = hist_on ? d_hist.p + (hist_steps + d.s0) * 3 * L.hist_stride : nullptr;
         L.ckpt = ckpt;
         L.ckpt_step0 = d.s0;
+        L.xtab = exact ? d_xtab.p : nullptr;
+        L.xnf = exact_fields(P);
         if (direct_rx) {
             L.dsx = d_sx.p;
             L.dsy = d_sy.p;
@@ -839,7 +900,8 @@ struct Scanner {
                 dim3 grid(nblk);
                 if (fast) {
                     const FastGrid g{d_desc.p + li, nullptr, nblk, nullptr};
-                    e = launch_fast(mi.km, P, NS, all_free() != 0, grid, smem, stream, g);
+                    e = exact ? launch_scan_fast_exact(P, NS, grid, smem, stream, g)
+                              : launch_fast(mi.km, P, NS, all_free() != 0, grid, smem, stream, g);
                 } else {
                     switch (mi.km) {
                     case KM_NORMAL: e = launch_scan_ref_normal(P, NS, grid, smem, stream, L); break;
@@ -2065,7 +2127,7 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
     sc.args = args;
     int rc = sc.validate();
     if (rc) return rc;
-    if (!sc.fast) {
+    if (!sc.fast || sc.exact) {
         set_err("mrl_scan_noalloc runs the MRL_NUMERICS_ACCURATE integrator only");
         return MRL_ERR_UNSUPPORTED;
     }

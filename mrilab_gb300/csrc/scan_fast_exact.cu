@@ -1,0 +1,214 @@
+// Exact relaxation-exchange propagator: the accurate scan kernel's
+// instantiations for free pools exchanging with MRL_NUMERICS_EXACT, and the
+// FP64 kernel that tabulates each voxel's propagator per distinct dt.
+//
+// Per step every pool is rotated exactly (rf or free precession, as in the
+// accurate mode), then the Bloch-McConnell equations without the rotation
+// are solved exactly over dt: x' = E_T x, y' = E_T y, z' = E_L z + c with
+// E = exp(A dt), A_T = -diag(1/T2) + K, A_L = -diag(1/T1) + K (K the
+// exchange generator: -sum of the outgoing rates on the diagonal, the
+// incoming rate p -> t at (t, p)), c = dt phi1(A_L dt) b, b = rho / (S T1).
+// The reference splits the exchange to first order instead
+// (BlochKernelME.cuh:320-343), which departs from the equations when k dt
+// is not small.
+#include "scan_launch.h"
+
+namespace mrl {
+
+namespace {
+using Kernel = void (*)(const FastLaunch *, const int2 *, int, int *);
+
+template <int P, int NS>
+Kernel pick() {
+    return scan_fast_kernel<KM_EXCH, P, NS, true, true>;
+}
+
+Kernel select(int P, int NS) {
+    if (P == 1 && NS == 1) return pick<1, 1>();
+    if (P == 1 && NS == 2) return pick<1, 2>();
+    if (P == 1 && NS == 4) return pick<1, 4>();
+    if (P == 2 && NS == 1) return pick<2, 1>();
+    if (P == 2 && NS == 2) return pick<2, 2>();
+    if (P == 2 && NS == 4) return pick<2, 4>();
+    if (P == 3 && NS == 1) return pick<3, 1>();
+    if (P == 3 && NS == 2) return pick<3, 2>();
+    return nullptr;
+}
+
+// exp(A) - I and phi1(A) = sum_k A^k / (k+1)! (row-major P x P): Taylor
+// series of A scaled by 2^-s to norm <= 1/4 (24 terms, far below FP64
+// rounding), then s squarings: e^{2B} - I = F^2 + 2F, phi1(2B) = phi1(B)(F + 2I)/2
+template <int P>
+__device__ void expm1_phi1(const double (&A)[P][P], double (&F)[P][P], double (&X)[P][P]) {
+    double norm = 0.0;
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+        double r = 0.0;
+#pragma unroll
+        for (int j = 0; j < P; ++j) r += fabs(A[i][j]);
+        norm = fmax(norm, r);
+    }
+    int s = 0;
+    while (norm > 0.25 && s < 60) {
+        norm *= 0.5;
+        ++s;
+    }
+    const double scale = ldexp(1.0, -s);
+    double B[P][P], T[P][P], U[P][P];
+#pragma unroll
+    for (int i = 0; i < P; ++i)
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            B[i][j] = A[i][j] * scale;
+            T[i][j] = i == j ? 1.0 : 0.0;
+            F[i][j] = 0.0;
+            X[i][j] = T[i][j];
+        }
+    for (int k = 1; k <= 24; ++k) {
+        const double ik = 1.0 / k, ik1 = 1.0 / (k + 1);
+#pragma unroll
+        for (int i = 0; i < P; ++i)
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+                double acc = 0.0;
+#pragma unroll
+                for (int m = 0; m < P; ++m) acc = fma(T[i][m], B[m][j], acc);
+                U[i][j] = acc * ik;
+            }
+#pragma unroll
+        for (int i = 0; i < P; ++i)
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+                T[i][j] = U[i][j];
+                F[i][j] += T[i][j];
+                X[i][j] = fma(T[i][j], ik1, X[i][j]);
+            }
+    }
+    for (int q = 0; q < s; ++q) {
+#pragma unroll
+        for (int i = 0; i < P; ++i)
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+                double a = 0.0, b = 0.0;
+#pragma unroll
+                for (int m = 0; m < P; ++m) {
+                    a = fma(X[i][m], F[m][j] + (m == j ? 2.0 : 0.0), a);
+                    b = fma(F[i][m], F[m][j], b);
+                }
+                U[i][j] = 0.5 * a;
+                T[i][j] = b + 2.0 * F[i][j];
+            }
+#pragma unroll
+        for (int i = 0; i < P; ++i)
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+                X[i][j] = U[i][j];
+                F[i][j] = T[i][j];
+            }
+    }
+}
+
+template <int P>
+__global__ void exact_table_kernel(const float *__restrict__ dts, int n_dt, int n_act, int S, int gm,
+                                   const float *__restrict__ rho, const float *__restrict__ t1,
+                                   const float *__restrict__ t2, const float *__restrict__ kch, float *tab) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)n_dt * n_act) return;
+    const int d = (int)(i / n_act), v = (int)(i % n_act);
+    const double dt = dts[d];
+    double At[P][P], Al[P][P], b[P];
+#pragma unroll
+    for (int t = 0; t < P; ++t) {
+        b[t] = 0.0;
+#pragma unroll
+        for (int p = 0; p < P; ++p) At[t][p] = Al[t][p] = 0.0;
+    }
+#pragma unroll
+    for (int t = 0; t < P; ++t) {
+        const double T1 = t1[(long long)t * n_act + v], T2 = t2[(long long)t * n_act + v],
+                     r = rho[(long long)t * n_act + v];
+        if (T1 == 0.0 || T2 == 0.0 || r == 0.0) continue;  // a pool left alone: identity row
+        At[t][t] = -1.0 / T2;
+        Al[t][t] = -1.0 / T1;
+        b[t] = r / (S * T1);
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+            if (p == t || !kch) continue;  // a self rate moves nothing
+            // ME: channel a*P+b is the rate a -> b; GM: channel b*P+a
+            const double kgo = kch[(long long)(gm ? p * P + t : t * P + p) * n_act + v];
+            const double kin = kch[(long long)(gm ? t * P + p : p * P + t) * n_act + v];
+            At[t][t] -= kgo;
+            Al[t][t] -= kgo;
+            At[t][p] += kin;
+            Al[t][p] += kin;
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < P; ++t)
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+            At[t][p] *= dt;
+            Al[t][p] *= dt;
+        }
+    double Ft[P][P], Xt[P][P], Fl[P][P], Xl[P][P];
+    expm1_phi1<P>(At, Ft, Xt);
+    expm1_phi1<P>(Al, Fl, Xl);
+    float *o = tab + (long long)d * exact_fields(P) * n_act + v;
+    int f = 0;
+#pragma unroll
+    for (int t = 0; t < P; ++t) o[(long long)(f++) * n_act] = (float)Ft[t][t];
+#pragma unroll
+    for (int t = 0; t < P; ++t)
+#pragma unroll
+        for (int p = 0; p < P; ++p)
+            if (p != t) o[(long long)(f++) * n_act] = (float)Ft[t][p];
+#pragma unroll
+    for (int t = 0; t < P; ++t) o[(long long)(f++) * n_act] = (float)Fl[t][t];
+#pragma unroll
+    for (int t = 0; t < P; ++t)
+#pragma unroll
+        for (int p = 0; p < P; ++p)
+            if (p != t) o[(long long)(f++) * n_act] = (float)Fl[t][p];
+#pragma unroll
+    for (int t = 0; t < P; ++t) {
+        double c = 0.0;
+#pragma unroll
+        for (int p = 0; p < P; ++p) c = fma(Xl[t][p], b[p], c);
+        o[(long long)(f++) * n_act] = (float)(dt * c);
+    }
+}
+}  // namespace
+
+cudaError_t launch_scan_fast_exact(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastGrid &g) {
+    Kernel k = select(P, NS);
+    if (!k) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, kBlock, smem, st>>>(g.descs, g.items, g.n_items, g.counter);
+    return cudaGetLastError();
+}
+
+int occupancy_scan_fast_exact(int P, int NS, size_t smem) {
+    Kernel k = select(P, NS);
+    int n = 0;
+    if (!k || cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kBlock, smem) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+cudaError_t launch_exact_table(int P, const float *dts, int n_dt, int n_act, int S, int gm, const float *rho,
+                               const float *t1, const float *t2, const float *kch, float *tab, cudaStream_t st) {
+    const long long n = (long long)n_dt * n_act;
+    if (n <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((n + 127) / 128);
+    switch (P) {
+    case 1: exact_table_kernel<1><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, rho, t1, t2, kch, tab); break;
+    case 2: exact_table_kernel<2><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, rho, t1, t2, kch, tab); break;
+    case 3: exact_table_kernel<3><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, rho, t1, t2, kch, tab); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace mrl

@@ -269,8 +269,9 @@ __host__ __device__ constexpr int fast_min_blocks() {
 // described by F, over F's step range.  kbase counts the record chunks this
 // block has staged before (it picks the buffer and mbarrier phase).
 // Returns false, block-uniformly, when a wait ran out (status word raised).
-template <int MODEL, int P, int NS, bool FREE>
+template <int MODEL, int P, int NS, bool FREE, bool EXACT = false>
 __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigned char *smem, uint32_t &kbase) {
+    static_assert(!EXACT || (MODEL == KM_EXCH && FREE), "the exact propagator covers free pools exchanging");
     const ScanLaunch &L = F.b;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     float4 *rbuf = reinterpret_cast<float4 *>(smem + 128);
@@ -420,6 +421,9 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     bool entered = false;
     // exchange / MT coefficients, cached per dt
     float yo[P], fin[P][P];
+    // exact propagator (EXACT): longitudinal off-diagonal terms and recovery
+    constexpr int kXP = EXACT ? P : 1;
+    float fL[kXP][kXP], cL[kXP];
 #pragma unroll
     for (int t = 0; t < P; ++t) {
         yo[t] = 0.f;
@@ -582,7 +586,30 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
             const float gzt = r0.y, gyt = r0.z, gxt = r0.w;
             // instantaneous common off-resonance (rad/s)
             const float wc = fmaf(om[3], gzt, fmaf(om[2], gyt, fmaf(om[1], gxt, om[0])));
-            if (active && (flags & kFlagDt)) {
+            if (active && (flags & kFlagDt) && EXACT) {
+                // the exact relaxation-exchange propagator of this dt, from the
+                // table [dt][field][n_act]: diag(E_T) - 1, E_T off-diagonal,
+                // diag(E_L) - 1, E_L off-diagonal, recovery (as y2, fin, y1, fL, cL)
+                const float *xt = L.xtab + (long long)(flags >> 8) * L.xnf * n + v;
+                int f = 0;
+#pragma unroll
+                for (int t = 0; t < P; ++t) {
+                    y2[t] = -xt[(long long)(f++) * n];
+                    yo[t] = 0.f;
+                }
+#pragma unroll
+                for (int t = 0; t < P; ++t)
+#pragma unroll
+                    for (int p = 0; p < P; ++p) fin[t][p] = p == t ? 0.f : xt[(long long)(f++) * n];
+#pragma unroll
+                for (int t = 0; t < P; ++t) y1[t] = -xt[(long long)(f++) * n];
+#pragma unroll
+                for (int t = 0; t < kXP; ++t)
+#pragma unroll
+                    for (int p = 0; p < kXP; ++p) fL[t][p] = p == t ? 0.f : xt[(long long)(f++) * n];
+#pragma unroll
+                for (int t = 0; t < kXP; ++t) cL[t] = xt[(long long)(f++) * n];
+            } else if (active && (flags & kFlagDt)) {
 #pragma unroll
                 for (int t = 0; t < P; ++t) {
                     y1[t] = one_minus_exp(dt * it1[t]);
@@ -644,8 +671,10 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 for (int t = 0; t < P; ++t) {
                     if (!has_frame<MODEL>(t)) continue;
                     // transverse decay of a free step: (1 - a) = (1 - y2)(1 - yo)
-                    const float a = (MODEL == KM_NORMAL || MODEL == KM_MT) ? y2[t]
-                                                                           : y2[t] + yo[t] - y2[t] * yo[t];
+                    // (EXACT: the increment is the pure rotation; decay and exchange follow)
+                    const float a = EXACT ? 0.f
+                                          : (MODEL == KM_NORMAL || MODEL == KM_MT) ? y2[t]
+                                                                                   : y2[t] + yo[t] - y2[t] * yo[t];
 #pragma unroll
                     for (int s = 0; s < NS; ++s) {
                         if (tvo >> t & 1u) {
@@ -731,7 +760,8 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 for (int t = 0; t < P; ++t)
 #pragma unroll
                     for (int p = 0; p < P; ++p) {
-                        const float2 r = cmul_conj(Pprev[p], Pc[t]);
+                        // (EXACT: the partner after its rotation, in its frame after the step)
+                        const float2 r = cmul_conj(EXACT ? Pc[p] : Pprev[p], Pc[t]);
                         const float f = (FREE || ((tvo >> t & 1u) && L.kind[p] == 0)) ? fin[t][p] : 0.f;
                         fr[t][p] = make_float2(f * r.x, f * r.y);
                     }
@@ -828,7 +858,16 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                         Y[s][t] = on ? y : py[t];
                         Z[s][t] = on ? z : pz[t];
                     }
-                    // relaxation and inflow after the rotation (the frames hold still)
+                    // relaxation and inflow after the rotation (the frames hold still);
+                    // the exact propagator takes the partners after their rotation
+                    if constexpr (EXACT) {
+#pragma unroll
+                        for (int t = 0; t < P; ++t) {
+                            px[t] = X[s][t];
+                            py[t] = Y[s][t];
+                            pz[t] = Z[s][t];
+                        }
+                    }
                     if constexpr (MODEL == KM_NORMAL || MODEL == KM_MT) {
 #pragma unroll
                         for (int t = 0; t < P; ++t) {
@@ -853,6 +892,28 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                             X[s][t] = fmaf(-yo[t], x, x) + ix;
                             Y[s][t] = fmaf(-yo[t], y, y) + iy;
                         }
+                    }
+                } else if constexpr (EXACT) {
+                    // every pool turns by its own step, then the exact propagator
+                    float wx[P], wy[P];
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        const float2 d = dm[s][t];
+                        wx[t] = px[t] + fmaf(d.x, px[t], -d.y * py[t]);
+                        wy[t] = py[t] + fmaf(d.x, py[t], d.y * px[t]);
+                    }
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        float ix = 0.f, iy = 0.f;
+#pragma unroll
+                        for (int p = 0; p < P; ++p) {
+                            if (p == t) continue;
+                            const float2 f = fr[t][p];
+                            ix = fmaf(f.x, wx[p], fmaf(-f.y, wy[p], ix));
+                            iy = fmaf(f.x, wy[p], fmaf(f.y, wx[p], iy));
+                        }
+                        X[s][t] = fmaf(-y2[t], wx[t], wx[t]) + ix;
+                        Y[s][t] = fmaf(-y2[t], wy[t], wy[t]) + iy;
                     }
                 } else {
 #pragma unroll
@@ -882,6 +943,15 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 if (MODEL == KM_NORMAL) {
 #pragma unroll
                     for (int t = 0; t < P; ++t) Z[s][t] = fmaf(y1[t], rhoS[t] - Z[s][t], Z[s][t]);
+                } else if (MODEL == KM_EXCH && EXACT) {
+#pragma unroll
+                    for (int t = 0; t < kXP; ++t) {
+                        float iz = 0.f;
+#pragma unroll
+                        for (int p = 0; p < kXP; ++p) iz = fmaf(fL[t][p], pz[p], iz);
+                        const float z = Z[s][t];
+                        Z[s][t] = fmaf(-y1[t], z, z) + iz + cL[t];
+                    }
                 } else if (MODEL == KM_EXCH) {
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
@@ -947,7 +1017,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 // takes items gridDim.x, gridDim.x + 1, ... from *counter (the batched
 // form: the tiles of many scans, ordered longest first).  Each item's
 // descriptor is copied from descs into shared memory.
-template <int MODEL, int P, int NS, bool FREE>
+template <int MODEL, int P, int NS, bool FREE, bool EXACT = false>
 __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>())
     scan_fast_kernel(const FastLaunch *__restrict__ descs, const int2 *__restrict__ items, int n_items, int *counter) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -966,7 +1036,7 @@ __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>())
         int *dst = reinterpret_cast<int *>(&fs);
         for (int w = threadIdx.x; w < (int)(sizeof(FastLaunch) / 4); w += blockDim.x) dst[w] = src[w];
         __syncthreads();
-        if (!scan_item<MODEL, P, NS, FREE>(fs, item.y, smem, kbase)) return;
+        if (!scan_item<MODEL, P, NS, FREE, EXACT>(fs, item.y, smem, kbase)) return;
         if (counter == nullptr) break;
         __syncthreads();  // every thread is done with fs and the item's shared memory
         if (threadIdx.x == 0) next_item = atomicAdd(counter, 1) + (int)gridDim.x;

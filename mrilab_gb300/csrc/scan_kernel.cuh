@@ -63,6 +63,10 @@ struct ScanLaunch {
     const int *amap;
     int A;
     double cr, sr;
+    // exact propagator (MRL_NUMERICS_EXACT): per distinct dt (index in the
+    // step flags' bits 8 and up) and voxel, xnf coefficients [dt][xnf][n_act]
+    const float *xtab;
+    int xnf;
     int *err;
     float *hist;            // RunMode 1: [step][Mx|My|Mz][P][S][n_act] from the launch's first step, or null
     long long hist_stride;  // P * S * n_act

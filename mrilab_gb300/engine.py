@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmrl_scan.so")
 
 MODEL = {"normal": 0, "me": 1, "mt": 2, "cest": 3, "gm": 4}
-NUMERICS = {"accurate": 0, "reference": 1}
+NUMERICS = {"accurate": 0, "reference": 1, "exact": 2}
 EXT_FETCH, EXT_PLUGIN = 1, 2
 ABI_VERSION = 1
 
