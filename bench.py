@@ -409,7 +409,7 @@ def main():
     ap.add_argument("--vox-scale", type=float, default=1.0, help="config3: scale of the instance voxel counts")
     ap.add_argument("--c5-size", default="256x256x128", help="config5: voxels NXxNYxNZ")
     ap.add_argument("--n-tr", type=int, default=None, help="TRs of the workload (default: all)")
-    ap.add_argument("--numerics", default="accurate", choices=["accurate", "reference"])
+    ap.add_argument("--numerics", default="accurate", choices=["accurate", "reference", "exact"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
 
