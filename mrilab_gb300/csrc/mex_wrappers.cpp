@@ -101,7 +101,7 @@ bool bind(mrl_scan_args &a) {
         const int *rm = ptr<int>("VCtl", "RunMode");
         a.ctl.run_mode = rm ? *rm : 0;
     }
-    // optional: VCtl.Numerics selects the integrator (0 accurate, 1 reference order)
+    // optional: VCtl.Numerics selects the integrator (0 accurate, 1 reference order, 2 exact propagator)
     const double *num = ptr<double>("VCtl", "Numerics");
     a.ctl.numerics = num ? (int)*num : MRL_NUMERICS_ACCURATE;
 
