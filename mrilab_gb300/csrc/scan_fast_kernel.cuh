@@ -176,18 +176,24 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], 
 // costs more than the rf steps it feeds.
 static __device__ __noinline__ float lineshape_f32(float rf_freq, float db0, float gyro, float t2b) {
     const float a = fmaf((float)(2 * kPiRef), rf_freq, db0 * gyro) * t2b;
-    float g = 0.f, comp = 0.f;
-    for (int p = 0; p < 1000; ++p) {
-        const float u = (float)p * 0.001f;
-        const float den = fmaf(3.f * u, u, -1.f);
-        const float inv = 1.f / den;
-        const float x = a * inv;
-        const float term = fabsf(inv) * __expf(-2.f * x * x) - comp;
-        const float sum = g + term;
-        comp = (sum - g) - term;
-        g = sum;
+    // four interleaved compensated partial sums (u = p / 1000 for p = 4i + j):
+    // independent chains, so the loop is not one serial dependency
+    float g[4] = {0.f, 0.f, 0.f, 0.f}, comp[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int p0 = 0; p0 < 1000; p0 += 4) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float u = (float)(p0 + j) * 0.001f;
+            const float den = fmaf(3.f * u, u, -1.f);
+            const float inv = 1.f / den;
+            const float x = a * inv;
+            const float term = fabsf(inv) * __expf(-2.f * x * x) - comp[j];
+            const float sum = g[j] + term;
+            comp[j] = (sum - g[j]) - term;
+            g[j] = sum;
+        }
     }
-    return g * (0.79788456080286536f * 0.001f) * t2b;  // sqrt(2 / pi) / 1000
+    const float total = ((g[0] - comp[0]) + (g[1] - comp[1])) + ((g[2] - comp[2]) + (g[3] - comp[3]));
+    return total * (0.79788456080286536f * 0.001f) * t2b;  // sqrt(2 / pi) / 1000
 }
 
 // y = 1 - exp(-x).  Relaxation and exchange arguments (dt / T, k dt) are
