@@ -298,6 +298,13 @@ int occupancy_fast(int km, int P, int NS, bool all_free, size_t smem) {
     }
 }
 
+// Receive-tile rows of the accurate kernel's general-model instantiations
+// with bound pools: one per sampled (free) pool, in pool order.
+void set_sampling(FastLaunch &F, const ScanLaunch &L, int P) {
+    F.n_samp = 0;
+    for (int t = 0; t < kMaxPool; ++t) F.samp_rank[t] = (t < P && L.kind[t] == 0) ? F.n_samp++ : -1;
+}
+
 struct ModelInfo {
     int km;        // KModel
     int nsamp;     // pools with a receive signal slot that can be nonzero
@@ -828,6 +835,7 @@ struct Scanner {
         F.omega = d_f2.p + o_om;
         F.txc = d_f2.p + o_txc;
         F.all_free = all_free();
+        set_sampling(F, L, P);
         for (int t = 0; t < kMaxPool; ++t) {  // 2 pi CS[t] as a (hi, lo) pair
             const double w = (t < P && args->ctl.cs) ? 2 * kPiRef * args->ctl.cs[t] : 0.0;
             F.cs_hi[t] = (float)w;
@@ -2227,6 +2235,7 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
     F.b = L;
     F.direct = 1;
     F.all_free = sc.all_free();
+    set_sampling(F, L, sc.P);
     F.rx_x = args->coil.rx_x;
     F.rx_y = args->coil.rx_y;
     F.gam_hi = (float)args->obj.gyro;

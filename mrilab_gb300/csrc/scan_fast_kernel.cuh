@@ -48,6 +48,11 @@ struct FastLaunch {
     const float *rx_x, *rx_y; // [rx][n]
     float gam_hi, gam_lo;     // gyromagnetic ratio split
     float cs_hi[kMaxPool], cs_lo[kMaxPool];  // 2 pi CS[t] split
+    // KM_EXCH with bound pools: the sampled (free) pools get the receive
+    // tile's rows, n_samp per sample; samp_rank[t] = the row of pool t within
+    // a sample, or -1 for a bound pool (its signal is zero)
+    int n_samp;
+    int samp_rank[kMaxPool];
 };
 static_assert(sizeof(FastLaunch) % 4 == 0, "FastLaunch is copied to shared memory as 32-bit words");
 
@@ -290,7 +295,10 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     // per-thread values read only at anchors, state changes and rf steps:
     // the isochromats' dWRnd and the low parts of gamma * (dB0, x, y, z)
     constexpr int kNSampP = kMTC ? 1 : P;
-    constexpr int kTile = (16 / kNSampP) < 1 ? 1 : 16 / kNSampP;  // samples per flush
+    // tile rows per sample and samples per flush (bound pools of KM_EXCH take no row)
+    constexpr bool kRank = MODEL == KM_EXCH && !FREE;
+    const int nsp = kRank ? max(1, F.n_samp) : kNSampP;
+    const int ktile = 16 / nsp;
     constexpr int kTRow = kBlock + 2;                             // padded row (float2)
     constexpr int kWarps = kBlock / 32;
     const int C4 = (L.rx + 3) & ~3;
@@ -522,14 +530,18 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         const float *red = wstage;
         const int nout = a_fill * kNSampP * L.rx;
         for (int o = tid; o < nout; o += kBlock) {
-            const int row = o / L.rx;  // = a * kNSampP + t
-            const int c = o - row * L.rx;
-            const int a = row / kNSampP, t = row - a * kNSampP;
+            const int pr = o / L.rx;  // = a * kNSampP + t
+            const int c = o - pr * L.rx;
+            const int a = pr / kNSampP, t = pr - a * kNSampP;
+            const int rank = kRank ? F.samp_rank[t] : t;
             float sx = 0.f, sy = 0.f;
+            if (rank >= 0) {
+                const int row = a * nsp + rank;
 #pragma unroll
-            for (int w = 0; w < kWarps; ++w) {
-                sx += red[(w * 16 + row) * (2 * C4) + 2 * c];
-                sy += red[(w * 16 + row) * (2 * C4) + 2 * c + 1];
+                for (int w = 0; w < kWarps; ++w) {
+                    sx += red[(w * 16 + row) * (2 * C4) + 2 * c];
+                    sy += red[(w * 16 + row) * (2 * C4) + 2 * c + 1];
+                }
             }
             if (L.dsx) {
                 direct_add(L, a_base + a, t, c, sx, sy);
@@ -708,11 +720,11 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                         sy += Y[s][t];
                     }
                     float2 m = cmul(make_float2(sx, sy), Pc[t]);
-                    const bool sampled = (MODEL != KM_EXCH) || FREE || (L.kind[t] == 0);
-                    if (!(active && sampled)) m = make_float2(0.f, 0.f);
-                    mtile[(a_fill * kNSampP + t) * kTRow + tid] = m;
+                    if (!active) m = make_float2(0.f, 0.f);
+                    const int rank = kRank ? F.samp_rank[t] : t;
+                    if (rank >= 0) mtile[(a_fill * nsp + rank) * kTRow + tid] = m;
                 }
-                if (++a_fill == kTile) flush();
+                if (++a_fill == ktile) flush();
             }
             if (!active) continue;
             if (flags & kFlagCkpt) {  // adjoint checkpoint: the state at the start of the step, lab frame
