@@ -177,6 +177,12 @@ def run_config3(args):
     t0 = time.perf_counter()
     engine.scan_batched(scans)
     e2e_s = time.perf_counter() - t0
+    # the same scans as MRiLab's batch mode runs them (BatchSim.m:160): one
+    # engine call per instance, host buffers
+    t0 = time.perf_counter()
+    for sc in scans:
+        engine.scan(sc)
+    plain_e2e_s = time.perf_counter() - t0
     # FP32 algorithmic work from the op table (every saturation step has rf on)
     flops = mufu = 0.0
     for sc, m in zip(scans, meta):
@@ -197,8 +203,12 @@ def run_config3(args):
                                "1/40, 10 us raster, 3 T" % args.vox_scale, "instances": len(scans),
                    "voxels": int(np.sum(vox)), "units_per_step": work["units"], "steps_per_step": work["steps"],
                    "l2": "flushed between timed steps (256 MiB write)", "tune_s": tune_s},
-        "plain": {"value": work["units"] / (ms_p * 1e-3), "ms_per_step": ms_p, "launches": work["plain_launches"]},
+        "plain": {"value": work["units"] / (ms_p * 1e-3), "ms_per_step": ms_p, "launches": work["plain_launches"],
+                  "form": "device: one launch and one reduction per instance, back to back on one stream",
+                  "e2e_ms_per_step": plain_e2e_s * 1e3,
+                  "e2e_form": "one mrl_scan call per instance with host buffers (MRiLab's batch mode)"},
         "batched_over_plain": ms_p / ms_b,
+        "batched_over_plain_e2e": plain_e2e_s / e2e_s,
         "e2e": {"value": work["units"] / e2e_s, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
                 "api": "mrl_scan_batched with host buffers"},
         "gpu_launches": work["launches"] * args.steps,
