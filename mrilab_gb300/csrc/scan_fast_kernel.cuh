@@ -56,6 +56,12 @@ struct FastLaunch {
 };
 static_assert(sizeof(FastLaunch) % 4 == 0, "FastLaunch is copied to shared memory as 32-bit words");
 
+// Coil sensitivities in shared memory: up to 16 coils (C4 <= 16) already
+// split into TF32 (big, small) pairs for the receive contraction; beyond,
+// as plain float2 split in the flush, which halves their footprint (32
+// coils: 33 KB instead of 66 KB, three blocks per SM instead of two).
+__host__ __device__ constexpr bool coil_presplit(int c4) { return c4 <= 16; }
+
 // ---- double-float helpers ------------------------------------------------
 struct df {
     float hi, lo;
@@ -303,9 +309,12 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     constexpr int kWarps = kBlock / 32;
     const int C4 = (L.rx + 3) & ~3;
     float2 *mtile = reinterpret_cast<float2 *>(rbuf + 2 * chunk * rstride);  // [16][kTRow]
-    // coil sensitivities as TF32 (big, small) pairs: [C4][kTRow][rx, ry]
+    // coil sensitivities: TF32 (big, small) pairs [C4][kTRow][rx, ry], or
+    // float2 [C4][kTRow] beyond 16 coils (coil_presplit)
+    const bool presplit = coil_presplit(C4);
     uint2 *rsq = reinterpret_cast<uint2 *>(mtile + 16 * kTRow);
-    float *wstage = reinterpret_cast<float *>(rsq + 2 * C4 * kTRow);               // [warp][16][2*C4]
+    float2 *rsf = reinterpret_cast<float2 *>(rsq);
+    float *wstage = reinterpret_cast<float *>(rsq + (presplit ? 2 : 1) * C4 * kTRow);  // [warp][16][2*C4]
     float *dwsm = wstage + kWarps * 16 * 2 * C4;                                   // [NS * P][kBlock]
     float *omlo = dwsm + NS * P * kBlock;                                        // [4][kBlock]
 
@@ -427,9 +436,13 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
             else
                 r = L.rxc[(long long)c * n + v];
         }
-        const uint32_t bx = tf32_rn(r.x), by = tf32_rn(r.y);
-        rsq[2 * (c * kTRow + tid) + 0] = make_uint2(bx, tf32_rn(r.x - __uint_as_float(bx)));
-        rsq[2 * (c * kTRow + tid) + 1] = make_uint2(by, tf32_rn(r.y - __uint_as_float(by)));
+        if (presplit) {
+            const uint32_t bx = tf32_rn(r.x), by = tf32_rn(r.y);
+            rsq[2 * (c * kTRow + tid) + 0] = make_uint2(bx, tf32_rn(r.x - __uint_as_float(bx)));
+            rsq[2 * (c * kTRow + tid) + 1] = make_uint2(by, tf32_rn(r.y - __uint_as_float(by)));
+        } else {
+            rsf[c * kTRow + tid] = r;
+        }
     }
     // the isochromats enter their frames at the first step: m_frame = m_lab / P_t
     bool entered = false;
@@ -481,6 +494,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         const uint32_t sgn = (cmp && !ri) ? 0x80000000u : 0u;  // -ry
         const float *mt1 = reinterpret_cast<const float *>(mtile) + ri;
         const uint2 *rs1 = rsq + bcomp;
+        const float *rf1 = reinterpret_cast<const float *>(rsf) + bcomp;
         const int nt_all = C4 / 4;
         float *rw = wstage + warp * 16 * (2 * C4);
         // n-tiles (4 coils each) in groups of kNG: the magnetisation operand
@@ -508,9 +522,18 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 for (int u = 0; u < kNG; ++u) {
                     if (nt0 + u >= nt_all) break;
                     const int c = (nt0 + u) * 4 + (g >> 1);
-                    // the coil operand was split once per launch; -ry flips the signs
-                    const uint2 q0 = rs1[2 * (c * kTRow + j0)], q1 = rs1[2 * (c * kTRow + j1)];
-                    const uint32_t bb[2] = {q0.x ^ sgn, q1.x ^ sgn}, bs[2] = {q0.y ^ sgn, q1.y ^ sgn};
+                    // the coil operand (split once per launch up to 16 coils, here
+                    // beyond); -ry flips the signs of both parts
+                    uint32_t bb[2], bs[2];
+                    if (presplit) {
+                        const uint2 q0 = rs1[2 * (c * kTRow + j0)], q1 = rs1[2 * (c * kTRow + j1)];
+                        bb[0] = q0.x ^ sgn, bb[1] = q1.x ^ sgn, bs[0] = q0.y ^ sgn, bs[1] = q1.y ^ sgn;
+                    } else {
+                        const float b0 = rf1[2 * (c * kTRow + j0)], b1 = rf1[2 * (c * kTRow + j1)];
+                        const uint32_t h0 = tf32_rn(b0), h1 = tf32_rn(b1);
+                        bb[0] = h0 ^ sgn, bb[1] = h1 ^ sgn;
+                        bs[0] = tf32_rn(b0 - __uint_as_float(h0)) ^ sgn, bs[1] = tf32_rn(b1 - __uint_as_float(h1)) ^ sgn;
+                    }
                     mma_tf32(accs[u], as, bb);
                     mma_tf32(accs[u], ab, bs);
                     mma_tf32(accb[u], ab, bb);

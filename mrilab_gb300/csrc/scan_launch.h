@@ -37,7 +37,7 @@ inline size_t scan_fast_smem_bytes(int stride4, int rx, int P, int NS) {
     const size_t c4 = (size_t)((rx + 3) & ~3);
     const size_t row = kBlock + 2;
     return 128 + (size_t)2 * kFastChunk * stride4 * 16  // staged step records
-           + 16 * row * 8 + c4 * row * 16           // receive tile, coil maps (TF32 big, small)
+           + 16 * row * 8 + c4 * row * (coil_presplit((int)c4) ? 16 : 8)  // receive tile, coil maps
            + (kBlock / 32) * 16 * 2 * c4 * 4        // per-warp receive sums
            + ((size_t)NS * P + 4) * kBlock * 4;     // dWRnd, low parts of omega
 }

@@ -375,3 +375,20 @@ def test_mt_epi_matches_fp64_oracle(built):
     port32 = rel_l2(signal(oracle.run_port(sc, "f32")), signal(ref))
     print(f"MT EPI shrunk: relative L2 {err:.2e} (reference algorithm in FP32: {port32:.2e})")
     assert err <= 2e-5 and err < port32
+
+
+@pytest.mark.gpu
+def test_many_coil_receive_matches_fp64_oracle(built):
+    """More than 16 Rx coils: the coil maps stay float2 in shared memory and
+    are split into TF32 parts in the receive flush (up to 16 they are split
+    once per launch).  Against the all-FP64 oracle."""
+    from mrilab_gb300 import engine, phantoms
+    import oracle
+
+    sc = phantoms.small_multipool("me", seed=61, n=8, pools=2, spins=2, coils=20, n_tr=2)
+    assert int(sc.VCoi["RxCoilNum"]) == 20
+    ref = oracle.run_port(sc, "f64")
+    out = engine.scan(sc)
+    err = rel_l2(signal(out), signal(ref))
+    print(f"20 coils: relative L2 {err:.2e}")
+    assert err <= 1e-5
