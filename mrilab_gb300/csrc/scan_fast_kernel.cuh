@@ -62,6 +62,11 @@ static_assert(sizeof(FastLaunch) % 4 == 0, "FastLaunch is copied to shared memor
 // coils: 33 KB instead of 66 KB, three blocks per SM instead of two).
 __host__ __device__ constexpr bool coil_presplit(int c4) { return c4 <= 16; }
 
+template <bool B>
+struct BoolTag {
+    static constexpr bool value = B;
+};
+
 // ---- double-float helpers ------------------------------------------------
 struct df {
     float hi, lo;
@@ -487,7 +492,10 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     // sample, pool, coil) is written.
     //   A[row][2j + ri] = (x, y)[ri] of thread j;  B[2j + ri][2c + cmp]:
     //   (x,x) = rx, (y,x) = ry, (x,y) = -ry, (y,y) = rx.
-    auto flush = [&]() {
+    // the flush in two compiled forms, one per coil-map layout (a branch
+    // inside its loops cost the 8-coil scan 4 %)
+    auto flush_form = [&](auto pre_tag) {
+        constexpr bool pre = decltype(pre_tag)::value;
         __syncthreads();
         const int g = lane >> 2, tig = lane & 3, ri = tig & 1, cmp = g & 1;
         const int bcomp = (ri == cmp) ? 0 : 1;                 // rx, else ry
@@ -525,7 +533,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     // the coil operand (split once per launch up to 16 coils, here
                     // beyond); -ry flips the signs of both parts
                     uint32_t bb[2], bs[2];
-                    if (presplit) {
+                    if (pre) {
                         const uint2 q0 = rs1[2 * (c * kTRow + j0)], q1 = rs1[2 * (c * kTRow + j1)];
                         bb[0] = q0.x ^ sgn, bb[1] = q1.x ^ sgn, bs[0] = q0.y ^ sgn, bs[1] = q1.y ^ sgn;
                     } else {
@@ -575,6 +583,12 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         a_base += a_fill;
         a_fill = 0;
         __syncthreads();
+    };
+    auto flush = [&]() {
+        if (presplit)
+            flush_form(BoolTag<true>{});
+        else
+            flush_form(BoolTag<false>{});
     };
 
     for (int k = 0; k < nchunks; ++k) {
