@@ -279,8 +279,14 @@ struct DevBuf {
     }
 };
 
+// Coefficient source of the accurate integrator (scan_item): the split
+// scheme's table for free pools exchanging with at most three pools, else
+// computed in the kernel.
+inline int split_source(int km, int P, bool all_free) { return km == KM_EXCH && all_free && P <= 3 ? 1 : 0; }
+
 cudaError_t launch_fast(int km, int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
-                        const FastGrid &g) {
+                        const FastGrid &g, int co = 0) {
+    if (co) return launch_scan_fast_tab(co, P, NS, grid, smem, st, g);
     switch (km) {
     case KM_NORMAL: return launch_scan_fast_normal(P, NS, all_free, grid, smem, st, g);
     case KM_EXCH: return launch_scan_fast_exch(P, NS, all_free, grid, smem, st, g);
@@ -289,7 +295,8 @@ cudaError_t launch_fast(int km, int P, int NS, bool all_free, dim3 grid, size_t 
     }
 }
 
-int occupancy_fast(int km, int P, int NS, bool all_free, size_t smem) {
+int occupancy_fast(int km, int P, int NS, bool all_free, size_t smem, int co = 0) {
+    if (co) return occupancy_scan_fast_tab(co, P, NS, smem);
     switch (km) {
     case KM_NORMAL: return occupancy_scan_fast_normal(P, NS, all_free, smem);
     case KM_EXCH: return occupancy_scan_fast_exch(P, NS, all_free, smem);
@@ -385,6 +392,7 @@ struct Scanner {
     // exact relaxation-exchange propagator: its coefficient table per
     // (distinct float dt, voxel) and the dt values so far (index = position)
     bool exact = false;
+    int coef = 0;  // coefficient source: 0 in the kernel, 1 split-scheme table, 2 exact table
     std::map<uint32_t, int> xdt_index;
     std::vector<float> xdts;
     DevBuf<float> d_xdts, d_xtab;
@@ -478,6 +486,7 @@ struct Scanner {
                        MRL_ERR_UNSUPPORTED;
             if (P > 3) return set_err("MRL_NUMERICS_EXACT supports TypeNum <= 3"), MRL_ERR_UNSUPPORTED;
         }
+        coef = exact ? 2 : (fast ? split_source(mi.km, P, all_free() != 0) : 0);
         hist_on = a.ctl.run_mode == 1;  // other values scan normally, as in the reference's switch
         if (hist_on && !fast)
             return set_err("RunMode 1 (per-step history) needs MRL_NUMERICS_ACCURATE"), MRL_ERR_UNSUPPORTED;
@@ -724,7 +733,7 @@ struct Scanner {
     // Exact propagator: the index of every step's float dt in its flags (bits
     // 8 and up), and the coefficient table of every dt value so far (FP64
     // exponentials, one thread per (dt, voxel)).
-    int exact_coefficients(std::vector<float> &rec) {
+    int tab_coefficients(std::vector<float> &rec) {
         const int stride = fast_stride_f4(TX) * 4;
         const size_t n_before = xdts.size();
         for (size_t q = 0; q < rec.size() / stride; ++q) {
@@ -750,12 +759,16 @@ struct Scanner {
         cudaError_t e = d_xdts.ensure(xdts.size());
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(d_xdts.p, xdts.data(), xdts.size() * sizeof(float), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = d_xtab.ensure(xdts.size() * (size_t)exact_fields(P) * n_act);
+        const int nf = coef == 2 ? exact_fields(P) : split_fields(P);
+        if (e == cudaSuccess) e = d_xtab.ensure(xdts.size() * (size_t)nf * n_act);
+        const float *kch = mi.nk > 0 ? d_f.p + o_k : nullptr;
         if (e == cudaSuccess)
-            e = launch_exact_table(P, d_xdts.p, (int)xdts.size(), n_act, S, mi.gm ? 1 : 0, d_f.p + o_rho,
-                                   d_f.p + o_t1, d_f.p + o_t2, mi.nk > 0 ? d_f.p + o_k : nullptr, d_xtab.p, st);
+            e = coef == 2 ? launch_exact_table(P, d_xdts.p, (int)xdts.size(), n_act, S, mi.gm ? 1 : 0,
+                                               d_f.p + o_rho, d_f.p + o_t1, d_f.p + o_t2, kch, d_xtab.p, st)
+                          : launch_split_table(P, d_xdts.p, (int)xdts.size(), n_act, mi.gm ? 1 : 0,
+                                               d_f.p + o_rho, d_f.p + o_t1, d_f.p + o_t2, kch, d_xtab.p, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) return fail_cuda(e, "exact propagator table");
+        if (e != cudaSuccess) return fail_cuda(e, "coefficient table");
         return MRL_OK;
     }
 
@@ -800,8 +813,8 @@ struct Scanner {
         if (fast) {
             pack_fast_records(ch, TX, fmom, frec, ckpt_every);
             recs = &frec;
-            if (exact) {
-                const int rc = exact_coefficients(frec);
+            if (coef) {
+                const int rc = tab_coefficients(frec);
                 if (rc) return rc;
             }
         }
@@ -856,8 +869,8 @@ struct Scanner {
         L.hist = hist_on ? d_hist.p + (hist_steps + d.s0) * 3 * L.hist_stride : nullptr;
         L.ckpt = ckpt;
         L.ckpt_step0 = d.s0;
-        L.xtab = exact ? d_xtab.p : nullptr;
-        L.xnf = exact_fields(P);
+        L.xtab = coef ? d_xtab.p : nullptr;
+        L.xnf = coef == 2 ? exact_fields(P) : split_fields(P);
         if (direct_rx) {
             L.dsx = d_sx.p;
             L.dsy = d_sy.p;
@@ -908,8 +921,7 @@ struct Scanner {
                 dim3 grid(nblk);
                 if (fast) {
                     const FastGrid g{d_desc.p + li, nullptr, nblk, nullptr};
-                    e = exact ? launch_scan_fast_exact(P, NS, grid, smem, stream, g)
-                              : launch_fast(mi.km, P, NS, all_free() != 0, grid, smem, stream, g);
+                    e = launch_fast(mi.km, P, NS, all_free() != 0, grid, smem, stream, g, coef);
                 } else {
                     switch (mi.km) {
                     case KM_NORMAL: e = launch_scan_ref_normal(P, NS, grid, smem, stream, L); break;
@@ -1366,7 +1378,7 @@ int batch_build(mrl_batch &b, long long max_steps) {
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b.st);
         if (e != cudaSuccess) return set_err("batch setup: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
-        const int occ = occupancy_fast(g.km, g.P, g.NS, g.free, g.smem);
+        const int occ = occupancy_fast(g.km, g.P, g.NS, g.free, g.smem, split_source(g.km, g.P, g.free));
         if (occ < 1) return set_err("batch: kernel does not fit (%zu bytes of shared memory)", g.smem), MRL_ERR_UNSUPPORTED;
         const int per_sm = g.cap > 0 ? std::min(g.cap, occ) : occ;
         g.grid = std::max(1, std::min(g.n_items, per_sm * b.sms));
@@ -1416,7 +1428,7 @@ int batch_record(mrl_batch &b, cudaStream_t s, bool reduce) {
         e = cudaStreamWaitEvent(g.st, b.fork, 0);
         if (e == cudaSuccess && g.n_items > 0)
             e = launch_fast(g.km, g.P, g.NS, g.free, dim3(g.grid), g.smem, g.st,
-                            FastGrid{g.descs.p, g.items.p, g.n_items, g.counter.p});
+                            FastGrid{g.descs.p, g.items.p, g.n_items, g.counter.p}, split_source(g.km, g.P, g.free));
         if (e == cudaSuccess) e = cudaEventRecord(g.done, g.st);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g.done, 0);
     }
@@ -1692,7 +1704,7 @@ int mrl_batch_execute(mrl_batch *b, int mode, void *stream) {
         if (e != cudaSuccess || sc.n_act == 0) continue;
         const int nblk = (int)sc.n_blocks();
         e = launch_fast(g.km, g.P, g.NS, g.free, dim3(nblk), scan_fast_smem_bytes(sc.stride4, sc.RX, sc.P, sc.NS), s,
-                        FastGrid{g.descs.p + it.slot, nullptr, nblk, nullptr});
+                        FastGrid{g.descs.p + it.slot, nullptr, nblk, nullptr}, split_source(g.km, g.P, g.free));
         const mrl::Scanner::LaunchDesc &d = it.ls[0];
         if (e == cudaSuccess && d.a_count > 0) {
             const int npairs = sc.mi.nsamp * sc.RX;
@@ -1739,7 +1751,7 @@ int mrl_batch_tune(mrl_batch *b, void *stream) {
             }
             if ((rc = batch_build(*b, kTrialSteps))) break;
             mrl_batch::Group &g = b->groups[b->in[set[0]].group];
-            const int occ = occupancy_fast(g.km, g.P, g.NS, g.free, g.smem);
+            const int occ = occupancy_fast(g.km, g.P, g.NS, g.free, g.smem, split_source(g.km, g.P, g.free));
             for (int cap : {occ, occ - 1}) {
                 if (cap < 1 || g.n_items == 0) continue;
                 const int grid = std::max(1, std::min(g.n_items, cap * b->sms));
@@ -1753,7 +1765,7 @@ int mrl_batch_tune(mrl_batch *b, void *stream) {
                     if (e == cudaSuccess) e = cudaEventRecord(e0, b->st);
                     if (e == cudaSuccess)
                         e = launch_fast(g.km, g.P, g.NS, g.free, dim3(grid), g.smem, b->st,
-                                        FastGrid{g.descs.p, g.items.p, g.n_items, g.counter.p});
+                                        FastGrid{g.descs.p, g.items.p, g.n_items, g.counter.p}, split_source(g.km, g.P, g.free));
                     if (e == cudaSuccess) e = cudaEventRecord(e1, b->st);
                     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
                     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);

@@ -1,6 +1,8 @@
-// Exact relaxation-exchange propagator: the accurate scan kernel's
-// instantiations for free pools exchanging with MRL_NUMERICS_EXACT, and the
-// FP64 kernel that tabulates each voxel's propagator per distinct dt.
+// Tabulated coefficients for free pools exchanging: the accurate scan
+// kernel's instantiations that read their relaxation / exchange step from a
+// table per (distinct dt, voxel) -- the reference's split exchange
+// (MRL_NUMERICS_ACCURATE, coefficient source 1) and the exact propagator
+// (MRL_NUMERICS_EXACT, source 2) -- and the FP64 kernels that fill the tables.
 //
 // Per step every pool is rotated exactly (rf or free precession, as in the
 // accurate mode), then the Bloch-McConnell equations without the rotation
@@ -19,19 +21,20 @@ namespace {
 using Kernel = void (*)(const FastLaunch *, const int2 *, int, int *);
 
 template <int P, int NS>
-Kernel pick() {
-    return scan_fast_kernel<KM_EXCH, P, NS, true, true>;
+Kernel pick(int co) {
+    return co == 2 ? scan_fast_kernel<KM_EXCH, P, NS, true, 2> : scan_fast_kernel<KM_EXCH, P, NS, true, 1>;
 }
 
-Kernel select(int P, int NS) {
-    if (P == 1 && NS == 1) return pick<1, 1>();
-    if (P == 1 && NS == 2) return pick<1, 2>();
-    if (P == 1 && NS == 4) return pick<1, 4>();
-    if (P == 2 && NS == 1) return pick<2, 1>();
-    if (P == 2 && NS == 2) return pick<2, 2>();
-    if (P == 2 && NS == 4) return pick<2, 4>();
-    if (P == 3 && NS == 1) return pick<3, 1>();
-    if (P == 3 && NS == 2) return pick<3, 2>();
+Kernel select(int co, int P, int NS) {
+    if (co != 1 && co != 2) return nullptr;
+    if (P == 1 && NS == 1) return pick<1, 1>(co);
+    if (P == 1 && NS == 2) return pick<1, 2>(co);
+    if (P == 1 && NS == 4) return pick<1, 4>(co);
+    if (P == 2 && NS == 1) return pick<2, 1>(co);
+    if (P == 2 && NS == 2) return pick<2, 2>(co);
+    if (P == 2 && NS == 4) return pick<2, 4>(co);
+    if (P == 3 && NS == 1) return pick<3, 1>(co);
+    if (P == 3 && NS == 2) return pick<3, 2>(co);
     return nullptr;
 }
 
@@ -177,10 +180,73 @@ __global__ void exact_table_kernel(const float *__restrict__ dts, int n_dt, int 
         o[(long long)(f++) * n_act] = (float)(dt * c);
     }
 }
+// The split scheme's coefficients (BlochKernelME.cuh:320-343, as the
+// accurate kernel computes them at a dt change) in FP64 per (dt, voxel):
+// y1 = 1 - e^{-dt/T1}, y2 = 1 - e^{-dt/T2}, yo = 1 - e^{-dt sum of the
+// outgoing rates}, fin[t][p] = 1 - e^{-dt k(p -> t)}; zero for a pool left
+// alone (T1, T2 or Rho zero).
+template <int P>
+__global__ void split_table_kernel(const float *__restrict__ dts, int n_dt, int n_act, int gm,
+                                   const float *__restrict__ rho, const float *__restrict__ t1,
+                                   const float *__restrict__ t2, const float *__restrict__ kch, float *tab) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)n_dt * n_act) return;
+    const int d = (int)(i / n_act), v = (int)(i % n_act);
+    const double dt = dts[d];
+    double y1[P], y2[P], yo[P], fin[P][P];
+#pragma unroll
+    for (int t = 0; t < P; ++t) {
+        y1[t] = y2[t] = yo[t] = 0.0;
+#pragma unroll
+        for (int p = 0; p < P; ++p) fin[t][p] = 0.0;
+        const double T1 = t1[(long long)t * n_act + v], T2 = t2[(long long)t * n_act + v],
+                     r = rho[(long long)t * n_act + v];
+        if (T1 == 0.0 || T2 == 0.0 || r == 0.0) continue;
+        y1[t] = -expm1(-dt / T1);
+        y2[t] = -expm1(-dt / T2);
+        double ksum = 0.0;
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+            if ((gm && p == t) || !kch) continue;
+            // ME: channel a*P+b is the rate a -> b; GM: channel b*P+a
+            const double kgo = kch[(long long)(gm ? p * P + t : t * P + p) * n_act + v];
+            const double kin = kch[(long long)(gm ? t * P + p : p * P + t) * n_act + v];
+            ksum += kgo;
+            if (kin != 0.0) fin[t][p] = -expm1(-dt * kin);
+        }
+        yo[t] = -expm1(-dt * ksum);
+    }
+    float *o = tab + (long long)d * split_fields(P) * n_act + v;
+    int f = 0;
+#pragma unroll
+    for (int t = 0; t < P; ++t) o[(long long)(f++) * n_act] = (float)y1[t];
+#pragma unroll
+    for (int t = 0; t < P; ++t) o[(long long)(f++) * n_act] = (float)y2[t];
+#pragma unroll
+    for (int t = 0; t < P; ++t) o[(long long)(f++) * n_act] = (float)yo[t];
+#pragma unroll
+    for (int t = 0; t < P; ++t)
+#pragma unroll
+        for (int p = 0; p < P; ++p) o[(long long)(f++) * n_act] = (float)fin[t][p];
+}
 }  // namespace
 
-cudaError_t launch_scan_fast_exact(int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastGrid &g) {
-    Kernel k = select(P, NS);
+cudaError_t launch_split_table(int P, const float *dts, int n_dt, int n_act, int gm, const float *rho,
+                               const float *t1, const float *t2, const float *kch, float *tab, cudaStream_t st) {
+    const long long n = (long long)n_dt * n_act;
+    if (n <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((n + 127) / 128);
+    switch (P) {
+    case 1: split_table_kernel<1><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, gm, rho, t1, t2, kch, tab); break;
+    case 2: split_table_kernel<2><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, gm, rho, t1, t2, kch, tab); break;
+    case 3: split_table_kernel<3><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, gm, rho, t1, t2, kch, tab); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_fast_tab(int co, int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastGrid &g) {
+    Kernel k = select(co, P, NS);
     if (!k) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -188,8 +254,8 @@ cudaError_t launch_scan_fast_exact(int P, int NS, dim3 grid, size_t smem, cudaSt
     return cudaGetLastError();
 }
 
-int occupancy_scan_fast_exact(int P, int NS, size_t smem) {
-    Kernel k = select(P, NS);
+int occupancy_scan_fast_tab(int co, int P, int NS, size_t smem) {
+    Kernel k = select(co, P, NS);
     int n = 0;
     if (!k || cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kBlock, smem) != cudaSuccess)

@@ -291,9 +291,14 @@ __host__ __device__ constexpr int fast_min_blocks() {
 // described by F, over F's step range.  kbase counts the record chunks this
 // block has staged before (it picks the buffer and mbarrier phase).
 // Returns false, block-uniformly, when a wait ran out (status word raised).
-template <int MODEL, int P, int NS, bool FREE, bool EXACT = false>
+// Coefficient source CO of the relaxation / exchange step: 0 computed in the
+// kernel at each dt change; 1 the same split-exchange coefficients from a
+// table per (dt, voxel) computed in FP64 (fewer live registers: no rates or
+// relaxation rates held); 2 the exact propagator's table (EXACT).
+template <int MODEL, int P, int NS, bool FREE, int CO = 0>
 __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigned char *smem, uint32_t &kbase) {
-    static_assert(!EXACT || (MODEL == KM_EXCH && FREE), "the exact propagator covers free pools exchanging");
+    constexpr bool EXACT = CO == 2;
+    static_assert(CO == 0 || (MODEL == KM_EXCH && FREE), "tabulated coefficients cover free pools exchanging");
     const ScanLaunch &L = F.b;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     float4 *rbuf = reinterpret_cast<float4 *>(smem + 128);
@@ -664,6 +669,21 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     for (int p = 0; p < kXP; ++p) fL[t][p] = p == t ? 0.f : xt[(long long)(f++) * n];
 #pragma unroll
                 for (int t = 0; t < kXP; ++t) cL[t] = xt[(long long)(f++) * n];
+            } else if (active && (flags & kFlagDt) && CO == 1) {
+                // the split scheme's coefficients of this dt from the table
+                // [dt][field][n_act]: y1[P], y2[P], yo[P], fin[P][P]
+                const float *xt = L.xtab + (long long)(flags >> 8) * L.xnf * n + v;
+                int f = 0;
+#pragma unroll
+                for (int t = 0; t < P; ++t) y1[t] = xt[(long long)(f++) * n];
+#pragma unroll
+                for (int t = 0; t < P; ++t) y2[t] = xt[(long long)(f++) * n];
+#pragma unroll
+                for (int t = 0; t < P; ++t) yo[t] = xt[(long long)(f++) * n];
+#pragma unroll
+                for (int t = 0; t < P; ++t)
+#pragma unroll
+                    for (int p = 0; p < P; ++p) fin[t][p] = xt[(long long)(f++) * n];
             } else if (active && (flags & kFlagDt)) {
 #pragma unroll
                 for (int t = 0; t < P; ++t) {
@@ -1072,7 +1092,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 // takes items gridDim.x, gridDim.x + 1, ... from *counter (the batched
 // form: the tiles of many scans, ordered longest first).  Each item's
 // descriptor is copied from descs into shared memory.
-template <int MODEL, int P, int NS, bool FREE, bool EXACT = false>
+template <int MODEL, int P, int NS, bool FREE, int CO = 0>
 __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>())
     scan_fast_kernel(const FastLaunch *__restrict__ descs, const int2 *__restrict__ items, int n_items, int *counter) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1091,7 +1111,7 @@ __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>())
         int *dst = reinterpret_cast<int *>(&fs);
         for (int w = threadIdx.x; w < (int)(sizeof(FastLaunch) / 4); w += blockDim.x) dst[w] = src[w];
         __syncthreads();
-        if (!scan_item<MODEL, P, NS, FREE, EXACT>(fs, item.y, smem, kbase)) return;
+        if (!scan_item<MODEL, P, NS, FREE, CO>(fs, item.y, smem, kbase)) return;
         if (counter == nullptr) break;
         __syncthreads();  // every thread is done with fs and the item's shared memory
         if (threadIdx.x == 0) next_item = atomicAdd(counter, 1) + (int)gridDim.x;
