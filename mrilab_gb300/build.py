@@ -106,7 +106,7 @@ def build(verbose: bool = False, jobs: int = 0) -> None:
             if verbose and out:
                 print(out)
     if _stale(LIB, objs):
-        _run([nvcc, "-shared", *GENCODE, "-o", LIB, *objs, "-lcudart"])
+        _run([nvcc, "-shared", *GENCODE, "-o", LIB, *objs, "-lcudart", "-lpthread"])
     peaks_src = os.path.join(CSRC, "peaks.cu")
     if _stale(PEAKS, [peaks_src]):
         _run([nvcc, "-std=c++17", "-O3", *GENCODE, "-Xcompiler", "-fPIC", "-shared", peaks_src, "-o", PEAKS])

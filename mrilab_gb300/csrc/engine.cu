@@ -22,7 +22,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <map>
+#include <thread>
 #include <memory>
 #include <mutex>
 #include <tuple>
@@ -360,6 +362,7 @@ struct Scanner {
     RawObject raw{};
     size_t o_om = 0, o_txc = 0;
     std::vector<float> frec;
+    bool frec_ready = false;  // frec packed ahead (batches pack on host threads)
     // offsets into d_f
     size_t o_gx = 0, o_gy = 0, o_gz = 0, o_db0 = 0, o_txmg = 0, o_txpe = 0, o_rho = 0, o_t1 = 0, o_t2 = 0, o_k = 0,
            o_dwr = 0;
@@ -811,7 +814,8 @@ struct Scanner {
         a_peak = std::max(a_peak, a_cnt);
         const std::vector<float> *recs = &ch.records;
         if (fast) {
-            pack_fast_records(ch, TX, fmom, frec, ckpt_every);
+            if (!frec_ready) pack_fast_records(ch, TX, fmom, frec, ckpt_every);
+            frec_ready = false;
             recs = &frec;
             if (coef) {
                 const int rc = tab_coefficients(frec);
@@ -1625,24 +1629,55 @@ int mrl_batch_create(mrl_scan_args *const *args, int n, mrl_batch **out) {
         sc.own_st = false;
         sc.partial_budget = 1e18;  // one launch per instance
         sc.no_direct = true;       // the batch reduces every instance's partials in one kernel
+        const int rc = sc.validate();
+        if (rc) {
+            const std::string why = g_err;
+            set_err("instance %d: %s", i, why.c_str());
+            return rc;
+        }
+    }
+    // the instances' sequences decoded and their records packed on host threads
+    // (independent per instance; the host's share of a batch of long trains)
+    std::vector<DecodeChunk> chunks(n);
+    {
+        std::atomic<int> next{0};
+        auto work = [&]() {
+            for (int i; (i = next.fetch_add(1)) < n;) {
+                mrl_batch::Inst &it = b->in[i];
+                Scanner &sc = *it.sc;
+                it.kx.assign(std::max(sc.A, 1), 0.0);
+                it.ky.assign(std::max(sc.A, 1), 0.0);
+                it.kz.assign(std::max(sc.A, 1), 0.0);
+                mrl_signal sig = it.args.sig;
+                sig.kx = it.kx.data();
+                sig.ky = it.ky.data();
+                sig.kz = it.kz.data();
+                DecodeState ds;
+                mrl_state none{};
+                load_state(ds, none, sc.TX);
+                decode_until_ext(ds, it.args.seq, sc.TX, it.args.obj.gyro, sig, chunks[i]);
+                if (!chunks[i].stopped_at_ext && sc.fast) {
+                    pack_fast_records(chunks[i], sc.TX, sc.fmom, sc.frec, sc.ckpt_every);
+                    sc.frec_ready = true;
+                }
+            }
+        };
+        const int nth = (int)std::max(1u, std::min<unsigned>((unsigned)n, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nth; ++t) pool.emplace_back(work);
+        work();
+        for (std::thread &t : pool) t.join();
+    }
+    for (int i = 0; i < n; ++i) {
+        mrl_batch::Inst &it = b->in[i];
+        Scanner &sc = *it.sc;
         int rc = sc.setup();
         if (rc) {
             const std::string why = g_err;
             set_err("instance %d: %s", i, why.c_str());
             return rc;
         }
-        it.kx.assign(std::max(sc.A, 1), 0.0);
-        it.ky.assign(std::max(sc.A, 1), 0.0);
-        it.kz.assign(std::max(sc.A, 1), 0.0);
-        mrl_signal sig = it.args.sig;
-        sig.kx = it.kx.data();
-        sig.ky = it.ky.data();
-        sig.kz = it.kz.data();
-        DecodeState ds;
-        mrl_state none{};
-        load_state(ds, none, sc.TX);
-        DecodeChunk ch;
-        decode_until_ext(ds, it.args.seq, sc.TX, it.args.obj.gyro, sig, ch);
+        const DecodeChunk &ch = chunks[i];
         if (ch.stopped_at_ext) return set_err("instance %d: the sequence has Ext events", i), MRL_ERR_UNSUPPORTED;
         if ((rc = sc.prepare_chunk(ch, it.ls))) return rc;
         if (it.ls.size() != 1) return set_err("instance %d: receive partials do not fit one launch", i), MRL_ERR_NOMEM;
