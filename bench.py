@@ -222,6 +222,42 @@ def run_config3(args):
     print(json.dumps(line))
 
 
+def time_adjoint_plan(plan, tx, ty, steps, warmup):
+    """Device time of an adjoint plan's forward scan (writing the
+    checkpoints) and adjoint kernel, each bracketed by CUDA events on the
+    launching stream with L2 flushed before it; the loss is the L2 distance
+    of the signal to (tx, ty).  Returns the per-step lists (ms)."""
+    import torch
+
+    stream = torch.cuda.Stream()
+    flush = torch.empty(int(256 * 2**20), dtype=torch.uint8, device="cuda")
+
+    def event_pair():
+        return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    fwd, adj = [], []
+    for i in range(max(3, warmup) + steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        (f0, f1), (b0, b1) = event_pair(), event_pair()
+        f0.record(stream)
+        plan.forward(stream.cuda_stream)
+        f1.record(stream)
+        stream.synchronize()
+        out = plan.signal()
+        gx, gy = 2 * (out["Sx"] - tx), 2 * (out["Sy"] - ty)
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        b0.record(stream)
+        plan.backward(gx, gy, stream.cuda_stream)
+        b1.record(stream)
+        b1.synchronize()
+        if i >= max(3, warmup):
+            fwd.append(f0.elapsed_time(f1))
+            adj.append(b0.elapsed_time(b1))
+    return fwd, adj
+
+
 def run_config4(args):
     """fwd+adjoint on the bSSFP adjoint workload (96 x 96 x 16 voxels, 2
     spins, free + short-T2 water exchanging, 4 Rx, 200 TRs with a
@@ -241,34 +277,7 @@ def run_config4(args):
     tx, ty = target["Sx"], target["Sy"]
     plan = engine.AdjointPlan(sc)
     work = plan.work()
-    stream = torch.cuda.Stream()
-    flush = torch.empty(int(256 * 2**20), dtype=torch.uint8, device="cuda")
-
-    def event_pair():
-        return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-
-    # device time: the forward scan (writing the checkpoints) and the adjoint
-    # kernel, each bracketed by CUDA events on the launching stream, L2 flushed
-    fwd, adj = [], []
-    for i in range(max(3, args.warmup) + args.steps):
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        (f0, f1), (b0, b1) = event_pair(), event_pair()
-        f0.record(stream)
-        plan.forward(stream.cuda_stream)
-        f1.record(stream)
-        stream.synchronize()
-        out = plan.signal()
-        gx, gy = 2 * (out["Sx"] - tx), 2 * (out["Sy"] - ty)
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        b0.record(stream)
-        plan.backward(gx, gy, stream.cuda_stream)
-        b1.record(stream)
-        b1.synchronize()
-        if i >= max(3, args.warmup):
-            fwd.append(f0.elapsed_time(f1))
-            adj.append(b0.elapsed_time(b1))
+    fwd, adj = time_adjoint_plan(plan, tx, ty, args.steps, args.warmup)
     g = plan.gradients()
     # iterations through the public calls with host buffers: forward, signal
     # download, dL/dS on the host, backward, gradient download and reductions
@@ -384,7 +393,37 @@ def run_config5(args):
                               "frac": mufu / (ms * 1e-3) / 1e9 / mufu_g}},
         "clocks": clk.summary(),
     }
+    if args.c5_adjoint:
+        line["fwd_adjoint"] = config5_adjoint(sc, args)
     print(json.dumps(line))
+
+
+def config5_adjoint(sc, args):
+    """fwd+adjoint of the config-5 scan: the L2 loss against the signal of
+    the same object with T1, T2 x 1.05, gradients of every per-voxel
+    parameter (the bound pool's saturation through its lineshape) and of the
+    rf waveform.  The checkpoints (every 16 steps, 3 components x 3 pools per
+    isochromat) must fit on the device: at 1/16 of the full voxel count they
+    take about 50 GB."""
+    from mrilab_gb300 import engine
+
+    tgt = sc.copy()
+    for k in ("T1", "T2"):
+        tgt.VObj[k] = np.asfortranarray(tgt.VObj[k] * np.float32(1.05))
+    target = engine.scan(tgt)
+    try:
+        plan = engine.AdjointPlan(sc)
+    except engine.ScanError as e:
+        return {"unavailable": str(e)}
+    try:
+        fwd, adj = time_adjoint_plan(plan, target["Sx"], target["Sy"], args.steps, args.warmup)
+        g = plan.gradients()
+    finally:
+        plan.close()
+    fwd_ms, adj_ms = float(np.mean(fwd)), float(np.mean(adj))
+    return {"forward_ms": fwd_ms, "adjoint_ms": adj_ms, "fwd_adjoint_ms": fwd_ms + adj_ms,
+            "adjoint_over_forward": adj_ms / fwd_ms, "checkpoint_every_steps": 16,
+            "check": float(np.abs(g["T2"]).sum())}
 
 
 def cpu_baseline(sc, target_s=12.0):
@@ -418,6 +457,7 @@ def main():
     ap.add_argument("--workload", default="config2", choices=["config2", "config1", "config3", "config4", "config5"])
     ap.add_argument("--vox-scale", type=float, default=1.0, help="config3: scale of the instance voxel counts")
     ap.add_argument("--c5-size", default="256x256x128", help="config5: voxels NXxNYxNZ")
+    ap.add_argument("--c5-adjoint", action="store_true", help="config5: also time fwd+adjoint")
     ap.add_argument("--n-tr", type=int, default=None, help="TRs of the workload (default: all)")
     ap.add_argument("--numerics", default="accurate", choices=["accurate", "reference", "exact"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")

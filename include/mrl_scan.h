@@ -226,8 +226,10 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n);
  * reference has no gradients; this runs the discrete map the integrator
  * applies (rotation, relaxation, split exchange) backwards, with the state
  * checkpointed every few steps and recomputed in between.
- * Scope: free-pool models (normal; ME, or GM without bound pools), one Tx
- * coil, RunMode 0, no Ext events, TypeNum <= 3, up to 8 Rx coils.
+ * Scope: the normal, ME and GM models (GM pools free or bound: a bound
+ * pool's saturation is differentiated through its lineshape, so g_t2 of a
+ * bound pool is dL/dT2b and g_db0 includes the lineshape's shift), one Tx
+ * coil, RunMode 0, no Ext events, TypeNum <= 3, up to 32 Rx coils.
  * Host arrays (NULL: not wanted), V voxels, layouts as in mrl_scan_args:
  *   grad_sx, grad_sy  [P][Rx][A]   inputs
  *   g_t1, g_t2, g_rho [P][V]       dL/dT1, dL/dT2, dL/dRho (the recovery

@@ -25,6 +25,16 @@
 // (m_r x lambda_r), J_l(v)^T u = u - c1 v x u + c2 v x (v x u),
 // c1 = (1 - cos a) / a^2, c2 = (a - sin a) / a^3, a = |v|.
 //
+// Bound pools of the general model (TypeFlag 1, BlochKernelGM.cuh; the
+// CPU engine's rule as the oracle restates it) take no rotation and keep
+// their transverse magnetisation; an rf step first saturates their
+// longitudinal magnetisation, z_r = q z with q = exp(-W dt),
+// W = pi (gamma |TxCoil| |A|)^2 G(a), G the super-Lorentzian lineshape at
+// a = (2 pi f_rf + gamma dB0) T2b, then relaxation and exchange act on
+// z alone.  Its gradients: dL/dW = -dt d1 lambda_z z_r, and through W the
+// rf amplitude (dW/dA = 2 pi (gamma |TxCoil|)^2 G A), dB0 (dG/da gamma T2b)
+// and T2b (dG/dT2b = (G + a dG/da) / T2b).
+//
 // One thread owns one isochromat (a voxel's spin, all its pools).  The
 // forward scan (the accurate integrator, whose frames are anchored to FP64
 // phase moments) stores the lab-frame state every kAdjWin steps
@@ -38,7 +48,33 @@ namespace mrl {
 
 namespace {
 
-constexpr int kAdjMaxRx = 8;
+// Super-Lorentzian lineshape of a bound pool and its slope, by the forward
+// kernel's rule (BlochKernelMT.cuh:348-358: u = p / 1000, p < 1000):
+//   G = c T2b sum_u |1/d| exp(-2 a^2 / d^2),  d = 3u^2 - 1,  c = sqrt(2 / pi) / 1000,
+//   dG/da = -4 a c T2b sum_u |1/d|^3 exp(-2 a^2 / d^2),
+// a = (2 pi f + gamma dB0) T2b.  Four interleaved partial sums (the value
+// compensated, as in the forward scan); returns (G, dG/da).
+static __device__ __noinline__ float2 lineshape_slope(float a, float t2b) {
+    float g[4] = {0.f, 0.f, 0.f, 0.f}, comp[4] = {0.f, 0.f, 0.f, 0.f}, h[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int p0 = 0; p0 < 1000; p0 += 4) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float u = (float)(p0 + j) * 0.001f;
+            const float inv = 1.f / fmaf(3.f * u, u, -1.f);
+            const float x = a * inv;
+            const float e = fabsf(inv) * __expf(-2.f * x * x);
+            const float term = e - comp[j];
+            const float sum = g[j] + term;
+            comp[j] = (sum - g[j]) - term;
+            g[j] = sum;
+            h[j] = fmaf(e, inv * inv, h[j]);
+        }
+    }
+    const float s0 = ((g[0] - comp[0]) + (g[1] - comp[1])) + ((g[2] - comp[2]) + (g[3] - comp[3]));
+    const float s2 = (h[0] + h[1]) + (h[2] + h[3]);
+    const float c = 0.79788456080286536f * 0.001f * t2b;
+    return make_float2(s0 * c, -4.f * a * s2 * c);
+}
 
 __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
     return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
@@ -92,8 +128,8 @@ struct KSum {
     }
 };
 
-template <int P, bool GM>
-__global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjLaunch L) {
+template <int P, bool GM, bool BOUND>
+__global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoint_kernel(AdjLaunch L) {
     extern __shared__ __align__(16) float adj_sm[];
     float *win = adj_sm;                                            // [kAdjWin][3P][kAdjBlock]
     float *rfp = adj_sm + kAdjWin * 3 * P * kAdjBlock;              // [kAdjWin][warp][2]
@@ -139,9 +175,42 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
             for (int i = 0; i < P * P; ++i) kc[i] = L.kch[(long long)i * n + v];
     }
     // a pool with T1, T2 or Rho zero is left alone (BlochKernel.cuh:103)
-    bool on[P];
+    bool on[P], bnd[P];
 #pragma unroll
-    for (int t = 0; t < P; ++t) on[t] = active && t1[t] != 0.f && t2[t] != 0.f && rhoS[t] != 0.f;
+    for (int t = 0; t < P; ++t) {
+        on[t] = active && t1[t] != 0.f && t2[t] != 0.f && rhoS[t] != 0.f;
+        bnd[t] = BOUND && (L.bound >> t & 1u);
+    }
+    // bound pools: (gamma |TxCoil|)^2, and the lineshape G, its slope dG/da
+    // and a at the rf frequency lsw (2 pi f) of the last rf step
+    const float gtx2 = L.gyro * L.gyro * fmaf(txc.x, txc.x, txc.y * txc.y);
+    float lsG[P], lsD[P], lsA[P];
+#pragma unroll
+    for (int t = 0; t < P; ++t) lsG[t] = lsD[t] = lsA[t] = 0.f;
+    float lsw = 0.f;
+    bool lsok = false;
+    auto lineshapes = [&](float wrf) {
+        if (lsok && wrf == lsw) return;
+        const float freq = wrf * 0.15915494309189535f;
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+            if (!bnd[t] || !on[t]) continue;
+            const float a = fmaf((float)(2 * kPiRef), freq, om[0]) * t2[t];
+            const float2 gs = lineshape_slope(a, t2[t]);
+            lsG[t] = gs.x;
+            lsD[t] = gs.y;
+            lsA[t] = a;
+        }
+        lsw = wrf;
+        lsok = true;
+    };
+    // saturation W / G = pi (gamma |TxCoil| |A|)^2 of an rf step (the forward
+    // scan's arithmetic: b1 = |A| |TxCoil|)
+    auto sat_wg = [&](float4 r1) {
+        const float b1 = sqrtf(fmaf(r1.x, r1.x, r1.y * r1.y)) * sqrtf(fmaf(txc.x, txc.x, txc.y * txc.y));
+        const float bg = b1 * L.gyro;
+        return (float)kPiRef * bg * bg;
+    };
 
     // ---- per-dt coefficients ------------------------------------------------
     // map: d2, d1, cc, fin; gradient: hT1 (of l.z mr.z), hR (of l.z), hT2 (of
@@ -197,21 +266,38 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
         if (rf) {
             const float2 vxy = rf_vxy(dt, r1);
             const float wz = wcom(r0) + r1.z;
+            float wg = 0.f;
+            if (BOUND) {
+                lineshapes(r1.z);
+                wg = sat_wg(r1);
+            }
 #pragma unroll
-            for (int t = 0; t < P; ++t) mr[t] = rot_apply(make_rot(make_float3(vxy.x, vxy.y, -dt * (wz + wres[t]))), m[t]);
+            for (int t = 0; t < P; ++t) {
+                if (bnd[t]) {
+                    const float q = 1.f - one_minus_exp(wg * lsG[t] * dt);
+                    mr[t] = make_float3(m[t].x, m[t].y, q * m[t].z);
+                } else {
+                    mr[t] = rot_apply(make_rot(make_float3(vxy.x, vxy.y, -dt * (wz + wres[t]))), m[t]);
+                }
+            }
         } else {
 #pragma unroll
             for (int t = 0; t < P; ++t)
-                mr[t] = make_float3(fmaf(m[t].x, cth[t], m[t].y * sth[t]), fmaf(-m[t].x, sth[t], m[t].y * cth[t]), m[t].z);
+                mr[t] = bnd[t] ? m[t]
+                               : make_float3(fmaf(m[t].x, cth[t], m[t].y * sth[t]),
+                                             fmaf(-m[t].x, sth[t], m[t].y * cth[t]), m[t].z);
         }
         float3 nm[P];
 #pragma unroll
         for (int t = 0; t < P; ++t) {
             float3 a = make_float3(d2[t] * mr[t].x, d2[t] * mr[t].y, fmaf(d1[t], mr[t].z, rhoS[t] * y1[t]));
+            if (bnd[t]) a = make_float3(m[t].x, m[t].y, a.z);  // transverse held
 #pragma unroll
             for (int p = 0; p < P; ++p) {
-                a.x = fmaf(fin[t][p], m[p].x, a.x);
-                a.y = fmaf(fin[t][p], m[p].y, a.y);
+                if (!bnd[t]) {
+                    a.x = fmaf(fin[t][p], m[p].x, a.x);
+                    a.y = fmaf(fin[t][p], m[p].y, a.y);
+                }
                 a.z = fmaf(fin[t][p], m[p].z, a.z);
             }
             nm[t] = on[t] ? a : m[t];
@@ -290,21 +376,58 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
             for (int t = 0; t < P; ++t)
                 mk[t] = make_float3(ws[(3 * t + 0) * kAdjBlock], ws[(3 * t + 1) * kAdjBlock], ws[(3 * t + 2) * kAdjBlock]);
             float2 vxy = make_float2(0.f, 0.f);
-            float wz = 0.f;
+            float wz = 0.f, wg = 0.f;
             if (rf) {
                 vxy = rf_vxy(dt, r1);
                 wz = wcom(r0) + r1.z;
+                if (BOUND) {
+                    lineshapes(r1.z);
+                    wg = sat_wg(r1);
+                }
             }
             float3 nl[P];
 #pragma unroll
             for (int t = 0; t < P; ++t) nl[t] = make_float3(0.f, 0.f, 0.f);
             float2 gv = make_float2(0.f, 0.f);  // dL/d(vx, vy) of the step, summed over the pools
+            float2 gs = make_float2(0.f, 0.f);  // dL/dA through the bound pools' saturation
 #pragma unroll
             for (int t = 0; t < P; ++t) {
                 if (!on[t]) {
                     nl[t].x += lam[t].x;
                     nl[t].y += lam[t].y;
                     nl[t].z += lam[t].z;
+                    continue;
+                }
+                if (bnd[t]) {
+                    // bound pool: transverse held, z saturated (rf) then relaxed and exchanged
+                    const float q = rf ? 1.f - one_minus_exp(wg * lsG[t] * dt) : 1.f;
+                    const float3 l = lam[t];
+                    const float mrz = q * mk[t].z;
+                    const float gd1 = l.z * mrz;
+                    wT1[t] = fmaf(gd1, hT1[t], fmaf(l.z, hR[t], wT1[t]));
+                    wrho[t] = fmaf(l.z, y1[t], wrho[t]);
+                    const float go_g = gd1 * e1[t];
+#pragma unroll
+                    for (int p = 0; p < P; ++p) {
+                        if (GM && p == t) continue;
+                        wk[ch(t, p)] += go_g;
+                        wk[ch(p, t)] = fmaf(l.z * mk[p].z, (1.f - fin[t][p]) * dtc, wk[ch(p, t)]);
+                        nl[p].z = fmaf(fin[t][p], l.z, nl[p].z);
+                    }
+                    const float lz = d1[t] * l.z;
+                    nl[t].x += l.x;
+                    nl[t].y += l.y;
+                    nl[t].z = fmaf(q, lz, nl[t].z);
+                    if (rf) {
+                        // dL/dW = dL/dq dq/dW, dq/dW = -dt q
+                        const float dw = -dt * lz * mrz;
+                        const float cA = 2.f * (float)kPiRef * gtx2 * lsG[t] * dw;
+                        gs.x = fmaf(cA, r1.x, gs.x);
+                        gs.y = fmaf(cA, r1.y, gs.y);
+                        const float dwg = dw * wg;  // dL/dG
+                        ww[t] = fmaf(dwg * lsD[t], t2[t], ww[t]);
+                        wT2[t] = fmaf(dwg, fmaf(lsA[t], lsD[t], lsG[t]) / t2[t], wT2[t]);
+                    }
                     continue;
                 }
                 // rotation of this step
@@ -357,17 +480,22 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
             }
             // receive before the step: lambda += sum_c G R_c
             const int a = __float_as_int(r2.x);
-            if (a >= 0 && active) {
+            if (a >= 0 && active) {  // (bound pools are not received)
 #pragma unroll
                 for (int t = 0; t < P; ++t) {
+                    if (bnd[t]) continue;
                     float2 src = make_float2(0.f, 0.f);
+                    const float2 *gt = L.gsig + (long long)t * L.rx * L.A + a;
+#pragma unroll 1
+                    for (int c0 = 0; c0 < L.rx; c0 += 8) {
 #pragma unroll
-                    for (int c = 0; c < kAdjMaxRx; ++c) {
-                        if (c >= L.rx) break;
-                        const float2 g = __ldg(L.gsig + ((long long)t * L.rx + c) * L.A + a);
-                        const float2 rc = L.rxc ? __ldg(L.rxc + (long long)c * n + v) : make_float2(1.f, 0.f);
-                        src.x = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src.x));
-                        src.y = fmaf(g.x, rc.y, fmaf(g.y, rc.x, src.y));
+                        for (int c = c0; c < c0 + 8; ++c) {
+                            if (c >= L.rx) break;
+                            const float2 g = __ldg(gt + (long long)c * L.A);
+                            const float2 rc = L.rxc ? __ldg(L.rxc + (long long)c * n + v) : make_float2(1.f, 0.f);
+                            src.x = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src.x));
+                            src.y = fmaf(g.x, rc.y, fmaf(g.y, rc.x, src.y));
+                        }
                     }
                     nl[t].x += src.x;
                     nl[t].y += src.y;
@@ -376,10 +504,12 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
 #pragma unroll
             for (int t = 0; t < P; ++t) lam[t] = active ? nl[t] : make_float3(0.f, 0.f, 0.f);
             // rf gradient of this step: dB/dA = TxCoil, dv/dB = -dt gamma, so
-            // dL/dA = -dt gamma conj(TxCoil) (gvx + i gvy), summed over the warp
+            // dL/dA = -dt gamma conj(TxCoil) (gvx + i gvy) + the saturation's
+            // share, summed over the warp
             if (rf) {
                 const float sc = -dt * L.gyro;
-                float2 gA = make_float2(sc * (txc.x * gv.x + txc.y * gv.y), sc * (txc.x * gv.y - txc.y * gv.x));
+                float2 gA = make_float2(fmaf(sc, fmaf(txc.x, gv.x, txc.y * gv.y), gs.x),
+                                        fmaf(sc, fmaf(txc.x, gv.y, -txc.y * gv.x), gs.y));
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     gA.x += __shfl_xor_sync(0xffffffffu, gA.x, o);
@@ -448,10 +578,10 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? 4 : 2) adjoint_kernel(AdjL
     }
 }
 
-template <int P, bool GM>
+template <int P, bool GM, bool BOUND = false>
 cudaError_t go(const AdjLaunch &L, cudaStream_t st) {
     const size_t smem = adjoint_smem_bytes(P);
-    auto k = adjoint_kernel<P, GM>;
+    auto k = adjoint_kernel<P, GM, BOUND>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const long long blocks = (L.n_iso + kAdjBlock - 1) / kAdjBlock;
@@ -462,11 +592,11 @@ cudaError_t go(const AdjLaunch &L, cudaStream_t st) {
 }  // namespace
 
 cudaError_t launch_adjoint(int P, const AdjLaunch &L, cudaStream_t st) {
-    const bool gm = L.exch_gm != 0;
+    const bool gm = L.exch_gm != 0, bound = gm && L.bound != 0;
     switch (P) {
     case 1: return go<1, false>(L, st);
-    case 2: return gm ? go<2, true>(L, st) : go<2, false>(L, st);
-    case 3: return gm ? go<3, true>(L, st) : go<3, false>(L, st);
+    case 2: return bound ? go<2, true, true>(L, st) : gm ? go<2, true>(L, st) : go<2, false>(L, st);
+    case 3: return bound ? go<3, true, true>(L, st) : gm ? go<3, true>(L, st) : go<3, false>(L, st);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -1933,12 +1933,21 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     int rc = plan_create_impl(&a, &p->fwd, kAdjWin, &ch);
     if (rc) return rc;
     Scanner &sc = p->fwd->sc;
-    if (!(sc.mi.km == KM_NORMAL || (sc.mi.km == KM_EXCH && sc.all_free())))
-        return set_err("the adjoint covers free-pool models (normal; ME, or GM without bound pools)"),
-               MRL_ERR_UNSUPPORTED;
+    if (!(sc.mi.km == KM_NORMAL || sc.mi.km == KM_EXCH))
+        return set_err("the adjoint covers the normal, ME and GM models (not MT or CEST)"), MRL_ERR_UNSUPPORTED;
     if (sc.TX != 1) return set_err("the adjoint supports one Tx coil"), MRL_ERR_UNSUPPORTED;
     if (sc.P > 3) return set_err("the adjoint supports TypeNum <= 3"), MRL_ERR_UNSUPPORTED;
-    if (sc.RX > 8) return set_err("the adjoint supports up to 8 Rx coils"), MRL_ERR_UNSUPPORTED;
+    if (sc.RX > 32) return set_err("the adjoint supports up to 32 Rx coils"), MRL_ERR_UNSUPPORTED;
+    // GM pools: free (TypeFlag 0) or bound (1); a bound pool needs a free one
+    unsigned bound = 0;
+    if (sc.mi.km == KM_EXCH && sc.mi.gm) {
+        for (int t = 0; t < sc.P; ++t) {
+            const double k = args->obj.type_flag[t];
+            if (k != 0 && k != 1) return set_err("the adjoint covers GM pools of TypeFlag 0 and 1"), MRL_ERR_UNSUPPORTED;
+            if (k == 1) bound |= 1u << t;
+        }
+        if (bound == (1u << sc.P) - 1) return set_err("the adjoint needs a free pool"), MRL_ERR_UNSUPPORTED;
+    }
     const int P = sc.P, S = sc.S, RX = sc.RX, A = sc.A;
     p->P = P, p->S = S, p->RX = RX, p->A = A, p->V = sc.V;
     p->rf_ref = args->var.rf_ref ? *args->var.rf_ref : 0.0;
@@ -2007,6 +2016,7 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     L.rx = RX;
     L.A = std::max(A, 1);
     L.exch_gm = sc.mi.gm ? 1 : 0;
+    L.bound = bound;
     L.n_iso = n_iso;
     L.gyro = (float)args->obj.gyro;
     L.gxg = sc.d_f.p + sc.o_gx;

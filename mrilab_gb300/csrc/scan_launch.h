@@ -92,6 +92,7 @@ constexpr int kAdjBlock = 128;  // threads (isochromats) per block
 // step index (int bits) or -1, 0, 0}.
 struct AdjLaunch {
     int n_act, S, rx, A, exch_gm;
+    unsigned bound;  // GM bound pools (TypeFlag 1), one bit per pool
     long long n_iso;  // n_act * S; isochromat i = spin (i / n_act) of voxel (i % n_act)
     float gyro;
     const float *gxg, *gyg, *gzg, *db0;  // [n_act]

@@ -157,7 +157,20 @@ def test_adjoint_three_pool_exchange(built):
     _run(phantoms.small_multipool("me", seed=34, n=5, pools=3, spins=1, coils=3, n_tr=2))
 
 
-def test_adjoint_rejects_bound_pools(built):
+def test_adjoint_gm_bound_pool(built):
+    """The general model with a bound pool (TypeFlag 1, T2b 10 us) under
+    off-resonance Gaussian saturation pulses: the saturation's share of the
+    rf gradient, and dB0 and T2b through the lineshape."""
+    _run(phantoms.small_multipool("gm", seed=38, n=5, pools=3, spins=1, coils=2, n_tr=3, seq="sat"))
+
+
+def test_adjoint_mt_epi_many_coils(built):
+    """The MT + exchange EPI (free, myelin and bound pools, 8 ms MT pulse)
+    on a small phantom with 12 receive coils."""
+    _run(phantoms.config5_mt_epi(seed=5, nx=4, ny=4, nz=1, spins=1, n_coils=12, n_read=8, n_pe=8))
+
+
+def test_adjoint_rejects_mt_model(built):
     sc = phantoms.small_multipool("mt", seed=33, n=4, pools=2, spins=1, coils=1, n_tr=1, seq="sat")
     with pytest.raises(engine.ScanError) as e:
         engine.adjoint(sc, np.zeros(1), np.zeros(1))
