@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     float *win = adj_sm;                                            // [kAdjWin][3P][kAdjBlock]
     float *rfp = adj_sm + kAdjWin * 3 * P * kAdjBlock;              // [kAdjWin][warp][2]
     float4 *wrec = reinterpret_cast<float4 *>(rfp + kAdjWin * (kAdjBlock / 32) * 2);  // [kAdjWin][3]
+    float2 *rxs = reinterpret_cast<float2 *>(wrec + kAdjWin * 3);                     // [rx][kAdjBlock]
     constexpr int kWarps = kAdjBlock / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long iso = (long long)blockIdx.x * kAdjBlock + tid;
@@ -174,6 +175,9 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
 #pragma unroll
             for (int i = 0; i < P * P; ++i) kc[i] = L.kch[(long long)i * n + v];
     }
+    // this thread's receive sensitivities, read once: every ADC step uses them
+    for (int c = 0; c < L.rx; ++c)
+        rxs[c * kAdjBlock + tid] = (active && L.rxc) ? L.rxc[(long long)c * n + v] : make_float2(1.f, 0.f);
     // a pool with T1, T2 or Rho zero is left alone (BlochKernel.cuh:103)
     bool on[P], bnd[P];
 #pragma unroll
@@ -485,14 +489,14 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 for (int t = 0; t < P; ++t) {
                     if (bnd[t]) continue;
                     float2 src = make_float2(0.f, 0.f);
-                    const float2 *gt = L.gsig + (long long)t * L.rx * L.A + a;
+                    const float2 *gt = L.gsig + ((long long)a * P + t) * L.rx;
 #pragma unroll 1
                     for (int c0 = 0; c0 < L.rx; c0 += 8) {
 #pragma unroll
                         for (int c = c0; c < c0 + 8; ++c) {
                             if (c >= L.rx) break;
-                            const float2 g = __ldg(gt + (long long)c * L.A);
-                            const float2 rc = L.rxc ? __ldg(L.rxc + (long long)c * n + v) : make_float2(1.f, 0.f);
+                            const float2 g = __ldg(gt + c);
+                            const float2 rc = rxs[c * kAdjBlock + tid];
                             src.x = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src.x));
                             src.y = fmaf(g.x, rc.y, fmaf(g.y, rc.x, src.y));
                         }
@@ -580,7 +584,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
 
 template <int P, bool GM, bool BOUND = false>
 cudaError_t go(const AdjLaunch &L, cudaStream_t st) {
-    const size_t smem = adjoint_smem_bytes(P);
+    const size_t smem = adjoint_smem_bytes(P, L.rx);
     auto k = adjoint_kernel<P, GM, BOUND>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

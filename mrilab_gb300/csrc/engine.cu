@@ -2065,11 +2065,16 @@ int mrl_adjoint_plan_backward(mrl_adjoint_plan *p, const double *grad_sx, const 
     // the signal is the receive sum rotated by exp(-i rfRef): dL/dS before
     // the rotation = exp(+i rfRef) dL/dS after it
     const double cr = std::cos(p->rf_ref), sr = std::sin(p->rf_ref);
+    // [P][Rx][A] (the signal's layout) -> [A][P][Rx] (one sample's values together)
     std::vector<float2> gs((size_t)p->P * p->RX * std::max(p->A, 1), make_float2(0.f, 0.f));
-    for (size_t i = 0; i < (size_t)p->P * p->RX * p->A; ++i) {
-        const double gx = grad_sx ? grad_sx[i] : 0.0, gy = grad_sy ? grad_sy[i] : 0.0;
-        gs[i] = make_float2((float)(gx * cr - gy * sr), (float)(gx * sr + gy * cr));
-    }
+    for (int t = 0; t < p->P; ++t)
+        for (int c = 0; c < p->RX; ++c)
+            for (int a = 0; a < p->A; ++a) {
+                const size_t i = ((size_t)t * p->RX + c) * p->A + a;
+                const double gx = grad_sx ? grad_sx[i] : 0.0, gy = grad_sy ? grad_sy[i] : 0.0;
+                gs[((size_t)a * p->P + t) * p->RX + c] =
+                    make_float2((float)(gx * cr - gy * sr), (float)(gx * sr + gy * cr));
+            }
     cudaError_t e = cudaMemcpyAsync(p->d_gs.p, gs.data(), gs.size() * sizeof(float2), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p->d_rf.p, 0, p->d_rf.n * sizeof(double), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p->d_g.p, 0, p->d_g.n * sizeof(float), st);

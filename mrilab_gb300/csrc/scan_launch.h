@@ -105,13 +105,14 @@ struct AdjLaunch {
     const float4 *rec;                   // [n_steps][3]
     long long n_steps;
     const float *ckpt;                   // [window][3P][n_iso], written by the forward scan
-    const float2 *gsig;                  // [P][rx][A] dL/dSx + i dL/dSy
+    const float2 *gsig;                  // [A][P][rx] dL/dSx + i dL/dSy, one sample's values together
     float *giso;                         // [fields][n_iso]: T1[P] T2[P] Rho[P] dB0 K[P*P] Mx0[P] My0[P] Mz0[P]
     double *grf;                         // [n_rf][2]
 };
-inline size_t adjoint_smem_bytes(int P) {  // window states, rf partials, window records
+// window states, rf partials, window records, the block's receive sensitivities
+inline size_t adjoint_smem_bytes(int P, int rx) {
     return (size_t)kAdjWin * 3 * P * kAdjBlock * 4 + (size_t)kAdjWin * (kAdjBlock / 32) * 2 * 4 +
-           (size_t)kAdjWin * 3 * 16;
+           (size_t)kAdjWin * 3 * 16 + (size_t)rx * kAdjBlock * 8;
 }
 inline int adjoint_fields(int P) { return 3 * P + 1 + P * P + 3 * P; }
 cudaError_t launch_adjoint(int P, const AdjLaunch &L, cudaStream_t st);
