@@ -485,24 +485,36 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             // receive before the step: lambda += sum_c G R_c
             const int a = __float_as_int(r2.x);
             if (a >= 0 && active) {  // (bound pools are not received)
+                // per pool: sum_c G R_c as four independent partial sums
+                // (re and im of the even and of the odd coils)
+                const float2 *ga = L.gsig + (long long)a * P * L.rx;
+                float4 src[P];
 #pragma unroll
-                for (int t = 0; t < P; ++t) {
-                    if (bnd[t]) continue;
-                    float2 src = make_float2(0.f, 0.f);
-                    const float2 *gt = L.gsig + ((long long)a * P + t) * L.rx;
+                for (int t = 0; t < P; ++t) src[t] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
-                    for (int c0 = 0; c0 < L.rx; c0 += 8) {
+                for (int c0 = 0; c0 < L.rx; c0 += 8) {
 #pragma unroll
-                        for (int c = c0; c < c0 + 8; ++c) {
-                            if (c >= L.rx) break;
-                            const float2 g = __ldg(gt + c);
-                            const float2 rc = rxs[c * kAdjBlock + tid];
-                            src.x = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src.x));
-                            src.y = fmaf(g.x, rc.y, fmaf(g.y, rc.x, src.y));
+                    for (int c = c0; c < c0 + 8; ++c) {
+                        if (c >= L.rx) break;
+                        const float2 rc = rxs[c * kAdjBlock + tid];
+#pragma unroll
+                        for (int t = 0; t < P; ++t) {
+                            if (bnd[t]) continue;
+                            const float2 g = __ldg(ga + t * L.rx + c);
+                            if (c & 1) {
+                                src[t].z = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src[t].z));
+                                src[t].w = fmaf(g.x, rc.y, fmaf(g.y, rc.x, src[t].w));
+                            } else {
+                                src[t].x = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src[t].x));
+                                src[t].y = fmaf(g.x, rc.y, fmaf(g.y, rc.x, src[t].y));
+                            }
                         }
                     }
-                    nl[t].x += src.x;
-                    nl[t].y += src.y;
+                }
+#pragma unroll
+                for (int t = 0; t < P; ++t) {
+                    nl[t].x += src[t].x + src[t].z;
+                    nl[t].y += src[t].y + src[t].w;
                 }
             }
 #pragma unroll
