@@ -135,6 +135,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     float *rfp = adj_sm + kAdjWin * 3 * P * kAdjBlock;              // [kAdjWin][warp][2]
     float4 *wrec = reinterpret_cast<float4 *>(rfp + kAdjWin * (kAdjBlock / 32) * 2);  // [kAdjWin][3]
     float2 *rxs = reinterpret_cast<float2 *>(wrec + kAdjWin * 3);                     // [rx][kAdjBlock]
+    const int PR = P * L.rx;                                        // dL/dS values of one sample
+    float2 *gbuf = rxs + L.rx * kAdjBlock;                          // [warp][2][PR]
     constexpr int kWarps = kAdjBlock / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long iso = (long long)blockIdx.x * kAdjBlock + tid;
@@ -175,6 +177,13 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
 #pragma unroll
             for (int i = 0; i < P * P; ++i) kc[i] = L.kch[(long long)i * n + v];
     }
+    // this warp's asynchronous copy of sample a's dL/dS into its buffer b
+    auto prefetch_g = [&](int a, int b) {
+        float2 *dst = gbuf + (warp * 2 + b) * PR;
+        const float2 *src = L.gsig + (long long)a * PR;
+        for (int i = lane; i < PR; i += 32) cp_async8(dst + i, src + i);
+        cp_async_commit();
+    };
     // this thread's receive sensitivities, read once: every ADC step uses them
     for (int c = 0; c < L.rx; ++c)
         rxs[c * kAdjBlock + tid] = (active && L.rxc) ? L.rxc[(long long)c * n + v] : make_float2(1.f, 0.f);
@@ -327,6 +336,9 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
         // the window's step records, staged in shared memory
         if (tid < 3 * nk) wrec[tid] = __ldg(L.rec + k0 * 3 + tid);
         __syncthreads();
+        // dL/dS of the window's last step (the first one the backward walk
+        // takes), fetched while the states are recomputed
+        if (__float_as_int(wrec[3 * (nk - 1) + 2].x) >= 0) prefetch_g(__float_as_int(wrec[3 * (nk - 1) + 2].x), (nk - 1) & 1);
         // recompute the window's states (before each step) into shared memory
         if (active) {
             const float *cp = L.ckpt + w * cs * L.n_iso + iso;
@@ -372,6 +384,17 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 if (fn & kFlagDt) set_dt(dt);
                 if (fn & kFlagState) set_state(dt, r0);
                 if (fn & (kFlagDt | kFlagState)) cur = r0;
+            }
+            // dL/dS of step j - 1 (the next step back), if it samples: into the
+            // buffer step j + 1 read, once every lane of the warp is done with it
+            bool pend = false;
+            if (j >= 1) {
+                const int an = __float_as_int(wrec[3 * (j - 1) + 2].x);
+                if (an >= 0) {
+                    __syncwarp();
+                    prefetch_g(an, (j - 1) & 1);
+                    pend = true;
+                }
             }
             const bool rf = (flags & kFlagRf) != 0;
             const float *ws = win + j * 3 * P * kAdjBlock + tid;
@@ -484,10 +507,17 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             }
             // receive before the step: lambda += sum_c G R_c
             const int a = __float_as_int(r2.x);
+            if (a >= 0) {  // this step's dL/dS copy complete and visible to the warp
+                if (pend)
+                    cp_async_wait<1>();
+                else
+                    cp_async_wait<0>();
+                __syncwarp();
+            }
             if (a >= 0 && active) {  // (bound pools are not received)
                 // per pool: sum_c G R_c as four independent partial sums
                 // (re and im of the even and of the odd coils)
-                const float2 *ga = L.gsig + (long long)a * P * L.rx;
+                const float2 *ga = gbuf + (warp * 2 + (j & 1)) * PR;
                 float4 src[P];
 #pragma unroll
                 for (int t = 0; t < P; ++t) src[t] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -500,7 +530,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
 #pragma unroll
                         for (int t = 0; t < P; ++t) {
                             if (bnd[t]) continue;
-                            const float2 g = __ldg(ga + t * L.rx + c);
+                            const float2 g = ga[t * L.rx + c];
                             if (c & 1) {
                                 src[t].z = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src[t].z));
                                 src[t].w = fmaf(g.x, rc.y, fmaf(g.y, rc.x, src[t].w));
@@ -563,6 +593,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
         }
         __syncthreads();
     }
+
+    cp_async_wait<0>();
 
     // ---- per-isochromat outputs -------------------------------------------
     if (!active) return;

@@ -109,10 +109,11 @@ struct AdjLaunch {
     float *giso;                         // [fields][n_iso]: T1[P] T2[P] Rho[P] dB0 K[P*P] Mx0[P] My0[P] Mz0[P]
     double *grf;                         // [n_rf][2]
 };
-// window states, rf partials, window records, the block's receive sensitivities
+// window states, rf partials, window records, the block's receive
+// sensitivities, and per warp two buffers of one sample's dL/dS
 inline size_t adjoint_smem_bytes(int P, int rx) {
     return (size_t)kAdjWin * 3 * P * kAdjBlock * 4 + (size_t)kAdjWin * (kAdjBlock / 32) * 2 * 4 +
-           (size_t)kAdjWin * 3 * 16 + (size_t)rx * kAdjBlock * 8;
+           (size_t)kAdjWin * 3 * 16 + (size_t)rx * kAdjBlock * 8 + (size_t)(kAdjBlock / 32) * 2 * P * rx * 8;
 }
 inline int adjoint_fields(int P) { return 3 * P + 1 + P * P + 3 * P; }
 cudaError_t launch_adjoint(int P, const AdjLaunch &L, cudaStream_t st);
