@@ -277,6 +277,7 @@ def run_config4(args):
     tx, ty = target["Sx"], target["Sy"]
     plan = engine.AdjointPlan(sc)
     work = plan.work()
+    ck = plan.checkpoints()
     fwd, adj = time_adjoint_plan(plan, tx, ty, args.steps, args.warmup)
     g = plan.gradients()
     # iterations through the public calls with host buffers: forward, signal
@@ -307,7 +308,7 @@ def run_config4(args):
                                % int(sc.VCtl["TRNum"]),
                    "units_per_iter": units, "steps": work["steps"], "rf_steps": work["rf_steps"],
                    "samples": work["samples"], "rf_entries": int(np.size(sc.VSeq["rfAmpLine"])),
-                   "checkpoint_every_steps": 16,
+                   "checkpoint_every_steps": ck["stored_every"], "checkpoint_gb": ck["bytes"] / 1e9,
                    "l2": "flushed before each timed forward scan and adjoint (256 MiB write); the checkpoints "
                          "(tens of GB) stream through HBM"},
         "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
@@ -402,9 +403,10 @@ def config5_adjoint(sc, args):
     """fwd+adjoint of the config-5 scan: the L2 loss against the signal of
     the same object with T1, T2 x 1.05, gradients of every per-voxel
     parameter (the bound pool's saturation through its lineshape) and of the
-    rf waveform.  The checkpoints (every 16 steps, 3 components x 3 pools per
-    isochromat) must fit on the device: at 1/16 of the full voxel count they
-    take about 50 GB."""
+    rf waveform.  Checkpoints (3 components x 3 pools per isochromat) are
+    stored every 16 steps while they fit in half the free device memory (at
+    1/16 of the full voxel count: 54 GB); at full size every 16 M steps, the
+    adjoint rebuilding each segment's 16-step checkpoints."""
     from mrilab_gb300 import engine
 
     tgt = sc.copy()
@@ -416,13 +418,15 @@ def config5_adjoint(sc, args):
     except engine.ScanError as e:
         return {"unavailable": str(e)}
     try:
+        ck = plan.checkpoints()
         fwd, adj = time_adjoint_plan(plan, target["Sx"], target["Sy"], args.steps, args.warmup)
         g = plan.gradients()
     finally:
         plan.close()
     fwd_ms, adj_ms = float(np.mean(fwd)), float(np.mean(adj))
     return {"forward_ms": fwd_ms, "adjoint_ms": adj_ms, "fwd_adjoint_ms": fwd_ms + adj_ms,
-            "adjoint_over_forward": adj_ms / fwd_ms, "checkpoint_every_steps": 16,
+            "adjoint_over_forward": adj_ms / fwd_ms, "checkpoint_every_steps": ck["stored_every"],
+            "rebuilt_every_steps": ck["window"], "checkpoint_gb": ck["bytes"] / 1e9,
             "check": float(np.abs(g["T2"]).sum())}
 
 

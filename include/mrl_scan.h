@@ -269,8 +269,13 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj);
  * gradients, destroy.  args must outlive the plan (its host arrays are
  * read at create and written by download).
  *   create     decodes the sequence once, uploads the object and sizes the
- *              checkpoints (MRL_ERR_NOMEM if they do not fit the free
- *              device memory); same scope as mrl_adjoint
+ *              checkpoints: one every 16 steps while they fit in half the
+ *              free device memory, else one every 16 M steps (M the
+ *              smallest power of two that fits) from which backward
+ *              rebuilds each segment's 16-step checkpoints (about one more
+ *              forward pass of work); environment MRL_ADJ_SEGMENT=M forces
+ *              M.  MRL_ERR_NOMEM if even that does not fit; same scope as
+ *              mrl_adjoint
  *   forward    runs the scan from the initial magnetisation on `stream`
  *              (NULL: the default stream), writing the checkpoints
  *   download   signal and final magnetisation of the last forward pass
@@ -279,7 +284,10 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj);
  *              enqueues the adjoint kernel on `stream`
  *   gradients  waits for the device and fills adj's outputs (its grad_sx,
  *              grad_sy are not read)
- *   work       out[0..4] as mrl_plan_work, out[5] = rf-on steps */
+ *   work       out[0..4] as mrl_plan_work, out[5] = rf-on steps
+ *   checkpoints out[0] = steps between stored checkpoints, out[1] = steps
+ *              between the checkpoints backward walks from (16), out[2] =
+ *              device bytes of both */
 typedef struct mrl_adjoint_plan mrl_adjoint_plan;
 int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out);
 int mrl_adjoint_plan_forward(mrl_adjoint_plan *plan, void *stream);
@@ -287,6 +295,7 @@ int mrl_adjoint_plan_download(mrl_adjoint_plan *plan, mrl_scan_args *args);
 int mrl_adjoint_plan_backward(mrl_adjoint_plan *plan, const double *grad_sx, const double *grad_sy, void *stream);
 int mrl_adjoint_plan_gradients(mrl_adjoint_plan *plan, mrl_adjoint_args *adj);
 int mrl_adjoint_plan_work(const mrl_adjoint_plan *plan, long long out[6]);
+int mrl_adjoint_plan_checkpoints(const mrl_adjoint_plan *plan, long long out[3]);
 void mrl_adjoint_plan_destroy(mrl_adjoint_plan *plan);
 
 /* Scan without allocating device memory.

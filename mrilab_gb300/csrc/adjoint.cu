@@ -324,38 +324,22 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     const long long cs = (long long)3 * P;  // checkpoint components
     // (dt, Gz, Gy, Gx) of the coefficients in registers
     float4 cur = make_float4(-1.f, 0.f, 0.f, 0.f);
-
-    // ---- backward sweep -----------------------------------------------------
-    float3 lam[P];
-#pragma unroll
-    for (int t = 0; t < P; ++t) lam[t] = make_float3(0.f, 0.f, 0.f);
-    KSum gT1[P], gT2[P], grho[P], gw[P], gk[P * P];
-    for (long long w = nwin - 1; w >= 0; --w) {
-        const long long k0 = w * kAdjWin;
-        const int nk = (int)min((long long)kAdjWin, N - k0);
-        // the window's step records, staged in shared memory
-        if (tid < 3 * nk) wrec[tid] = __ldg(L.rec + k0 * 3 + tid);
-        __syncthreads();
-        // dL/dS of the window's last step (the first one the backward walk
-        // takes), fetched while the states are recomputed
-        if (__float_as_int(wrec[3 * (nk - 1) + 2].x) >= 0) prefetch_g(__float_as_int(wrec[3 * (nk - 1) + 2].x), (nk - 1) & 1);
-        // recompute the window's states (before each step) into shared memory
-        if (active) {
-            const float *cp = L.ckpt + w * cs * L.n_iso + iso;
-#pragma unroll
-            for (int t = 0; t < P; ++t)
-                m[t] = make_float3(cp[(3 * t + 0) * L.n_iso], cp[(3 * t + 1) * L.n_iso], cp[(3 * t + 2) * L.n_iso]);
-        }
+    // the nk steps of the window in wrec from the state m: with `states`,
+    // the state before each step into shared memory and the last step not
+    // taken (the backward walk starts from it); without, every step taken
+    auto recompute = [&](int nk, float *states) {
         for (int j = 0; j < nk; ++j) {
             const float4 r0 = wrec[3 * j], r1 = wrec[3 * j + 1];
             const int flags = __float_as_int(r1.w);
             const float dt = r0.x;
-            float *ws = win + j * 3 * P * kAdjBlock + tid;
+            if (states) {
+                float *ws = states + j * 3 * P * kAdjBlock + tid;
 #pragma unroll
-            for (int t = 0; t < P; ++t) {
-                ws[(3 * t + 0) * kAdjBlock] = m[t].x;
-                ws[(3 * t + 1) * kAdjBlock] = m[t].y;
-                ws[(3 * t + 2) * kAdjBlock] = m[t].z;
+                for (int t = 0; t < P; ++t) {
+                    ws[(3 * t + 0) * kAdjBlock] = m[t].x;
+                    ws[(3 * t + 1) * kAdjBlock] = m[t].y;
+                    ws[(3 * t + 2) * kAdjBlock] = m[t].z;
+                }
             }
             if (j == 0) {  // the coefficients of the window's first step, if not in registers
                 if (dt != cur.x) set_dt(dt);
@@ -366,8 +350,67 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 if (flags & kFlagState) set_state(dt, r0);
                 cur = r0;
             }
-            if (j + 1 < nk) fwd(dt, r0, r1, (flags & kFlagRf) != 0);
+            if (!states || j + 1 < nk) fwd(dt, r0, r1, (flags & kFlagRf) != 0);
         }
+    };
+
+    // ---- backward sweep -----------------------------------------------------
+    float3 lam[P];
+#pragma unroll
+    for (int t = 0; t < P; ++t) lam[t] = make_float3(0.f, 0.f, 0.f);
+    KSum gT1[P], gT2[P], grho[P], gw[P], gk[P * P];
+    for (long long w = nwin - 1; w >= 0; --w) {
+        const long long k0 = w * kAdjWin;
+        const int nk = (int)min((long long)kAdjWin, N - k0);
+        // two-level checkpoints (seg > 1): entering a segment (its last
+        // window first), rebuild the states at its windows' starts from the
+        // segment's stored checkpoint into ck2
+        const long long wseg = w / L.seg * L.seg;  // the segment's first window
+        const float *wck = L.ckpt + w * cs * L.n_iso + iso;
+        if (L.seg > 1) {
+            float *c2 = L.ck2 + iso;
+            if (w == nwin - 1 || w % L.seg == L.seg - 1) {
+                if (active) {
+                    const float *cp = L.ckpt + (w / L.seg) * cs * L.n_iso + iso;
+#pragma unroll
+                    for (int t = 0; t < P; ++t)
+                        m[t] = make_float3(cp[(3 * t + 0) * L.n_iso], cp[(3 * t + 1) * L.n_iso],
+                                           cp[(3 * t + 2) * L.n_iso]);
+                }
+                for (long long u = wseg; u <= w; ++u) {
+                    if (active) {
+                        float *o = c2 + (u - wseg) * cs * L.n_iso;
+#pragma unroll
+                        for (int t = 0; t < P; ++t) {
+                            o[(3 * t + 0) * L.n_iso] = m[t].x;
+                            o[(3 * t + 1) * L.n_iso] = m[t].y;
+                            o[(3 * t + 2) * L.n_iso] = m[t].z;
+                        }
+                    }
+                    if (u == w) break;
+                    // window u's records, then all its steps (full windows: u < w)
+                    __syncthreads();
+                    if (tid < 3 * kAdjWin) wrec[tid] = __ldg(L.rec + u * kAdjWin * 3 + tid);
+                    __syncthreads();
+                    recompute(kAdjWin, nullptr);
+                }
+                __syncthreads();
+            }
+            wck = c2 + (w - wseg) * cs * L.n_iso;
+        }
+        // the window's step records, staged in shared memory
+        if (tid < 3 * nk) wrec[tid] = __ldg(L.rec + k0 * 3 + tid);
+        __syncthreads();
+        // dL/dS of the window's last step (the first one the backward walk
+        // takes), fetched while the states are recomputed
+        if (__float_as_int(wrec[3 * (nk - 1) + 2].x) >= 0) prefetch_g(__float_as_int(wrec[3 * (nk - 1) + 2].x), (nk - 1) & 1);
+        // recompute the window's states (before each step) into shared memory
+        if (active) {
+#pragma unroll
+            for (int t = 0; t < P; ++t)
+                m[t] = make_float3(wck[(3 * t + 0) * L.n_iso], wck[(3 * t + 1) * L.n_iso], wck[(3 * t + 2) * L.n_iso]);
+        }
+        recompute(nk, win);
         // window partial sums of the parameter gradients
         float wT1[P], wT2[P], wrho[P], ww[P], wk[P * P];
 #pragma unroll

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <atomic>
 #include <map>
@@ -873,6 +874,7 @@ struct Scanner {
         L.hist = hist_on ? d_hist.p + (hist_steps + d.s0) * 3 * L.hist_stride : nullptr;
         L.ckpt = ckpt;
         L.ckpt_step0 = d.s0;
+        L.ckpt_every = std::max(1, ckpt_every);
         L.xtab = coef ? d_xtab.p : nullptr;
         L.xnf = coef == 2 ? exact_fields(P) : split_fields(P);
         if (direct_rx) {
@@ -1475,8 +1477,29 @@ int mrl_scan(mrl_scan_args *args, mrl_ext_fn ext, void *user) {
 }  // extern "C"
 
 namespace {
+// Windows of kAdjWin steps per checkpoint segment of an adjoint plan: 1 (a
+// stored checkpoint every kAdjWin steps) while those fit in half the free
+// device memory, else the smallest power of two M for which the stored
+// checkpoints (one every M windows) and one segment's rebuilt window
+// checkpoints (M) fit.  MRL_ADJ_SEGMENT=M overrides the choice.
+int adjoint_segment(long long n_steps, long long n_iso, int P) {
+    if (const char *e = std::getenv("MRL_ADJ_SEGMENT")) {
+        const int m = std::atoi(e);
+        if (m >= 1) return m;
+    }
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    const double one = 3.0 * P * (double)std::max(1LL, n_iso) * sizeof(float);
+    const long long nwin = std::max(1LL, (n_steps + mrl::kAdjWin - 1) / mrl::kAdjWin);
+    long long M = 1;
+    for (; M < nwin; M *= 2)
+        if (one * (double)((nwin + M - 1) / M + (M > 1 ? M : 0)) <= 0.5 * (double)fr) break;
+    return (int)std::min<long long>(M, 1 << 20);
+}
+
 // A prepared scan.  ckpt_every > 0 flags every ckpt_every-th step for an
-// adjoint checkpoint; `keep` (optional) receives the decoded sequence.
+// adjoint checkpoint (< 0: kAdjWin times adjoint_segment's choice); `keep`
+// (optional) receives the decoded sequence.
 int plan_create_impl(const mrl_scan_args *args, mrl_plan **out, int ckpt_every, mrl::DecodeChunk *keep) {
     mrl::g_err.clear();
     if (!args || !out) {
@@ -1499,7 +1522,6 @@ int plan_create_impl(const mrl_scan_args *args, mrl_plan **out, int ckpt_every, 
         delete p;
         return rc;
     }
-    sc.ckpt_every = ckpt_every;
     const int A = sc.A;
     p->kx.assign(std::max(A, 1), 0.0);
     p->ky.assign(std::max(A, 1), 0.0);
@@ -1519,6 +1541,8 @@ int plan_create_impl(const mrl_scan_args *args, mrl_plan **out, int ckpt_every, 
         delete p;
         return MRL_ERR_UNSUPPORTED;
     }
+    if (ckpt_every < 0) ckpt_every = mrl::kAdjWin * adjoint_segment(ch.n_steps, (long long)sc.n_act * sc.S, sc.P);
+    sc.ckpt_every = ckpt_every;
     if ((rc = sc.prepare_chunk(ch, p->ls))) {
         delete p;
         return rc;
@@ -1903,14 +1927,14 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n) {
 struct mrl_adjoint_plan {
     mrl_plan *fwd = nullptr;
     mrl::DevBuf<float4> d_rec;
-    mrl::DevBuf<float> d_ck, d_g;
+    mrl::DevBuf<float> d_ck, d_ck2, d_g;
     mrl::DevBuf<float2> d_gs;
     mrl::DevBuf<double> d_rf;
     mrl::AdjLaunch L{};
     std::vector<int> rf_uts, rf_src;  // per rf step: uts index; rfAmpLine, rfPhaseLine entries held
     std::vector<double> rf_a;         // per rf step: Re A, Im A
-    int P = 0, S = 0, RX = 0, A = 0, n_rf = 0;
-    long long V = 0, n_iso = 0, N = 0;
+    int P = 0, S = 0, RX = 0, A = 0, n_rf = 0, ck_every = 0;
+    long long V = 0, n_iso = 0, N = 0, ck_bytes = 0;
     double rf_ref = 0;
     bool forward_done = false, backward_done = false;
     ~mrl_adjoint_plan() {
@@ -1930,7 +1954,7 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     mrl_scan_args a = *args;
     a.ctl.numerics = MRL_NUMERICS_ACCURATE;  // the checkpoints come from the accurate integrator
     DecodeChunk ch;
-    int rc = plan_create_impl(&a, &p->fwd, kAdjWin, &ch);
+    int rc = plan_create_impl(&a, &p->fwd, -1, &ch);
     if (rc) return rc;
     Scanner &sc = p->fwd->sc;
     if (!(sc.mi.km == KM_NORMAL || sc.mi.km == KM_EXCH))
@@ -1991,8 +2015,13 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     const int n = std::max(1, sc.n_act);
     const long long n_iso = (long long)sc.n_act * S;
     p->n_iso = n_iso;
-    const long long nwin = (N + kAdjWin - 1) / kAdjWin;
-    const double ck_bytes = (double)nwin * 3 * P * std::max(1LL, n_iso) * sizeof(float);
+    // stored checkpoints every ckpt_every steps; with M > 1 windows per
+    // segment the adjoint rebuilds a segment's window checkpoints into d_ck2
+    const int M = std::max(1, sc.ckpt_every / kAdjWin);
+    const long long nck = (N + sc.ckpt_every - 1) / sc.ckpt_every;
+    const double ck_bytes = (double)(nck + (M > 1 ? M : 0)) * 3 * P * std::max(1LL, n_iso) * sizeof(float);
+    p->ck_every = sc.ckpt_every;
+    p->ck_bytes = (long long)ck_bytes;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     if (ck_bytes > 0.85 * (double)free_b)
@@ -2001,7 +2030,8 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
                MRL_ERR_NOMEM;
     const int nf = adjoint_fields(P);
     cudaError_t e = p->d_rec.ensure(rec.size());
-    if (e == cudaSuccess) e = p->d_ck.ensure((size_t)std::max(1LL, nwin * 3 * P * n_iso));
+    if (e == cudaSuccess) e = p->d_ck.ensure((size_t)std::max(1LL, nck * 3 * P * n_iso));
+    if (e == cudaSuccess) e = p->d_ck2.ensure((size_t)std::max(1LL, (M > 1 ? M : 0) * 3 * P * n_iso));
     if (e == cudaSuccess) e = p->d_g.ensure((size_t)nf * std::max(1LL, n_iso));
     if (e == cudaSuccess) e = p->d_gs.ensure((size_t)P * RX * std::max(A, 1));
     if (e == cudaSuccess) e = p->d_rf.ensure((size_t)2 * std::max(1, p->n_rf));
@@ -2035,6 +2065,8 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     L.rec = p->d_rec.p;
     L.n_steps = N;
     L.ckpt = p->d_ck.p;
+    L.seg = M;
+    L.ck2 = M > 1 ? p->d_ck2.p : nullptr;
     L.gsig = p->d_gs.p;
     L.giso = p->d_g.p;
     L.grf = p->d_rf.p;
@@ -2153,6 +2185,14 @@ int mrl_adjoint_plan_work(const mrl_adjoint_plan *p, long long out[6]) {
     if (!p || !out) return MRL_ERR_ARG;
     for (int i = 0; i < 5; ++i) out[i] = p->fwd->work[i];
     out[5] = p->n_rf;
+    return MRL_OK;
+}
+
+int mrl_adjoint_plan_checkpoints(const mrl_adjoint_plan *p, long long out[3]) {
+    if (!p || !out) return MRL_ERR_ARG;
+    out[0] = p->ck_every;
+    out[1] = mrl::kAdjWin;
+    out[2] = p->ck_bytes;
     return MRL_OK;
 }
 

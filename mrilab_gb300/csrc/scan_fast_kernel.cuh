@@ -787,7 +787,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
             if (flags & kFlagCkpt) {  // adjoint checkpoint: the state at the start of the step, lab frame
                 const long long g = L.ckpt_step0 + (long long)k * chunk + q;
                 const long long niso = (long long)L.S * n;
-                float *c = L.ckpt + (g / kAdjWin) * 3 * P * niso;
+                float *c = L.ckpt + (g / L.ckpt_every) * 3 * P * niso;
 #pragma unroll
                 for (int s = 0; s < NS; ++s)
 #pragma unroll

@@ -70,12 +70,14 @@ struct ScanLaunch {
     int *err;
     float *hist;            // RunMode 1: [step][Mx|My|Mz][P][S][n_act] from the launch's first step, or null
     long long hist_stride;  // P * S * n_act
-    // adjoint checkpoints: at steps flagged kFlagCkpt (every kAdjWin-th step
-    // of the scan), the lab-frame state before the step into slot
-    // (step / kAdjWin) of [slot][3P: Mx, My, Mz of pool t at 3t + 0, 1, 2][S][n_act];
+    // adjoint checkpoints: at steps flagged kFlagCkpt (every ckpt_every-th
+    // step of the scan, a multiple of kAdjWin), the lab-frame state before
+    // the step into slot (step / ckpt_every) of
+    // [slot][3P: Mx, My, Mz of pool t at 3t + 0, 1, 2][S][n_act];
     // ckpt_step0 = the scan step index of the launch's first step
     float *ckpt;
     long long ckpt_step0;
+    int ckpt_every;
     float cs2pi[kMaxPool];  // (float)(2*pi*(float)CS[t])
     int kind[kMaxPool];     // KM_EXCH: 0 free, 1 bound, other values: pool left untouched
 };

@@ -104,7 +104,9 @@ struct AdjLaunch {
     float cs2pi[kMaxPool];
     const float4 *rec;                   // [n_steps][3]
     long long n_steps;
-    const float *ckpt;                   // [window][3P][n_iso], written by the forward scan
+    const float *ckpt;                   // [slot][3P][n_iso], every seg windows, written by the forward scan
+    int seg;                             // windows (of kAdjWin steps) per stored checkpoint
+    float *ck2;                          // seg > 1: [seg][3P][n_iso] the current segment's window checkpoints
     const float2 *gsig;                  // [A][P][rx] dL/dSx + i dL/dSy, one sample's values together
     float *giso;                         // [fields][n_iso]: T1[P] T2[P] Rho[P] dB0 K[P*P] Mx0[P] My0[P] Mz0[P]
     double *grf;                         // [n_rf][2]

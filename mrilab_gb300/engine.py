@@ -412,6 +412,7 @@ class AdjointPlan:
         lib.mrl_adjoint_plan_backward.argtypes = [ctypes.c_void_p, _d, _d, ctypes.c_void_p]
         lib.mrl_adjoint_plan_gradients.argtypes = [ctypes.c_void_p, ctypes.POINTER(AdjointArgs)]
         lib.mrl_adjoint_plan_work.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
+        lib.mrl_adjoint_plan_checkpoints.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
         lib.mrl_adjoint_plan_destroy.argtypes = [ctypes.c_void_p]
         self.lib = lib
         self.sc = sc
@@ -430,6 +431,13 @@ class AdjointPlan:
         buf = (ctypes.c_longlong * 6)()
         self.lib.mrl_adjoint_plan_work(self.ptr, buf)
         return dict(units=buf[0], steps=buf[1], rf_steps=buf[2], samples=buf[3], launches=buf[4], n_rf=buf[5])
+
+    def checkpoints(self) -> Dict[str, int]:
+        """Steps between stored checkpoints, between the checkpoints the
+        backward walk starts from, and their device bytes."""
+        buf = (ctypes.c_longlong * 3)()
+        self._check(self.lib.mrl_adjoint_plan_checkpoints(self.ptr, buf))
+        return dict(stored_every=buf[0], window=buf[1], bytes=buf[2])
 
     def forward(self, stream: Optional[int] = None) -> None:
         self._check(self.lib.mrl_adjoint_plan_forward(self.ptr, ctypes.c_void_p(stream or 0)))

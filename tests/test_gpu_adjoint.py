@@ -170,6 +170,36 @@ def test_adjoint_mt_epi_many_coils(built):
     _run(phantoms.config5_mt_epi(seed=5, nx=4, ny=4, nz=1, spins=1, n_coils=12, n_read=8, n_pe=8))
 
 
+def test_adjoint_two_level_checkpoints(built, monkeypatch):
+    """Checkpoints stored every 4 windows (64 steps), the adjoint rebuilding
+    each segment's window checkpoints: the gradients of the one-level plan,
+    to the FP32 rounding of the rebuilt states."""
+    sc = _phase_modulated(phantoms.small_multipool("gm", seed=39, n=5, pools=3, spins=2, coils=3, n_tr=3,
+                                                   seq="sat"), 10)
+    tx, ty = _target(sc)
+    out = engine.scan(sc)
+    gx, gy = 2 * (out["Sx"] - tx), 2 * (out["Sy"] - ty)
+    one = engine.adjoint(sc, gx, gy)
+    for seg in ("4", "3"):
+        monkeypatch.setenv("MRL_ADJ_SEGMENT", seg)
+        plan = engine.AdjointPlan(sc)
+        try:
+            ck = plan.checkpoints()
+            assert ck["stored_every"] == 16 * int(seg) and ck["window"] == 16
+            plan.forward()
+            o2 = plan.signal()
+            np.testing.assert_array_equal(o2["Sx"], out["Sx"])
+            plan.backward(gx, gy)
+            g = plan.gradients()
+        finally:
+            plan.close()
+        for k in ("T1", "T2", "Rho", "dB0", "K", "Mz0", "rf"):
+            a, b = np.asarray(g[k], np.float64), np.asarray(one[k], np.float64)
+            err = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+            print(f"segment {seg}: {k} relative difference {err:.2e}")
+            assert err <= 1e-4
+
+
 def test_adjoint_rejects_mt_model(built):
     sc = phantoms.small_multipool("mt", seed=33, n=4, pools=2, spins=1, coils=1, n_tr=1, seq="sat")
     with pytest.raises(engine.ScanError) as e:
