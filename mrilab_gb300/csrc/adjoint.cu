@@ -366,7 +366,6 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
         // window first), rebuild the states at its windows' starts from the
         // segment's stored checkpoint into ck2
         const long long wseg = w / L.seg * L.seg;  // the segment's first window
-        const float *wck = L.ckpt + w * cs * L.n_iso + iso;
         if (L.seg > 1) {
             float *c2 = L.ck2 + iso;
             if (w == nwin - 1 || w % L.seg == L.seg - 1) {
@@ -396,8 +395,9 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 }
                 __syncthreads();
             }
-            wck = c2 + (w - wseg) * cs * L.n_iso;
         }
+        // this window's starting state
+        const float *wck = L.seg > 1 ? L.ck2 + (w - wseg) * cs * L.n_iso + iso : L.ckpt + w * cs * L.n_iso + iso;
         // the window's step records, staged in shared memory
         if (tid < 3 * nk) wrec[tid] = __ldg(L.rec + k0 * 3 + tid);
         __syncthreads();
