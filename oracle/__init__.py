@@ -67,6 +67,7 @@ class PortArgs(ctypes.Structure):
         ("ext_cb", _EXT_CB), ("ext_user", ctypes.c_void_p),
         ("run_mode", ctypes.c_int), ("mxs", _f), ("mys", _f), ("mzs", _f), ("muts", _d),
         ("exact", ctypes.c_int),
+        ("steps_out", _d), ("steps_cap", ctypes.c_longlong),
     ]
 
 
@@ -99,19 +100,31 @@ def _f64(a):
 
 
 def run_port(scan, precision: str = "f32", threads: int = 0, max_steps: int = -1,
-             ext_cb=None, exact: bool = False) -> Dict[str, np.ndarray]:
+             ext_cb=None, exact: bool = False, step_records: int = 0) -> Dict[str, np.ndarray]:
     """Run the C oracle on a ``phantoms.Scan``; returns Sx, Sy, Kx, Ky, Kz,
     final Mx, My, Mz (flattened column-major) and ``steps``.  ``exact``: the
     exact relaxation-exchange propagator instead of the reference's split
-    exchange (ME, and GM without bound pools)."""
+    exchange (ME, and GM without bound pools).  ``step_records`` > 0: also
+    ``records``, the decoded dt > 0 steps ([steps][10]: dt, Gz, Gy, Gx, Tx-0
+    amplitude, phase, frequency, rf_sum, ADC flag, signal index), at most
+    that many."""
     lib = ctypes.CDLL(PORT_SO)
     fn = lib.mrl_port_scan_f32 if precision == "f32" else lib.mrl_port_scan_f64
     fn.argtypes = [ctypes.POINTER(PortArgs), ctypes.POINTER(ctypes.c_longlong)]
     fn.restype = ctypes.c_int
     steps = ctypes.c_longlong(0)
-    out = _call_with_args(scan, lambda args: fn(ctypes.byref(args), ctypes.byref(steps)), threads, max_steps,
-                          ext_cb, exact)
+    rec = np.zeros((max(step_records, 1), 10))
+
+    def call(args):
+        if step_records > 0:
+            args.steps_out = _ptr(rec, _d)
+            args.steps_cap = step_records
+        return fn(ctypes.byref(args), ctypes.byref(steps))
+
+    out = _call_with_args(scan, call, threads, max_steps, ext_cb, exact)
     out["steps"] = int(steps.value)
+    if step_records > 0:
+        out["records"] = rec[: min(out["steps"], step_records)].copy()
     return out
 
 

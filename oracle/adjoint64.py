@@ -1,0 +1,200 @@
+"""FP64 reference gradient of the scan -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/`` use this module, as the checker of the adjoint kernel.  The
+C oracle's discrete map (``port/mrl_port_impl.h``, the reference's
+algorithm: ``BlochKernel.h:38-368`` for the normal model,
+``BlochKernelME.cuh:154-343`` and ``BlochKernelGM.cuh:159-471`` for the
+exchange models, receive ``DoScanAtCPU.cpp:445-491``) is restated step by
+step in float64 PyTorch on the CPU, vectorised over isochromats, and
+differentiated by reverse-mode automatic differentiation: a double-precision
+gradient derived independently of the hand-written adjoint.  The steps are
+the C oracle's own decode (``run_port(..., step_records=N)``), so both walk
+the same step list.  The autograd graph holds every step: small cases only.
+
+Scope as the adjoint kernel's: normal, ME and GM models (GM pools of
+TypeFlag 0 and 1), one transmit coil.
+"""
+from __future__ import annotations
+
+from typing import Dict
+
+import numpy as np
+import torch
+
+from . import run_port
+
+PI = 3.14159265359  # the reference's constant
+
+
+def _flat(arr) -> np.ndarray:
+    return np.asarray(arr).ravel(order="F").astype(np.float32).astype(np.float64)
+
+
+def _lineshape(freq: float, db0: torch.Tensor, gyro: float, t2b: torch.Tensor) -> torch.Tensor:
+    """Super-Lorentzian lineshape of a bound pool, the oracle's 1000-point
+    rule (BlochKernelMT.cuh:348-358), per voxel."""
+    u = torch.arange(1000, dtype=torch.float64) * 0.001
+    den = 3 * u * u - 1
+    x = ((2 * PI * freq + db0 * gyro) * t2b)[:, None] / den
+    return (np.sqrt(2 / PI) * t2b[:, None] / den.abs() * torch.exp(-2 * x * x) * 0.001).sum(-1)
+
+
+def _rotate(x, y, z, vx, vy, vz):
+    """exp([v]x) m by Rodrigues' formula, with the series of sin a / a and
+    (1 - cos a) / a^2 near a = 0 (kept off the division there, so the
+    gradient stays finite)."""
+    a2 = vx * vx + vy * vy + vz * vz
+    small = a2 < 1e-8
+    a2s = torch.where(small, torch.ones_like(a2), a2)
+    a = torch.sqrt(a2s)
+    s1 = torch.where(small, 1 - a2 / 6, torch.sin(a) / a)
+    s2 = torch.where(small, 0.5 - a2 / 24, (1 - torch.cos(a)) / a2s)
+    cx, cy, cz = vy * z - vz * y, vz * x - vx * z, vx * y - vy * x  # v x m
+    dx, dy, dz = vy * cz - vz * cy, vz * cx - vx * cz, vx * cy - vy * cx  # v x (v x m)
+    return x + s1 * cx + s2 * dx, y + s1 * cy + s2 * dy, z + s1 * cz + s2 * dz
+
+
+def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
+    """dL/dtheta of L = sum(grad_sx * Sx + grad_sy * Sy) over the scan's
+    signal (so its gradient is the adjoint's for those dL/dS), in the
+    adjoint's layouts: T1, T2, Rho [P*V], dB0 [V], K [nK*V], Mx0, My0, Mz0
+    [P*S*V], rf [n_rf, 2] (dL/dRe A, dL/dIm A of each rf-on step), plus
+    Sx, Sy (the signal of the restated map)."""
+    o, mag, coil, ctl = sc.VObj, sc.VMag, sc.VCoi, sc.VCtl
+    model = sc.model
+    if model not in ("normal", "me", "gm"):
+        raise ValueError("the FP64 adjoint covers the normal, ME and GM models")
+    P, S = int(o["TypeNum"]), int(o["SpinNum"])
+    TX, RX = int(coil["TxCoilNum"]), int(coil["RxCoilNum"])
+    if TX != 1:
+        raise ValueError("one transmit coil")
+    A = int(sc.VSig["SignalNum"])
+    V = int(np.asarray(o["Rho"]).size // P)
+    gyro = float(o["Gyro"])
+    n = run_port(sc, "f64")["steps"]
+    rec = run_port(sc, "f64", step_records=max(n, 1))["records"]
+
+    def leaf(a):
+        return torch.tensor(a, dtype=torch.float64, requires_grad=True)
+
+    T1 = leaf(_flat(o["T1"]).reshape(P, V))
+    T2 = leaf(_flat(o["T2"]).reshape(P, V))
+    Rho = leaf(_flat(o["Rho"]).reshape(P, V))
+    dB0 = leaf(_flat(mag["dB0"]))
+    has_k = model != "normal"
+    K = leaf(_flat(o["K"]).reshape(-1, V)) if has_k else None
+    Mx0 = leaf(_flat(o["Mx"]).reshape(P, S, V))
+    My0 = leaf(_flat(o["My"]).reshape(P, S, V))
+    Mz0 = leaf(_flat(o["Mz"]).reshape(P, S, V))
+    rf_on = rec[:, 7] != 0
+    amp, ph = rec[rf_on, 4], rec[rf_on, 5]
+    rfa = leaf(np.stack([amp * np.cos(ph), amp * np.sin(ph)], 1))
+
+    t = lambda a: torch.tensor(a, dtype=torch.float64)
+    dwr = t(_flat(mag["dWRnd"]).reshape(P, S, V))
+    gzg, gyg, gxg = (t(_flat(mag[k])) for k in ("Gzgrid", "Gygrid", "Gxgrid"))
+    mg, pe = t(_flat(coil["TxCoilmg"])[:V]), t(_flat(coil["TxCoilpe"])[:V])
+    txc_re, txc_im = mg * torch.cos(pe), mg * torch.sin(pe)
+    if float(coil["RxCoilDefault"]) == 0:
+        rxr, rxi = t(_flat(coil["RxCoilx"]).reshape(RX, V)), t(_flat(coil["RxCoily"]).reshape(RX, V))
+    else:
+        rxr, rxi = torch.ones(RX, V, dtype=torch.float64), torch.zeros(RX, V, dtype=torch.float64)
+    cs = np.asarray(ctl["CS"], np.float64).ravel()
+    kind = np.zeros(P, int) if model != "gm" else np.asarray(o["TypeFlag"], np.float64).ravel().astype(int)
+    rf_ref = float(sc.VVar["rfRef"])
+    gx_t = t(np.asarray(grad_sx, np.float64).reshape(P, RX, A))
+    gy_t = t(np.asarray(grad_sy, np.float64).reshape(P, RX, A))
+
+    on = ((T1 != 0) & (T2 != 0) & (Rho != 0)).detach()  # [P, V]
+    T1s = torch.where(on, T1, torch.ones_like(T1))
+    T2s = torch.where(on, T2, torch.ones_like(T2))
+    if has_k:
+        def kgo(a, b):  # rate a -> b (ME channel a*P+b, GM b*P+a)
+            return K[a * P + b] if model == "me" else K[b * P + a]
+
+    X, Y, Z = Mx0, My0, Mz0
+    loss = torch.zeros((), dtype=torch.float64)
+    sig_x = torch.zeros(P, RX, A, dtype=torch.float64)
+    sig_y = torch.zeros(P, RX, A, dtype=torch.float64)
+    cr, sr = np.cos(-rf_ref), np.sin(-rf_ref)
+    ri = 0
+    for r in rec:
+        dt, gz, gy, gx, _, _, freq, rf_sum, adc, sidx = (float(q) for q in r)
+        if adc and int(sidx) < A:
+            # receive before the step: sum over spins and voxels of m conj(R_c)
+            for tp in range(P):
+                if kind[tp] != 0:
+                    continue
+                mx, my = X[tp].sum(0), Y[tp].sum(0)  # [V]
+                b1 = (mx[None] * rxr + my[None] * rxi).sum(1)  # [RX]
+                b3 = (my[None] * rxr - mx[None] * rxi).sum(1)
+                if rf_ref != 0:
+                    b1, b3 = b1 * cr - b3 * sr, b1 * sr + b3 * cr
+                a = int(sidx)
+                loss = loss + (gx_t[tp, :, a] * b1).sum() + (gy_t[tp, :, a] * b3).sum()
+                sig_x[tp, :, a] = b1.detach()
+                sig_y[tp, :, a] = b3.detach()
+        w = (dB0 * gyro)[None, None] + dwr + t(2 * PI * cs)[:, None, None] \
+            + (gzg * (gz * gyro) + gyg * (gy * gyro) + gxg * (gx * gyro))[None, None]
+        rf = rf_sum != 0
+        if rf:
+            Ar, Ai = rfa[ri, 0], rfa[ri, 1]
+            ri += 1
+            vx = (-dt * gyro) * (txc_re * Ar - txc_im * Ai)
+            vy = (-dt * gyro) * (txc_re * Ai + txc_im * Ar)
+            vz = -dt * (w + 2 * PI * freq)
+            xr, yr, zr = _rotate(X, Y, Z, vx[None, None].expand_as(X), vy[None, None].expand_as(X), vz)
+        else:
+            zero = torch.zeros_like(X)
+            xr, yr, zr = _rotate(X, Y, Z, zero, zero, -dt * w)
+        nx, ny, nz = [], [], []
+        for tp in range(P):
+            e1 = torch.exp(torch.clamp(-dt / T1s[tp], min=-200.0))[None]
+            e2 = torch.exp(torch.clamp(-dt / T2s[tp], min=-200.0))[None]
+            m0 = (Rho[tp] * (1 - e1[0]) / S)[None]
+            act = on[tp][None].expand(S, V)
+            if model == "normal":
+                x1, y1, z1 = xr[tp] * e2, yr[tp] * e2, zr[tp] * e1 + m0
+            elif kind[tp] not in (0, 1):
+                x1, y1, z1 = X[tp], Y[tp], Z[tp]
+            else:
+                ksum = torch.zeros(V, dtype=torch.float64)
+                ix = torch.zeros(S, V, dtype=torch.float64)
+                iy = torch.zeros(S, V, dtype=torch.float64)
+                iz = torch.zeros(S, V, dtype=torch.float64)
+                for p in range(P):
+                    if model == "gm" and p == tp:
+                        continue
+                    ksum = ksum + kgo(tp, p)
+                    f = 1 - torch.exp(-dt * kgo(p, tp))[None]
+                    if kind[tp] == 0:
+                        ix = ix + f * X[p]
+                        iy = iy + f * Y[p]
+                    iz = iz + f * Z[p]
+                kout = torch.exp(-dt * ksum)[None]
+                if kind[tp] == 0:
+                    x1, y1 = xr[tp] * e2 * kout + ix, yr[tp] * e2 * kout + iy
+                    zb = zr[tp]
+                else:
+                    x1, y1 = X[tp], Y[tp]
+                    zb = Z[tp]
+                    if rf:
+                        b1 = mg * torch.sqrt(Ar * Ar + Ai * Ai)
+                        W = PI * (b1 * gyro) ** 2 * _lineshape(freq, dB0, gyro, T2s[tp])
+                        zb = zb * torch.exp(-W * dt)[None]
+                z1 = zb * e1 * kout + iz + m0
+            nx.append(torch.where(act, x1, X[tp]))
+            ny.append(torch.where(act, y1, Y[tp]))
+            nz.append(torch.where(act, z1, Z[tp]))
+        X, Y, Z = torch.stack(nx), torch.stack(ny), torch.stack(nz)
+    loss.backward()
+
+    def g(x):
+        return np.zeros(0) if x is None or x.grad is None else x.grad.numpy().ravel().copy()
+
+    out = dict(T1=g(T1), T2=g(T2), Rho=g(Rho), dB0=g(dB0), Mx0=g(Mx0), My0=g(My0), Mz0=g(Mz0),
+               rf=rfa.grad.numpy().copy() if rfa.grad is not None else np.zeros((0, 2)),
+               Sx=sig_x.numpy().ravel(), Sy=sig_y.numpy().ravel())
+    if has_k:
+        out["K"] = g(K)
+    return out

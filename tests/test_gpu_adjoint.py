@@ -200,6 +200,43 @@ def test_adjoint_two_level_checkpoints(built, monkeypatch):
             assert err <= 1e-4
 
 
+@pytest.mark.parametrize("case", ["gre", "me3", "gm_bound", "bssfp"])
+def test_adjoint_vs_fp64_adjoint(built, case):
+    """The FP32 adjoint kernel against the FP64 reference gradient
+    (oracle.adjoint64: the oracle's map in float64, differentiated by
+    autograd) for the same dL/dS, every element of every family, norm-wise
+    per family."""
+    pytest.importorskip("torch")
+    from oracle import adjoint64
+
+    sc = {"gre": lambda: phantoms.config1_gre(seed=41, n=6, n_tr=2),
+          "me3": lambda: phantoms.small_multipool("me", seed=42, n=4, pools=3, spins=2, coils=3, n_tr=2),
+          "gm_bound": lambda: phantoms.small_multipool("gm", seed=43, n=4, pools=3, spins=1, coils=2, n_tr=2,
+                                                       seq="sat"),
+          "bssfp": lambda: phantoms.config4_adjoint(seed=44, nx=4, ny=4, nz=2, n_tr=2)}[case]()
+    sc = _phase_modulated(sc, 12)
+    tx, ty = _target(sc)
+    _, gx, gy = _loss(sc, (tx, ty))
+    g = engine.adjoint(sc, gx, gy)
+    ref = adjoint64.gradients(sc, gx, gy)
+    o = sc.VObj
+    P, S = int(o["TypeNum"]), int(o["SpinNum"])
+    act = ((o["Rho"] != 0) & (o["T1"] != 0) & (o["T2"] != 0)).ravel(order="F")
+    vact = act.reshape(-1, P, order="F").any(axis=1)
+    fams = [("T1", act), ("T2", act), ("Rho", act), ("dB0", vact),
+            ("Mz0", np.tile(vact, P * S)), ("Mx0", np.tile(vact, P * S))]
+    if "K" in ref:
+        fams.append(("K", np.ones(ref["K"].size, bool)))
+    for key, sel in fams:
+        a, b = np.asarray(g[key], np.float64)[sel], ref[key][sel]
+        err = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        print(f"{case} {key}: |grad| {np.linalg.norm(b):.4e}, relative error {err:.2e} over {b.size} elements")
+        assert err <= TOL
+    err = float(np.linalg.norm(g["rf"] - ref["rf"]) / np.linalg.norm(ref["rf"]))
+    print(f"{case} rf: relative error {err:.2e} over {ref['rf'].shape[0]} steps")
+    assert err <= TOL
+
+
 def test_adjoint_rejects_mt_model(built):
     sc = phantoms.small_multipool("mt", seed=33, n=4, pools=2, spins=1, coils=1, n_tr=1, seq="sat")
     with pytest.raises(engine.ScanError) as e:

@@ -163,3 +163,49 @@ def test_exact_oracle_matches_bloch_mcconnell_expm(built, model):
     got = np.concatenate([out["Mx"], out["My"], out["Mz"]])
     # the oracle's FP64 state is returned in the single-precision state arrays
     assert np.abs(got - ref[:-1]).max() <= 2e-7 * np.abs(ref[:-1]).max()
+
+
+def _fp64_adjoint_case(name):
+    if name == "me2":
+        return phantoms.small_multipool("me", seed=32, n=5, pools=2, spins=2, coils=2, n_tr=2)
+    return phantoms.small_multipool("gm", seed=38, n=4, pools=3, spins=1, coils=2, n_tr=2, seq="sat")
+
+
+@pytest.mark.parametrize("name", ["me2", "gm_bound"])
+def test_fp64_adjoint_pinned(name):
+    """The FP64 reference gradient (oracle.adjoint64: the oracle's map
+    restated in float64 PyTorch, differentiated by autograd) is pinned to
+    the C oracle: its signal is the FP64 port's, and its gradient of
+    L = gx.Sx + gy.Sy matches central differences of the FP64 port (step
+    1e-3 relative, dB0 1e-10 T) element by element."""
+    pytest.importorskip("torch")
+    from oracle import adjoint64
+
+    sc = _fp64_adjoint_case(name)
+    P, RX, A = int(sc.VObj["TypeNum"]), int(sc.VCoi["RxCoilNum"]), int(sc.VSig["SignalNum"])
+    gx = np.random.default_rng(0).normal(size=P * RX * A)
+    gy = np.random.default_rng(1).normal(size=P * RX * A)
+    g = adjoint64.gradients(sc, gx, gy)
+    ref = oracle.run_port(sc, "f64")
+    assert rel_l2(g["Sx"] + 1j * g["Sy"], ref["Sx"] + 1j * ref["Sy"]) <= 1e-12
+
+    def loss(s):
+        o = oracle.run_port(s, "f64")
+        return float(np.dot(gx, o["Sx"]) + np.dot(gy, o["Sy"]))
+
+    for struct, key in (("VObj", "T1"), ("VObj", "T2"), ("VObj", "Rho"), ("VMag", "dB0"), ("VObj", "K")):
+        arr = getattr(sc, struct)[key]
+        base = np.asarray(arr, np.float64).ravel(order="F")
+        nz = np.flatnonzero(base)
+        for i in nz[:: max(1, nz.size // 3)][:3]:
+            h = 1e-10 if key == "dB0" else 1e-3 * abs(base[i])
+            out = []
+            for sgn in (1, -1):
+                b = base.copy()
+                b[i] = np.float32(base[i] + sgn * h)
+                s = sc.copy()
+                d = getattr(s, struct)
+                d[key] = np.asfortranarray(b.astype(arr.dtype).reshape(arr.shape, order="F"))
+                out.append((loss(s), b[i]))
+            fd = (out[0][0] - out[1][0]) / (out[0][1] - out[1][1])
+            assert abs(g[key][i] - fd) <= 1e-5 * abs(fd) + 1e-12, (key, i, g[key][i], fd)
