@@ -37,11 +37,17 @@
 //
 // One thread owns one isochromat (a voxel's spin, all its pools).  The
 // forward scan (the accurate integrator, whose frames are anchored to FP64
-// phase moments) stores the lab-frame state every kAdjWin steps
-// (checkpoints, in HBM); this kernel takes the windows last to first,
-// recomputes each window's states from its checkpoint into shared memory
-// with the map above and walks them in reverse.  The rf gradient of a step is summed over the block (warp
-// shuffles, then the warps) and added to its FP64 slot.
+// phase moments) stores the lab-frame state every seg * kAdjWin steps
+// (checkpoints, in HBM); this kernel takes the windows of kAdjWin steps
+// last to first, recomputes each window's states from its starting state
+// into shared memory with the map above and walks them in reverse.  With
+// seg > 1, entering a segment it first runs the segment forward from its
+// checkpoint and keeps every window's starting state in ck2.  The rf
+// gradient of a step is summed over the block (warp shuffles, then the
+// warps) and added to its FP64 slot.  The receive term reads the thread's
+// coil sensitivities from shared memory (staged once) and the step's dL/dS
+// from a per-warp shared buffer that cp.async filled during the step
+// before.
 #include "scan_launch.h"
 
 namespace mrl {
