@@ -1,16 +1,16 @@
 """CPU oracle for the MRiLab scan engine -- TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
-baseline / reference arm may use this package, and only as the checker or
-as the timed CPU baseline; the product (``mrilab_gb300``) never imports it.
+baseline / reference arm may use this package, and only as the reference
+results the product is compared with or as the timed CPU baseline; the product (``mrilab_gb300``) never imports it.
 
 Three oracles live here:
 
 * ``run_port``: ``port/mrl_port.c``, a plain-C restatement of the reference
   scan algorithm (sequence decode ``DoScanAtCPU.cpp:246-420``; single-pool
   kernel ``BlochKernel.h``; ME/MT/CEST/GM kernels ``BlochKernel*.cuh``) in
-  single precision (``"f32"``) and all-double (``"f64"``).  It travels to the
-  GPU machine and is built there by ``build()``.
+  single precision (``"f32"``) and all-double (``"f64"``).  It travels with
+  the repository and is built where it runs by ``build()``.
 * ``run_ref_cpu``: the reference CPU engine itself
   (``Lib/src/engine/CPUEngine/DoScanAtCPU.cpp``), compiled unmodified from
   the reference tree against project-written mex/IPP shims into ``_ref/``
@@ -73,7 +73,7 @@ class PortArgs(ctypes.Structure):
 
 def build(force: bool = False) -> None:
     """Compile the port (always) and the reference objects (where the
-    reference tree exists).  Building the checker is not using it."""
+    reference tree exists).  Building the oracle is not using it."""
     src = os.path.join(HERE, "port", "mrl_port.c")
     hdr = os.path.join(HERE, "port", "mrl_port_impl.h")
     if force or not os.path.exists(PORT_SO) or os.path.getmtime(PORT_SO) < max(

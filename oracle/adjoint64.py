@@ -1,6 +1,7 @@
 """FP64 reference gradient of the scan -- TEST INFRASTRUCTURE ONLY.
 
-Only ``tests/`` use this module, as the checker of the adjoint kernel.  The
+Only ``tests/`` use this module, as the reference the adjoint kernel is
+compared with.  The
 C oracle's discrete map (``port/mrl_port_impl.h``, the reference's
 algorithm: ``BlochKernel.h:38-368`` for the normal model,
 ``BlochKernelME.cuh:154-343`` and ``BlochKernelGM.cuh:159-471`` for the

@@ -3,7 +3,7 @@
  *
  * A plain-C restatement of the reference's scan algorithm, used only by the
  * tests, __graft_entry__.smoke() and bench.py's cpu_baseline/reference arm
- * as the checker and as the timed CPU baseline.  It is never part of the
+ * as the reference results and as the timed CPU baseline.  It is never part of the
  * product path.  Each step follows the reference file it cites:
  *
  *   sequence decode          Lib/src/engine/CPUEngine/DoScanAtCPU.cpp:246-420
