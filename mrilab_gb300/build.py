@@ -49,6 +49,7 @@ UNITS = {
     "scan_fast_cest.cu": [],
     "adjoint.cu": [],
     "scan_fast_exact.cu": [],
+    "scan_fast_exact_bound.cu": [],
     "decode.cpp": None,  # host C++
 }
 

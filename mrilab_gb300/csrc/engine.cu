@@ -289,7 +289,7 @@ inline int split_source(int km, int P, bool all_free) { return km == KM_EXCH && 
 
 cudaError_t launch_fast(int km, int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
                         const FastGrid &g, int co = 0) {
-    if (co) return launch_scan_fast_tab(co, P, NS, grid, smem, st, g);
+    if (co) return launch_scan_fast_tab(co, P, NS, all_free, grid, smem, st, g);
     switch (km) {
     case KM_NORMAL: return launch_scan_fast_normal(P, NS, all_free, grid, smem, st, g);
     case KM_EXCH: return launch_scan_fast_exch(P, NS, all_free, grid, smem, st, g);
@@ -299,7 +299,7 @@ cudaError_t launch_fast(int km, int P, int NS, bool all_free, dim3 grid, size_t 
 }
 
 int occupancy_fast(int km, int P, int NS, bool all_free, size_t smem, int co = 0) {
-    if (co) return occupancy_scan_fast_tab(co, P, NS, smem);
+    if (co) return occupancy_scan_fast_tab(co, P, NS, all_free, smem);
     switch (km) {
     case KM_NORMAL: return occupancy_scan_fast_normal(P, NS, all_free, smem);
     case KM_EXCH: return occupancy_scan_fast_exch(P, NS, all_free, smem);
@@ -407,6 +407,14 @@ struct Scanner {
         if (st && own_st) cudaStreamDestroy(st);
     }
 
+    // the general model's bound pools (TypeFlag 1), one bit per pool
+    unsigned bound_mask() const {
+        unsigned m = 0;
+        for (int t = 0; mi.km == KM_EXCH && mi.gm && t < P; ++t)
+            if ((int)args->obj.type_flag[t] == 1) m |= 1u << t;
+        return m;
+    }
+
     // every pool of an exchange model is a free pool (ME, or GM without bound pools)
     int all_free() const {
         if (mi.km != KM_EXCH) return 0;
@@ -483,10 +491,16 @@ struct Scanner {
             return set_err("unknown numerics %d", a.ctl.numerics), MRL_ERR_ARG;
         exact = a.ctl.numerics == MRL_NUMERICS_EXACT && mi.km != KM_NORMAL;
         if (exact) {
-            bool free_pools = mi.km == KM_EXCH;
-            for (int t = 0; free_pools && mi.gm && t < P; ++t) free_pools = (int)a.obj.type_flag[t] == 0;
-            if (!free_pools)
-                return set_err("MRL_NUMERICS_EXACT covers free pools exchanging (ME, GM without bound pools)"),
+            // ME, or GM pools free (TypeFlag 0) or bound (1) with a free one
+            bool ok = mi.km == KM_EXCH, any_free = !mi.gm;
+            for (int t = 0; ok && mi.gm && t < P; ++t) {
+                const int k = (int)a.obj.type_flag[t];
+                ok = k == 0 || k == 1;
+                any_free = any_free || k == 0;
+            }
+            if (!ok || !any_free)
+                return set_err("MRL_NUMERICS_EXACT covers the ME model and GM pools of TypeFlag 0 and 1 "
+                               "(with a free pool)"),
                        MRL_ERR_UNSUPPORTED;
             if (P > 3) return set_err("MRL_NUMERICS_EXACT supports TypeNum <= 3"), MRL_ERR_UNSUPPORTED;
         }
@@ -768,7 +782,8 @@ struct Scanner {
         const float *kch = mi.nk > 0 ? d_f.p + o_k : nullptr;
         if (e == cudaSuccess)
             e = coef == 2 ? launch_exact_table(P, d_xdts.p, (int)xdts.size(), n_act, S, mi.gm ? 1 : 0,
-                                               d_f.p + o_rho, d_f.p + o_t1, d_f.p + o_t2, kch, d_xtab.p, st)
+                                               bound_mask(), d_f.p + o_rho, d_f.p + o_t1, d_f.p + o_t2, kch,
+                                               d_xtab.p, st)
                           : launch_split_table(P, d_xdts.p, (int)xdts.size(), n_act, mi.gm ? 1 : 0,
                                                d_f.p + o_rho, d_f.p + o_t1, d_f.p + o_t2, kch, d_xtab.p, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);

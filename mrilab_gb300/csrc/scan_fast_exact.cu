@@ -18,15 +18,16 @@
 namespace mrl {
 
 namespace {
-using Kernel = void (*)(const FastLaunch *, const int2 *, int, int *);
+using Kernel = FastKernel;
 
 template <int P, int NS>
 Kernel pick(int co) {
     return co == 2 ? scan_fast_kernel<KM_EXCH, P, NS, true, 2> : scan_fast_kernel<KM_EXCH, P, NS, true, 1>;
 }
 
-Kernel select(int co, int P, int NS) {
+Kernel select(int co, int P, int NS, bool all_free) {
     if (co != 1 && co != 2) return nullptr;
+    if (!all_free) return co == 2 ? select_exact_bound(P, NS) : nullptr;
     if (P == 1 && NS == 1) return pick<1, 1>(co);
     if (P == 1 && NS == 2) return pick<1, 2>(co);
     if (P == 1 && NS == 4) return pick<1, 4>(co);
@@ -113,7 +114,7 @@ __device__ void expm1_phi1(const double (&A)[P][P], double (&F)[P][P], double (&
 
 template <int P>
 __global__ void exact_table_kernel(const float *__restrict__ dts, int n_dt, int n_act, int S, int gm,
-                                   const float *__restrict__ rho, const float *__restrict__ t1,
+                                   unsigned bound, const float *__restrict__ rho, const float *__restrict__ t1,
                                    const float *__restrict__ t2, const float *__restrict__ kch, float *tab) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)n_dt * n_act) return;
@@ -131,7 +132,10 @@ __global__ void exact_table_kernel(const float *__restrict__ dts, int n_dt, int 
         const double T1 = t1[(long long)t * n_act + v], T2 = t2[(long long)t * n_act + v],
                      r = rho[(long long)t * n_act + v];
         if (T1 == 0.0 || T2 == 0.0 || r == 0.0) continue;  // a pool left alone: identity row
-        At[t][t] = -1.0 / T2;
+        // a bound pool: no transverse generator (identity row), and no free
+        // pool takes transverse inflow from it
+        const bool bt = bound >> t & 1u;
+        if (!bt) At[t][t] = -1.0 / T2;
         Al[t][t] = -1.0 / T1;
         b[t] = r / (S * T1);
 #pragma unroll
@@ -140,9 +144,9 @@ __global__ void exact_table_kernel(const float *__restrict__ dts, int n_dt, int 
             // ME: channel a*P+b is the rate a -> b; GM: channel b*P+a
             const double kgo = kch[(long long)(gm ? p * P + t : t * P + p) * n_act + v];
             const double kin = kch[(long long)(gm ? t * P + p : p * P + t) * n_act + v];
-            At[t][t] -= kgo;
+            if (!bt) At[t][t] -= kgo;
             Al[t][t] -= kgo;
-            At[t][p] += kin;
+            if (!bt && !(bound >> p & 1u)) At[t][p] += kin;
             Al[t][p] += kin;
         }
     }
@@ -245,8 +249,9 @@ cudaError_t launch_split_table(int P, const float *dts, int n_dt, int n_act, int
     return cudaGetLastError();
 }
 
-cudaError_t launch_scan_fast_tab(int co, int P, int NS, dim3 grid, size_t smem, cudaStream_t st, const FastGrid &g) {
-    Kernel k = select(co, P, NS);
+cudaError_t launch_scan_fast_tab(int co, int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
+                                 const FastGrid &g) {
+    Kernel k = select(co, P, NS, all_free);
     if (!k) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -254,8 +259,8 @@ cudaError_t launch_scan_fast_tab(int co, int P, int NS, dim3 grid, size_t smem, 
     return cudaGetLastError();
 }
 
-int occupancy_scan_fast_tab(int co, int P, int NS, size_t smem) {
-    Kernel k = select(co, P, NS);
+int occupancy_scan_fast_tab(int co, int P, int NS, bool all_free, size_t smem) {
+    Kernel k = select(co, P, NS, all_free);
     int n = 0;
     if (!k || cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kBlock, smem) != cudaSuccess)
@@ -263,15 +268,16 @@ int occupancy_scan_fast_tab(int co, int P, int NS, size_t smem) {
     return n;
 }
 
-cudaError_t launch_exact_table(int P, const float *dts, int n_dt, int n_act, int S, int gm, const float *rho,
-                               const float *t1, const float *t2, const float *kch, float *tab, cudaStream_t st) {
+cudaError_t launch_exact_table(int P, const float *dts, int n_dt, int n_act, int S, int gm, unsigned bound,
+                               const float *rho, const float *t1, const float *t2, const float *kch, float *tab,
+                               cudaStream_t st) {
     const long long n = (long long)n_dt * n_act;
     if (n <= 0) return cudaSuccess;
     const unsigned blocks = (unsigned)((n + 127) / 128);
     switch (P) {
-    case 1: exact_table_kernel<1><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, rho, t1, t2, kch, tab); break;
-    case 2: exact_table_kernel<2><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, rho, t1, t2, kch, tab); break;
-    case 3: exact_table_kernel<3><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, rho, t1, t2, kch, tab); break;
+    case 1: exact_table_kernel<1><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, bound, rho, t1, t2, kch, tab); break;
+    case 2: exact_table_kernel<2><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, bound, rho, t1, t2, kch, tab); break;
+    case 3: exact_table_kernel<3><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, bound, rho, t1, t2, kch, tab); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

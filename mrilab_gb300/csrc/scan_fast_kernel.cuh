@@ -298,7 +298,8 @@ __host__ __device__ constexpr int fast_min_blocks() {
 template <int MODEL, int P, int NS, bool FREE, int CO = 0>
 __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigned char *smem, uint32_t &kbase) {
     constexpr bool EXACT = CO == 2;
-    static_assert(CO == 0 || (MODEL == KM_EXCH && FREE), "tabulated coefficients cover free pools exchanging");
+    static_assert(CO == 0 || (MODEL == KM_EXCH && (FREE || CO == 2)),
+                  "tabulated coefficients: free pools exchanging (split), general-model pools (exact)");
     const ScanLaunch &L = F.b;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     float4 *rbuf = reinterpret_cast<float4 *>(smem + 128);
@@ -934,10 +935,12 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                         Z[s][t] = on ? z : pz[t];
                     }
                     // relaxation and inflow after the rotation (the frames hold still);
-                    // the exact propagator takes the partners after their rotation
+                    // the exact propagator takes the partners after their rotation,
+                    // and bound pools after their saturation (sat is zero for the others)
                     if constexpr (EXACT) {
 #pragma unroll
                         for (int t = 0; t < P; ++t) {
+                            if constexpr (!FREE) Z[s][t] = fmaf(-sat[t], Z[s][t], Z[s][t]);
                             px[t] = X[s][t];
                             py[t] = Y[s][t];
                             pz[t] = Z[s][t];

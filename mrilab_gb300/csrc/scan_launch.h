@@ -68,22 +68,29 @@ cudaError_t launch_scan_fast_mt(int P, int NS, bool all_free, dim3 grid, size_t 
 cudaError_t launch_scan_fast_cest(int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
                                   const FastGrid &g);
 // ---- tabulated coefficients and the exact propagator (scan_fast_exact.cu) ------
-// Free pools exchanging (ME, GM without bound pools), TypeNum <= 3.  Fields
-// of the coefficient table per (dt, voxel): diag(E_T) - 1 [P], E_T off the
-// diagonal [P][P] row-major without the diagonal, diag(E_L) - 1 [P], E_L
-// off the diagonal, recovery dt phi1(A_L dt) b [P].
+// Split scheme: free pools exchanging (ME, GM without bound pools); exact
+// propagator: ME and GM pools free or bound (a bound pool has no transverse
+// generator: identity rows and no inflow); TypeNum <= 3.  Fields of the
+// exact table per (dt, voxel): diag(E_T) - 1 [P], E_T off the diagonal
+// [P][P] row-major without the diagonal, diag(E_L) - 1 [P], E_L off the
+// diagonal, recovery dt phi1(A_L dt) b [P].
 __host__ __device__ inline int exact_fields(int P) { return 2 * P * P + P; }
 // The split scheme's table (coefficient source 1): y1 [P], y2 [P], yo [P], fin [P][P].
 __host__ __device__ inline int split_fields(int P) { return 3 * P + P * P; }
-// The instantiations reading a table: co = 1 split scheme, 2 exact propagator.
-cudaError_t launch_scan_fast_tab(int co, int P, int NS, dim3 grid, size_t smem, cudaStream_t st,
+// The instantiations reading a table: co = 1 split scheme, 2 exact propagator
+// (all_free false: general-model pools with bound ones, co = 2 only).
+cudaError_t launch_scan_fast_tab(int co, int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
                                  const FastGrid &g);
-int occupancy_scan_fast_tab(int co, int P, int NS, size_t smem);
+int occupancy_scan_fast_tab(int co, int P, int NS, bool all_free, size_t smem);
+using FastKernel = void (*)(const FastLaunch *, const int2 *, int, int *);
+FastKernel select_exact_bound(int P, int NS);  // scan_fast_exact_bound.cu
 cudaError_t launch_split_table(int P, const float *dts, int n_dt, int n_act, int gm, const float *rho,
                                const float *t1, const float *t2, const float *kch, float *tab, cudaStream_t st);
 // tab[(d * exact_fields(P) + f) * n_act + v] for the n_dt values dts[]
-cudaError_t launch_exact_table(int P, const float *dts, int n_dt, int n_act, int S, int gm, const float *rho,
-                               const float *t1, const float *t2, const float *kch, float *tab, cudaStream_t st);
+// (bound: one bit per bound pool)
+cudaError_t launch_exact_table(int P, const float *dts, int n_dt, int n_act, int S, int gm, unsigned bound,
+                               const float *rho, const float *t1, const float *t2, const float *kch, float *tab,
+                               cudaStream_t st);
 // ---- adjoint (adjoint.cu) ----------------------------------------------------
 constexpr int kAdjBlock = 128;  // threads (isochromats) per block
 

@@ -104,7 +104,7 @@ def run_port(scan, precision: str = "f32", threads: int = 0, max_steps: int = -1
     """Run the C oracle on a ``phantoms.Scan``; returns Sx, Sy, Kx, Ky, Kz,
     final Mx, My, Mz (flattened column-major) and ``steps``.  ``exact``: the
     exact relaxation-exchange propagator instead of the reference's split
-    exchange (ME, and GM without bound pools).  ``step_records`` > 0: also
+    exchange (ME, and GM with free and bound pools).  ``step_records`` > 0: also
     ``records``, the decoded dt > 0 steps ([steps][10]: dt, Gz, Gy, Gx, Tx-0
     amplitude, phase, frequency, rf_sum, ADC flag, signal index), at most
     that many."""

@@ -66,8 +66,9 @@ typedef struct mrl_port_args {
     int run_mode;
     float *mxs, *mys, *mzs;
     double *muts;
-    /* exact relaxation-exchange propagator (ME, and GM without bound pools):
-     * each step rotates every pool, then applies x' = E_T x, y' = E_T y,
+    /* exact relaxation-exchange propagator (ME, and GM with free and bound
+     * pools): each step rotates every free pool and saturates every bound
+     * one (exp(-W dt) on its z), then applies x' = E_T x, y' = E_T y,
      * z' = E_L z + dt phi1(A_L dt) b with E = exp(A dt) of the relaxation-
      * exchange generator (Bloch-McConnell equations without the rotation);
      * not in the reference, which splits the exchange (first order) */

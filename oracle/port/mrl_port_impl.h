@@ -232,13 +232,19 @@ static void PORT_T(update)(const mrl_port_args *a, REAL *MX, REAL *MY, REAL *MZ,
     }
 
     if ((a->model == MRL_PORT_ME || a->model == MRL_PORT_GM) && a->exact) {
-        /* exact relaxation-exchange propagator after the rotation of every pool */
+        /* exact relaxation-exchange propagator after the rotation of every
+         * free pool and the saturation of every bound (GM TypeFlag 1) pool;
+         * a bound pool has no transverse generator (its transverse
+         * magnetisation is held, and no free pool takes transverse inflow
+         * from it) but takes part in the longitudinal one */
         REAL rx[MRL_PORT_MAX_POOL], ry[MRL_PORT_MAX_POOL], rz[MRL_PORT_MAX_POOL];
         double At[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL] = {0}, Al[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL] = {0};
         double Ft[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL], Fl[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL];
         double Xt[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL], Xl[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL];
         double b[MRL_PORT_MAX_POOL] = {0};
-        int on[MRL_PORT_MAX_POOL];
+        int on[MRL_PORT_MAX_POOL], bnd[MRL_PORT_MAX_POOL];
+        for (int t = 0; t < P; ++t)
+            bnd[t] = a->model == MRL_PORT_GM && (int)a->type_flag[t] == 1;
         for (int t = 0; t < P; ++t) {
             REAL T1 = a->t1[PIDX(t)], T2 = a->t2[PIDX(t)], rho = a->rho[PIDX(t)];
             on[t] = !(T2 == 0 || T1 == 0 || rho == 0);
@@ -246,17 +252,22 @@ static void PORT_T(update)(const mrl_port_args *a, REAL *MX, REAL *MY, REAL *MZ,
             ry[t] = MY[IDX(t)];
             rz[t] = MZ[IDX(t)];
             if (!on[t]) continue;
-            PORT_T(rotate)(&rx[t], &ry[t], &rz[t], DW(t), st, tx, gyro, mg, pe, rf_sum);
-            At[t * P + t] = -1.0 / (double)T2;
+            if (!bnd[t]) {
+                PORT_T(rotate)(&rx[t], &ry[t], &rz[t], DW(t), st, tx, gyro, mg, pe, rf_sum);
+                At[t * P + t] = -1.0 / (double)T2;
+            } else if (rf_sum != 0) {
+                REAL w = PORT_T(bound_w)(st, tx, gyro, mg, db0, T2);
+                rz[t] = rz[t] * REXP((REAL)(-w * dt));
+            }
             Al[t * P + t] = -1.0 / (double)T1;
             b[t] = (double)rho / ((double)S * (double)T1);
             for (int p = 0; p < P; ++p) {
                 if (p == t) continue; /* a self rate moves nothing */
                 const double kgo = a->model == MRL_PORT_ME ? a->k[(long)(t * P + p) * V + v] : a->k[(long)(p * P + t) * V + v];
                 const double kin = a->model == MRL_PORT_ME ? a->k[(long)(p * P + t) * V + v] : a->k[(long)(t * P + p) * V + v];
-                At[t * P + t] -= kgo;
+                if (!bnd[t]) At[t * P + t] -= kgo;
                 Al[t * P + t] -= kgo;
-                At[t * P + p] += kin;
+                if (!bnd[t] && !bnd[p]) At[t * P + p] += kin;
                 Al[t * P + p] += kin;
             }
         }
@@ -440,10 +451,10 @@ int PORT_FN(const mrl_port_args *a, long long *steps_done) {
         return -1;
     if ((a->model == MRL_PORT_MT && a->type_num != 2) || (a->model == MRL_PORT_CEST && a->type_num < 2))
         return -1;
-    if (a->exact) { /* free pools exchanging: ME, or GM without bound pools */
+    if (a->exact) { /* ME, or GM with free (TypeFlag 0) and bound (1) pools */
         if (a->model != MRL_PORT_ME && a->model != MRL_PORT_GM) return -1;
         for (int t = 0; a->model == MRL_PORT_GM && t < a->type_num; ++t)
-            if ((int)a->type_flag[t] != 0) return -1;
+            if ((int)a->type_flag[t] != 0 && (int)a->type_flag[t] != 1) return -1;
     }
     const long V = (long)a->ny * a->nx * a->nz;
     const int P = a->type_num, S = a->spin_num, TX = a->tx_num, RX = a->rx_num, A = a->signal_num;

@@ -110,14 +110,18 @@ def test_port_history_matches_live_reference_cpu_engine(built):
     np.testing.assert_array_equal(out["Muts"], ref["Muts"])
 
 
-@pytest.mark.parametrize("model", ["me", "gm"])
+@pytest.mark.parametrize("model", ["me", "gm", "gm_bound"])
 def test_exact_oracle_matches_bloch_mcconnell_expm(built, model):
     """The oracle's exact propagator (rotate every pool, then exp of the
     relaxation-exchange generator) equals the exponential of the whole
     Bloch-McConnell generator when every pool precesses at the same
     frequency (rotation about z then commutes with relaxation and exchange):
     one voxel, three pools with stiff exchange, free precession at dB0, the
-    state read after the last of several uneven steps."""
+    state read after the last of several uneven steps.  ``gm_bound``: pool 2
+    is a bound pool (no transverse generator: its transverse state held, no
+    transverse inflow from it; in the longitudinal one like the others)."""
+    bound = model == "gm_bound"
+    model = "gm" if bound else model
     scipy_linalg = pytest.importorskip("scipy.linalg")
     from mrilab_gb300 import seq as S
 
@@ -134,7 +138,9 @@ def test_exact_oracle_matches_bloch_mcconnell_expm(built, model):
     times = [0, 1_500_000, 1_700_000, 6_000_000, 6_010_000, 18_000_000, 30_000_000]
     tr.adc(times[1:-1])
     lines = S.concat([tr])
-    tf = np.zeros(P) if model == "gm" else None
+    tf = (np.array([0.0, 0.0, 1.0]) if bound else np.zeros(P)) if model == "gm" else None
+    if bound:
+        t2[..., 2] = 12e-6
     sc = phantoms.assemble(rho, t1, t2, db0_hz=np.full((1, 1, 1), 37.0), model=model, rates=rates,
                            type_flag=tf, seqlines=lines)
     m0 = np.array([[0.3, -0.2, 0.4], [0.05, 0.1, 0.02], [-0.03, 0.04, 0.05]])  # [pool][x, y, z]
@@ -145,15 +151,19 @@ def test_exact_oracle_matches_bloch_mcconnell_expm(built, model):
     w = float(sc.VObj["Gyro"]) * float(sc.VMag["dB0"].ravel()[0])
     n = 3 * P + 1
     G = np.zeros((n, n))
+    bnd = [bound and t == 2 for t in range(P)]
     for t in range(P):
         kout = sum(rates[0, 0, 0, t, p] for p in range(P) if p != t)
         for c, r in ((0, 1 / t2[0, 0, 0, t]), (1, 1 / t2[0, 0, 0, t]), (2, 1 / t1[0, 0, 0, t])):
+            if c < 2 and bnd[t]:
+                continue  # a bound pool's transverse state is held
             G[c * P + t, c * P + t] = -r - kout
             for p in range(P):
-                if p != t:
+                if p != t and not (c < 2 and bnd[p]):
                     G[c * P + t, c * P + p] = rates[0, 0, 0, p, t]
-        G[0 * P + t, 1 * P + t] += w   # dx/dt = w y
-        G[1 * P + t, 0 * P + t] -= w   # dy/dt = -w x
+        if not bnd[t]:
+            G[0 * P + t, 1 * P + t] += w   # dx/dt = w y
+            G[1 * P + t, 0 * P + t] -= w   # dy/dt = -w x
         G[2 * P + t, n - 1] = rho[0, 0, 0, t] / t1[0, 0, 0, t]
     state = np.concatenate([m0[:, 0], m0[:, 1], m0[:, 2], [1.0]])
     # the integrated time: every dt > 0 step of the decoded sequence
