@@ -55,9 +55,11 @@ typedef enum {
      * in place of the reference's first-order split exchange: after each
      * step's rotation, x' = E_T x, y' = E_T y, z' = E_L z + dt phi1(A_L dt) b,
      * E = exp(A dt) of the relaxation-exchange generator, computed in FP64 per
-     * voxel and distinct dt.  Free pools exchanging (ME; GM without bound
-     * pools), TypeNum <= 3; the normal model runs as MRL_NUMERICS_ACCURATE
-     * (its relaxation is exact already).  No reference counterpart. */
+     * voxel and distinct dt.  ME, and GM with free and bound pools (a bound
+     * pool is saturated on rf steps before the propagator and has no
+     * transverse generator), TypeNum <= 3; the normal model runs as
+     * MRL_NUMERICS_ACCURATE (its relaxation is exact already); MT and CEST
+     * are refused.  No reference counterpart. */
     MRL_NUMERICS_EXACT = 2
 } mrl_numerics;
 
