@@ -12,8 +12,10 @@ gradient derived independently of the hand-written adjoint.  The steps are
 the C oracle's own decode (``run_port(..., step_records=N)``), so both walk
 the same step list.  The autograd graph holds every step: small cases only.
 
-Scope as the adjoint kernel's: normal, ME and GM models (GM pools of
-TypeFlag 0 and 1), one transmit coil.
+Models: normal, ME and GM (GM pools of TypeFlag 0 and 1) as the adjoint
+kernel covers them, and MT and CEST (``BlochKernelMT.cuh:180-411``,
+``BlochKernelCEST.cuh:280-606``: pool 0 free water, pool 1 the bound pool,
+CEST pools exchanging with pool 0); one transmit coil.
 """
 from __future__ import annotations
 
@@ -55,6 +57,55 @@ def _rotate(x, y, z, vx, vy, vz):
     return x + s1 * cx + s2 * dx, y + s1 * cy + s2 * dy, z + s1 * cz + s2 * dz
 
 
+def _mt_cest_step(model, P, S, dt, rf, X, Y, Z, xr, yr, zr, T1, T2, Rho, K, on, b1, freq, dB0, gyro):
+    """One step of the MT / CEST maps (the oracle's, BlochKernelMT.cuh:324-407,
+    BlochKernelCEST.cuh:364-600): pool 0 free water exchanging with the
+    bound pool 1 (K12 free -> bound, K21 back) and, for CEST, with pools
+    2..P-1, each rotated at its own frequency; the bound pool saturated by
+    rf (W = pi (gamma b1)^2 G), then relaxed.  An isochromat whose pool 0 is
+    empty is left alone.  (xr, yr, zr): every pool's rotated state."""
+    ex = torch.exp
+    if model == "mt":
+        K12, K21 = K[1], K[2]
+    else:
+        K12, K21 = K[0], K[P - 1]
+    x0, y0, z0, zb0 = X[0], Y[0], Z[0], Z[1]
+    e2 = ex(-dt / T2[0])
+    e1k = ex(-dt / T1[0] - dt * K12)
+    m0 = Rho[0] * (1 - ex(-dt / T1[0])) / S
+    ek = 1 - ex(-dt * K21)
+    nx, ny, nz = [None] * P, [None] * P, [None] * P
+    if model == "mt":
+        nx[0], ny[0], nz[0] = xr[0] * e2, yr[0] * e2, zr[0] * e1k + m0 + zb0 * ek
+    else:
+        kout = torch.ones_like(e2)
+        kx, ky, kz = torch.zeros_like(x0), torch.zeros_like(x0), torch.zeros_like(x0)
+        for t in range(2, P):
+            kout = kout * ex(-dt * K[t - 1])
+            f = 1 - ex(-dt * K[t + P - 2])
+            kx, ky, kz = kx + f * X[t], ky + f * Y[t], kz + f * Z[t]
+        nx[0] = xr[0] * e2 * kout + kx
+        ny[0] = yr[0] * e2 * kout + ky
+        nz[0] = zr[0] * e1k * kout + kz + zb0 * ek + m0
+        for t in range(2, P):
+            c2, c1 = ex(-dt / T2[t]), ex(-dt / T1[t])
+            ko = ex(-dt * K[t + P - 2])
+            f = 1 - ex(-dt * K[t - 1])
+            nx[t] = xr[t] * c2 * ko + f * x0
+            ny[t] = yr[t] * c2 * ko + f * y0
+            nz[t] = zr[t] * c1 * ko + f * z0 + Rho[t] * (1 - c1) / S
+    bz = Z[1]
+    if rf:
+        W = PI * (b1 * gyro) ** 2 * _lineshape(freq, dB0, gyro, T2[1])
+        bz = bz * ex(-W * dt)
+    nz[1] = bz * ex(-dt / T1[1] - dt * K21) + Rho[1] * (1 - ex(-dt / T1[1])) / S + z0 * (1 - ex(-dt * K12))
+    nx[1], ny[1] = X[1], Y[1]
+    act = on[0][None].expand_as(x0)
+    return (torch.stack([torch.where(act, a, b) for a, b in zip(nx, X)]),
+            torch.stack([torch.where(act, a, b) for a, b in zip(ny, Y)]),
+            torch.stack([torch.where(act, a, b) for a, b in zip(nz, Z)]))
+
+
 def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
     """dL/dtheta of L = sum(grad_sx * Sx + grad_sy * Sy) over the scan's
     signal (so its gradient is the adjoint's for those dL/dS), in the
@@ -63,8 +114,8 @@ def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
     Sx, Sy (the signal of the restated map)."""
     o, mag, coil, ctl = sc.VObj, sc.VMag, sc.VCoi, sc.VCtl
     model = sc.model
-    if model not in ("normal", "me", "gm"):
-        raise ValueError("the FP64 adjoint covers the normal, ME and GM models")
+    if model not in ("normal", "me", "gm", "mt", "cest"):
+        raise ValueError("unknown model")
     P, S = int(o["TypeNum"]), int(o["SpinNum"])
     TX, RX = int(coil["TxCoilNum"]), int(coil["RxCoilNum"])
     if TX != 1:
@@ -102,6 +153,9 @@ def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
         rxr, rxi = torch.ones(RX, V, dtype=torch.float64), torch.zeros(RX, V, dtype=torch.float64)
     cs = np.asarray(ctl["CS"], np.float64).ravel()
     kind = np.zeros(P, int) if model != "gm" else np.asarray(o["TypeFlag"], np.float64).ravel().astype(int)
+    mtc = model in ("mt", "cest")
+    # pools the receiver samples: the free pools; MT / CEST: pool 0 only
+    sampled = [(tp == 0) if mtc else kind[tp] == 0 for tp in range(P)]
     rf_ref = float(sc.VVar["rfRef"])
     gx_t = t(np.asarray(grad_sx, np.float64).reshape(P, RX, A))
     gy_t = t(np.asarray(grad_sy, np.float64).reshape(P, RX, A))
@@ -124,7 +178,7 @@ def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
         if adc and int(sidx) < A:
             # receive before the step: sum over spins and voxels of m conj(R_c)
             for tp in range(P):
-                if kind[tp] != 0:
+                if not sampled[tp]:
                     continue
                 mx, my = X[tp].sum(0), Y[tp].sum(0)  # [V]
                 b1 = (mx[None] * rxr + my[None] * rxi).sum(1)  # [RX]
@@ -148,6 +202,10 @@ def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
         else:
             zero = torch.zeros_like(X)
             xr, yr, zr = _rotate(X, Y, Z, zero, zero, -dt * w)
+        if mtc:
+            X, Y, Z = _mt_cest_step(model, P, S, dt, rf, X, Y, Z, xr, yr, zr, T1s, T2s, Rho, K, on,
+                                    (mg * torch.sqrt(Ar * Ar + Ai * Ai)) if rf else None, freq, dB0, gyro)
+            continue
         nx, ny, nz = [], [], []
         for tp in range(P):
             e1 = torch.exp(torch.clamp(-dt / T1s[tp], min=-200.0))[None]

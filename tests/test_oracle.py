@@ -176,12 +176,17 @@ def test_exact_oracle_matches_bloch_mcconnell_expm(built, model):
 
 
 def _fp64_adjoint_case(name):
-    if name == "me2":
-        return phantoms.small_multipool("me", seed=32, n=5, pools=2, spins=2, coils=2, n_tr=2)
-    return phantoms.small_multipool("gm", seed=38, n=4, pools=3, spins=1, coils=2, n_tr=2, seq="sat")
+    return {
+        "me2": lambda: phantoms.small_multipool("me", seed=32, n=5, pools=2, spins=2, coils=2, n_tr=2),
+        "gm_bound": lambda: phantoms.small_multipool("gm", seed=38, n=4, pools=3, spins=1, coils=2, n_tr=2,
+                                                     seq="sat"),
+        "mt": lambda: phantoms.small_multipool("mt", seed=61, n=4, pools=2, spins=2, coils=2, n_tr=2, seq="sat"),
+        "cest4": lambda: phantoms.small_multipool("cest", seed=62, n=4, pools=4, spins=1, coils=2, n_tr=2,
+                                                  seq="sat"),
+    }[name]()
 
 
-@pytest.mark.parametrize("name", ["me2", "gm_bound"])
+@pytest.mark.parametrize("name", ["me2", "gm_bound", "mt", "cest4"])
 def test_fp64_adjoint_pinned(name):
     """The FP64 reference gradient (oracle.adjoint64: the oracle's map
     restated in float64 PyTorch, differentiated by autograd) is pinned to
@@ -218,4 +223,5 @@ def test_fp64_adjoint_pinned(name):
                 d[key] = np.asfortranarray(b.astype(arr.dtype).reshape(arr.shape, order="F"))
                 out.append((loss(s), b[i]))
             fd = (out[0][0] - out[1][0]) / (out[0][1] - out[1][1])
-            assert abs(g[key][i] - fd) <= 1e-5 * abs(fd) + 1e-12, (key, i, g[key][i], fd)
+            # (the differences' own truncation reaches 1e-5 for a bound pool's T2)
+            assert abs(g[key][i] - fd) <= 5e-5 * abs(fd) + 1e-12, (key, i, g[key][i], fd)
