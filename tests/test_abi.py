@@ -114,3 +114,31 @@ def test_batch_argument_errors_are_status_codes(built):
     arr = (ctypes.POINTER(engine.ScanArgs) * 1)(ctypes.pointer(hs.args))
     assert lib.mrl_batch_create(ctypes.cast(arr, ctypes.c_void_p), 1, ctypes.byref(ptr)) == -6
     assert b"ACCURATE" in lib.mrl_last_error()
+
+
+def test_adjoint_plan_argument_errors_are_status_codes(built):
+    """The adjoint plan calls reject NULL plans and outputs with
+    MRL_ERR_ARG before touching a device."""
+    lib = engine.library()
+    buf = (ctypes.c_longlong * 6)()
+    for name in ("mrl_adjoint_plan_checkpoints", "mrl_adjoint_plan_work"):
+        fn = getattr(lib, name)
+        fn.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
+        assert fn(None, buf) == -1
+    lib.mrl_adjoint_plan_forward.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    assert lib.mrl_adjoint_plan_forward(None, None) == -1
+    lib.mrl_adjoint_plan_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+    ptr = ctypes.c_void_p()
+    assert lib.mrl_adjoint_plan_create(None, ctypes.byref(ptr)) == -1
+
+
+def test_adjoint_without_gpu_fails_loudly(built):
+    """No CPU fallback for the gradients either."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    sc = phantoms.small_multipool("gm", seed=3, n=4, pools=3, spins=1, coils=2, n_tr=1, seq="sat")
+    with pytest.raises(engine.ScanError) as e:
+        engine.adjoint(sc, np.zeros(1), np.zeros(1))
+    assert e.value.status in (-7, -2)
