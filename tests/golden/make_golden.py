@@ -7,7 +7,7 @@ seeded single-pool scans and stores its outputs, together with the all-FP64
 oracle's outputs on the same inputs, as small ``.npz`` files.  The scans are
 rebuilt from their seeds by ``mrilab_gb300.phantoms`` at test time.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name ...]   # all, or the named ones
 """
 import os
 import sys
@@ -30,6 +30,13 @@ MULTIPOOL = {
     "mp_gm_p3_s2_c2": dict(model="gm", seed=3, pools=3, spins=2, coils=2, seq="sat"),
     "mp_mt_p2_s2_c2": dict(model="mt", seed=3, pools=2, spins=2, coils=2, seq="sat"),
     "mp_cest_p4_s2_c2": dict(model="cest", seed=3, pools=4, spins=2, coils=2, seq="sat"),
+    "mp_cest_p5_s1_c2": dict(model="cest", seed=3, pools=5, spins=1, coils=2, seq="sat"),
+}
+
+# the MT + exchange EPI's tissue and sequence (general model with a bound
+# pool, 8 ms MT pulse, single-shot EPI), small; reference kernels as above
+MT_EPI = {
+    "mt_epi_gm_p3_s2_c4": dict(seed=7, nx=6, ny=6, nz=2, spins=2, n_coils=4, n_read=8, n_pe=8),
 }
 
 HISTORY = {
@@ -45,11 +52,16 @@ CASES = {
 }
 
 
-def main():
+def main(only=()):
+    def wanted(name):
+        return not only or name in only
+
     oracle.build()
     if not oracle.ref_available():
         raise SystemExit("the reference engine is not built (needs the reference tree)")
     for name, kw in CASES.items():
+        if not wanted(name):
+            continue
         sc = phantoms.config1_gre(**kw)
         ref = oracle.run_ref_cpu(sc, threads=1)
         f64 = oracle.run_port(sc, "f64")
@@ -64,6 +76,8 @@ def main():
         s64 = f64["Sx"] + 1j * f64["Sy"]
         print(name, "reference vs FP64 oracle: %.3e" % (np.linalg.norm(s_ref - s64) / np.linalg.norm(s64)))
     for name, kw in HISTORY.items():
+        if not wanted(name):
+            continue
         sc = phantoms.with_history(phantoms.config1_gre(**kw))
         ref = oracle.run_ref_cpu(sc, threads=1)
         f64 = oracle.run_port(sc, "f64")
@@ -74,13 +88,17 @@ def main():
             ref_Muts=ref["Muts"], f64_Mxs=f64["Mxs"], f64_Mys=f64["Mys"], f64_Mzs=f64["Mzs"],
         )
         print(name, "history: reference vs FP64 oracle max abs %.3e" % np.abs(ref["Mxs"] - f64["Mxs"]).max())
-    for name, kw in MULTIPOOL.items():
-        sc = phantoms.small_multipool(**kw)
+    multi = [(n, "small_multipool", kw) for n, kw in MULTIPOOL.items()]
+    multi += [(n, "config5_mt_epi", kw) for n, kw in MT_EPI.items()]
+    for name, builder, kw in multi:
+        if not wanted(name):
+            continue
+        sc = getattr(phantoms, builder)(**kw)
         ref = oracle.run_ref_kernel(sc)
         f64 = oracle.run_port(sc, "f64")
         np.savez_compressed(
             os.path.join(HERE, name + ".npz"),
-            builder=np.array("small_multipool"), kwargs=np.array(repr(kw)),
+            builder=np.array(builder), kwargs=np.array(repr(kw)),
             ref_Sx=ref["Sx"], ref_Sy=ref["Sy"], ref_Mz=ref["Mz"], ref_Mx=ref["Mx"], ref_My=ref["My"],
             f64_Sx=f64["Sx"], f64_Sy=f64["Sy"],
         )
@@ -90,4 +108,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

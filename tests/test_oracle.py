@@ -66,6 +66,26 @@ def test_port_matches_reference_kernels(built, model, pools, seq, spins, coils):
     np.testing.assert_allclose(out["Mz"], ref["Mz"], atol=1e-4)
 
 
+MULTI_GOLDEN = ["mp_me_p2_s2_c2", "mp_me_p3_s1_c1", "mp_gm_p3_s2_c2", "mp_mt_p2_s2_c2", "mp_cest_p4_s2_c2",
+                "mp_cest_p5_s1_c2", "mt_epi_gm_p3_s2_c4"]
+
+
+@pytest.mark.parametrize("name", MULTI_GOLDEN)
+def test_port_matches_reference_kernel_golden(built, name):
+    """The single-precision port against the committed outputs of the
+    reference's own multi-pool kernels (ME, GM, MT, CEST up to 5 pools, and
+    the MT + exchange EPI: make_golden.py), without the reference tree: the
+    signal at float-rounding distance, the final Mz within 1e-4."""
+    sc, g = load_golden(name)
+    out = oracle.run_port(sc, "f32")
+    err = rel_l2(signal(out), g["ref_Sx"] + 1j * g["ref_Sy"])
+    assert err <= 2e-5, err
+    np.testing.assert_allclose(out["Mz"], g["ref_Mz"], atol=1e-4)
+    # and the FP64 oracle is where it was when the fixture was made
+    f64 = oracle.run_port(sc, "f64")
+    assert rel_l2(signal(f64), g["f64_Sx"] + 1j * g["f64_Sy"]) <= 1e-12
+
+
 def test_port_ext_callback_zeroes_transverse(built):
     """Ext events reach the callback with the state written back; an ideal
     spoiler plugin (DoExtPlugin case 6) zeroes Mxy."""
