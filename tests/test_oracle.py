@@ -52,6 +52,31 @@ def test_port_matches_live_reference_cpu_engine(built, seed, n, n_tr):
 
 
 @pytest.mark.skipif(not oracle.ref_available(), reason="reference tree not mounted")
+@pytest.mark.parametrize("case", ["two_voxels", "rf_ref", "empty_object"])
+def test_port_edge_cases_match_live_reference_cpu_engine(built, case):
+    """Edge cases against the reference CPU engine: a 2x2 phantom, a
+    nonzero receiver phase (VVar.rfRef), and an empty object (Rho and the
+    initial Mz zero: a zero signal, k-space still accumulated)."""
+    if case == "two_voxels":
+        sc = phantoms.config1_gre(seed=9, n=2, n_tr=2)
+    else:
+        sc = phantoms.config1_gre(seed=10, n=8, n_tr=2)
+    if case == "rf_ref":
+        sc.VVar["rfRef"] = np.float64(0.4)
+    if case == "empty_object":
+        for k in ("Rho", "Mz"):
+            sc.VObj[k] = np.asfortranarray(sc.VObj[k] * 0)
+    ref = oracle.run_ref_cpu(sc)
+    out = oracle.run_port(sc, "f32")
+    if case == "empty_object":
+        assert not np.any(signal(ref)) and not np.any(signal(out))
+    else:
+        assert rel_l2(signal(out), signal(ref)) <= 1e-6
+    np.testing.assert_array_equal(out["Kx"], ref["Kx"])
+    np.testing.assert_allclose(out["Mz"], ref["Mz"], atol=1e-6)
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference tree not mounted")
 @pytest.mark.parametrize("model,pools,seq", [("me", 2, "gre"), ("me", 3, "gre"), ("gm", 3, "sat"),
                                              ("mt", 2, "sat"), ("cest", 3, "sat"), ("cest", 4, "sat")])
 @pytest.mark.parametrize("spins,coils", [(1, 1), (2, 2)])
