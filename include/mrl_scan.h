@@ -332,6 +332,15 @@ void mrl_adjoint_plan_destroy(mrl_adjoint_plan *plan);
  * capture.  Limits: MRL_NUMERICS_ACCURATE, one Tx coil, no Ext events. */
 int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, void *stream);
 
+/* The decoded step list of args' sequence, host only (no device needed):
+ * the dt > 0 steps the integrator takes, in order, 5 + 3 Tx doubles each --
+ * dt, Gz, Gy, Gx, ADC sample index (-1: none), then amplitude, phase and
+ * frequency of every Tx coil as held by the decoder (DoScanAtGPU.cu:339-477
+ * rules).  Ext stops are decoded through without running a plugin; the
+ * caller's VVar and VSig are not written.  *n_steps receives the count;
+ * MRL_ERR_ARG (with the count) if it exceeds cap. */
+int mrl_decode(const mrl_scan_args *args, double *steps, long long cap, long long *n_steps);
+
 /* Human-readable text for a status code (reference: errors were printed
  * with mexPrintf or raised with mexErrMsgTxt, DoScanAtGPU.cu:231-242,566). */
 const char *mrl_status_string(int status);

@@ -2412,6 +2412,49 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
     return MRL_OK;
 }
 
+int mrl_decode(const mrl_scan_args *args, double *steps, long long cap, long long *n_steps) {
+    using namespace mrl;
+    g_err.clear();
+    if (!args || !n_steps || (cap > 0 && !steps)) return set_err("NULL argument"), MRL_ERR_ARG;
+    *n_steps = 0;
+    if (args->abi_version != MRL_ABI_VERSION)
+        return set_err("abi_version %d, expected %d", args->abi_version, MRL_ABI_VERSION), MRL_ERR_ARG;
+    const int TX = args->coil.tx_num;
+    if (TX < 1 || TX > kMaxTx) return set_err("TxCoilNum %d outside 1..%d", TX, kMaxTx), MRL_ERR_UNSUPPORTED;
+    const mrl_sequence &q = args->seq;
+    if (!q.uts || !q.ts || !q.flags || q.n_uts < 1 || q.n_ts < 1) return set_err("VSeq lines missing"), MRL_ERR_ARG;
+    // k-space goes to scratch: the caller's arrays are not touched
+    const size_t A = (size_t)std::max(1, args->sig.signal_num);
+    std::vector<double> kx(A, 0.0), ky(A, 0.0), kz(A, 0.0);
+    mrl_signal sig = args->sig;
+    sig.kx = kx.data(), sig.ky = ky.data(), sig.kz = kz.data();
+    DecodeState ds;
+    load_state(ds, args->var, TX);
+    ds.i = 0;
+    ds.signali = 0;
+    const int stride = 5 + 3 * TX;
+    long long n = 0;
+    // Ext stops: decoding resumes where it stopped (no plugin runs); each
+    // stop consumes at least one tsLine entry
+    for (long long guard = 0; guard <= (long long)q.n_ts + 1; ++guard) {
+        DecodeChunk ch;
+        decode_until_ext(ds, q, TX, args->obj.gyro, sig, ch);
+        for (const StepInfo &si : ch.steps) {
+            if (n < cap) {
+                double *r = steps + n * stride;
+                r[0] = si.dt, r[1] = si.gz, r[2] = si.gy, r[3] = si.gx, r[4] = si.adc;
+                for (int c = 0; c < TX; ++c)
+                    r[5 + 3 * c] = si.amp[c], r[6 + 3 * c] = si.phase[c], r[7 + 3 * c] = si.freq[c];
+            }
+            ++n;
+        }
+        if (!ch.stopped_at_ext) break;
+    }
+    *n_steps = n;
+    if (n > cap) return set_err("%lld steps, room for %lld", n, cap), MRL_ERR_ARG;
+    return MRL_OK;
+}
+
 const char *mrl_status_string(int status) {
     switch (status) {
     case MRL_OK: return "ok";

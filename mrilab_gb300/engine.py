@@ -220,6 +220,28 @@ def scan(sc, model: Optional[str] = None, numerics: str = "accurate", gpu_index:
     return run(HostScan(sc, model=model, numerics=numerics, gpu_index=gpu_index), ext)
 
 
+def decode(sc) -> np.ndarray:
+    """``mrl_decode``: the dt > 0 steps of ``sc``'s sequence as the engine
+    decodes them (host only, no device), one row each: dt, Gz, Gy, Gx, ADC
+    sample index (-1: none), then amplitude, phase and frequency of every Tx
+    coil."""
+    lib = library()
+    lib.mrl_decode.argtypes = [ctypes.POINTER(ScanArgs), ctypes.POINTER(ctypes.c_double), ctypes.c_longlong,
+                               ctypes.POINTER(ctypes.c_longlong)]
+    hs = HostScan(sc)
+    stride = 5 + 3 * int(sc.VCoi["TxCoilNum"])
+    n = ctypes.c_longlong(0)
+    rc = lib.mrl_decode(ctypes.byref(hs.args), None, 0, ctypes.byref(n))
+    if rc != 0 and n.value == 0:
+        raise ScanError(rc, lib.mrl_last_error().decode())
+    out = np.zeros((max(n.value, 1), stride))
+    rc = lib.mrl_decode(ctypes.byref(hs.args), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n.value,
+                        ctypes.byref(n))
+    if rc != 0:
+        raise ScanError(rc, lib.mrl_last_error().decode())
+    return out[: n.value]
+
+
 class Plan:
     """A prepared scan (``mrl_plan``): inputs resident on the device, the
     sequence decoded once; ``execute(stream)`` re-runs the whole scan from
