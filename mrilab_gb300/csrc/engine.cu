@@ -2455,6 +2455,32 @@ int mrl_decode(const mrl_scan_args *args, double *steps, long long cap, long lon
     return MRL_OK;
 }
 
+// Test hook (not declared in mrl_scan.h): the accurate integrator's step
+// records of args' sequence (one Tx coil, no Ext events), host only: 16
+// floats per step as pack_fast_records writes them.
+int mrl_selftest_pack(const mrl_scan_args *args, int ckpt_every, float *out, long long cap, long long *n_steps) {
+    using namespace mrl;
+    if (!args || !n_steps || (cap > 0 && !out) || args->coil.tx_num != 1) return MRL_ERR_ARG;
+    const size_t A = (size_t)std::max(1, args->sig.signal_num);
+    std::vector<double> kx(A, 0.0), ky(A, 0.0), kz(A, 0.0);
+    mrl_signal sig = args->sig;
+    sig.kx = kx.data(), sig.ky = ky.data(), sig.kz = kz.data();
+    DecodeState ds;
+    load_state(ds, args->var, 1);
+    ds.i = 0;
+    ds.signali = 0;
+    DecodeChunk ch;
+    decode_until_ext(ds, args->seq, 1, args->obj.gyro, sig, ch);
+    if (ch.stopped_at_ext) return MRL_ERR_UNSUPPORTED;
+    FrameMoments fm;
+    std::vector<float> rec;
+    pack_fast_records(ch, 1, fm, rec, ckpt_every);
+    *n_steps = ch.n_steps;
+    if (ch.n_steps > cap) return MRL_ERR_ARG;
+    std::copy(rec.begin(), rec.end(), out);
+    return MRL_OK;
+}
+
 const char *mrl_status_string(int status) {
     switch (status) {
     case MRL_OK: return "ok";

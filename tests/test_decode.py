@@ -80,3 +80,51 @@ def test_decode_reports_the_count_when_short(built):
                                ctypes.POINTER(ctypes.c_longlong)]
     assert lib.mrl_decode(ctypes.byref(hs.args), buf, 1, ctypes.byref(n)) == -1
     assert n.value == engine.decode(sc).shape[0] > 1
+
+
+def _pack(sc, ckpt_every=0):
+    import ctypes
+
+    lib = engine.library()
+    fn = lib.mrl_selftest_pack
+    fn.argtypes = [ctypes.POINTER(engine.ScanArgs), ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.c_longlong,
+                   ctypes.POINTER(ctypes.c_longlong)]
+    hs = engine.HostScan(sc)
+    n = ctypes.c_longlong(0)
+    fn(ctypes.byref(hs.args), ckpt_every, None, 0, ctypes.byref(n))
+    out = np.zeros((n.value, 16), np.float32)
+    assert fn(ctypes.byref(hs.args), ckpt_every, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n.value,
+              ctypes.byref(n)) == 0
+    return out
+
+
+@pytest.mark.parametrize("name", ["gre", "bssfp", "mt_epi"])
+def test_step_records_carry_fp64_phase_moments(built, name):
+    """The accurate integrator's step records: the frame's phase moments
+    (elapsed free-precession time and gradient areas, summed over the steps
+    without rf before each step) travel as float (hi, lo) pairs whose sum is
+    the FP64 sum to ~2^-48 relative; the step flags mark ADC, rf, a change
+    of the float dt or gradients, and every ckpt_every-th step."""
+    sc = SEQUENCES[name]()
+    d = engine.decode(sc)
+    rec = _pack(sc, ckpt_every=16)
+    assert rec.shape[0] == d.shape[0]
+    rf = d[:, 5].astype(np.float32) != 0
+    free = ~rf
+    dt, gz, gy, gx = d[:, 0], d[:, 1], d[:, 2], d[:, 3]
+    for col, w in ((8, np.ones_like(dt)), (10, gx), (12, gy), (14, gz)):
+        before = np.concatenate([[0.0], np.cumsum(np.where(free, w * dt, 0.0))[:-1]])
+        got = rec[:, col].astype(np.float64) + rec[:, col + 1].astype(np.float64)
+        scale = max(1e-300, float(np.abs(before).max()))
+        assert np.abs(got - before).max() <= 2.0 ** -46 * scale
+    flags = rec[:, 7].view(np.int32)
+    np.testing.assert_array_equal((flags & 1) != 0, d[:, 4] >= 0)       # ADC
+    np.testing.assert_array_equal((flags & 2) != 0, rf)                 # rf
+    f32 = d[:, :4].astype(np.float32)
+    prev = np.vstack([np.full((1, 4), np.nan, np.float32), f32[:-1]])
+    prev[0, 0] = -1.0
+    prev[0, 1:] = 0.0
+    new_dt = f32[:, 0] != prev[:, 0]
+    np.testing.assert_array_equal((flags & 16) != 0, new_dt)            # dt changed
+    np.testing.assert_array_equal((flags & 8) != 0, new_dt | (f32[:, 1:] != prev[:, 1:]).any(axis=1))
+    np.testing.assert_array_equal((flags & 32) != 0, np.arange(len(d)) % 16 == 0)
