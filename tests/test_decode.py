@@ -26,8 +26,19 @@ def _compare(sc):
     return d
 
 
+def _gre_with_ext():
+    sc = phantoms.config1_gre(seed=4, n=8, n_tr=3)
+    lines, _ = phantoms.gre_lines(n_read=8, n_pe=3, fov=(0.24,) * 3, tr_ms=20.0, te_ms=(5.0,), flip=30.0,
+                                  rf_ms=2.0, rf_raster_us=10.0, tbw=4.0, bw_hz=32000.0, ext_every=1)
+    sc.VSeq = lines
+    return sc
+
+
 SEQUENCES = {
     "gre": lambda: phantoms.config1_gre(seed=1, n=16, n_tr=4),
+    # one Ext event per TR: decoded through (no plugin) the step list is the
+    # one without stops
+    "gre_ext": _gre_with_ext,
     "sat_gre": lambda: phantoms.small_multipool("mt", seed=2, n=4, pools=2, n_tr=3, seq="sat"),
     "bssfp": lambda: phantoms.config4_adjoint(seed=3, nx=4, ny=4, nz=2, n_tr=6),
     "mt_epi": lambda: phantoms.config5_mt_epi(seed=4, nx=4, ny=4, nz=2, spins=1, n_coils=2, n_read=16, n_pe=8),
