@@ -216,10 +216,12 @@ def with_history(sc: Scan) -> Scan:
 
 def gre_lines(*, n_read, n_pe, n_par=1, fov=(0.24, 0.24, 0.24), tr_ms=20.0, te_ms=(5.0,),
               flip=30.0, rf_ms=2.0, rf_raster_us=10.0, tbw=4.0, bw_hz=32000.0,
-              spoil=True, n_tr=None, ext_every=0, gamma=GAMMA):
+              spoil=True, n_tr=None, ext_every=0, tx_coils=1, gamma=GAMMA):
     """Cartesian (multi-echo) gradient echo, 2D (n_par=1) or 3D.
 
-    RF: windowed sinc; slab gradient on z during RF, rephased after;
+    RF: windowed sinc (``tx_coils`` > 1: the same pulse on every Tx coil,
+    coil c scaled by 1 / c and shifted in phase by 0.7 (c - 1) rad); slab
+    gradient on z during RF, rephased after;
     phase encode on y (and partition encode on z); monopolar readouts on x
     centred at each TE (ms, from the RF centre) with a rewinder between
     echoes; a spoiler lobe after the last echo.
@@ -241,6 +243,8 @@ def gre_lines(*, n_read, n_pe, n_par=1, fov=(0.24, 0.24, 0.24), tr_ms=20.0, te_m
         tr = S.TR(tr_ns)
         t_rf, a_rf = S.sinc_rf(0, rf_ns, raster_ns, flip, tbw)
         tr.rf(t_rf, a_rf)
+        for c in range(2, tx_coils + 1):
+            tr.rf(t_rf, np.asarray(a_rf) / c, 0.7 * (c - 1), 0.0, coil=c)
         tr.trap("z", 0, rf_ns, gslab, ramp_ns=raster_ns)
         # encoding window between the RF end and the first readout
         first_ro = rf_center + int(round(te_ms[0] * 1e6)) - ro_ns // 2
@@ -286,7 +290,7 @@ def gre_lines(*, n_read, n_pe, n_par=1, fov=(0.24, 0.24, 0.24), tr_ms=20.0, te_m
             tr.ext_t += [tr_ns]
             tr.ext_v += [0.0]
         trs.append(tr)
-    return S.concat(trs), total
+    return S.concat(trs, multi_transmit=tx_coils > 1), total
 
 
 # ---------------------------------------------------------------------------
@@ -311,6 +315,31 @@ def config1_gre(seed=0, n=64, n_tr=None) -> Scan:
                            flip=30.0, rf_ms=2.0, rf_raster_us=10.0, tbw=4.0, bw_hz=32000.0,
                            n_tr=n_tr)
     return assemble(rho, t1, t2, db0_hz=db0, res=(fov / X, fov / Y, 0.005), seqlines=lines,
+                    tr_num=ntr, seed=seed)
+
+
+def multi_tx_gre(seed=0, n=8, n_tr=2, tx_coils=2, rx_coils=2) -> Scan:
+    """A small single-pool 2D GRE transmitting on ``tx_coils`` coils with
+    seeded smooth magnitude / phase maps (the B1 of a step is the complex
+    sum over the coils, BlochKernel.h:62-110), ``rx_coils`` receive coils."""
+    rng = np.random.default_rng(seed)
+    Y = X = n
+    yy, xx = np.mgrid[0:Y, 0:X]
+    r = np.hypot((xx - (X - 1) / 2) / (X / 2), (yy - (Y - 1) / 2) / (Y / 2))
+    inside = (r <= 0.9)[..., None]
+    rho = np.where(inside, rng.uniform(0.5, 1.0, (Y, X, 1)), 0).astype(np.float32)
+    t1 = np.where(inside, rng.uniform(0.5, 1.5, (Y, X, 1)), 0).astype(np.float32)
+    t2 = np.where(inside, rng.uniform(0.04, 0.12, (Y, X, 1)), 0).astype(np.float32)
+    db0 = rng.normal(0.0, 10.0, (Y, X, 1))
+    fov = 0.24
+    res = (fov / X, fov / Y, 0.005)
+    tx_mg = np.stack([0.6 + 0.4 * np.cos(np.pi * (xx / X + c / tx_coils))[..., None]
+                      for c in range(tx_coils)], -1).astype(np.float32)
+    tx_pe = np.stack([(0.5 * c + 0.3 * (yy / Y))[..., None] for c in range(tx_coils)], -1).astype(np.float32)
+    rx = _cylinder_coils((Y, X, 1), res, rx_coils, rng) if rx_coils > 1 else None
+    lines, ntr = gre_lines(n_read=n, n_pe=n, fov=(fov, fov, fov), tr_ms=20.0, te_ms=(5.0,), flip=30.0,
+                           rf_ms=2.0, rf_raster_us=10.0, tbw=4.0, bw_hz=32000.0, n_tr=n_tr, tx_coils=tx_coils)
+    return assemble(rho, t1, t2, db0_hz=db0, res=res, tx_mg=tx_mg, tx_pe=tx_pe, rx=rx, seqlines=lines,
                     tr_num=ntr, seed=seed)
 
 

@@ -105,15 +105,16 @@ def run_port(scan, precision: str = "f32", threads: int = 0, max_steps: int = -1
     final Mx, My, Mz (flattened column-major) and ``steps``.  ``exact``: the
     exact relaxation-exchange propagator instead of the reference's split
     exchange (ME, and GM with free and bound pools).  ``step_records`` > 0: also
-    ``records``, the decoded dt > 0 steps ([steps][10]: dt, Gz, Gy, Gx, Tx-0
-    amplitude, phase, frequency, rf_sum, ADC flag, signal index), at most
-    that many."""
+    ``records``, the decoded dt > 0 steps ([steps][10 + 3 (Tx - 1)]: dt, Gz,
+    Gy, Gx, Tx-0 amplitude, phase, frequency, rf_sum, ADC flag, signal
+    index, then amplitude, phase, frequency of each further Tx coil), at
+    most that many."""
     lib = ctypes.CDLL(PORT_SO)
     fn = lib.mrl_port_scan_f32 if precision == "f32" else lib.mrl_port_scan_f64
     fn.argtypes = [ctypes.POINTER(PortArgs), ctypes.POINTER(ctypes.c_longlong)]
     fn.restype = ctypes.c_int
     steps = ctypes.c_longlong(0)
-    rec = np.zeros((max(step_records, 1), 10))
+    rec = np.zeros((max(step_records, 1), 10 + 3 * (int(scan.VCoi["TxCoilNum"]) - 1)))
 
     def call(args):
         if step_records > 0:

@@ -74,9 +74,10 @@ typedef struct mrl_port_args {
      * not in the reference, which splits the exchange (first order) */
     int exact;
     /* optional decoded-step capture (the FP64 adjoint's step list): for
-     * every dt > 0 step, 10 doubles -- dt, Gz, Gy, Gx, Tx-0 amplitude and
-     * phase after the negative-amplitude fold, Tx-0 frequency, rf_sum, ADC
-     * flag, signal index -- up to steps_cap records */
+     * every dt > 0 step, 10 + 3 (Tx - 1) doubles -- dt, Gz, Gy, Gx, Tx-0
+     * amplitude and phase after the negative-amplitude fold, Tx-0
+     * frequency, rf_sum, ADC flag, signal index, then amplitude, phase and
+     * frequency of every further Tx coil -- up to steps_cap records */
     double *steps_out;
     long long steps_cap;
 } mrl_port_args;

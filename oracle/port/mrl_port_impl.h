@@ -589,10 +589,13 @@ int PORT_FN(const mrl_port_args *a, long long *steps_done) {
         st.gx = (REAL)GxAmp;
         st.adc = ADC == 1;
         if (a->steps_out && done < a->steps_cap) {
-            double *r = a->steps_out + done * 10;
+            double *r = a->steps_out + done * (10 + 3 * (TX - 1));
             r[0] = dt, r[1] = GzAmp, r[2] = GyAmp, r[3] = GxAmp;
             r[4] = (double)st.amp[0], r[5] = (double)st.phase[0], r[6] = (double)st.freq[0];
             r[7] = (double)rf_sum, r[8] = st.adc ? 1.0 : 0.0, r[9] = (double)signali;
+            for (int c = 1; c < TX; ++c)
+                r[10 + 3 * (c - 1)] = (double)st.amp[c], r[11 + 3 * (c - 1)] = (double)st.phase[c],
+                r[12 + 3 * (c - 1)] = (double)st.freq[c];
         }
 
         /* receive before this step's rotation (DoScanAtCPU.cpp:445-491) */

@@ -39,6 +39,13 @@ MT_EPI = {
     "mt_epi_gm_p3_s2_c4": dict(seed=7, nx=6, ny=6, nz=2, spins=2, n_coils=4, n_read=8, n_pe=8),
 }
 
+# several transmit coils (B1 the complex sum over the coils): the
+# reference CPU engine's multi-Tx branch (BlochKernel.h:62-110)
+MULTI_TX = {
+    "gre_tx2_n8_seed1": dict(seed=1, n=8, n_tr=2, tx_coils=2),
+    "gre_tx3_n8_seed2": dict(seed=2, n=8, n_tr=2, tx_coils=3),
+}
+
 HISTORY = {
     # RunMode 1: the reference CPU engine's per-time-point state history
     "history_gre2d_n4_tr2_seed4": dict(seed=4, n=4, n_tr=2),
@@ -71,6 +78,21 @@ def main(only=()):
             ref_Sx=ref["Sx"], ref_Sy=ref["Sy"], ref_Kx=ref["Kx"], ref_Ky=ref["Ky"], ref_Kz=ref["Kz"],
             ref_Mz=ref["Mz"], ref_Mx=ref["Mx"], ref_My=ref["My"],
             f64_Sx=f64["Sx"], f64_Sy=f64["Sy"],
+        )
+        s_ref = ref["Sx"] + 1j * ref["Sy"]
+        s64 = f64["Sx"] + 1j * f64["Sy"]
+        print(name, "reference vs FP64 oracle: %.3e" % (np.linalg.norm(s_ref - s64) / np.linalg.norm(s64)))
+    for name, kw in MULTI_TX.items():
+        if not wanted(name):
+            continue
+        sc = phantoms.multi_tx_gre(**kw)
+        ref = oracle.run_ref_cpu(sc, threads=1)
+        f64 = oracle.run_port(sc, "f64")
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            builder=np.array("multi_tx_gre"), kwargs=np.array(repr(kw)),
+            ref_Sx=ref["Sx"], ref_Sy=ref["Sy"], ref_Kx=ref["Kx"], ref_Ky=ref["Ky"], ref_Kz=ref["Kz"],
+            ref_Mz=ref["Mz"], ref_Mx=ref["Mx"], ref_My=ref["My"], f64_Sx=f64["Sx"], f64_Sy=f64["Sy"],
         )
         s_ref = ref["Sx"] + 1j * ref["Sy"]
         s64 = f64["Sx"] + 1j * f64["Sy"]

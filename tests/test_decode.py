@@ -14,15 +14,19 @@ def _compare(sc):
     d = engine.decode(sc)
     o = oracle.run_port(sc, "f64", step_records=max(1, d.shape[0]) + 16)
     r = o["records"]
+    tx = int(sc.VCoi["TxCoilNum"])
     assert d.shape[0] == r.shape[0] == o["steps"]
     np.testing.assert_array_equal(d[:, 0], r[:, 0])            # dt
     np.testing.assert_array_equal(d[:, 1:4], r[:, 1:4])        # Gz, Gy, Gx
     np.testing.assert_array_equal(d[:, 4], np.where(r[:, 8] != 0, r[:, 9], -1))  # ADC sample
     np.testing.assert_array_equal(d[:, 7], r[:, 6])            # rf frequency
-    a_eng = d[:, 5] * np.exp(1j * d[:, 6])
-    a_ora = r[:, 4] * np.exp(1j * r[:, 5])
-    scale = max(1e-30, float(np.abs(a_ora).max()))
-    assert np.abs(a_eng - a_ora).max() <= 1e-12 * scale
+    for c in range(tx):  # every Tx coil: complex amplitude and frequency
+        a_eng = d[:, 5 + 3 * c] * np.exp(1j * d[:, 6 + 3 * c])
+        j = 4 if c == 0 else 10 + 3 * (c - 1)
+        a_ora = r[:, j] * np.exp(1j * r[:, j + 1])
+        scale = max(1e-30, float(np.abs(a_ora).max()))
+        assert np.abs(a_eng - a_ora).max() <= 1e-12 * scale
+        np.testing.assert_array_equal(d[:, 7 + 3 * c], r[:, j + 2])
     return d
 
 
@@ -43,6 +47,8 @@ SEQUENCES = {
     "bssfp": lambda: phantoms.config4_adjoint(seed=3, nx=4, ny=4, nz=2, n_tr=6),
     "mt_epi": lambda: phantoms.config5_mt_epi(seed=4, nx=4, ny=4, nz=2, spins=1, n_coils=2, n_read=16, n_pe=8),
     "cest_train": lambda: phantoms.cest_instance(5, 64, 4, 3.5, 2.0, 2.0),
+    "gre_tx2": lambda: phantoms.multi_tx_gre(seed=6, n=6, n_tr=2, tx_coils=2),
+    "gre_tx3": lambda: phantoms.multi_tx_gre(seed=7, n=6, n_tr=2, tx_coils=3),
 }
 
 

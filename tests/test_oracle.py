@@ -6,7 +6,9 @@ import oracle
 from mrilab_gb300 import phantoms
 from conftest import load_golden, rel_l2, signal
 
-GOLDEN = ["gre2d_n16_tr4_seed1", "gre2d_n32_tr8_seed2", "gre2d_n64_full_seed0"]
+GOLDEN = ["gre2d_n16_tr4_seed1", "gre2d_n32_tr8_seed2", "gre2d_n64_full_seed0",
+          # two and three transmit coils
+          "gre_tx2_n8_seed1", "gre_tx3_n8_seed2"]
 
 
 @pytest.mark.parametrize("name", GOLDEN)
