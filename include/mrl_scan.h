@@ -302,29 +302,34 @@ void mrl_adjoint_plan_destroy(mrl_adjoint_plan *plan);
 
 /* Scan without allocating device memory.
  *
- * For callers that cannot call cudaMalloc themselves -- code running inside
- * a host application or framework that owns the whole device heap (a
- * MATLAB session handing over gpuArray storage, a serving process with a
- * fixed memory pool), or code recording a CUDA graph, where allocation is
- * not allowed -- this variant of the accurate scan kernel works entirely in
- * buffers the caller already owns.  It has no counterpart in the reference,
- * whose engines allocate and free every device array per call
+ * For callers that cannot call cudaMalloc themselves: code running inside a
+ * host application or framework that owns the whole device heap and hands
+ * out only its own buffers (a MATLAB session passing gpuArray storage, a
+ * serving process with a fixed, pre-reserved memory pool), where an
+ * allocation behind the host's back would fail or break its accounting.
+ * This variant of the accurate scan kernel works entirely in buffers the
+ * caller already owns.  It has no counterpart in the reference, whose
+ * engines allocate and free every device array per call
  * (DoScanAtGPU.cu:257-334,765-784).
  *
  * Pointers in `args`: obj.rho/t1/t2/k/mx/my/mz, mag.*, coil.tx_mg/tx_pe/
  * rx_x/rx_y and sig.sx/sy are DEVICE pointers in the layouts above
  * (uncompacted); seq.*, ctl.cs, obj.type_flag, var.* and sig.kx/ky/kz are
  * host pointers.  Mx/My/Mz are updated in place and every acquired sample
- * of Sx/Sy is assigned.  `d_steps` is a device buffer of `step_bytes`
- * bytes for the decoded step records (16 floats per step; len(uts) * 64
- * bytes always suffices).  Work is queued on `stream` (a cudaStream_t, NULL
- * for the legacy stream) and the call returns when it has finished.
+ * of Sx/Sy is assigned.  `d_steps` is a 16-byte aligned device buffer of
+ * `step_bytes` bytes for the decoded step records (16 floats per step;
+ * len(uts) * 64 bytes always suffices); MRL_ERR_ARG if it is misaligned or
+ * too small.  Work is queued on `stream` (a cudaStream_t, NULL for the
+ * legacy stream) and the call returns when it has finished.
  *
  * Its only scratch is one statically allocated device array of 32 MiB
  * (held by every GPU that loads the library until the process exits): a
  * status word, the ADC map of one launch and the receive partial sums of
  * (thread blocks x Rx x pools) per sample.  Objects for which a single
- * sample does not fit are rejected with MRL_ERR_UNSUPPORTED.  The scratch
+ * sample does not fit are rejected with MRL_ERR_UNSUPPORTED; when all the
+ * samples of the scan do not fit at once, the scan runs as several kernel
+ * launches that reuse the scratch in turn (mrl_last_timing's [5] gives the
+ * count).  The scratch
  * is shared by every call: calls that overlap on the GPU (different
  * streams or threads) race and must be serialised by the caller.  The
  * first call on a device looks up the scratch's device address on that
@@ -348,7 +353,8 @@ const char *mrl_status_string(int status);
 /* Detail of the last failure on the calling thread ("" if none). */
 const char *mrl_last_error(void);
 
-/* Timing of the last mrl_scan on the calling thread: [0] whole call (ms),
+/* Timing of the last mrl_scan (or mrl_scan_noalloc: [0] and [5] only) on
+ * the calling thread: [0] whole call (ms),
  * [1] device time of the scan kernels (ms), [2] device time of the receive
  * reduction (ms), [3] host-to-device copies (ms), [4] device-to-host copies
  * (ms), [5] kernel launches, [6] bytes copied host-to-device, [7] bytes

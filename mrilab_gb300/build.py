@@ -6,7 +6,8 @@
   without MATLAB.
 * ``mex/Do*ScanAtGPU.so``: the mex wrappers with the reference engine names,
   linked against the stand-in (inside MATLAB they are built with ``mex``
-  against MATLAB's own headers instead).
+  against MATLAB's own headers instead: ``mex -DMRL_WRAP_MODEL=<model>
+  csrc/mex_wrappers.cpp -lmrl_scan``).
 
 Nothing is built for the host's GPU or any other architecture:
 ``-gencode arch=compute_103a,code=sm_103a``.

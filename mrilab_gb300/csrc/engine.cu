@@ -2244,8 +2244,16 @@ int mrl_adjoint(mrl_scan_args *args, mrl_adjoint_args *adj) {
 int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, void *stream) {
     using namespace mrl;
     g_err.clear();
+    for (double &x : g_timing) x = 0;
+    const auto t_start = std::chrono::steady_clock::now();
     if (!args || !d_steps) {
         set_err("NULL argument");
+        return MRL_ERR_ARG;
+    }
+    // the kernel stages step records with bulk copies, which need a 16-byte
+    // aligned global source
+    if ((reinterpret_cast<uintptr_t>(d_steps) & 15) != 0) {
+        set_err("d_steps must be 16-byte aligned");
         return MRL_ERR_ARG;
     }
     Scanner sc;  // validation only: nothing of it is allocated
@@ -2300,17 +2308,25 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
     const long long nblk = std::max(1LL, ((long long)n * sc.tpv + kBlock - 1) / kBlock);
     const int npairs = sc.mi.nsamp * sc.RX;
     const long long nslices = nblk * partial_slices(true);
-    const double per_sample = sizeof(int) + (double)nslices * npairs * sizeof(float2);
-    const long long a_cap = (long long)((kNoAllocScratchBytes - 256 - kNoAllocDescBytes) / per_sample);
+    // layout: [status 256 B][descriptor][ADC map, rounded up to 256 B][partials];
+    // the ADC map's rounding adds at most 252 B, reserved up front
+    const unsigned long long per_sample = sizeof(int) + (unsigned long long)nslices * npairs * sizeof(float2);
+    const unsigned long long room = kNoAllocScratchBytes - 2 * 256 - kNoAllocDescBytes;
+    const long long a_cap = (long long)std::min<unsigned long long>(room / per_sample, (unsigned long long)INT32_MAX);
     if (a_cap < 1) {
-        set_err("object too large for the %zu-byte scratch: one ADC sample needs %.0f bytes", kNoAllocScratchBytes,
+        set_err("object too large for the %zu-byte scratch: one ADC sample needs %llu bytes", kNoAllocScratchBytes,
                 per_sample);
+        return MRL_ERR_UNSUPPORTED;
+    }
+    const size_t amap_bytes = ((size_t)a_cap * sizeof(int) + 255) / 256 * 256;
+    const size_t part_off = 256 + kNoAllocDescBytes + amap_bytes;
+    if (part_off + (size_t)a_cap * nslices * npairs * sizeof(float2) > kNoAllocScratchBytes) {
+        set_err("internal: scratch layout exceeds %zu bytes", kNoAllocScratchBytes);
         return MRL_ERR_UNSUPPORTED;
     }
     FastLaunch *d_desc = reinterpret_cast<FastLaunch *>(scratch + 256);
     int *d_amap = reinterpret_cast<int *>(scratch + 256 + kNoAllocDescBytes);
-    float2 *d_part =
-        reinterpret_cast<float2 *>(scratch + 256 + kNoAllocDescBytes + ((a_cap * sizeof(int) + 255) / 256) * 256);
+    float2 *d_part = reinterpret_cast<float2 *>(scratch + part_off);
     if ((e = cudaMemsetAsync(d_status, 0, sizeof(int), st)) != cudaSuccess) return sc.fail_cuda(e, "status reset");
     if ((e = cudaMemcpyAsync(d_steps, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice, st)) !=
         cudaSuccess)
@@ -2368,7 +2384,9 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
     // walk the steps, one launch per a_cap samples
     long long s0 = 0;
     std::vector<int> amap;
+    int n_launch = 0;
     auto launch = [&](long long s1) -> int {
+        ++n_launch;
         F.b.s0 = s0;
         F.b.s1 = s1;
         F.b.a_launch = (int)amap.size();
@@ -2409,6 +2427,8 @@ int mrl_scan_noalloc(mrl_scan_args *args, float *d_steps, size_t step_bytes, voi
         set_err("a device wait timed out (status bits %d)", status);
         return MRL_ERR_TIMEOUT;
     }
+    g_timing[5] = n_launch;
+    g_timing[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
     return MRL_OK;
 }
 

@@ -773,3 +773,40 @@ def config5_mt_epi(seed=0, nx=256, ny=256, nz=128, spins=4, n_coils=32, n_read=1
     return assemble(rho.astype(np.float32), t1.astype(np.float32), t2.astype(np.float32), spin_num=spins,
                     t2star=0.7 * t2, db0_hz=db0, res=res, model="gm", rates=rates,
                     type_flag=np.array([0.0, 0.0, 1.0]), rx=(rxx, rxy), seqlines=lines, tr_num=ntr, seed=seed)
+
+
+def crop(sc: Scan, ys, xs, zs) -> Scan:
+    """The scan restricted to the voxels at rows ``ys``, columns ``xs`` and
+    slices ``zs`` (index arrays or slices), each keeping its position, maps,
+    coil sensitivities and state.  Voxels are independent in the engine
+    (pool exchange is within a voxel), so the cropped scan's signal is the
+    full scan's signal minus the other voxels' contributions: a subset of
+    the same workload, for checks at full sequence length."""
+    out = sc.copy()
+    ix = np.ix_(np.arange(sc.dims[0])[ys], np.arange(sc.dims[1])[xs], np.arange(sc.dims[2])[zs])
+
+    def cut(a):
+        a = np.asarray(a)
+        return np.asfortranarray(a[ix]) if a.ndim >= 3 else a
+
+    for d, keys in ((out.VObj, ("Rho", "T1", "T2", "K", "Mx", "My", "Mz")),
+                    (out.VMag, ("dB0", "dWRnd", "Gzgrid", "Gygrid", "Gxgrid")),
+                    (out.VCoi, ("TxCoilmg", "TxCoilpe", "RxCoilx", "RxCoily")),
+                    (out.VSig, ("Mx", "My", "Mz"))):
+        for k in keys:
+            if k in d:
+                d[k] = cut(d[k])
+    if out.rates is not None:
+        out.rates = out.rates[ix]
+    out.info = dict(sc.info, crop=True)
+    return out
+
+
+def config2_subset(seed=0, step=8, offset=4, n_tr=None) -> Scan:
+    """The two-pool multi-echo GRE benchmark scan (config2_me_gre at its
+    full 128 x 128 x 32 size and full sequence length) restricted to every
+    ``step``-th row and column from ``offset``, all slices: 16 x 16 x 32
+    voxels spread over the field of view by default, the whole 256-TR
+    sequence, all 8 Rx coils."""
+    sc = config2_me_gre(seed=seed, n_tr=n_tr)
+    return crop(sc, slice(offset, None, step), slice(offset, None, step), slice(None))

@@ -33,7 +33,10 @@ PORT_SO = os.path.join(HERE, "port", "libmrl_port.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_CPU_SO = os.path.join(REF_DIR, "DoScanAtCPU.so")
 REF_KERN_SO = os.path.join(REF_DIR, "libmrl_refkern.so")
-REFERENCE_ROOT = "/root/reference"
+# The MRiLab reference tree to build the reference objects from: taken from
+# the environment only (no default); unset, only the port is built and the
+# tests that need the reference objects skip.
+REFERENCE_ROOT = os.environ.get("MRILAB_REFERENCE_ROOT", "")
 
 MODEL_ID = {"normal": 0, "me": 1, "mt": 2, "cest": 3, "gm": 4}
 
@@ -79,8 +82,11 @@ def build(force: bool = False) -> None:
     if force or not os.path.exists(PORT_SO) or os.path.getmtime(PORT_SO) < max(
             os.path.getmtime(src), os.path.getmtime(hdr)):
         subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", src, "-o", PORT_SO, "-lm"])
-    if os.path.isdir(REFERENCE_ROOT):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref"])
+    if REFERENCE_ROOT:
+        if not os.path.isdir(os.path.join(REFERENCE_ROOT, "Lib", "src", "engine")):
+            raise RuntimeError(f"MRILAB_REFERENCE_ROOT={REFERENCE_ROOT!r} is not an MRiLab tree "
+                               "(no Lib/src/engine)")
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REFROOT={REFERENCE_ROOT}"])
 
 
 def ref_available() -> bool:

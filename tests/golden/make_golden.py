@@ -7,7 +7,7 @@ seeded single-pool scans and stores its outputs, together with the all-FP64
 oracle's outputs on the same inputs, as small ``.npz`` files.  The scans are
 rebuilt from their seeds by ``mrilab_gb300.phantoms`` at test time.
 
-    python tests/golden/make_golden.py [name ...]   # all, or the named ones
+    MRILAB_REFERENCE_ROOT=<MRiLab tree> python tests/golden/make_golden.py [name ...]   # all, or the named ones
 """
 import os
 import sys
@@ -50,6 +50,16 @@ HISTORY = {
     # RunMode 1: the reference CPU engine's per-time-point state history
     "history_gre2d_n4_tr2_seed4": dict(seed=4, n=4, n_tr=2),
 }
+
+# the benchmark's two-pool multi-echo GRE at its full sequence length (256
+# TRs, 220,416 steps) on a voxel subset spread over the field of view; the
+# signal is stored at every SAMPLE_STRIDE-th sample of each (pool, coil)
+# (the whole signal is 50 MB), with the relative L2 distances over the whole
+# signal recorded beside it
+FULL_LENGTH = {
+    "config2_full_length_subset": dict(seed=0, step=8, offset=4),
+}
+SAMPLE_STRIDE = 127
 
 CASES = {
     # name: (builder kwargs)
@@ -110,6 +120,32 @@ def main(only=()):
             ref_Muts=ref["Muts"], f64_Mxs=f64["Mxs"], f64_Mys=f64["Mys"], f64_Mzs=f64["Mzs"],
         )
         print(name, "history: reference vs FP64 oracle max abs %.3e" % np.abs(ref["Mxs"] - f64["Mxs"]).max())
+    for name, kw in FULL_LENGTH.items():
+        if not wanted(name):
+            continue
+        import time
+
+        sc = phantoms.config2_subset(**kw)
+        P, C, A = int(sc.VObj["TypeNum"]), int(sc.VCoi["RxCoilNum"]), sc.signal_num
+        keep = np.arange(0, A, SAMPLE_STRIDE)
+        runs, secs = {}, {}
+        for tag, fn in (("ref", oracle.run_ref_kernel), ("f64", lambda s: oracle.run_port(s, "f64")),
+                        ("f32", lambda s: oracle.run_port(s, "f32"))):
+            t0 = time.time()
+            o = fn(sc)
+            secs[tag] = time.time() - t0
+            runs[tag] = (o["Sx"] + 1j * o["Sy"]).reshape(P, C, A)
+        rl = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            builder=np.array("config2_subset"), kwargs=np.array(repr(kw)), sample_index=keep,
+            ref_S=runs["ref"][..., keep], f64_S=runs["f64"][..., keep], f32_S=runs["f32"][..., keep],
+            full_ref_vs_f64=np.float64(rl(runs["ref"], runs["f64"])),
+            full_f32_vs_f64=np.float64(rl(runs["f32"], runs["f64"])),
+        )
+        print(name, "reference kernels vs FP64 oracle: %.3e (sampled %.3e); FP32 port vs FP64 %.3e; seconds %s" % (
+            rl(runs["ref"], runs["f64"]), rl(runs["ref"][..., keep], runs["f64"][..., keep]),
+            rl(runs["f32"], runs["f64"]), secs))
     multi = [(n, "small_multipool", kw) for n, kw in MULTIPOOL.items()]
     multi += [(n, "config5_mt_epi", kw) for n, kw in MT_EPI.items()]
     for name, builder, kw in multi:

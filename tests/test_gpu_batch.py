@@ -19,6 +19,8 @@ def _instances():
         phantoms.small_multipool("mt", seed=25, n=12, pools=2, spins=2, coils=2, n_tr=2, seq="sat"),
         phantoms.small_multipool("gm", seed=26, n=7, pools=3, spins=2, coils=2, n_tr=2, seq="sat"),
         phantoms.small_multipool("cest", seed=27, n=9, pools=3, spins=1, coils=2, n_tr=1, seq="sat"),
+        # five pools: water, MT and three CEST pools (config 3's largest instances)
+        phantoms.small_multipool("cest", seed=28, n=5, pools=5, spins=1, coils=2, n_tr=1, seq="sat"),
     ]
 
 

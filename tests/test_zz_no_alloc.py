@@ -1,6 +1,8 @@
 """mrl_scan_noalloc: the scan entry point for callers that cannot allocate
-device memory (a host application that owns the device heap, or code
-recording a CUDA graph).  The caller owns every input and output buffer --
+device memory (a host application that owns the whole device heap and hands
+out only its own buffers, such as a MATLAB session passing gpuArray storage
+or a server with a fixed memory pool).  The caller owns every input and
+output buffer --
 here torch tensors stand in for them -- and the call must reproduce the
 allocating entry point, mrl_scan, on the same inputs, call after call.
 
@@ -59,17 +61,29 @@ def _call(lib, hs, dev, steps):
     return dict(Sx=sx, Sy=sy, Mx=dev["mx"].cpu().numpy(), My=dev["my"].cpu().numpy(), Mz=dev["mz"].cpu().numpy())
 
 
-@pytest.mark.parametrize("case", ["gre2d", "two_pool_coils"])
-def test_noalloc_matches_mrl_scan_twice(built, case):
-    torch = pytest.importorskip("torch")
+def _lib():
     lib = engine.library()
     lib.mrl_scan_noalloc.argtypes = [ctypes.POINTER(engine.ScanArgs), ctypes.c_void_p, ctypes.c_size_t,
                                      ctypes.c_void_p]
     lib.mrl_scan_noalloc.restype = ctypes.c_int
+    return lib
+
+
+@pytest.mark.parametrize("case", ["gre2d", "two_pool_coils", "split_launches"])
+def test_noalloc_matches_mrl_scan_twice(built, case):
+    torch = pytest.importorskip("torch")
+    lib = _lib()
     if case == "gre2d":
         sc = phantoms.config1_gre(seed=2, n=32, n_tr=6)
-    else:
+    elif case == "two_pool_coils":
         sc = phantoms.small_multipool("me", seed=6, n=12, pools=2, spins=2, coils=3, n_tr=3)
+    else:
+        # 8192 voxels (at least 64 blocks of 128 threads), 2 pools x 8 Rx
+        # coils: one sample's partial sums take at least 8 KiB, so the 32 MiB
+        # scratch holds at most about 4090 samples and the scan's 6144 samples
+        # take more than one launch
+        sc = phantoms.config2_me_gre(seed=3, nx=32, ny=32, nz=8, n_pe=4, n_par=2, n_read=128, n_tr=8)
+        assert sc.signal_num > 4096
     expect = engine.scan(sc, numerics="accurate")
     hs, dev, steps = _device_args(sc, torch)
     m0 = {k: dev[k].clone() for k in ("mx", "my", "mz")}
@@ -84,20 +98,45 @@ def test_noalloc_matches_mrl_scan_twice(built, case):
         dev["sx"].zero_()
         dev["sy"].zero_()
         out = _call(lib, hs, dev, steps)
+        launches = engine.last_timing()["launches"]
         err = rel_l2(signal(out), signal(expect))
-        print(f"{case} call {call}: no-alloc vs mrl_scan signal {err:.2e}")
+        print(f"{case} call {call}: no-alloc vs mrl_scan signal {err:.2e} ({launches:.0f} launches)")
         assert err <= TOL
         for k in ("Mx", "My", "Mz"):
             assert rel_l2(out[k], expect[k]) <= TOL
+        if case == "split_launches":
+            assert launches > 1
+            # and against the all-FP64 oracle
+            if call == 0:
+                import oracle
+
+                f64 = oracle.run_port(sc, "f64")
+                err64 = rel_l2(signal(out), signal(f64))
+                print(f"split launches: no-alloc vs FP64 oracle {err64:.2e}")
+                assert err64 <= TOL
+        else:
+            assert launches == 1
 
 
 def test_noalloc_rejects_small_step_buffer(built):
     torch = pytest.importorskip("torch")
-    lib = engine.library()
-    lib.mrl_scan_noalloc.argtypes = [ctypes.POINTER(engine.ScanArgs), ctypes.c_void_p, ctypes.c_size_t,
-                                     ctypes.c_void_p]
+    lib = _lib()
     sc = phantoms.config1_gre(seed=2, n=8, n_tr=1)
     hs, dev, steps = _device_args(sc, torch)
     rc = lib.mrl_scan_noalloc(ctypes.byref(hs.args), ctypes.c_void_p(steps.data_ptr()), ctypes.c_size_t(64), None)
     assert rc == -1
     assert b"needed" in lib.mrl_last_error()
+
+
+def test_noalloc_rejects_misaligned_step_buffer(built):
+    """The step records are staged by bulk copies that need a 16-byte aligned
+    source: a buffer at an odd offset is refused on the host, before any
+    launch."""
+    torch = pytest.importorskip("torch")
+    lib = _lib()
+    sc = phantoms.config1_gre(seed=2, n=8, n_tr=1)
+    hs, dev, steps = _device_args(sc, torch)
+    rc = lib.mrl_scan_noalloc(ctypes.byref(hs.args), ctypes.c_void_p(steps.data_ptr() + 4),
+                              ctypes.c_size_t(steps.numel() * 4 - 16), None)
+    assert rc == -1
+    assert b"aligned" in lib.mrl_last_error()
