@@ -1,10 +1,13 @@
 """Build the native parts of mrilab_gb300 in-tree.
 
-* ``libmrl_scan.so``: the C-ABI scan engine (``include/mrl_scan.h``), CUDA
-  for sm_103a only; translation units compile in parallel.
+* ``libmrl_scan.so``: the C-ABI scan engine (``include/mrl_scan.h``) and
+  SAR engine (``include/mrl_sar.h``), CUDA for sm_103a only; translation
+  units compile in parallel.
 * ``mex/libfakemex.so``: the MATLAB stand-in used to drive the mex layer
   without MATLAB.
-* ``mex/Do*ScanAtGPU.so``: the mex wrappers with the reference engine names,
+* ``mex/Do*ScanAtGPU.so``, ``mex/DoCalSARAtGPU.so``: the mex wrappers with
+  the reference engine names (the SAR one named after the reference's
+  DoCalSARAtCPU, for the GPU),
   linked against the stand-in (inside MATLAB they are built with ``mex``
   against MATLAB's own headers instead: ``mex -DMRL_WRAP_MODEL=<model>
   csrc/mex_wrappers.cpp -lmrl_scan``).
@@ -51,6 +54,7 @@ UNITS = {
     "adjoint.cu": [],
     "scan_fast_exact.cu": [],
     "scan_fast_exact_bound.cu": [],
+    "sar.cu": [],
     "decode.cpp": None,  # host C++
 }
 
@@ -75,7 +79,7 @@ def _stale(target: str, deps) -> bool:
 
 def _headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    return hs + [os.path.join(ROOT, "include", "mrl_scan.h")]
+    return hs + [os.path.join(ROOT, "include", f) for f in ("mrl_scan.h", "mrl_sar.h")]
 
 
 def _run(cmd):
@@ -117,6 +121,11 @@ def build(verbose: bool = False, jobs: int = 0) -> None:
     if _stale(FAKEMEX, [fm_src, os.path.join(MEX, "mex.h"), os.path.join(MEX, "matrix.h")]):
         _run(["gcc", "-O2", "-fPIC", "-shared", f"-I{MEX}", fm_src, "-o", FAKEMEX])
     wsrc = os.path.join(CSRC, "mex_wrappers.cpp")
+    sar_src = os.path.join(CSRC, "sar_mex.cpp")
+    sar_out = os.path.join(MEX, "DoCalSARAtGPU.so")
+    if _stale(sar_out, [sar_src, LIB, FAKEMEX] + hdrs):
+        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", f"-I{MEX}", sar_src, "-o", sar_out, f"-L{HERE}",
+              "-lmrl_scan", f"-L{MEX}", "-lfakemex", "-Wl,-rpath,$ORIGIN/..", "-Wl,-rpath,$ORIGIN"])
     for name, model in WRAPPERS.items():
         out = os.path.join(MEX, name + ".so")
         if _stale(out, [wsrc, LIB, FAKEMEX] + hdrs):

@@ -52,6 +52,17 @@ void set_err(const char *fmt, ...) {
     g_err = buf;
 }
 
+}  // namespace
+
+// Error text and timing of the calling thread, for the other engines of the
+// library (mrl_sar): read back through mrl_last_error / mrl_last_timing.
+void record_error(const char *msg) { g_err = msg ? msg : ""; }
+void record_timing(const double t[8]) {
+    for (int i = 0; i < 8; ++i) g_timing[i] = t[i];
+}
+
+namespace {
+
 // Receive reduction: Sx/Sy[pool][coil][signal] = sum over blocks of the
 // per-block partial sums, in FP64, then demodulated by rfRef
 // (BlochKernel.cuh:160-170 applies the same rotation per isochromat).

@@ -810,3 +810,50 @@ def config2_subset(seed=0, step=8, offset=4, n_tr=None) -> Scan:
     sequence, all 8 Rx coils."""
     sc = config2_me_gre(seed=seed, n_tr=n_tr)
     return crop(sc, slice(offset, None, step), slice(offset, None, step), slice(None))
+
+
+def sar_case(seed=0, n=16, nz=2, tx_coils=2, n_tr=3, sample_fracs=(0.0, 0.3, 0.5, 0.8, 1.0)) -> Scan:
+    """A local-SAR calculation as the SAR watcher sets it up
+    (Src/Main/DoSARWatchExec.m:36-105): an n x n x nz object with a mass
+    density and per-component conductivity factors (VObj.MassDen, ECon), a
+    seeded smooth E-field map per Tx coil and component (VCoi.TxE1x/y/z,
+    per unit rf amplitude), a GRE transmitting on ``tx_coils`` coils, and
+    sample times at the given fractions of the sequence's length
+    (VSig.tSample, unique and sorted; VSig.SAR / tRealSample / Muts and
+    VVar.SAR / SARi zeroed)."""
+    rng = np.random.default_rng(seed)
+    Y = X = n
+    Z = nz
+    yy, xx, zz = np.meshgrid(np.arange(Y), np.arange(X), np.arange(Z), indexing="ij")
+    r = np.hypot((xx - (X - 1) / 2) / (X / 2), (yy - (Y - 1) / 2) / (Y / 2))
+    inside = r <= 0.9
+    massden = np.where(inside, rng.uniform(900.0, 1100.0, (Y, X, Z)), 0.0).astype(np.float32)
+    econ = np.stack([np.where(inside, rng.uniform(0.3, 0.7, (Y, X, Z)), 0.0) for _ in range(3)], -1)
+    # E-field per unit rf amplitude (V/m per T): smooth fields, one per coil and component
+    e1 = []
+    for comp in range(3):
+        maps = []
+        for c in range(tx_coils):
+            ph = 2 * np.pi * rng.uniform()
+            kx, ky = rng.uniform(0.5, 1.5, 2)
+            maps.append(4e5 * (0.3 + np.cos(np.pi * kx * xx / X + ph) * np.sin(np.pi * ky * yy / Y + 0.4 * c)
+                               + 0.1 * zz / max(Z, 1)))
+        e1.append(np.stack(maps, -1).astype(np.float32))
+    lines, ntr = gre_lines(n_read=16, n_pe=max(n_tr, 1), fov=(0.24, 0.24, 0.24), tr_ms=20.0, te_ms=(5.0,),
+                           flip=30.0, rf_ms=2.0, rf_raster_us=10.0, tbw=4.0, bw_hz=32000.0, n_tr=n_tr,
+                           tx_coils=tx_coils)
+    uts = lines["utsLine"]
+    d = np.diff(uts)
+    t_end = float(np.sum(d[d > 0]))
+    t_sample = np.unique(np.asarray(sample_fracs, np.float64) * t_end)
+    vobj = dict(MassDen=np.asfortranarray(massden), ECon=np.asfortranarray(econ.astype(np.float32)))
+    vcoi = dict(TxE1x=np.asfortranarray(e1[0]), TxE1y=np.asfortranarray(e1[1]), TxE1z=np.asfortranarray(e1[2]),
+                TxCoilNum=np.int32(tx_coils))
+    vctl = dict(TRNum=np.int32(ntr), MaxThreadNum=np.int32(1))
+    vvar = dict(t=np.float64(0), dt=np.float64(0), rfAmp=np.zeros(tx_coils), rfPhase=np.zeros(tx_coils),
+                rfFreq=np.zeros(tx_coils), rfCoil=np.float64(0), Ext=np.float64(0),
+                SAR=np.asfortranarray(np.zeros((Y, X, Z, 3), np.float32)), SARi=np.int32(0), utsi=np.int32(0),
+                rfi=np.int32(0), Exti=np.int32(0), TRCount=np.int32(1))
+    vsig = dict(SAR=np.asfortranarray(np.zeros((Y, X, Z, t_sample.size), np.float32)), Muts=np.zeros(uts.size),
+                tSample=t_sample, tRealSample=np.zeros(t_sample.size))
+    return Scan(vobj, {}, vcoi, vctl, dict(lines), vvar, vsig, model="sar", info=dict(seed=seed))

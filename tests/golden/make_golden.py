@@ -61,6 +61,14 @@ FULL_LENGTH = {
 }
 SAMPLE_STRIDE = 127
 
+# local SAR (the reference SAR engine DoCalSARAtCPU, compiled from its
+# source): phantoms.sar_case kwargs
+SAR = {
+    "sar_tx1_n6_seed2": dict(seed=2, n=6, nz=1, tx_coils=1, n_tr=3),
+    "sar_tx2_n8_seed1": dict(seed=1, n=8, nz=2, tx_coils=2, n_tr=2),
+    "sar_tx3_n6_seed3": dict(seed=3, n=6, nz=3, tx_coils=3, n_tr=2, sample_fracs=(0.1, 0.45, 0.7)),
+}
+
 CASES = {
     # name: (builder kwargs)
     "gre2d_n16_tr4_seed1": dict(seed=1, n=16, n_tr=4),
@@ -146,6 +154,24 @@ def main(only=()):
         print(name, "reference kernels vs FP64 oracle: %.3e (sampled %.3e); FP32 port vs FP64 %.3e; seconds %s" % (
             rl(runs["ref"], runs["f64"]), rl(runs["ref"][..., keep], runs["f64"][..., keep]),
             rl(runs["f32"], runs["f64"]), secs))
+    from oracle import sar as osar
+
+    for name, kw in SAR.items():
+        if not wanted(name):
+            continue
+        sc = phantoms.sar_case(**kw)
+        ref = osar.run_ref_sar(sc)
+        f64 = osar.run_sar_port(sc, "f64")
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            builder=np.array("sar_case"), kwargs=np.array(repr(kw)),
+            ref_SAR=ref["SAR"].astype(np.float32), ref_SARacc=ref["SARacc"].astype(np.float32),
+            ref_Muts=ref["Muts"], ref_tRealSample=ref["tRealSample"],
+            ref_cursor=np.array([ref["SARi"], ref["utsi"], ref["rfi"], ref["TRCount"]]),
+            f64_SAR=f64["SAR"], f64_SARacc=f64["SARacc"],
+        )
+        print(name, "reference SAR engine vs FP64 oracle: %.3e" % (
+            np.linalg.norm(ref["SAR"] - f64["SAR"]) / np.linalg.norm(f64["SAR"])))
     multi = [(n, "small_multipool", kw) for n, kw in MULTIPOOL.items()]
     multi += [(n, "config5_mt_epi", kw) for n, kw in MT_EPI.items()]
     for name, builder, kw in multi:

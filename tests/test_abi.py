@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol(built):
 
 
 @pytest.mark.parametrize("wrapper", ["DoScanAtGPU", "DoMEScanAtGPU", "DoMTScanAtGPU", "DoCESTScanAtGPU",
-                                     "DoGMScanAtGPU"])
+                                     "DoGMScanAtGPU", "DoCalSARAtGPU"])
 def test_mex_wrappers_export_mexfunction(built, wrapper):
     so = os.path.join(ROOT, "mrilab_gb300", "mex", wrapper + ".so")
     lib = ctypes.CDLL(so)
