@@ -124,14 +124,26 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def peaks():
-    from mrilab_gb300 import build
+_PEAKS = {}
 
-    lib = ctypes.CDLL(build.PEAKS)
-    lib.mrl_probe_peaks.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
-    f, m = ctypes.c_double(), ctypes.c_double()
-    lib.mrl_probe_peaks(ctypes.byref(f), ctypes.byref(m))
-    return f.value, m.value
+
+def peaks():
+    """(FP32 TFLOP/s, MUFU Gop/s) measured on this GPU: the FP32 figure is
+    the larger of scalar FFMA chains and packed f32x2 FFMA chains (the scan
+    kernels use both), so a kernel's fraction is taken against the best the
+    FP32 pipe delivers."""
+    if "v" not in _PEAKS:
+        from mrilab_gb300 import build
+
+        lib = ctypes.CDLL(build.PEAKS)
+        lib.mrl_probe_peaks.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        lib.mrl_probe_ffma2.argtypes = [ctypes.POINTER(ctypes.c_double)]
+        f, m, f2 = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        lib.mrl_probe_peaks(ctypes.byref(f), ctypes.byref(m))
+        lib.mrl_probe_ffma2(ctypes.byref(f2))
+        _PEAKS["v"] = (max(f.value, f2.value), m.value)
+        _PEAKS["detail"] = {"ffma_tflops": f.value, "ffma2_tflops": f2.value, "mufu_gops": m.value}
+    return _PEAKS["v"]
 
 
 def run_config3(args):
@@ -714,7 +726,8 @@ def main():
     roof = {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_tf, "unit": "TFLOP/s",
             "frac": achieved_tf / fp32_tf, "traffic": None,
             "mufu": {"achieved": achieved_mufu, "peak": mufu_g, "unit": "Gop/s", "frac": achieved_mufu / mufu_g},
-            "peak_source": "measured on this GPU by libmrl_peaks.so (FFMA / MUFU.SIN chains)",
+            "peak_source": "measured on this GPU by libmrl_peaks.so (the larger of FFMA and packed f32x2 FFMA "
+                           "chains; MUFU.SIN chains)", "peak_detail": _PEAKS.get("detail"),
             "kernel": "scan kernel", "share_of_step": scan_share,
             "flops_per_scan": flops, "mufu_per_scan": mufu, "scan_kernel_ms_per_scan": scan_ms}
     line = {

@@ -312,6 +312,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     // per-thread values read only at anchors, state changes and rf steps:
     // the isochromats' dWRnd and the low parts of gamma * (dB0, x, y, z)
     constexpr int kNSampP = kMTC ? 1 : P;
+    constexpr int NQ = (NS + 1) / 2;  // spin pairs of a thread
     // tile rows per sample and samples per flush (bound pools of KM_EXCH take no row)
     constexpr bool kRank = MODEL == KM_EXCH && !FREE;
     const int nsp = kRank ? max(1, F.n_samp) : kNSampP;
@@ -326,8 +327,8 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     uint2 *rsq = reinterpret_cast<uint2 *>(mtile + 16 * kTRow);
     float2 *rsf = reinterpret_cast<float2 *>(rsq);
     float *wstage = reinterpret_cast<float *>(rsq + (presplit ? 2 : 1) * C4 * kTRow);  // [warp][16][2*C4]
-    float *dwsm = wstage + kWarps * 16 * 2 * C4;                                   // [NS * P][kBlock]
-    float *omlo = dwsm + NS * P * kBlock;                                        // [4][kBlock]
+    float2 *dwsm = reinterpret_cast<float2 *>(wstage + kWarps * 16 * 2 * C4);     // [NQ][P][kBlock] spin pairs
+    float *omlo = reinterpret_cast<float *>(dwsm + NQ * P * kBlock);              // [4][kBlock]
 
     const int tid = threadIdx.x;
     const long long gt = (long long)tile * kBlock + tid;
@@ -336,8 +337,20 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     bool active = v < L.n_act;
     const int n = L.n_act;
 
-    float X[NS][P], Y[NS][P], Z[NS][P];
-    float2 dm[NS][P];     // free-step increment of the frame magnetisation
+    // isochromat state, and the free-step increment of the frame
+    // magnetisation dm = (dmX, dmY) per spin; the packed paths read and write
+    // spins 2q and 2q + 1 as the two lanes of an f32x2 value (PAIR / UNPAIR)
+    float Xs[NS][P], Ys[NS][P], Zs[NS][P];
+    float dmXs[NS][P], dmYs[NS][P];
+#define XS(s, t) Xs[s][t]
+#define YS(s, t) Ys[s][t]
+#define ZS(s, t) Zs[s][t]
+#define DMX(s, t) dmXs[s][t]
+#define DMY(s, t) dmYs[s][t]
+#define PAIR(A, q, t) make_float2(A[2 * (q)][t], A[2 * (q) + 1][t])
+#define UNPAIR(A, q, t, v) (A[2 * (q)][t] = (v).x, A[2 * (q) + 1][t] = (v).y)
+#define DWS(s, t) (((s) & 1) ? dwsm[((s) >> 1) * P * kBlock + (t) * kBlock + tid].y \
+                             : dwsm[((s) >> 1) * P * kBlock + (t) * kBlock + tid].x)
     float2 Pc[P], Dc[P];  // frame phasor of each pool and its free-step increment
     float rhoS[P], it1[P], it2[P], t2v[P], y1[P], y2[P];
     unsigned act = 0;
@@ -354,10 +367,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         Pc[t] = make_float2(1.f, 0.f);
         Dc[t] = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            X[s][t] = Y[s][t] = Z[s][t] = 0.f;
-            dm[s][t] = make_float2(0.f, 0.f);
-        }
+        for (int s = 0; s < NS; ++s) Xs[s][t] = Ys[s][t] = Zs[s][t] = dmXs[s][t] = dmYs[s][t] = 0.f;
     }
     if (active) {
         db0 = L.db0[v];
@@ -404,10 +414,10 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 #pragma unroll
             for (int t = 0; t < P; ++t) {
                 const long long i = ((long long)t * L.S + sp) * n + v;
-                X[s][t] = L.mx[i];
-                Y[s][t] = L.my[i];
-                Z[s][t] = L.mz[i];
-                dwsm[(s * P + t) * kBlock + tid] = L.dwrnd[i];
+                XS(s, t) = L.mx[i];
+                YS(s, t) = L.my[i];
+                ZS(s, t) = L.mz[i];
+                DWS(s, t) = L.dwrnd[i];
             }
         }
     }
@@ -468,6 +478,13 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 #pragma unroll
         for (int p = 0; p < P; ++p) fin[t][p] = 0.f;
     }
+    // packed free steps (two spins per f32x2 operation): the all-free exchange
+    // model with the split scheme and an even spin count per thread
+    constexpr bool kPack = MODEL == KM_EXCH && FREE && !EXACT && NS % 2 == 0;
+    // rf steps packed too while a thread's state is small (with 8 isochromat-
+    // pools the packed rf step's temporaries spill; rf steps are rare there)
+    constexpr bool kPackRf = kPack && NS * P <= 4;
+    bool selfx = false;  // some pool of this voxel exchanges with itself (a nonzero K diagonal)
     float mt_y1k = 0.f, mt_y21 = 0.f, mt_y1bk = 0.f, mt_y1b = 0.f, mt_y12 = 0.f;
     LineshapeCache lc;
     float4 satk = make_float4(0.f, 0.f, 0.f, -1.f);  // (Re A, Im A, 2 pi f, dt) of satv
@@ -502,7 +519,9 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     // inside its loops cost the 8-coil scan 4 %)
     auto flush_form = [&](auto pre_tag) {
         constexpr bool pre = decltype(pre_tag)::value;
-        __syncthreads();
+        // a warp's tile columns are its own threads' (k = the warp's voxels): the
+        // tile needs no block barrier before the contraction
+        __syncwarp();
         const int g = lane >> 2, tig = lane & 3, ri = tig & 1, cmp = g & 1;
         const int bcomp = (ri == cmp) ? 0 : 1;                 // rx, else ry
         const uint32_t sgn = (cmp && !ri) ? 0x80000000u : 0u;  // -ry
@@ -635,9 +654,9 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     if (!entered) {
 #pragma unroll
                         for (int s = 0; s < NS; ++s) {  // m_frame = m_lab * conj(P)
-                            const float2 m = cmul_conj(make_float2(X[s][t], Y[s][t]), pn);
-                            X[s][t] = m.x;
-                            Y[s][t] = m.y;
+                            const float2 m = cmul_conj(make_float2(XS(s, t), YS(s, t)), pn);
+                            XS(s, t) = m.x;
+                            YS(s, t) = m.y;
                         }
                     }
                     Pc[t] = pn;
@@ -738,6 +757,11 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     }
                 }
             }
+            if (kPack && active && (flags & kFlagDt)) {
+                selfx = false;
+#pragma unroll
+                for (int t = 0; t < P; ++t) selfx |= fin[t][t] != 0.f;
+            }
             if (active && (flags & kFlagState)) {
                 const bool new_dt = (flags & kFlagDt) != 0;  // kFlagDt implies kFlagState
 #pragma unroll
@@ -756,12 +780,14 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                         if (tvo >> t & 1u) {
                             // the isochromat's own step in its pool's frame: a function of dt alone
                             if (new_dt) {
-                                const float2 p = phase_step(dwsm[(s * P + t) * kBlock + tid] * dt);
-                                dm[s][t] = make_float2(fmaf(p.x, 1.f - a, -a), p.y * (1.f - a));
+                                const float2 p = phase_step(DWS(s, t) * dt);
+                                DMX(s, t) = fmaf(p.x, 1.f - a, -a);
+                                DMY(s, t) = p.y * (1.f - a);
                             }
                         } else {
                             // constant in the lab: m_frame turns back by the frame's step
-                            dm[s][t] = make_float2(Dc[t].x, -Dc[t].y);
+                            DMX(s, t) = Dc[t].x;
+                            DMY(s, t) = -Dc[t].y;
                         }
                     }
                 }
@@ -774,8 +800,8 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     float sx = 0.f, sy = 0.f;
 #pragma unroll
                     for (int s = 0; s < NS; ++s) {
-                        sx += X[s][t];
-                        sy += Y[s][t];
+                        sx += XS(s, t);
+                        sy += YS(s, t);
                     }
                     float2 m = cmul(make_float2(sx, sy), Pc[t]);
                     if (!active) m = make_float2(0.f, 0.f);
@@ -793,12 +819,12 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 for (int s = 0; s < NS; ++s)
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
-                        float2 m = make_float2(X[s][t], Y[s][t]);
+                        float2 m = make_float2(XS(s, t), YS(s, t));
                         if (has_frame<MODEL>(t)) m = cmul(m, Pc[t]);
                         const long long i = (long long)(sg * NS + s) * n + v;
                         c[(3 * t + 0) * niso + i] = m.x;
                         c[(3 * t + 1) * niso + i] = m.y;
-                        c[(3 * t + 2) * niso + i] = Z[s][t];
+                        c[(3 * t + 2) * niso + i] = ZS(s, t);
                     }
             }
             if (L.hist != nullptr) {  // RunMode 1: the state at the start of the step, lab frame
@@ -807,12 +833,12 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 for (int s = 0; s < NS; ++s)
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
-                        float2 m = make_float2(X[s][t], Y[s][t]);
+                        float2 m = make_float2(XS(s, t), YS(s, t));
                         if (has_frame<MODEL>(t)) m = cmul(m, Pc[t]);
                         const long long i = ((long long)t * L.S + sg * NS + s) * n + v;
                         h[i] = m.x;
                         h[L.hist_stride + i] = m.y;
-                        h[2 * L.hist_stride + i] = Z[s][t];
+                        h[2 * L.hist_stride + i] = ZS(s, t);
                     }
             }
 
@@ -911,14 +937,163 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
             }
             const float wrf = r1.z;  // 2 pi sum of active rf frequencies
 
+            if constexpr (kPack) {
+                if (!rf) {
+                    // the free step of the loop below for spins 2q and 2q + 1 at
+                    // once: m_t += dm_t m_t + sum_p fr[t][p] m_p (transverse, in the
+                    // frames), z_t = (1 - yo)(1 - y1) z_t + sum_p fin[t][p] z_p +
+                    // rho_t y1 / S, every partner taken before the step
+                    auto step = [&](auto self_tag) {
+                        constexpr bool kSelf = decltype(self_tag)::value;
+#pragma unroll
+                        for (int qq = 0; qq < NQ; ++qq) {
+                            float2 nx[P], ny[P], nz[P];
+#pragma unroll
+                            for (int t = 0; t < P; ++t) {
+                                const float2 px = PAIR(Xs, qq, t), py = PAIR(Ys, qq, t);
+                                const float2 dx = PAIR(dmXs, qq, t), dy = PAIR(dmYs, qq, t);
+                                float2 ax = __fmul2_rn(dx, px);  // real part: ax - bx
+                                float2 bx = __fmul2_rn(dy, py);
+                                float2 iy = __ffma2_rn(dx, py, __fmul2_rn(dy, px));
+#pragma unroll
+                                for (int p = 0; p < P; ++p) {
+                                    if (p == t && !kSelf) continue;
+                                    const float2 f1 = make_float2(fr[t][p].x, fr[t][p].x);
+                                    const float2 f2 = make_float2(fr[t][p].y, fr[t][p].y);
+                                    ax = __ffma2_rn(f1, PAIR(Xs, qq, p), ax);
+                                    bx = __ffma2_rn(f2, PAIR(Ys, qq, p), bx);
+                                    iy = __ffma2_rn(f1, PAIR(Ys, qq, p), iy);
+                                    iy = __ffma2_rn(f2, PAIR(Xs, qq, p), iy);
+                                }
+                                nx[t] = __fadd2_rn(px, __fadd2_rn(ax, make_float2(-bx.x, -bx.y)));
+                                ny[t] = __fadd2_rn(py, iy);
+                                float2 iz = __fmul2_rn(make_float2(fin[t][0], fin[t][0]), PAIR(Zs, qq, 0));
+#pragma unroll
+                                for (int p = 1; p < P; ++p)
+                                    iz = __ffma2_rn(make_float2(fin[t][p], fin[t][p]), PAIR(Zs, qq, p), iz);
+                                const float2 z1 =
+                                    __ffma2_rn(make_float2(-y1[t], -y1[t]), PAIR(Zs, qq, t), PAIR(Zs, qq, t));
+                                const float2 z2 = __ffma2_rn(make_float2(-yo[t], -yo[t]), z1, z1);
+                                const float c = rhoS[t] * y1[t];
+                                nz[t] = __fadd2_rn(z2, __fadd2_rn(iz, make_float2(c, c)));
+                            }
+#pragma unroll
+                            for (int t = 0; t < P; ++t) {
+                                UNPAIR(Xs, qq, t, nx[t]);
+                                UNPAIR(Ys, qq, t, ny[t]);
+                                UNPAIR(Zs, qq, t, nz[t]);
+                            }
+                        }
+                    };
+                    if (selfx)
+                        step(BoolTag<true>{});
+                    else
+                        step(BoolTag<false>{});
+                    continue;
+                }
+                if constexpr (kPackRf) {
+                    // the rf step of the loop below for spins 2q and 2q + 1 at once:
+                    // rotation exp([v]x) with v = (vt, -dt dW), dW per spin, then
+                    // relaxation and inflow (partners taken before the step)
+                    auto rfstep = [&](auto self_tag) {
+                        constexpr bool kSelf = decltype(self_tag)::value;
+#pragma unroll
+                        for (int qq = 0; qq < NQ; ++qq) {
+                            float2 rx[P], ry[P], rz[P];
+#pragma unroll
+                            for (int t = 0; t < P; ++t) {
+                                const float2 x = PAIR(Xs, qq, t), y = PAIR(Ys, qq, t), z = PAIR(Zs, qq, t);
+                                const float w0 = wc + F.cs_hi[t] + wrf;
+                                const float2 dwp = dwsm[qq * P * kBlock + t * kBlock + tid];
+                                // nvz = -v_z = dt dW per spin
+                                const float2 nvz =
+                                    __fmul2_rn(make_float2(dt, dt), __fadd2_rn(dwp, make_float2(w0, w0)));
+                                const float2 vz = make_float2(-nvz.x, -nvz.y);
+                                const float vx = vt[t].x, vy = vt[t].y;
+                                const float vv = fmaf(vx, vx, vy * vy);
+                                const float2 a2 = __ffma2_rn(nvz, nvz, make_float2(vv, vv));
+                                float2 s1, s2;
+                                if (a2.x < 0.0625f && a2.y < 0.0625f) {
+                                    s1 = __ffma2_rn(
+                                        __ffma2_rn(__ffma2_rn(a2, make_float2(-1.f / 5040.f, -1.f / 5040.f),
+                                                              make_float2(1.f / 120.f, 1.f / 120.f)),
+                                                   a2, make_float2(-1.f / 6.f, -1.f / 6.f)),
+                                        a2, make_float2(1.f, 1.f));
+                                    s2 = __ffma2_rn(
+                                        __ffma2_rn(__ffma2_rn(a2, make_float2(-1.f / 40320.f, -1.f / 40320.f),
+                                                              make_float2(1.f / 720.f, 1.f / 720.f)),
+                                                   a2, make_float2(-1.f / 24.f, -1.f / 24.f)),
+                                        a2, make_float2(0.5f, 0.5f));
+                                } else {
+                                    const float2 c0 = rot_coeffs(a2.x), c1 = rot_coeffs(a2.y);
+                                    s1 = make_float2(c0.x, c1.x);
+                                    s2 = make_float2(c0.y, c1.y);
+                                }
+                                const float2 bvx = make_float2(vx, vx), bvy = make_float2(vy, vy);
+                                const float2 bnvx = make_float2(-vx, -vx), bnvy = make_float2(-vy, -vy);
+                                // c = v x m, e = v x c
+                                const float2 cx = __ffma2_rn(bvy, z, __fmul2_rn(nvz, y));
+                                const float2 cy = __ffma2_rn(vz, x, __fmul2_rn(bnvx, z));
+                                const float2 cz = __ffma2_rn(bvx, y, __fmul2_rn(bnvy, x));
+                                const float2 ex = __ffma2_rn(bvy, cz, __fmul2_rn(nvz, cy));
+                                const float2 ey = __ffma2_rn(vz, cx, __fmul2_rn(bnvx, cz));
+                                const float2 ez = __ffma2_rn(bvx, cy, __fmul2_rn(bnvy, cx));
+                                const bool on = tvo >> t & 1u;
+                                rx[t] = on ? __fadd2_rn(x, __ffma2_rn(s1, cx, __fmul2_rn(s2, ex))) : x;
+                                ry[t] = on ? __fadd2_rn(y, __ffma2_rn(s1, cy, __fmul2_rn(s2, ey))) : y;
+                                rz[t] = on ? __fadd2_rn(z, __ffma2_rn(s1, cz, __fmul2_rn(s2, ez))) : z;
+                            }
+                            float2 nx[P], ny[P], nz[P];
+#pragma unroll
+                            for (int t = 0; t < P; ++t) {
+                                float2 ax = make_float2(0.f, 0.f), bx = ax, iy = ax;
+#pragma unroll
+                                for (int p = 0; p < P; ++p) {
+                                    if (p == t && !kSelf) continue;
+                                    const float2 f1 = make_float2(fr[t][p].x, fr[t][p].x);
+                                    const float2 f2 = make_float2(fr[t][p].y, fr[t][p].y);
+                                    ax = __ffma2_rn(f1, PAIR(Xs, qq, p), ax);
+                                    bx = __ffma2_rn(f2, PAIR(Ys, qq, p), bx);
+                                    iy = __ffma2_rn(f1, PAIR(Ys, qq, p), iy);
+                                    iy = __ffma2_rn(f2, PAIR(Xs, qq, p), iy);
+                                }
+                                const float2 ny2 = make_float2(-y2[t], -y2[t]), nyo = make_float2(-yo[t], -yo[t]);
+                                const float2 x1 = __ffma2_rn(ny2, rx[t], rx[t]);
+                                const float2 y1v = __ffma2_rn(ny2, ry[t], ry[t]);
+                                nx[t] = __fadd2_rn(__ffma2_rn(nyo, x1, x1), __fadd2_rn(ax, make_float2(-bx.x, -bx.y)));
+                                ny[t] = __fadd2_rn(__ffma2_rn(nyo, y1v, y1v), iy);
+                                float2 iz = __fmul2_rn(make_float2(fin[t][0], fin[t][0]), PAIR(Zs, qq, 0));
+#pragma unroll
+                                for (int p = 1; p < P; ++p)
+                                    iz = __ffma2_rn(make_float2(fin[t][p], fin[t][p]), PAIR(Zs, qq, p), iz);
+                                const float2 z1 = __ffma2_rn(make_float2(-y1[t], -y1[t]), rz[t], rz[t]);
+                                const float c = rhoS[t] * y1[t];
+                                nz[t] = __fadd2_rn(__ffma2_rn(nyo, z1, z1), __fadd2_rn(iz, make_float2(c, c)));
+                            }
+#pragma unroll
+                            for (int t = 0; t < P; ++t) {
+                                UNPAIR(Xs, qq, t, nx[t]);
+                                UNPAIR(Ys, qq, t, ny[t]);
+                                UNPAIR(Zs, qq, t, nz[t]);
+                            }
+                        }
+                    };
+                    if (selfx)
+                        rfstep(BoolTag<true>{});
+                    else
+                        rfstep(BoolTag<false>{});
+                    continue;
+                }
+            }
+
 #pragma unroll
             for (int s = 0; s < NS; ++s) {
                 float px[P], py[P], pz[P];
 #pragma unroll
                 for (int t = 0; t < P; ++t) {
-                    px[t] = X[s][t];
-                    py[t] = Y[s][t];
-                    pz[t] = Z[s][t];
+                    px[t] = XS(s, t);
+                    py[t] = YS(s, t);
+                    pz[t] = ZS(s, t);
                 }
                 // ---- transverse ----------------------------------------------
                 if (rf) {
@@ -926,13 +1101,13 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     for (int t = 0; t < P; ++t) {
                         if (!has_frame<MODEL>(t)) continue;
                         float x = px[t], y = py[t], z = pz[t];
-                        const float dW = wc + dwsm[(s * P + t) * kBlock + tid] + F.cs_hi[t] + wrf;
+                        const float dW = wc + DWS(s, t) + F.cs_hi[t] + wrf;
                         const float vz = -dt * dW;
                         rot_exp(x, y, z, vt[t].x, vt[t].y, vz, rot_coeffs(fmaf(vz, vz, fmaf(vt[t].x, vt[t].x, vt[t].y * vt[t].y))));
                         const bool on = tvo >> t & 1u;
-                        X[s][t] = on ? x : px[t];
-                        Y[s][t] = on ? y : py[t];
-                        Z[s][t] = on ? z : pz[t];
+                        XS(s, t) = on ? x : px[t];
+                        YS(s, t) = on ? y : py[t];
+                        ZS(s, t) = on ? z : pz[t];
                     }
                     // relaxation and inflow after the rotation (the frames hold still);
                     // the exact propagator takes the partners after their rotation,
@@ -940,18 +1115,18 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     if constexpr (EXACT) {
 #pragma unroll
                         for (int t = 0; t < P; ++t) {
-                            if constexpr (!FREE) Z[s][t] = fmaf(-sat[t], Z[s][t], Z[s][t]);
-                            px[t] = X[s][t];
-                            py[t] = Y[s][t];
-                            pz[t] = Z[s][t];
+                            if constexpr (!FREE) ZS(s, t) = fmaf(-sat[t], ZS(s, t), ZS(s, t));
+                            px[t] = XS(s, t);
+                            py[t] = YS(s, t);
+                            pz[t] = ZS(s, t);
                         }
                     }
                     if constexpr (MODEL == KM_NORMAL || MODEL == KM_MT) {
 #pragma unroll
                         for (int t = 0; t < P; ++t) {
                             if (!has_frame<MODEL>(t)) continue;
-                            X[s][t] = fmaf(-y2[t], X[s][t], X[s][t]);
-                            Y[s][t] = fmaf(-y2[t], Y[s][t], Y[s][t]);
+                            XS(s, t) = fmaf(-y2[t], XS(s, t), XS(s, t));
+                            YS(s, t) = fmaf(-y2[t], YS(s, t), YS(s, t));
                         }
                     } else {
 #pragma unroll
@@ -965,10 +1140,10 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                                 ix = fmaf(f.x, px[p], fmaf(-f.y, py[p], ix));
                                 iy = fmaf(f.x, py[p], fmaf(f.y, px[p], iy));
                             }
-                            const float x = fmaf(-y2[t], X[s][t], X[s][t]);
-                            const float y = fmaf(-y2[t], Y[s][t], Y[s][t]);
-                            X[s][t] = fmaf(-yo[t], x, x) + ix;
-                            Y[s][t] = fmaf(-yo[t], y, y) + iy;
+                            const float x = fmaf(-y2[t], XS(s, t), XS(s, t));
+                            const float y = fmaf(-y2[t], YS(s, t), YS(s, t));
+                            XS(s, t) = fmaf(-yo[t], x, x) + ix;
+                            YS(s, t) = fmaf(-yo[t], y, y) + iy;
                         }
                     }
                 } else if constexpr (EXACT) {
@@ -976,7 +1151,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     float wx[P], wy[P];
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
-                        const float2 d = dm[s][t];
+                        const float2 d = make_float2(DMX(s, t), DMY(s, t));
                         wx[t] = px[t] + fmaf(d.x, px[t], -d.y * py[t]);
                         wy[t] = py[t] + fmaf(d.x, py[t], d.y * px[t]);
                     }
@@ -990,14 +1165,14 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                             ix = fmaf(f.x, wx[p], fmaf(-f.y, wy[p], ix));
                             iy = fmaf(f.x, wy[p], fmaf(f.y, wx[p], iy));
                         }
-                        X[s][t] = fmaf(-y2[t], wx[t], wx[t]) + ix;
-                        Y[s][t] = fmaf(-y2[t], wy[t], wy[t]) + iy;
+                        XS(s, t) = fmaf(-y2[t], wx[t], wx[t]) + ix;
+                        YS(s, t) = fmaf(-y2[t], wy[t], wy[t]) + iy;
                     }
                 } else {
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
                         if (!has_frame<MODEL>(t)) continue;
-                        float2 d = dm[s][t];
+                        float2 d = make_float2(DMX(s, t), DMY(s, t));
                         if (MODEL == KM_EXCH) {  // self exchange (a nonzero K diagonal)
                             d.x += fr[t][t].x;
                             d.y += fr[t][t].y;
@@ -1013,22 +1188,22 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                             ix = fmaf(f.x, px[p], fmaf(-f.y, py[p], ix));
                             iy = fmaf(f.x, py[p], fmaf(f.y, px[p], iy));
                         }
-                        X[s][t] = px[t] + ix;
-                        Y[s][t] = py[t] + iy;
+                        XS(s, t) = px[t] + ix;
+                        YS(s, t) = py[t] + iy;
                     }
                 }
                 // ---- longitudinal (and the bound pools) -----------------------
                 if (MODEL == KM_NORMAL) {
 #pragma unroll
-                    for (int t = 0; t < P; ++t) Z[s][t] = fmaf(y1[t], rhoS[t] - Z[s][t], Z[s][t]);
+                    for (int t = 0; t < P; ++t) ZS(s, t) = fmaf(y1[t], rhoS[t] - ZS(s, t), ZS(s, t));
                 } else if (MODEL == KM_EXCH && EXACT) {
 #pragma unroll
                     for (int t = 0; t < kXP; ++t) {
                         float iz = 0.f;
 #pragma unroll
                         for (int p = 0; p < kXP; ++p) iz = fmaf(fL[t][p], pz[p], iz);
-                        const float z = Z[s][t];
-                        Z[s][t] = fmaf(-y1[t], z, z) + iz + cL[t];
+                        const float z = ZS(s, t);
+                        ZS(s, t) = fmaf(-y1[t], z, z) + iz + cL[t];
                     }
                 } else if (MODEL == KM_EXCH) {
 #pragma unroll
@@ -1036,14 +1211,14 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                         float iz = 0.f;
 #pragma unroll
                         for (int p = 0; p < P; ++p) iz = fmaf(fin[t][p], pz[p], iz);
-                        float z = Z[s][t];
+                        float z = ZS(s, t);
                         if (!FREE && rf) z = fmaf(-sat[t], z, z);
                         z = fmaf(-y1[t], z, z);
-                        Z[s][t] = fmaf(-yo[t], z, z) + iz + rhoS[t] * y1[t];
+                        ZS(s, t) = fmaf(-yo[t], z, z) + iz + rhoS[t] * y1[t];
                     }
                 } else {  // MT / CEST
                     const float zb0 = pz[1], z0 = pz[0];
-                    float z = Z[s][0];
+                    float z = ZS(s, 0);
                     if (MODEL == KM_MT) {
                         z = fmaf(-mt_y1k, z, z) + rhoS[0] * y1[0] + zb0 * mt_y21;
                     } else {
@@ -1054,14 +1229,14 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                         z = fmaf(-yo[0], z, z) + iz + zb0 * mt_y21 + rhoS[0] * y1[0];
 #pragma unroll
                         for (int t = 2; t < P; ++t) {
-                            const float cz = fmaf(-y1[t], Z[s][t], Z[s][t]);
-                            Z[s][t] = fmaf(-yo[t], cz, cz) + fin[t][0] * z0 + rhoS[t] * y1[t];
+                            const float cz = fmaf(-y1[t], ZS(s, t), ZS(s, t));
+                            ZS(s, t) = fmaf(-yo[t], cz, cz) + fin[t][0] * z0 + rhoS[t] * y1[t];
                         }
                     }
                     float bz = zb0;
                     if (rf) bz = fmaf(-sat[1], bz, bz);
-                    Z[s][1] = fmaf(-mt_y1bk, bz, bz) + rhoS[1] * mt_y1b + z0 * mt_y12;
-                    Z[s][0] = z;
+                    ZS(s, 1) = fmaf(-mt_y1bk, bz, bz) + rhoS[1] * mt_y1b + z0 * mt_y12;
+                    ZS(s, 0) = z;
                 }
             }
         }
@@ -1076,17 +1251,25 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 #pragma unroll
             for (int t = 0; t < P; ++t) {
                 // back to the lab frame: m_lab = m_frame * P
-                float2 m = make_float2(X[s][t], Y[s][t]);
+                float2 m = make_float2(XS(s, t), YS(s, t));
                 if (entered && has_frame<MODEL>(t)) m = cmul(m, Pc[t]);
                 const long long i = ((long long)t * L.S + sp) * n + v;
                 L.mx[i] = m.x;
                 L.my[i] = m.y;
-                L.mz[i] = Z[s][t];
+                L.mz[i] = ZS(s, t);
             }
         }
     }
     kbase += (uint32_t)nchunks;
     return true;
+#undef XS
+#undef YS
+#undef ZS
+#undef DMX
+#undef DMY
+#undef DWS
+#undef PAIR
+#undef UNPAIR
 }
 
 // The accurate scan kernel.  A block works through items (instance, tile):

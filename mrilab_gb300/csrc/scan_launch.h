@@ -39,7 +39,7 @@ inline size_t scan_fast_smem_bytes(int stride4, int rx, int P, int NS) {
     return 128 + (size_t)2 * kFastChunk * stride4 * 16  // staged step records
            + 16 * row * 8 + c4 * row * (coil_presplit((int)c4) ? 16 : 8)  // receive tile, coil maps
            + (kBlock / 32) * 16 * 2 * c4 * 4        // per-warp receive sums
-           + ((size_t)NS * P + 4) * kBlock * 4;     // dWRnd, low parts of omega
+           + ((size_t)2 * ((NS + 1) / 2) * P + 4) * kBlock * 4;  // dWRnd (spin pairs), low parts of omega
 }
 
 // One launch of the accurate kernel: n_items work items (instance, tile)

@@ -59,7 +59,9 @@ def test_batch_tuned_matches_within_rounding(built):
         b.execute("persistent")
         for o, a in zip(b.download(), alone):
             # another spins-per-thread choice sums the spins in another order
-            assert rel_l2(signal(o), signal(a)) <= 1e-6
+            # (and pairs of spins take the packed f32x2 path, which adds the
+            # increments in another order)
+            assert rel_l2(signal(o), signal(a)) <= 3e-6
             np.testing.assert_allclose(o["Mz"], a["Mz"], rtol=0, atol=1e-6)
     finally:
         b.close()
