@@ -15,9 +15,15 @@ water exchanging, 8 Rx coils, 6 echoes; 32 x 8 phase/partition encodes of
 * ``roofline``: FP32-pipe bound of the scan kernel from the algorithmic op
   table (flops per isochromat-pool-step), against FP32 and MUFU peaks
   measured on this GPU by ``libmrl_peaks.so``.
-* ``cpu_baseline``: the reference scan algorithm on the host cores (the
-  single-precision oracle port, all threads) on a bounded sample of the same
-  workload.
+* ``cpu_baseline``: the reference's CPU path on the host cores, all
+  threads: its CUDA kernel for the model compiled from source as host C
+  where it is built (from the reference tree, or the kernel headers staged
+  into ``oracle/_ref/stage``), else the single-precision oracle port; on a
+  bounded sample of the same workload (whole TRs on a subset of voxel rows).
+* ``parity``, ``reference_order``, ``batched``, ``fwd_adjoint``: the
+  full-length parity of the headline scan on a voxel subset, the reference-
+  order integrator's rate, and the metric's other two parts (config 3
+  batched vs plain, config 4 fwd+adjoint), timed in the same run.
 
 ``--impl reference`` times that CPU implementation alone (the reference's
 own CPU path; there is no GPU reference on this path) and prints its line.
@@ -554,12 +560,19 @@ def extras(args):
     return out
 
 
-def cpu_baseline(sc, target_s=12.0):
-    """The reference scan algorithm on the host cores (single-precision
-    oracle port, all threads) on whole TRs of the same workload: every TR of
-    the scan has the same step structure (excitation, encoding, readouts),
-    so k whole TRs carry the scan's own mix of rf, free and sampled steps."""
+def cpu_baseline(sc, target_s=12.0, workload="config2"):
+    """The reference's CPU path on the host cores, all threads: the
+    reference's own CUDA kernel for the model compiled from its source as
+    host C (BlochKernelME.cuh for the two-pool workload; the reference CPU
+    engine refuses multi-pool objects) where it is built, else the
+    single-precision oracle port.  The sample is whole TRs (every TR of the
+    scan has the same step structure, so it carries the scan's own mix of
+    rf, free and sampled steps) on every r-th row of voxels (voxels are
+    independent), sized to about target_s seconds."""
     import oracle
+
+    if oracle.ref_kernel_available():
+        return _ref_kernel_baseline(sc, target_s, workload)
 
     threads = os.cpu_count() or 1
     n_tr = max(1, int(sc.VCtl["TRNum"]))
@@ -576,6 +589,31 @@ def cpu_baseline(sc, target_s=12.0):
     return dict(value=units / el, unit=UNIT, cores=threads, kind="port",
                 sample=f"the first {k} whole TR(s) of {n_tr} ({out['steps']} dt>0 steps, {units:.3g} units, "
                        f"{el:.1f} s)")
+
+
+def _ref_kernel_baseline(sc, target_s, workload):
+    import oracle
+    from mrilab_gb300 import phantoms
+
+    threads = os.cpu_count() or 1
+    n_tr = max(1, int(sc.VCtl["TRNum"]))
+    one, _ = workload_args(workload, 1)  # the scan's first TR, every voxel
+
+    def sample(stride):
+        return phantoms.crop(one, slice(0, None, stride), slice(None), slice(None))
+
+    probe = sample(32)
+    t0 = time.perf_counter()
+    oracle.run_ref_kernel(probe, threads=threads)
+    rate = probe.units() / max(time.perf_counter() - t0, 1e-3)
+    stride = int(min(one.dims[0], max(1, round(one.units() / (rate * target_s)))))
+    sub = sample(stride)
+    t0 = time.perf_counter()
+    oracle.run_ref_kernel(sub, threads=threads)
+    el = time.perf_counter() - t0
+    return dict(value=sub.units() / el, unit=UNIT, cores=threads, kind="reference",
+                sample=f"the reference's {sc.model.upper()} kernel source compiled as host C (OpenMP): the first whole "
+                       f"TR of {n_tr} on every {stride}-th voxel row ({sub.units():.3g} units, {el:.1f} s)")
 
 
 def config_of(sc, desc):
@@ -648,7 +686,7 @@ def main():
         # stable rate and keep the arm within a few minutes
         n_warm, n_steps = min(args.warmup, 1), min(args.steps, 5)
         for i in range(n_warm + n_steps):
-            base = cpu_baseline(sc, target_s=8.0)
+            base = cpu_baseline(sc, target_s=8.0, workload=args.workload)
             if i >= n_warm:
                 vals.append(base["value"])
         v = float(np.mean(vals))
@@ -748,7 +786,7 @@ def main():
         line["reference_order"] = reference_order_rate(local)
         line.update(extras(args))
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(sc)
+        line["cpu_baseline"] = cpu_baseline(sc, workload=args.workload)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

@@ -1,13 +1,15 @@
 """Build the native parts of mrilab_gb300 in-tree.
 
-* ``libmrl_scan.so``: the C-ABI scan engine (``include/mrl_scan.h``) and
-  SAR engine (``include/mrl_sar.h``), CUDA for sm_103a only; translation
-  units compile in parallel.
+* ``libmrl_scan.so``: the C-ABI scan engine (``include/mrl_scan.h``), SAR
+  engine (``include/mrl_sar.h``) and reconstruction
+  (``include/mrl_recon.h``), CUDA for sm_103a only; translation units
+  compile in parallel.
 * ``mex/libfakemex.so``: the MATLAB stand-in used to drive the mex layer
   without MATLAB.
-* ``mex/Do*ScanAtGPU.so``, ``mex/DoCalSARAtGPU.so``: the mex wrappers with
-  the reference engine names (the SAR one named after the reference's
-  DoCalSARAtCPU, for the GPU),
+* ``mex/Do*ScanAtGPU.so``, ``mex/DoCalSARAtGPU.so``, ``mex/DoGridding.so``,
+  ``mex/DoCartReconGPU.so``: the mex wrappers with the reference engine
+  names (the SAR one named after the reference's DoCalSARAtCPU, for the
+  GPU; DoCartReconGPU new, for the transform of DoCartRecon.m),
   linked against the stand-in (inside MATLAB they are built with ``mex``
   against MATLAB's own headers instead: ``mex -DMRL_WRAP_MODEL=<model>
   csrc/mex_wrappers.cpp -lmrl_scan``).
@@ -55,6 +57,7 @@ UNITS = {
     "scan_fast_exact.cu": [],
     "scan_fast_exact_bound.cu": [],
     "sar.cu": [],
+    "recon.cu": [],
     "decode.cpp": None,  # host C++
 }
 
@@ -79,7 +82,7 @@ def _stale(target: str, deps) -> bool:
 
 def _headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    return hs + [os.path.join(ROOT, "include", f) for f in ("mrl_scan.h", "mrl_sar.h")]
+    return hs + [os.path.join(ROOT, "include", f) for f in ("mrl_scan.h", "mrl_sar.h", "mrl_recon.h")]
 
 
 def _run(cmd):
@@ -112,7 +115,7 @@ def build(verbose: bool = False, jobs: int = 0) -> None:
             if verbose and out:
                 print(out)
     if _stale(LIB, objs):
-        _run([nvcc, "-shared", *GENCODE, "-o", LIB, *objs, "-lcudart", "-lpthread"])
+        _run([nvcc, "-shared", *GENCODE, "-o", LIB, *objs, "-lcudart", "-lcufft", "-lpthread"])
     peaks_src = os.path.join(CSRC, "peaks.cu")
     if _stale(PEAKS, [peaks_src]):
         _run([nvcc, "-std=c++17", "-O3", *GENCODE, "-Xcompiler", "-fPIC", "-shared", peaks_src, "-o", PEAKS])
@@ -126,6 +129,12 @@ def build(verbose: bool = False, jobs: int = 0) -> None:
     if _stale(sar_out, [sar_src, LIB, FAKEMEX] + hdrs):
         _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", f"-I{MEX}", sar_src, "-o", sar_out, f"-L{HERE}",
               "-lmrl_scan", f"-L{MEX}", "-lfakemex", "-Wl,-rpath,$ORIGIN/..", "-Wl,-rpath,$ORIGIN"])
+    rsrc = os.path.join(CSRC, "recon_mex.cpp")
+    for name, flag in (("DoGridding", "MRL_WRAP_GRID"), ("DoCartReconGPU", "MRL_WRAP_CART")):
+        out = os.path.join(MEX, name + ".so")
+        if _stale(out, [rsrc, LIB, FAKEMEX] + hdrs):
+            _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", f"-D{flag}", f"-I{MEX}", rsrc, "-o", out, f"-L{HERE}",
+                  "-lmrl_scan", f"-L{MEX}", "-lfakemex", "-Wl,-rpath,$ORIGIN/..", "-Wl,-rpath,$ORIGIN"])
     for name, model in WRAPPERS.items():
         out = os.path.join(MEX, name + ".so")
         if _stale(out, [wsrc, LIB, FAKEMEX] + hdrs):

@@ -148,7 +148,43 @@ int fm_call(fm_mex_fn fn) {
     return 0;
 }
 
+int fm_call_args(fm_mex_fn fn, int nlhs, mxArray **plhs, int nrhs, const mxArray **prhs) {
+    jmp_buf env;
+    jmp_buf *prev = g_jmp;
+    g_err[0] = 0;
+    g_jmp = &env;
+    if (setjmp(env) != 0) {
+        g_jmp = prev;
+        return 1;
+    }
+    fn(nlhs, plhs, nrhs, prhs);
+    g_jmp = prev;
+    return 0;
+}
+
+void fm_free_array(mxArray *pm) { fm_free(pm); }
+
 /* ---- MATLAB API --------------------------------------------------------- */
+
+double *mxGetPr(const mxArray *pm) { return pm && pm->class_id == mxDOUBLE_CLASS ? (double *)pm->data : NULL; }
+size_t mxGetM(const mxArray *pm) { return pm ? (size_t)pm->dims[0] : 0; }
+size_t mxGetN(const mxArray *pm) {
+    if (!pm) return 0;
+    size_t n = 1;
+    for (int i = 1; i < pm->ndims; ++i) n *= (size_t)pm->dims[i];
+    return n;
+}
+mxArray *mxCreateDoubleMatrix(size_t m, size_t n, mxComplexity flag) {
+    (void)flag;
+    int dims[2] = {(int)m, (int)n};
+    return fm_new_numeric(mxDOUBLE_CLASS, 2, dims);
+}
+mxArray *mxCreateNumericArray(size_t ndim, const mwSize *dims, mxClassID classid, mxComplexity flag) {
+    (void)flag;
+    int d[8];
+    for (size_t i = 0; i < ndim && i < 8; ++i) d[i] = dims[i];
+    return fm_new_numeric(classid, (int)(ndim < 8 ? ndim : 8), d);
+}
 
 const mxArray *mexGetVariablePtr(const char *workspace, const char *name) {
     (void)workspace;

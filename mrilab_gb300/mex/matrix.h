@@ -35,6 +35,13 @@ mwSize mxGetNumberOfDimensions(const mxArray *pm);
 const mwSize *mxGetDimensions(const mxArray *pm);
 void *mxCalloc(size_t n, size_t size);
 bool mxUnshareArray(mxArray *pm, bool noDeepCopy);
+/* argument-passing mex functions (DoGridding.cpp:51-66) */
+typedef enum { mxREAL = 0, mxCOMPLEX = 1 } mxComplexity;
+double *mxGetPr(const mxArray *pm);
+size_t mxGetM(const mxArray *pm);
+size_t mxGetN(const mxArray *pm);
+mxArray *mxCreateDoubleMatrix(size_t m, size_t n, mxComplexity flag);
+mxArray *mxCreateNumericArray(size_t ndim, const mwSize *dims, mxClassID classid, mxComplexity flag);
 
 /* ---- harness side (not part of MATLAB's API) ---------------------------- */
 
@@ -57,6 +64,10 @@ void fm_set_eval_handler(fm_eval_fn fn);
  * (the message is then available from fm_last_error()). */
 typedef void (*fm_mex_fn)(int, mxArray **, int, const mxArray **);
 int fm_call(fm_mex_fn fn);
+/* Call a mexFunction with arguments; plhs receives the outputs it creates
+ * (free them with fm_free_array). */
+int fm_call_args(fm_mex_fn fn, int nlhs, mxArray **plhs, int nrhs, const mxArray **prhs);
+void fm_free_array(mxArray *pm);
 const char *fm_last_error(void);
 void fm_set_verbose(int verbose);
 

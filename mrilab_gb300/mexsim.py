@@ -53,6 +53,10 @@ def _lib() -> ctypes.CDLL:
     lib.fm_call.restype = ctypes.c_int
     lib.fm_last_error.restype = ctypes.c_char_p
     lib.fm_set_verbose.argtypes = [ctypes.c_int]
+    lib.fm_call_args.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                 ctypes.POINTER(ctypes.c_void_p)]
+    lib.fm_call_args.restype = ctypes.c_int
+    lib.fm_free_array.argtypes = [ctypes.c_void_p]
     return lib
 
 
@@ -141,6 +145,35 @@ class MexSession:
                 raise RuntimeError(f"engine library {so_path} is missing")
             self._engines[so_path] = ctypes.CDLL(so_path, mode=ctypes.RTLD_LOCAL)
         return self._engines[so_path]
+
+    def _array(self, arr) -> np.ndarray:
+        nd = self.lib.mxGetNumberOfDimensions(arr)
+        dp = self.lib.mxGetDimensions(arr)
+        dims = tuple(dp[i] for i in range(nd))
+        cls = ctypes.cast(arr, ctypes.POINTER(ctypes.c_int))[0]
+        dt = np.dtype(_DTYPE[cls])
+        n = int(np.prod(dims))
+        buf = (ctypes.c_char * (n * dt.itemsize)).from_address(self.lib.fm_data(arr))
+        return np.frombuffer(buf, dtype=dt, count=n).reshape(dims, order="F").copy()
+
+    def call_args(self, so_path: str, args, nlhs: int):
+        """Run a mexFunction that takes its inputs as arguments (prhs) and
+        returns nlhs outputs (plhs), as MATLAB's [a, b] = f(x, y, ...)."""
+        eng = self.load(so_path)
+        fn = ctypes.cast(eng.mexFunction, ctypes.c_void_p)
+        prhs = (ctypes.c_void_p * max(1, len(args)))(*[self._numeric(np.asarray(a)) for a in args])
+        plhs = (ctypes.c_void_p * max(1, nlhs))()
+        rc = self.lib.fm_call_args(fn, nlhs, plhs, len(args), prhs)
+        try:
+            if rc != 0:
+                raise MexError(self.lib.fm_last_error().decode())
+            return [self._array(plhs[i]) for i in range(nlhs)]
+        finally:
+            for i in range(len(args)):
+                self.lib.fm_free_array(prhs[i])
+            for i in range(nlhs):
+                if plhs[i]:
+                    self.lib.fm_free_array(plhs[i])
 
     def call(self, so_path: str) -> None:
         """Run an engine's mexFunction against the current globals."""

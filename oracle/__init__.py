@@ -87,10 +87,20 @@ def build(force: bool = False) -> None:
             raise RuntimeError(f"MRILAB_REFERENCE_ROOT={REFERENCE_ROOT!r} is not an MRiLab tree "
                                "(no Lib/src/engine)")
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REFROOT={REFERENCE_ROOT}"])
+    elif os.path.isdir(os.path.join(REF_DIR, "stage")):
+        # the reference kernel headers staged by `make stage` (a copy of the
+        # working tree on a machine without the reference tree)
+        subprocess.check_call(["make", "-s", "-C", HERE, "refkern"])
 
 
 def ref_available() -> bool:
     return os.path.exists(REF_CPU_SO) and os.path.exists(REF_KERN_SO)
+
+
+def ref_kernel_available() -> bool:
+    """The reference's CUDA kernels compiled as host C (from the reference
+    tree, or from its staged kernel headers)."""
+    return os.path.exists(REF_KERN_SO)
 
 
 def _ptr(a, typ):

@@ -69,6 +69,25 @@ SAR = {
     "sar_tx3_n6_seed3": dict(seed=3, n=6, nz=3, tx_coils=3, n_tr=2, sample_fracs=(0.1, 0.45, 0.7)),
 }
 
+# gridding (the reference DoGridding mex, compiled from its source): inputs
+# drawn from the seed by grid_inputs below
+GRID = {
+    "grid2d_n400_g32_seed0": dict(seed=0, n=400, grid=32, half_width=2.0, nk=101),
+    "grid2d_n900_g48_seed1": dict(seed=1, n=900, grid=48, half_width=3.0, nk=201),
+}
+
+
+def grid_inputs(seed, n, grid, half_width, nk):
+    """Seeded gridding inputs: k-space locations in [-0.5, 0.5], complex
+    samples, density weights and a Gaussian-like kernel table."""
+    rng = np.random.default_rng(seed)
+    kx, ky = rng.uniform(-0.5, 0.5, n), rng.uniform(-0.5, 0.5, n)
+    sx, sy = rng.normal(size=n), rng.normal(size=n)
+    dcf = rng.uniform(0.2, 1.5, n)
+    ker = np.exp(-3.0 * np.linspace(0.0, 1.0, nk) ** 2)
+    return kx, ky, sx, sy, dcf, ker, grid, half_width
+
+
 CASES = {
     # name: (builder kwargs)
     "gre2d_n16_tr4_seed1": dict(seed=1, n=16, n_tr=4),
@@ -154,7 +173,16 @@ def main(only=()):
         print(name, "reference kernels vs FP64 oracle: %.3e (sampled %.3e); FP32 port vs FP64 %.3e; seconds %s" % (
             rl(runs["ref"], runs["f64"]), rl(runs["ref"][..., keep], runs["f64"][..., keep]),
             rl(runs["f32"], runs["f64"]), secs))
+    from oracle import recon as orc
     from oracle import sar as osar
+
+    for name, kw in GRID.items():
+        if not wanted(name):
+            continue
+        gx, gy = orc.run_ref_grid(*grid_inputs(**kw))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), builder=np.array("grid_inputs"),
+                            kwargs=np.array(repr(kw)), ref_gx=gx, ref_gy=gy)
+        print(name, "gridded points:", int(np.count_nonzero(gx)))
 
     for name, kw in SAR.items():
         if not wanted(name):

@@ -30,7 +30,7 @@ def test_library_exports_every_declared_symbol(built):
         assert hasattr(lib, n), n
 
 
-@pytest.mark.parametrize("wrapper", ["DoScanAtGPU", "DoMEScanAtGPU", "DoMTScanAtGPU", "DoCESTScanAtGPU",
+@pytest.mark.parametrize("wrapper", ["DoScanAtGPU", "DoMEScanAtGPU", "DoMTScanAtGPU", "DoCESTScanAtGPU", "DoGridding", "DoCartReconGPU",
                                      "DoGMScanAtGPU", "DoCalSARAtGPU"])
 def test_mex_wrappers_export_mexfunction(built, wrapper):
     so = os.path.join(ROOT, "mrilab_gb300", "mex", wrapper + ".so")
