@@ -57,9 +57,11 @@ typedef enum {
      * E = exp(A dt) of the relaxation-exchange generator, computed in FP64 per
      * voxel and distinct dt.  ME, and GM with free and bound pools (a bound
      * pool is saturated on rf steps before the propagator and has no
-     * transverse generator), TypeNum <= 3; the normal model runs as
-     * MRL_NUMERICS_ACCURATE (its relaxation is exact already); MT and CEST
-     * are refused.  No reference counterpart. */
+     * transverse generator), TypeNum <= 3; MT and CEST (pool 1 bound, the
+     * models' K channels and transverse map: no transverse outflow to the
+     * bound pool; only pool 0 sampled), CEST with TypeNum <= 5; the normal
+     * model runs as MRL_NUMERICS_ACCURATE (its relaxation is exact
+     * already).  No reference counterpart. */
     MRL_NUMERICS_EXACT = 2
 } mrl_numerics;
 

@@ -407,6 +407,12 @@ struct Scanner {
     // exact relaxation-exchange propagator: its coefficient table per
     // (distinct float dt, voxel) and the dt values so far (index = position)
     bool exact = false;
+    // MT / CEST under the exact propagator: integrated as the general model
+    // with pool 1 bound (the kernel's bound-pool exact instantiation), the
+    // model's own K layout read by the table kernel, only pool 0 sampled;
+    // km_obj keeps the object's model for the active-voxel rule
+    bool mtc_exact = false;
+    int km_obj = 0;
     int coef = 0;  // coefficient source: 0 in the kernel, 1 split-scheme table, 2 exact table
     std::map<uint32_t, int> xdt_index;
     std::vector<float> xdts;
@@ -419,16 +425,25 @@ struct Scanner {
     }
 
     // the general model's bound pools (TypeFlag 1), one bit per pool
+    // kind of pool t for the exchange kernels: 0 free, 1 bound (GM TypeFlag;
+    // pool 1 of MT / CEST under the exact propagator)
+    int pool_kind(int t) const {
+        if (mtc_exact) return t == 1 ? 1 : 0;
+        return (mi.gm && t < P) ? (int)args->obj.type_flag[t] : 0;
+    }
     unsigned bound_mask() const {
         unsigned m = 0;
-        for (int t = 0; mi.km == KM_EXCH && mi.gm && t < P; ++t)
-            if ((int)args->obj.type_flag[t] == 1) m |= 1u << t;
+        for (int t = 0; mi.km == KM_EXCH && (mi.gm || mtc_exact) && t < P; ++t)
+            if (pool_kind(t) == 1) m |= 1u << t;
         return m;
     }
+    // layout of the exchange channels for the table kernels: 0 ME, 1 GM, 2 MT, 3 CEST
+    int k_layout() const { return mtc_exact ? (km_obj == KM_MT ? 2 : 3) : (mi.gm ? 1 : 0); }
 
     // every pool of an exchange model is a free pool (ME, or GM without bound pools)
     int all_free() const {
         if (mi.km != KM_EXCH) return 0;
+        if (mtc_exact) return 0;
         if (!mi.gm) return 1;
         for (int t = 0; t < P; ++t)
             if ((int)args->obj.type_flag[t] != 0) return 0;
@@ -501,7 +516,14 @@ struct Scanner {
             a.ctl.numerics != MRL_NUMERICS_EXACT)
             return set_err("unknown numerics %d", a.ctl.numerics), MRL_ERR_ARG;
         exact = a.ctl.numerics == MRL_NUMERICS_EXACT && mi.km != KM_NORMAL;
-        if (exact) {
+        km_obj = mi.km;
+        if (exact && (mi.km == KM_MT || mi.km == KM_CEST)) {
+            if (P > 5) return set_err("MRL_NUMERICS_EXACT supports CEST with TypeNum <= 5"), MRL_ERR_UNSUPPORTED;
+            mtc_exact = true;
+            // every pool has a signal slot in the exchange kernels' receive
+            // layout; only pool 0 is sampled (set_sampling below)
+            mi = {KM_EXCH, P, mi.nk, false};
+        } else if (exact) {
             // ME, or GM pools free (TypeFlag 0) or bound (1) with a free one
             bool ok = mi.km == KM_EXCH, any_free = !mi.gm;
             for (int t = 0; ok && mi.gm && t < P; ++t) {
@@ -522,7 +544,7 @@ struct Scanner {
         if (hist_on && (!a.sig.mxs || !a.sig.mys || !a.sig.mzs))
             return set_err("RunMode 1 needs the history arrays VSig.Mx/My/Mz"), MRL_ERR_ARG;
         if (fast && TX > 1) {
-            bool bound = mi.km == KM_MT || mi.km == KM_CEST;
+            bool bound = mi.km == KM_MT || mi.km == KM_CEST || mtc_exact;
             if (mi.gm)
                 for (int t = 0; t < P; ++t) bound |= (int)a.obj.type_flag[t] == 1;
             if (bound)
@@ -534,6 +556,9 @@ struct Scanner {
             const int ns = atoi(e);
             if ((ns == 1 || ns == 2 || ns == 4) && S % ns == 0) NS = ns;
         }
+        // the exact propagator's bound-pool instantiations hold one spin per
+        // thread from four pools up (their tables fill the registers)
+        if (exact && !all_free() && P >= 4) NS = 1;
         tpv = S / NS;
         stride4 = fast ? fast_stride_f4(TX) : record_stride_f4(TX);
         return MRL_OK;
@@ -545,7 +570,7 @@ struct Scanner {
         const mrl_scan_args &a = *args;
         act.clear();
         for (long long v = 0; v < V; ++v)
-            if (voxel_active(a, mi.km, v, V)) act.push_back((int)v);
+            if (voxel_active(a, km_obj, v, V)) act.push_back((int)v);
         n_act = (int)act.size();
         const size_t n = std::max(1, n_act);
         size_t off = 0;
@@ -733,7 +758,7 @@ struct Scanner {
         L.err = d_err.p;
         for (int t = 0; t < kMaxPool; ++t) {
             L.cs2pi[t] = t < P && a.ctl.cs ? (float)(2 * kPiRef * (double)(float)a.ctl.cs[t]) : 0.f;
-            L.kind[t] = (mi.gm && t < P) ? (int)a.obj.type_flag[t] : 0;
+            L.kind[t] = t < P ? pool_kind(t) : 0;
         }
         (void)rf_ref;
         return L;
@@ -792,7 +817,7 @@ struct Scanner {
         if (e == cudaSuccess) e = d_xtab.ensure(xdts.size() * (size_t)nf * n_act);
         const float *kch = mi.nk > 0 ? d_f.p + o_k : nullptr;
         if (e == cudaSuccess)
-            e = coef == 2 ? launch_exact_table(P, d_xdts.p, (int)xdts.size(), n_act, S, mi.gm ? 1 : 0,
+            e = coef == 2 ? launch_exact_table(P, d_xdts.p, (int)xdts.size(), n_act, S, k_layout(),
                                                bound_mask(), d_f.p + o_rho, d_f.p + o_t1, d_f.p + o_t2, kch,
                                                d_xtab.p, st)
                           : launch_split_table(P, d_xdts.p, (int)xdts.size(), n_act, mi.gm ? 1 : 0,
@@ -880,6 +905,10 @@ struct Scanner {
         F.txc = d_f2.p + o_txc;
         F.all_free = all_free();
         set_sampling(F, L, P);
+        if (mtc_exact) {  // MT / CEST sample pool 0 only (BlochKernelMT.cuh:230)
+            F.n_samp = 1;
+            for (int t = 0; t < kMaxPool; ++t) F.samp_rank[t] = t == 0 ? 0 : -1;
+        }
         for (int t = 0; t < kMaxPool; ++t) {  // 2 pi CS[t] as a (hi, lo) pair
             const double w = (t < P && args->ctl.cs) ? 2 * kPiRef * args->ctl.cs[t] : 0.0;
             F.cs_hi[t] = (float)w;

@@ -112,8 +112,26 @@ __device__ void expm1_phi1(const double (&A)[P][P], double (&F)[P][P], double (&
     }
 }
 
+// Exchange rate from pool t to pool p of voxel v in each model's K layout
+// (layout 0 ME: channel t*P+p; 1 GM: p*P+t; 2 MT: channel 1 = K12 (0 -> 1),
+// 2 = K21 (1 -> 0); 3 CEST: 0 = 0 -> MT, P-1 = MT -> 0, t-1 = 0 -> t,
+// t+P-2 = t -> 0), 0 where the model has no such rate.
 template <int P>
-__global__ void exact_table_kernel(const float *__restrict__ dts, int n_dt, int n_act, int S, int gm,
+__device__ __forceinline__ double exch_rate(const float *kch, int n_act, int v, int layout, int t, int p) {
+    int ch = -1;
+    if (layout == 0) ch = t * P + p;
+    else if (layout == 1) ch = p * P + t;
+    else if (layout == 2) ch = (t == 0 && p == 1) ? 1 : ((t == 1 && p == 0) ? 2 : -1);
+    else if (t == 0) ch = p == 1 ? 0 : p - 1;
+    else if (p == 0) ch = t == 1 ? P - 1 : t + P - 2;
+    return ch < 0 ? 0.0 : (double)kch[(long long)ch * n_act + v];
+}
+
+// layout as exch_rate.  MT and CEST (layout 2, 3) keep their models'
+// transverse map: a free pool's transverse magnetisation does not flow out
+// to the bound pool (BlochKernelMT.cuh:324-333, BlochKernelCEST.cuh:364-395).
+template <int P>
+__global__ void exact_table_kernel(const float *__restrict__ dts, int n_dt, int n_act, int S, int layout,
                                    unsigned bound, const float *__restrict__ rho, const float *__restrict__ t1,
                                    const float *__restrict__ t2, const float *__restrict__ kch, float *tab) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -131,6 +149,7 @@ __global__ void exact_table_kernel(const float *__restrict__ dts, int n_dt, int 
     for (int t = 0; t < P; ++t) {
         const double T1 = t1[(long long)t * n_act + v], T2 = t2[(long long)t * n_act + v],
                      r = rho[(long long)t * n_act + v];
+        const bool mtc = layout >= 2;
         if (T1 == 0.0 || T2 == 0.0 || r == 0.0) continue;  // a pool left alone: identity row
         // a bound pool: no transverse generator (identity row), and no free
         // pool takes transverse inflow from it
@@ -141,10 +160,9 @@ __global__ void exact_table_kernel(const float *__restrict__ dts, int n_dt, int 
 #pragma unroll
         for (int p = 0; p < P; ++p) {
             if (p == t || !kch) continue;  // a self rate moves nothing
-            // ME: channel a*P+b is the rate a -> b; GM: channel b*P+a
-            const double kgo = kch[(long long)(gm ? p * P + t : t * P + p) * n_act + v];
-            const double kin = kch[(long long)(gm ? t * P + p : p * P + t) * n_act + v];
-            if (!bt) At[t][t] -= kgo;
+            const double kgo = exch_rate<P>(kch, n_act, v, layout, t, p);
+            const double kin = exch_rate<P>(kch, n_act, v, layout, p, t);
+            if (!bt && !(mtc && (bound >> p & 1u))) At[t][t] -= kgo;
             Al[t][t] -= kgo;
             if (!bt && !(bound >> p & 1u)) At[t][p] += kin;
             Al[t][p] += kin;
@@ -268,18 +286,23 @@ int occupancy_scan_fast_tab(int co, int P, int NS, bool all_free, size_t smem) {
     return n;
 }
 
-cudaError_t launch_exact_table(int P, const float *dts, int n_dt, int n_act, int S, int gm, unsigned bound,
+cudaError_t launch_exact_table(int P, const float *dts, int n_dt, int n_act, int S, int layout, unsigned bound,
                                const float *rho, const float *t1, const float *t2, const float *kch, float *tab,
                                cudaStream_t st) {
     const long long n = (long long)n_dt * n_act;
     if (n <= 0) return cudaSuccess;
     const unsigned blocks = (unsigned)((n + 127) / 128);
+#define MRL_XTAB(PP) \
+    exact_table_kernel<PP><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, layout, bound, rho, t1, t2, kch, tab)
     switch (P) {
-    case 1: exact_table_kernel<1><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, bound, rho, t1, t2, kch, tab); break;
-    case 2: exact_table_kernel<2><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, bound, rho, t1, t2, kch, tab); break;
-    case 3: exact_table_kernel<3><<<blocks, 128, 0, st>>>(dts, n_dt, n_act, S, gm, bound, rho, t1, t2, kch, tab); break;
+    case 1: MRL_XTAB(1); break;
+    case 2: MRL_XTAB(2); break;
+    case 3: MRL_XTAB(3); break;
+    case 4: MRL_XTAB(4); break;
+    case 5: MRL_XTAB(5); break;
     default: return cudaErrorInvalidValue;
     }
+#undef MRL_XTAB
     return cudaGetLastError();
 }
 

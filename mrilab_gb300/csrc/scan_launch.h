@@ -87,8 +87,9 @@ FastKernel select_exact_bound(int P, int NS);  // scan_fast_exact_bound.cu
 cudaError_t launch_split_table(int P, const float *dts, int n_dt, int n_act, int gm, const float *rho,
                                const float *t1, const float *t2, const float *kch, float *tab, cudaStream_t st);
 // tab[(d * exact_fields(P) + f) * n_act + v] for the n_dt values dts[]
-// (bound: one bit per bound pool)
-cudaError_t launch_exact_table(int P, const float *dts, int n_dt, int n_act, int S, int gm, unsigned bound,
+// (bound: one bit per bound pool; layout of the exchange channels: 0 ME,
+// 1 GM, 2 MT, 3 CEST)
+cudaError_t launch_exact_table(int P, const float *dts, int n_dt, int n_act, int S, int layout, unsigned bound,
                                const float *rho, const float *t1, const float *t2, const float *kch, float *tab,
                                cudaStream_t st);
 // ---- adjoint (adjoint.cu) ----------------------------------------------------

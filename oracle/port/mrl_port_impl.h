@@ -195,6 +195,27 @@ static REAL PORT_T(relax_exp)(REAL dt, REAL t) {
     return REXP((REAL)e);
 }
 
+/* Exchange rate from pool t to pool p of voxel v in each model's K layout:
+ * ME channel t*P+p, GM channel p*P+t (BlochKernelME.cuh, BlochKernelGM.cuh);
+ * MT channel 1 = K12 (0 -> 1), 2 = K21 (1 -> 0) (BlochKernelMT.cuh:324-407);
+ * CEST channel 0 = 0 -> MT, P-1 = MT -> 0, t-1 = 0 -> t, t+P-2 = t -> 0
+ * (BlochKernelCEST.cuh:364-600). */
+static double PORT_T(rate)(const mrl_port_args *a, long V, int v, int t, int p) {
+    const int P = a->type_num;
+    long ch = -1;
+    switch (a->model) {
+    case MRL_PORT_ME: ch = (long)t * P + p; break;
+    case MRL_PORT_GM: ch = (long)p * P + t; break;
+    case MRL_PORT_MT: ch = (t == 0 && p == 1) ? 1 : (t == 1 && p == 0) ? 2 : -1; break;
+    case MRL_PORT_CEST:
+        if (t == 0) ch = p == 1 ? 0 : p - 1;
+        else if (p == 0) ch = t == 1 ? P - 1 : t + P - 2;
+        break;
+    default: break;
+    }
+    return ch < 0 ? 0.0 : (double)a->k[ch * V + v];
+}
+
 /* One dt > 0 step of one isochromat group (voxel v, spin s) for the model. */
 static void PORT_T(update)(const mrl_port_args *a, REAL *MX, REAL *MY, REAL *MZ, long V, int v, int s,
                            const PORT_T(step) *st, REAL rf_sum, REAL gyro) {
@@ -231,12 +252,18 @@ static void PORT_T(update)(const mrl_port_args *a, REAL *MX, REAL *MY, REAL *MZ,
         return;
     }
 
-    if ((a->model == MRL_PORT_ME || a->model == MRL_PORT_GM) && a->exact) {
+    const int mtc = a->model == MRL_PORT_MT || a->model == MRL_PORT_CEST;
+    if ((a->model == MRL_PORT_ME || a->model == MRL_PORT_GM || mtc) && a->exact) {
         /* exact relaxation-exchange propagator after the rotation of every
-         * free pool and the saturation of every bound (GM TypeFlag 1) pool;
-         * a bound pool has no transverse generator (its transverse
-         * magnetisation is held, and no free pool takes transverse inflow
-         * from it) but takes part in the longitudinal one */
+         * free pool and the saturation of every bound (GM TypeFlag 1; MT /
+         * CEST pool 1) pool; a bound pool has no transverse generator (its
+         * transverse magnetisation is held, and no free pool takes
+         * transverse inflow from it) but takes part in the longitudinal one.
+         * MT / CEST keep their models' transverse map: a free pool's
+         * transverse magnetisation does not flow out to the bound pool
+         * (BlochKernelMT.cuh:324-333, BlochKernelCEST.cuh:364-395); only
+         * voxels whose pool 0 is active evolve */
+        if (mtc && (a->t2[PIDX(0)] == 0 || a->t1[PIDX(0)] == 0 || a->rho[PIDX(0)] == 0)) return;
         REAL rx[MRL_PORT_MAX_POOL], ry[MRL_PORT_MAX_POOL], rz[MRL_PORT_MAX_POOL];
         double At[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL] = {0}, Al[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL] = {0};
         double Ft[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL], Fl[MRL_PORT_MAX_POOL * MRL_PORT_MAX_POOL];
@@ -244,7 +271,7 @@ static void PORT_T(update)(const mrl_port_args *a, REAL *MX, REAL *MY, REAL *MZ,
         double b[MRL_PORT_MAX_POOL] = {0};
         int on[MRL_PORT_MAX_POOL], bnd[MRL_PORT_MAX_POOL];
         for (int t = 0; t < P; ++t)
-            bnd[t] = a->model == MRL_PORT_GM && (int)a->type_flag[t] == 1;
+            bnd[t] = (a->model == MRL_PORT_GM && (int)a->type_flag[t] == 1) || (mtc && t == 1);
         for (int t = 0; t < P; ++t) {
             REAL T1 = a->t1[PIDX(t)], T2 = a->t2[PIDX(t)], rho = a->rho[PIDX(t)];
             on[t] = !(T2 == 0 || T1 == 0 || rho == 0);
@@ -263,9 +290,8 @@ static void PORT_T(update)(const mrl_port_args *a, REAL *MX, REAL *MY, REAL *MZ,
             b[t] = (double)rho / ((double)S * (double)T1);
             for (int p = 0; p < P; ++p) {
                 if (p == t) continue; /* a self rate moves nothing */
-                const double kgo = a->model == MRL_PORT_ME ? a->k[(long)(t * P + p) * V + v] : a->k[(long)(p * P + t) * V + v];
-                const double kin = a->model == MRL_PORT_ME ? a->k[(long)(p * P + t) * V + v] : a->k[(long)(t * P + p) * V + v];
-                if (!bnd[t]) At[t * P + t] -= kgo;
+                const double kgo = PORT_T(rate)(a, V, v, t, p), kin = PORT_T(rate)(a, V, v, p, t);
+                if (!bnd[t] && !(mtc && bnd[p])) At[t * P + t] -= kgo;
                 Al[t * P + t] -= kgo;
                 if (!bnd[t] && !bnd[p]) At[t * P + p] += kin;
                 Al[t * P + p] += kin;
@@ -451,8 +477,8 @@ int PORT_FN(const mrl_port_args *a, long long *steps_done) {
         return -1;
     if ((a->model == MRL_PORT_MT && a->type_num != 2) || (a->model == MRL_PORT_CEST && a->type_num < 2))
         return -1;
-    if (a->exact) { /* ME, or GM with free (TypeFlag 0) and bound (1) pools */
-        if (a->model != MRL_PORT_ME && a->model != MRL_PORT_GM) return -1;
+    if (a->exact) { /* ME, MT, CEST, or GM with free (TypeFlag 0) and bound (1) pools */
+        if (a->model == MRL_PORT_NORMAL) return -1;
         for (int t = 0; a->model == MRL_PORT_GM && t < a->type_num; ++t)
             if ((int)a->type_flag[t] != 0 && (int)a->type_flag[t] != 1) return -1;
     }

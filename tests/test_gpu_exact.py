@@ -24,6 +24,12 @@ CASES = {
     "gm3_bound": lambda: phantoms.small_multipool("gm", seed=58, n=6, pools=3, spins=2, coils=2, n_tr=2, seq="sat"),
     # the MT + exchange EPI's tissue and sequence (8 ms MT pulse), small
     "mt_epi": lambda: phantoms.config5_mt_epi(seed=6, nx=6, ny=6, nz=2, spins=2, n_coils=4, n_read=8, n_pe=8),
+    # the MT and CEST models (pool 1 bound, the models' K layouts and
+    # transverse maps) under saturation pulses, up to five pools
+    "mt": lambda: phantoms.small_multipool("mt", seed=59, n=6, pools=2, spins=2, coils=2, n_tr=2, seq="sat"),
+    "cest3": lambda: phantoms.small_multipool("cest", seed=60, n=6, pools=3, spins=2, coils=2, n_tr=2, seq="sat"),
+    "cest4": lambda: phantoms.small_multipool("cest", seed=61, n=5, pools=4, spins=1, coils=2, n_tr=2, seq="sat"),
+    "cest5": lambda: phantoms.small_multipool("cest", seed=62, n=5, pools=5, spins=1, coils=2, n_tr=1, seq="sat"),
 }
 # the MT EPI's FP32 bounds (signal, final Mz): as for its accurate mode
 # against the FP64 oracle, the 8 ms MT pulse's single-precision state
@@ -73,13 +79,20 @@ def test_exact_plan_repeats_scan(built):
         plan.close()
 
 
-@pytest.mark.parametrize("model", ["mt", "cest"])
-def test_exact_refuses_mt_and_cest(built, model):
-    sc = phantoms.small_multipool(model, seed=55, n=4, pools=3 if model == "cest" else 2, spins=1, coils=1,
-                                  n_tr=1, seq="sat")
-    with pytest.raises(engine.ScanError) as e:
-        engine.scan(sc, numerics="exact")
-    assert e.value.status == -6
+def test_exact_cest_with_config3_exchange(built):
+    """Config 3's fastest exchange (k up to 5000 1/s: k dt reaches 0.05 per
+    10 us step and far more over the sequence's long gaps) with five pools:
+    the exact mode follows the exact solution; the reference's split scheme
+    departs from it."""
+    sc = phantoms.small_multipool("cest", seed=63, n=5, pools=5, spins=1, coils=1, n_tr=1, seq="sat")
+    k = np.asarray(sc.VObj["K"], np.float32)
+    sc.VObj["K"] = np.asfortranarray(np.where(k > 0, np.float32(5000.0), k).astype(np.float32))
+    ref = oracle.run_port(sc, "f64", exact=True)
+    out = engine.scan(sc, numerics="exact")
+    err = rel_l2(signal(out), signal(ref))
+    split = rel_l2(signal(oracle.run_port(sc, "f64")), signal(ref))
+    print(f"CEST k = 5000: exact GPU vs exact FP64 {err:.2e}, split scheme vs exact {split:.2e}")
+    assert err <= 1e-5 and split > 1.0
 
 
 def test_exact_normal_model_is_the_accurate_mode(built):

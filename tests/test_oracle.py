@@ -157,7 +157,7 @@ def test_port_history_matches_live_reference_cpu_engine(built):
     np.testing.assert_array_equal(out["Muts"], ref["Muts"])
 
 
-@pytest.mark.parametrize("model", ["me", "gm", "gm_bound"])
+@pytest.mark.parametrize("model", ["me", "gm", "gm_bound", "mt", "cest"])
 def test_exact_oracle_matches_bloch_mcconnell_expm(built, model):
     """The oracle's exact propagator (rotate every pool, then exp of the
     relaxation-exchange generator) equals the exponential of the whole
@@ -166,21 +166,32 @@ def test_exact_oracle_matches_bloch_mcconnell_expm(built, model):
     one voxel, three pools with stiff exchange, free precession at dB0, the
     state read after the last of several uneven steps.  ``gm_bound``: pool 2
     is a bound pool (no transverse generator: its transverse state held, no
-    transverse inflow from it; in the longitudinal one like the others)."""
+    transverse inflow from it; in the longitudinal one like the others).
+    ``mt`` / ``cest``: pool 1 is the bound MT pool, rates only between pool 0
+    and each other pool (the models' K layouts), and a free pool's
+    transverse state does not flow out to the bound pool (the models'
+    transverse map)."""
     bound = model == "gm_bound"
+    mtc = model in ("mt", "cest")
     model = "gm" if bound else model
     scipy_linalg = pytest.importorskip("scipy.linalg")
     from mrilab_gb300 import seq as S
 
-    P = 3
-    rho = np.array([[[[0.7, 0.2, 0.1]]]], np.float32)
-    t1 = np.array([[[[1.1, 0.45, 0.8]]]], np.float32)
-    t2 = np.array([[[[0.07, 0.015, 0.03]]]], np.float32)
+    P = 2 if model == "mt" else 3
+    rho = np.array([[[[0.7, 0.2, 0.1][:P]]]], np.float32)
+    t1 = np.array([[[[1.1, 0.45, 0.8][:P]]]], np.float32)
+    t2 = np.array([[[[0.07, 0.015, 0.03][:P]]]], np.float32)
     rates = np.zeros((1, 1, 1, P, P), np.float32)
-    rates[..., 1, 0], rates[..., 2, 0], rates[..., 1, 2] = 300.0, 120.0, 40.0
+    rates[..., 1, 0] = 300.0
     rates[..., 0, 1] = rates[..., 1, 0] * rho[..., 1] / rho[..., 0]
-    rates[..., 0, 2] = rates[..., 2, 0] * rho[..., 2] / rho[..., 0]
-    rates[..., 2, 1] = rates[..., 1, 2] * rho[..., 1] / rho[..., 2]
+    if P == 3:
+        rates[..., 2, 0] = 120.0
+        rates[..., 0, 2] = rates[..., 2, 0] * rho[..., 2] / rho[..., 0]
+        if not mtc:
+            rates[..., 1, 2] = 40.0
+            rates[..., 2, 1] = rates[..., 1, 2] * rho[..., 1] / rho[..., 2]
+    if mtc:
+        t2[..., 1] = 12e-6
     tr = S.TR(30_000_000)
     times = [0, 1_500_000, 1_700_000, 6_000_000, 6_010_000, 18_000_000, 30_000_000]
     tr.adc(times[1:-1])
@@ -190,7 +201,9 @@ def test_exact_oracle_matches_bloch_mcconnell_expm(built, model):
         t2[..., 2] = 12e-6
     sc = phantoms.assemble(rho, t1, t2, db0_hz=np.full((1, 1, 1), 37.0), model=model, rates=rates,
                            type_flag=tf, seqlines=lines)
-    m0 = np.array([[0.3, -0.2, 0.4], [0.05, 0.1, 0.02], [-0.03, 0.04, 0.05]])  # [pool][x, y, z]
+    m0 = np.array([[0.3, -0.2, 0.4], [0.05, 0.1, 0.02], [-0.03, 0.04, 0.05]])[:P]  # [pool][x, y, z]
+    if mtc:
+        m0[1, :2] = 0.0  # the MT pool carries no transverse magnetisation
     for k, comp in (("Mx", 0), ("My", 1), ("Mz", 2)):
         sc.VObj[k] = np.asfortranarray(m0[:, comp].reshape(1, 1, 1, 1, P).astype(np.float32))
     out = oracle.run_port(sc, "f64", exact=True)
@@ -198,12 +211,12 @@ def test_exact_oracle_matches_bloch_mcconnell_expm(built, model):
     w = float(sc.VObj["Gyro"]) * float(sc.VMag["dB0"].ravel()[0])
     n = 3 * P + 1
     G = np.zeros((n, n))
-    bnd = [bound and t == 2 for t in range(P)]
+    bnd = [(bound and t == 2) or (mtc and t == 1) for t in range(P)]
     for t in range(P):
-        kout = sum(rates[0, 0, 0, t, p] for p in range(P) if p != t)
         for c, r in ((0, 1 / t2[0, 0, 0, t]), (1, 1 / t2[0, 0, 0, t]), (2, 1 / t1[0, 0, 0, t])):
             if c < 2 and bnd[t]:
                 continue  # a bound pool's transverse state is held
+            kout = sum(rates[0, 0, 0, t, p] for p in range(P) if p != t and not (mtc and c < 2 and bnd[p]))
             G[c * P + t, c * P + t] = -r - kout
             for p in range(P):
                 if p != t and not (c < 2 and bnd[p]):
