@@ -782,7 +782,10 @@ def main():
     if world == 1 and not args.no_extras and args.workload == "config2":
         plan.close()
         del plan
-        line["parity"] = parity_subset(local)
+        try:
+            line["parity"] = parity_subset(local)
+        except Exception as e:  # reported, not hidden
+            line["parity"] = {"error": repr(e)}
         line["reference_order"] = reference_order_rate(local)
         line.update(extras(args))
     if not args.no_cpu:

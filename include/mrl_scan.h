@@ -230,9 +230,10 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n);
  * reference has no gradients; this runs the discrete map the integrator
  * applies (rotation, relaxation, split exchange) backwards, with the state
  * checkpointed every few steps and recomputed in between.
- * Scope: the normal, ME and GM models (GM pools free or bound: a bound
- * pool's saturation is differentiated through its lineshape, so g_t2 of a
- * bound pool is dL/dT2b and g_db0 includes the lineshape's shift), one Tx
+ * Scope: the normal, ME, GM, MT and CEST models (GM pools free or bound,
+ * MT / CEST pool 1 bound: a bound pool's saturation is differentiated
+ * through its lineshape, so g_t2 of a bound pool is dL/dT2b and g_db0
+ * includes the lineshape's shift; g_k in each model's own channels), one Tx
  * coil, RunMode 0, no Ext events, TypeNum <= 3, up to 32 Rx coils.
  * Host arrays (NULL: not wanted), V voxels, layouts as in mrl_scan_args:
  *   grad_sx, grad_sy  [P][Rx][A]   inputs

@@ -241,27 +241,30 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
         for (int t = 0; t < P; ++t) {
             const float y1t = on[t] ? one_minus_exp(dt / t1[t]) : 0.f;
             const float y2t = on[t] ? one_minus_exp(dt / t2[t]) : 0.f;
-            float ksum = 0.f;
+            float ksum = 0.f, ksum_t = 0.f;  // outflow: all partners, transverse partners
 #pragma unroll
             for (int p = 0; p < P; ++p) {
                 fin[t][p] = 0.f;
                 if (GM && p == t) continue;
                 const float kgo = kc[ch(t, p)], kin = kc[ch(p, t)];
                 ksum += kgo;
+                if (!(L.mtc && bnd[p])) ksum_t += kgo;
                 if (on[t] && kin != 0.f) fin[t][p] = one_minus_exp(dt * kin);
             }
             const float yot = on[t] ? one_minus_exp(dt * ksum) : 0.f;
+            // MT / CEST: the transverse outflow leaves out the bound pool
+            const float yot_t = L.mtc ? (on[t] ? one_minus_exp(dt * ksum_t) : 0.f) : yot;
             y1[t] = y1t;
             d1[t] = (1.f - yot) * (1.f - y1t);
-            d2[t] = (1.f - yot) * (1.f - y2t);
+            d2[t] = (1.f - yot_t) * (1.f - y2t);
             // dy1/dT1 = -(1 - y1) dt / T1^2, dyo/dk = (1 - yo) dt
             const float fT1 = on[t] ? -(1.f - y1t) * dt / (t1[t] * t1[t]) : 0.f;
             const float fT2 = on[t] ? -(1.f - y2t) * dt / (t2[t] * t2[t]) : 0.f;
             const float fyo = (1.f - yot) * dt;
             hT1[t] = -(1.f - yot) * fT1;
             hR[t] = rhoS[t] * fT1;
-            hT2[t] = -(1.f - yot) * fT2;
-            e2[t] = -(1.f - y2t) * fyo;
+            hT2[t] = -(1.f - yot_t) * fT2;
+            e2[t] = -(1.f - y2t) * (1.f - yot_t) * dt;
             e1[t] = -(1.f - y1t) * fyo;
         }
         dtc = dt;
@@ -523,11 +526,11 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 wT2[t] = fmaf(gd2, hT2[t], wT2[t]);
                 wrho[t] = fmaf(l.z, y1[t], wrho[t]);
                 // exchange rates: the outflow of t (yo_t) and the inflow to t (f_tp)
-                const float go_g = fmaf(gd2, e2[t], gd1 * e1[t]);
+                const float go_l = gd1 * e1[t], go_t = gd2 * e2[t];
 #pragma unroll
                 for (int p = 0; p < P; ++p) {
                     if (GM && p == t) continue;
-                    wk[ch(t, p)] += go_g;
+                    wk[ch(t, p)] += (L.mtc && bnd[p]) ? go_l : go_l + go_t;
                     // df_tp/dk_pt = (1 - f_tp) dt
                     wk[ch(p, t)] = fmaf(dot3(l, mk[p]), (1.f - fin[t][p]) * dtc, wk[ch(p, t)]);
                     // inflow to t from p's magnetisation before the step
@@ -578,7 +581,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                         const float2 rc = rxs[c * kAdjBlock + tid];
 #pragma unroll
                         for (int t = 0; t < P; ++t) {
-                            if (bnd[t]) continue;
+                            if (bnd[t] || (L.mtc && t != 0)) continue;  // MT / CEST receive pool 0
                             const float2 g = ga[t * L.rx + c];
                             if (c & 1) {
                                 src[t].z = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src[t].z));
@@ -687,6 +690,30 @@ cudaError_t go(const AdjLaunch &L, cudaStream_t st) {
 }
 
 }  // namespace
+
+namespace {
+// MT (layout 2: channel 1 = K12 (0 -> 1), 2 = K21 (1 -> 0)) and CEST
+// (layout 3: 0 = 0 -> MT, P-1 = MT -> 0, t-1 = 0 -> t, t+P-2 = t -> 0)
+// exchange channels into the general model's layout (p*P+t = rate t -> p)
+__global__ void remap_k_mtc(int P, int layout, const float *__restrict__ src, float *dst, int n_act) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_act) return;
+    for (int t = 0; t < P; ++t)
+        for (int p = 0; p < P; ++p) {
+            int c = -1;
+            if (layout == 2) c = (t == 0 && p == 1) ? 1 : ((t == 1 && p == 0) ? 2 : -1);
+            else if (t == 0 && p != 0) c = p == 1 ? 0 : p - 1;
+            else if (p == 0 && t != 0) c = t == 1 ? P - 1 : t + P - 2;
+            dst[(long long)(p * P + t) * n_act + v] = c < 0 ? 0.f : src[(long long)c * n_act + v];
+        }
+}
+}  // namespace
+
+cudaError_t launch_remap_k_mtc(int P, int layout, const float *k_src, float *k_gm, int n_act, cudaStream_t st) {
+    if (n_act <= 0) return cudaSuccess;
+    remap_k_mtc<<<(n_act + 127) / 128, 128, 0, st>>>(P, layout, k_src, k_gm, n_act);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_adjoint(int P, const AdjLaunch &L, cudaStream_t st) {
     const bool gm = L.exch_gm != 0, bound = gm && L.bound != 0;

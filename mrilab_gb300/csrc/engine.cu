@@ -1982,7 +1982,7 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n) {
 struct mrl_adjoint_plan {
     mrl_plan *fwd = nullptr;
     mrl::DevBuf<float4> d_rec;
-    mrl::DevBuf<float> d_ck, d_ck2, d_g;
+    mrl::DevBuf<float> d_ck, d_ck2, d_g, d_kgm;  // d_kgm: MT / CEST channels in the general layout
     mrl::DevBuf<float2> d_gs;
     mrl::DevBuf<double> d_rf;
     mrl::AdjLaunch L{};
@@ -2012,10 +2012,14 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     int rc = plan_create_impl(&a, &p->fwd, -1, &ch);
     if (rc) return rc;
     Scanner &sc = p->fwd->sc;
-    if (!(sc.mi.km == KM_NORMAL || sc.mi.km == KM_EXCH))
-        return set_err("the adjoint covers the normal, ME and GM models (not MT or CEST)"), MRL_ERR_UNSUPPORTED;
+    // MT and CEST run as the general model with pool 1 bound (their K
+    // channels remapped), their transverse map and pool-0 receive
+    const bool mtc = sc.mi.km == KM_MT || sc.mi.km == KM_CEST;
+    if (!(sc.mi.km == KM_NORMAL || sc.mi.km == KM_EXCH || mtc))
+        return set_err("unknown model for the adjoint"), MRL_ERR_UNSUPPORTED;
     if (sc.TX != 1) return set_err("the adjoint supports one Tx coil"), MRL_ERR_UNSUPPORTED;
     if (sc.P > 3) return set_err("the adjoint supports TypeNum <= 3"), MRL_ERR_UNSUPPORTED;
+    if (mtc && sc.P < 2) return set_err("the MT / CEST adjoint needs the bound pool"), MRL_ERR_UNSUPPORTED;
     if (sc.RX > 32) return set_err("the adjoint supports up to 32 Rx coils"), MRL_ERR_UNSUPPORTED;
     // GM pools: free (TypeFlag 0) or bound (1); a bound pool needs a free one
     unsigned bound = 0;
@@ -2027,6 +2031,7 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
         }
         if (bound == (1u << sc.P) - 1) return set_err("the adjoint needs a free pool"), MRL_ERR_UNSUPPORTED;
     }
+    if (mtc) bound = 1u << 1;
     const int P = sc.P, S = sc.S, RX = sc.RX, A = sc.A;
     p->P = P, p->S = S, p->RX = RX, p->A = A, p->V = sc.V;
     p->rf_ref = args->var.rf_ref ? *args->var.rf_ref : 0.0;
@@ -2090,6 +2095,11 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     if (e == cudaSuccess) e = p->d_g.ensure((size_t)nf * std::max(1LL, n_iso));
     if (e == cudaSuccess) e = p->d_gs.ensure((size_t)P * RX * std::max(A, 1));
     if (e == cudaSuccess) e = p->d_rf.ensure((size_t)2 * std::max(1, p->n_rf));
+    if (e == cudaSuccess && mtc) {
+        e = p->d_kgm.ensure((size_t)P * P * std::max(1, sc.n_act));
+        if (e == cudaSuccess)
+            e = launch_remap_k_mtc(P, sc.mi.km == KM_MT ? 2 : 3, sc.d_f.p + sc.o_k, p->d_kgm.p, sc.n_act, sc.st);
+    }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_rec.p, rec.data(), rec.size() * sizeof(float4), cudaMemcpyHostToDevice, sc.st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(sc.st);
@@ -2100,8 +2110,9 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     L.S = S;
     L.rx = RX;
     L.A = std::max(A, 1);
-    L.exch_gm = sc.mi.gm ? 1 : 0;
+    L.exch_gm = (sc.mi.gm || mtc) ? 1 : 0;
     L.bound = bound;
+    L.mtc = mtc ? 1 : 0;
     L.n_iso = n_iso;
     L.gyro = (float)args->obj.gyro;
     L.gxg = sc.d_f.p + sc.o_gx;
@@ -2111,7 +2122,7 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     L.rho = sc.d_f.p + sc.o_rho;
     L.t1 = sc.d_f.p + sc.o_t1;
     L.t2 = sc.d_f.p + sc.o_t2;
-    L.kch = sc.mi.nk > 0 ? sc.d_f.p + sc.o_k : nullptr;
+    L.kch = mtc ? p->d_kgm.p : (sc.mi.nk > 0 ? sc.d_f.p + sc.o_k : nullptr);
     L.dwrnd = sc.d_f.p + sc.o_dwr;
     L.rxc = args->coil.rx_default == 0 ? sc.d_rx.p : nullptr;
     L.txc = sc.d_f2.p + sc.o_txc;
@@ -2210,8 +2221,23 @@ int mrl_adjoint_plan_gradients(mrl_adjoint_plan *p, mrl_adjoint_args *adj) {
                 if (adj->g_mz0) adj->g_mz0[i] = field(F_M0 + 2 * P + t, s2, j);
             }
             if (adj->g_db0) adj->g_db0[v] += field(F_DB0, s2, j);
-            if (adj->g_k && sc.mi.nk > 0)
-                for (int k = 0; k < P * P; ++k) adj->g_k[k * V + v] += field(F_K + k, s2, j);
+            if (adj->g_k && sc.mi.nk > 0) {
+                if (sc.mi.km == KM_MT) {  // K12 = rate 0 -> 1 (GM channel 1*P+0), K21 = rate 1 -> 0 (0*P+1)
+                    adj->g_k[1 * V + v] += field(F_K + 1 * P + 0, s2, j);
+                    adj->g_k[2 * V + v] += field(F_K + 0 * P + 1, s2, j);
+                } else if (sc.mi.km == KM_CEST) {  // channel c <-> rate a -> b, GM channel b*P+a
+                    for (int c = 0; c < 2 * (P - 1); ++c) {
+                        int ra, rb;
+                        if (c == 0) ra = 0, rb = 1;
+                        else if (c == P - 1) ra = 1, rb = 0;
+                        else if (c < P - 1) ra = 0, rb = c + 1;
+                        else ra = c - P + 2, rb = 0;
+                        adj->g_k[(long long)c * V + v] += field(F_K + rb * P + ra, s2, j);
+                    }
+                } else {
+                    for (int k = 0; k < P * P; ++k) adj->g_k[k * V + v] += field(F_K + k, s2, j);
+                }
+            }
         }
     }
     if (n_rf <= adj->rf_capacity) {

@@ -101,6 +101,10 @@ constexpr int kAdjBlock = 128;  // threads (isochromats) per block
 struct AdjLaunch {
     int n_act, S, rx, A, exch_gm;
     unsigned bound;  // GM bound pools (TypeFlag 1), one bit per pool
+    // MT / CEST (pool 1 bound, kch remapped to the GM layout): a free pool's
+    // transverse magnetisation does not flow out to the bound pool, and only
+    // pool 0 is received
+    int mtc;
     long long n_iso;  // n_act * S; isochromat i = spin (i / n_act) of voxel (i % n_act)
     float gyro;
     const float *gxg, *gyg, *gzg, *db0;  // [n_act]
@@ -127,6 +131,9 @@ inline size_t adjoint_smem_bytes(int P, int rx) {
 }
 inline int adjoint_fields(int P) { return 3 * P + 1 + P * P + 3 * P; }
 cudaError_t launch_adjoint(int P, const AdjLaunch &L, cudaStream_t st);
+// MT / CEST exchange channels [nk][n_act] (model layout, see exch_rate) into
+// the general model's layout [P*P][n_act] (channel p*P+t = rate t -> p)
+cudaError_t launch_remap_k_mtc(int P, int layout, const float *k_src, float *k_gm, int n_act, cudaStream_t st);
 
 // resident blocks per SM of an instantiation at `smem` bytes (0 if none)
 int occupancy_scan_fast_normal(int P, int NS, bool all_free, size_t smem);

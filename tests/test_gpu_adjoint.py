@@ -164,6 +164,20 @@ def test_adjoint_gm_bound_pool(built):
     _run(phantoms.small_multipool("gm", seed=38, n=5, pools=3, spins=1, coils=2, n_tr=3, seq="sat"))
 
 
+def test_adjoint_mt_model(built):
+    """The MT model (free pool + bound pool, K12 / K21 in channels 1 and 2)
+    under off-resonance saturation pulses: relaxation, exchange, the bound
+    pool's saturation through its lineshape, and the rf waveform, against
+    FP64 central differences."""
+    _run(phantoms.small_multipool("mt", seed=47, n=5, pools=2, spins=2, coils=2, n_tr=2, seq="sat"))
+
+
+def test_adjoint_cest_model(built):
+    """The CEST model with water, the MT pool and one CEST pool (its own
+    chemical shift, exchanging with water only)."""
+    _run(phantoms.small_multipool("cest", seed=48, n=5, pools=3, spins=1, coils=2, n_tr=2, seq="sat"))
+
+
 def test_adjoint_mt_epi_many_coils(built):
     """The MT + exchange EPI (free, myelin and bound pools, 8 ms MT pulse)
     on a small phantom with 12 receive coils."""
@@ -200,7 +214,7 @@ def test_adjoint_two_level_checkpoints(built, monkeypatch):
             assert err <= 1e-4
 
 
-@pytest.mark.parametrize("case", ["gre", "me3", "gm_bound", "bssfp"])
+@pytest.mark.parametrize("case", ["gre", "me3", "gm_bound", "bssfp", "mt", "cest3"])
 def test_adjoint_vs_fp64_adjoint(built, case):
     """The FP32 adjoint kernel against the FP64 reference gradient
     (oracle.adjoint64: the oracle's map in float64, differentiated by
@@ -213,7 +227,13 @@ def test_adjoint_vs_fp64_adjoint(built, case):
           "me3": lambda: phantoms.small_multipool("me", seed=42, n=4, pools=3, spins=2, coils=3, n_tr=2),
           "gm_bound": lambda: phantoms.small_multipool("gm", seed=43, n=4, pools=3, spins=1, coils=2, n_tr=2,
                                                        seq="sat"),
-          "bssfp": lambda: phantoms.config4_adjoint(seed=44, nx=4, ny=4, nz=2, n_tr=2)}[case]()
+          "bssfp": lambda: phantoms.config4_adjoint(seed=44, nx=4, ny=4, nz=2, n_tr=2),
+          # MT and CEST: pool 1 bound (saturated through its lineshape), the
+          # models' K channels, no transverse outflow to the bound pool, pool
+          # 0 received
+          "mt": lambda: phantoms.small_multipool("mt", seed=45, n=4, pools=2, spins=2, coils=2, n_tr=2, seq="sat"),
+          "cest3": lambda: phantoms.small_multipool("cest", seed=46, n=4, pools=3, spins=1, coils=2, n_tr=2,
+                                                    seq="sat")}[case]()
     sc = _phase_modulated(sc, 12)
     tx, ty = _target(sc)
     _, gx, gy = _loss(sc, (tx, ty))
@@ -237,8 +257,8 @@ def test_adjoint_vs_fp64_adjoint(built, case):
     assert err <= TOL
 
 
-def test_adjoint_rejects_mt_model(built):
-    sc = phantoms.small_multipool("mt", seed=33, n=4, pools=2, spins=1, coils=1, n_tr=1, seq="sat")
+def test_adjoint_rejects_four_cest_pools(built):
+    sc = phantoms.small_multipool("cest", seed=33, n=4, pools=4, spins=1, coils=1, n_tr=1, seq="sat")
     with pytest.raises(engine.ScanError) as e:
         engine.adjoint(sc, np.zeros(1), np.zeros(1))
     assert e.value.status == -6
