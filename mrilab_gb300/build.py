@@ -1,9 +1,9 @@
 """Build the native parts of mrilab_gb300 in-tree.
 
 * ``libmrl_scan.so``: the C-ABI scan engine (``include/mrl_scan.h``), SAR
-  engine (``include/mrl_sar.h``) and reconstruction
-  (``include/mrl_recon.h``), CUDA for sm_103a only; translation units
-  compile in parallel.
+  engine (``include/mrl_sar.h``), reconstruction (``include/mrl_recon.h``)
+  and sequence compiler (``include/mrl_seq.h``), CUDA for sm_103a only;
+  translation units compile in parallel.
 * ``mex/libfakemex.so``: the MATLAB stand-in used to drive the mex layer
   without MATLAB.
 * ``mex/Do*ScanAtGPU.so``, ``mex/DoCalSARAtGPU.so``, ``mex/DoGridding.so``,
@@ -59,6 +59,7 @@ UNITS = {
     "sar.cu": [],
     "recon.cu": [],
     "decode.cpp": None,  # host C++
+    "seqc.cpp": None,  # host C++
 }
 
 
@@ -82,7 +83,7 @@ def _stale(target: str, deps) -> bool:
 
 def _headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    return hs + [os.path.join(ROOT, "include", f) for f in ("mrl_scan.h", "mrl_sar.h", "mrl_recon.h")]
+    return hs + [os.path.join(ROOT, "include", f) for f in ("mrl_scan.h", "mrl_sar.h", "mrl_recon.h", "mrl_seq.h")]
 
 
 def _run(cmd):

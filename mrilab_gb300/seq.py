@@ -1,19 +1,11 @@
 """Build MRiLab ``VSeq`` sequence lines for synthetic scans.
 
 The scan engine consumes the pulse sequence as flat "lines"
-(``VSeq.rfAmpLine ... flagsLine, utsLine, tsLine``).  Each TR's events are
-merged as MRiLab's compiled PSD functions do
-(``PSD/3D/GradientEcho/PSD_GRE3D/PSD_GRE3D.m:317-359``):
-
-* ``ts`` = the TR's start/end pair, then the rf, Gz, Gy, Gx, ADC and Ext
-  sample times, stably sorted, with a 6-row ``flags`` column per entry
-  marking which channel the entry belongs to;
-* ``uts`` = the unique times;
-* each channel's values are sorted by their own times and the first and
-  last value of every channel (except ``rfCoil``) are forced to zero;
-
-and the TRs are concatenated (``Src/Main/DoPulseGen.m:43-111``), so time
-restarts at 0 every TR and ``utsLine`` has a negative step at each TR
+(``VSeq.rfAmpLine ... flagsLine, utsLine, tsLine``).  ``TR`` collects one
+TR's sequence-element samples; ``concat`` hands them to the native sequence
+compiler (``mrl_seq_compile``), which merges each TR as MRiLab's compiled
+PSD functions do and concatenates the TRs (``Src/Main/DoPulseGen.m``), so
+time restarts at 0 every TR and ``utsLine`` has a negative step at each TR
 boundary.
 
 Shapes are restated from MRiLab's sequence elements: Hamming-windowed sinc
@@ -84,25 +76,15 @@ class TR:
         self.ext_t.append(int(t_ns))
         self.ext_v.append(float(value))
 
-    # -- PSD-style merge ----------------------------------------------------
-    def lines(self) -> Dict[str, np.ndarray]:
-        """One TR's lines exactly as a compiled MRiLab PSD returns them."""
+    # -- channels for the compiler -------------------------------------------
+    def channels(self):
+        """The TR's channels as the sequence compiler takes them, times in
+        seconds: every channel gets at least one sample (a zero at the TR's
+        start and end), as MRiLab's PSDs require (DoWriteXML2m.m:263-286)."""
         t0, t1 = 0, int(self.duration_ns)
-        chans = [
-            (self.rf_t, 0),
-            (self.g_t["z"], 1),
-            (self.g_t["y"], 2),
-            (self.g_t["x"], 3),
-            (self.adc_t, 4),
-            (self.ext_t, 5),
-        ]
-        # every channel needs at least one entry (PSD_GRE3D.m:300-317)
-        if not self.g_t["z"]:
-            self.grad("z", [t0, t1], [0.0, 0.0])
-        if not self.g_t["y"]:
-            self.grad("y", [t0, t1], [0.0, 0.0])
-        if not self.g_t["x"]:
-            self.grad("x", [t0, t1], [0.0, 0.0])
+        for axis in ("z", "y", "x"):
+            if not self.g_t[axis]:
+                self.grad(axis, [t0, t1], [0.0, 0.0])
         if not self.adc_t:
             self.adc_t += [t0, t1]
             self.adc_v += [0.0, 0.0]
@@ -111,63 +93,28 @@ class TR:
             self.ext_v += [0.0, 0.0]
         if not self.rf_t:
             self.rf([t0, t1], 0.0)
-        chans = [
-            (self.rf_t, 0),
-            (self.g_t["z"], 1),
-            (self.g_t["y"], 2),
-            (self.g_t["x"], 3),
-            (self.adc_t, 4),
-            (self.ext_t, 5),
-        ]
-        ts = [t0, t1]
-        flags = [np.zeros(6), np.zeros(6)]
-        for times, row in chans:
-            for t in times:
-                ts.append(int(t))
-                f = np.zeros(6)
-                f[row] = 1
-                flags.append(f)
-        ts = np.asarray(ts, dtype=np.int64) - t0
-        order = np.argsort(ts, kind="stable")
-        ts = ts[order]
-        flags = np.stack(flags, axis=1)[:, order]
-        uts = np.unique(ts)
-
-        def sort_by(times, *vals):
-            o = np.argsort(np.asarray(times, dtype=np.int64), kind="stable")
-            return [np.asarray(v, dtype=float)[o] for v in vals]
-
-        rf_amp, rf_ph, rf_fr, rf_co = sort_by(self.rf_t, self.rf_amp, self.rf_phase, self.rf_freq, self.rf_coil)
-        gz, = sort_by(self.g_t["z"], self.g_a["z"])
-        gy, = sort_by(self.g_t["y"], self.g_a["y"])
-        gx, = sort_by(self.g_t["x"], self.g_a["x"])
-        adc, = sort_by(self.adc_t, self.adc_v)
-        ext, = sort_by(self.ext_t, self.ext_v)
-        for a in (rf_amp, rf_ph, rf_fr, gz, gy, gx, adc, ext):
-            a[0] = 0.0
-            a[-1] = 0.0
-        return dict(
-            rfAmp=rf_amp, rfPhase=rf_ph, rfFreq=rf_fr, rfCoil=rf_co,
-            GzAmp=gz, GyAmp=gy, GxAmp=gx, ADC=adc, Ext=ext,
-            uts=uts.astype(np.float64) * NS, ts=ts.astype(np.float64) * NS, flags=flags,
-        )
+        sec = lambda t: np.asarray(t, dtype=np.int64).astype(np.float64) * NS
+        f = lambda v: np.asarray(v, dtype=np.float64)
+        return dict(span=(t0 * NS, t1 * NS), rf=(sec(self.rf_t), f(self.rf_amp), f(self.rf_phase), f(self.rf_freq),
+                                                 f(self.rf_coil)),
+                    gz=(sec(self.g_t["z"]), f(self.g_a["z"])), gy=(sec(self.g_t["y"]), f(self.g_a["y"])),
+                    gx=(sec(self.g_t["x"]), f(self.g_a["x"])), adc=(sec(self.adc_t), f(self.adc_v)),
+                    ext=(sec(self.ext_t), f(self.ext_v)))
 
 
-def concat(trs: List[TR], multi_transmit: bool = False) -> Dict[str, np.ndarray]:
-    """Concatenate TRs into VSeq lines (DoPulseGen.m:43-111,118-123)."""
-    per = [tr.lines() for tr in trs]
-    out = {}
-    for key, name in [
-        ("rfAmp", "rfAmpLine"), ("rfPhase", "rfPhaseLine"), ("rfFreq", "rfFreqLine"),
-        ("rfCoil", "rfCoilLine"), ("GzAmp", "GzAmpLine"), ("GyAmp", "GyAmpLine"),
-        ("GxAmp", "GxAmpLine"), ("ADC", "ADCLine"), ("Ext", "ExtLine"),
-        ("uts", "utsLine"), ("ts", "tsLine"),
-    ]:
-        out[name] = np.concatenate([p[key] for p in per]).astype(np.float64)
-    out["flagsLine"] = np.concatenate([p["flags"] for p in per], axis=1).astype(np.float64)
-    if not multi_transmit:
-        out["rfCoilLine"] = np.ones_like(out["rfCoilLine"])
-    return out
+def concat(trs: List[TR], multi_transmit: bool = False, dummy_trs: int = 0, tx_coil_num: int = 0,
+           master_tx_coil: int = 1, max_grad: float = 0.0, max_slew: float = 0.0,
+           min_upd_rate: float = 0.0) -> Dict[str, np.ndarray]:
+    """The VSeq lines of the TRs, from the native sequence compiler
+    (mrl_seq_compile, ``include/mrl_seq.h``): each TR merged as MRiLab's
+    compiled PSDs do, the TRs concatenated with ``dummy_trs`` dummies
+    (gradients and ADC zeroed), rfCoil forced to 1 without multi-transmit,
+    and the multi-transmit, gradient and update-rate checks (0: skipped)."""
+    from . import seqc
+
+    return seqc.compile_lines([tr.channels() for tr in trs], multi_transmit=multi_transmit, dummy_trs=dummy_trs,
+                              tx_coil_num=tx_coil_num, master_tx_coil=master_tx_coil, max_grad=max_grad,
+                              max_slew=max_slew, min_upd_rate=min_upd_rate)
 
 
 # ---------------------------------------------------------------------------

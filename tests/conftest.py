@@ -12,9 +12,11 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
-@pytest.fixture(scope="session")
+@pytest.fixture(scope="session", autouse=True)
 def built():
-    """Build the engine and the CPU oracle in-tree (no-op when up to date)."""
+    """Build the engine and the CPU oracle in-tree (no-op when up to date);
+    every session builds first: the phantoms' sequences come from the native
+    sequence compiler in libmrl_scan.so."""
     import oracle
     from mrilab_gb300 import build
 
