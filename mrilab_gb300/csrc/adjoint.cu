@@ -316,7 +316,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             if (bnd[t]) a = make_float3(m[t].x, m[t].y, a.z);  // transverse held
 #pragma unroll
             for (int p = 0; p < P; ++p) {
-                if (!bnd[t]) {
+                // (MT / CEST: no transverse inflow from the bound pool)
+                if (!bnd[t] && !(L.mtc && bnd[p])) {
                     a.x = fmaf(fin[t][p], m[p].x, a.x);
                     a.y = fmaf(fin[t][p], m[p].y, a.y);
                 }
@@ -531,11 +532,16 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 for (int p = 0; p < P; ++p) {
                     if (GM && p == t) continue;
                     wk[ch(t, p)] += (L.mtc && bnd[p]) ? go_l : go_l + go_t;
+                    // inflow to t from p's magnetisation before the step (MT /
+                    // CEST: the bound pool's longitudinal part only)
+                    const bool xy = !(L.mtc && bnd[p]);
                     // df_tp/dk_pt = (1 - f_tp) dt
-                    wk[ch(p, t)] = fmaf(dot3(l, mk[p]), (1.f - fin[t][p]) * dtc, wk[ch(p, t)]);
-                    // inflow to t from p's magnetisation before the step
-                    nl[p].x = fmaf(fin[t][p], l.x, nl[p].x);
-                    nl[p].y = fmaf(fin[t][p], l.y, nl[p].y);
+                    const float lm = xy ? dot3(l, mk[p]) : l.z * mk[p].z;
+                    wk[ch(p, t)] = fmaf(lm, (1.f - fin[t][p]) * dtc, wk[ch(p, t)]);
+                    if (xy) {
+                        nl[p].x = fmaf(fin[t][p], l.x, nl[p].x);
+                        nl[p].y = fmaf(fin[t][p], l.y, nl[p].y);
+                    }
                     nl[p].z = fmaf(fin[t][p], l.z, nl[p].z);
                 }
                 // adjoint with respect to the rotated magnetisation
