@@ -166,7 +166,7 @@ def main(only=()):
         np.savez_compressed(
             os.path.join(HERE, name + ".npz"),
             builder=np.array("config2_subset"), kwargs=np.array(repr(kw)), sample_index=keep,
-            ref_S=runs["ref"][..., keep], f64_S=runs["f64"][..., keep], f32_S=runs["f32"][..., keep],
+            ref_S=runs["ref"][..., keep].astype(np.complex64), f64_S=runs["f64"][..., keep].astype(np.complex64),
             full_ref_vs_f64=np.float64(rl(runs["ref"], runs["f64"])),
             full_f32_vs_f64=np.float64(rl(runs["f32"], runs["f64"])),
         )
