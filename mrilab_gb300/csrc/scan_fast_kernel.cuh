@@ -158,6 +158,20 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 
+// a - b on a spin pair (sub.rn.f32x2, sm_100 and later): the difference of two
+// products without a separate negation
+__device__ __forceinline__ float2 fsub2_rn(float2 a, float2 b) {
+    float2 r;
+    asm("{.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
 __device__ __forceinline__ float2 cmul_conj(float2 a, float2 b) {  // a * conj(b)
     return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
 }
@@ -862,6 +876,10 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 for (int t = 0; t < P; ++t)
 #pragma unroll
                     for (int p = 0; p < P; ++p) {
+                        if (kPack && p == t && !selfx) {  // fin[t][t] = 0: no self-exchange
+                            fr[t][p] = make_float2(0.f, 0.f);
+                            continue;
+                        }
                         // (EXACT: the partner after its rotation, in its frame after the step)
                         const float2 r = cmul_conj(EXACT ? Pc[p] : Pprev[p], Pc[t]);
                         const float f = (FREE || ((tvo >> t & 1u) && L.kind[p] == 0)) ? fin[t][p] : 0.f;
@@ -965,17 +983,20 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                                     iy = __ffma2_rn(f1, PAIR(Ys, qq, p), iy);
                                     iy = __ffma2_rn(f2, PAIR(Xs, qq, p), iy);
                                 }
-                                nx[t] = __fadd2_rn(px, __fadd2_rn(ax, make_float2(-bx.x, -bx.y)));
+                                nx[t] = __fadd2_rn(px, fsub2_rn(ax, bx));
                                 ny[t] = __fadd2_rn(py, iy);
-                                float2 iz = __fmul2_rn(make_float2(fin[t][0], fin[t][0]), PAIR(Zs, qq, 0));
-#pragma unroll
-                                for (int p = 1; p < P; ++p)
-                                    iz = __ffma2_rn(make_float2(fin[t][p], fin[t][p]), PAIR(Zs, qq, p), iz);
                                 const float2 z1 =
                                     __ffma2_rn(make_float2(-y1[t], -y1[t]), PAIR(Zs, qq, t), PAIR(Zs, qq, t));
                                 const float2 z2 = __ffma2_rn(make_float2(-yo[t], -yo[t]), z1, z1);
+                                // inflow and recovery: rho_t y1 / S + sum_p fin[t][p] z_p
                                 const float c = rhoS[t] * y1[t];
-                                nz[t] = __fadd2_rn(z2, __fadd2_rn(iz, make_float2(c, c)));
+                                float2 iz = make_float2(c, c);
+#pragma unroll
+                                for (int p = 0; p < P; ++p) {
+                                    if (p == t && !kSelf) continue;
+                                    iz = __ffma2_rn(make_float2(fin[t][p], fin[t][p]), PAIR(Zs, qq, p), iz);
+                                }
+                                nz[t] = __fadd2_rn(z2, iz);
                             }
 #pragma unroll
                             for (int t = 0; t < P; ++t) {
@@ -1060,15 +1081,17 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                                 const float2 ny2 = make_float2(-y2[t], -y2[t]), nyo = make_float2(-yo[t], -yo[t]);
                                 const float2 x1 = __ffma2_rn(ny2, rx[t], rx[t]);
                                 const float2 y1v = __ffma2_rn(ny2, ry[t], ry[t]);
-                                nx[t] = __fadd2_rn(__ffma2_rn(nyo, x1, x1), __fadd2_rn(ax, make_float2(-bx.x, -bx.y)));
+                                nx[t] = __fadd2_rn(__ffma2_rn(nyo, x1, x1), fsub2_rn(ax, bx));
                                 ny[t] = __fadd2_rn(__ffma2_rn(nyo, y1v, y1v), iy);
-                                float2 iz = __fmul2_rn(make_float2(fin[t][0], fin[t][0]), PAIR(Zs, qq, 0));
-#pragma unroll
-                                for (int p = 1; p < P; ++p)
-                                    iz = __ffma2_rn(make_float2(fin[t][p], fin[t][p]), PAIR(Zs, qq, p), iz);
-                                const float2 z1 = __ffma2_rn(make_float2(-y1[t], -y1[t]), rz[t], rz[t]);
                                 const float c = rhoS[t] * y1[t];
-                                nz[t] = __fadd2_rn(__ffma2_rn(nyo, z1, z1), __fadd2_rn(iz, make_float2(c, c)));
+                                float2 iz = make_float2(c, c);
+#pragma unroll
+                                for (int p = 0; p < P; ++p) {
+                                    if (p == t && !kSelf) continue;
+                                    iz = __ffma2_rn(make_float2(fin[t][p], fin[t][p]), PAIR(Zs, qq, p), iz);
+                                }
+                                const float2 z1 = __ffma2_rn(make_float2(-y1[t], -y1[t]), rz[t], rz[t]);
+                                nz[t] = __fadd2_rn(__ffma2_rn(nyo, z1, z1), iz);
                             }
 #pragma unroll
                             for (int t = 0; t < P; ++t) {
