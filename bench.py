@@ -72,8 +72,10 @@ def workload_args(name, n_tr):
     return sc, desc
 
 
-def op_counts(work, desc):
-    """Algorithmic FP32 flops and MUFU ops of one scan from the op table."""
+def op_counts(work, desc, parts=False):
+    """Algorithmic FP32 flops and MUFU ops of one scan from the op table
+    (with ``parts``: also the Bloch integration's flops alone, without the
+    receive row)."""
     iso_pools = work["units"] / max(1, work["steps"])
     steps, rf, samples = work["steps"], work["rf_steps"], work["samples"]
     P = desc["pools"]
@@ -81,8 +83,17 @@ def op_counts(work, desc):
     mufu = iso_pools * (rf * OPS["rf_mufu"] + (steps - rf) * OPS["free_mufu"])
     if desc["model"] in ("me", "gm"):
         flops += iso_pools * steps * (P - 1) * OPS["exch_flops"]
+    bloch = flops
     flops += samples * iso_pools * desc["rx"] * OPS["recv_flops"]
-    return flops, mufu
+    return (flops, mufu, bloch) if parts else (flops, mufu)
+
+
+# DRAM traffic of the headline scan kernel: dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch measured by ncu on the first 2 TRs of
+# the same scan (1,722 steps, 1,536 samples, 4,094,447,616 spin*pool*steps:
+# 202.9 MB read, 426.7 MB written, the writes the receive partials), per
+# spin*pool*step; steps and samples grow together over the scan's TRs.
+HEADLINE_TRAFFIC_PER_UNIT = (202.868992e6 + 426.745088e6) / 4094447616
 
 
 class ClockSampler:
@@ -755,14 +766,25 @@ def main():
             dist.destroy_process_group()
         return
     fp32_tf, mufu_g = peaks()
-    flops, mufu = op_counts(work, desc)
+    flops, mufu, bloch = op_counts(work, desc, parts=True)
     ms_per_scan = total_ms / args.steps
     scan_share = tm["scan_ms"] / max(1e-9, tm["scan_ms"] + tm["reduce_ms"])
     scan_ms = ms_per_scan * scan_share
     achieved_tf = flops / (scan_ms * 1e-3) / 1e12
     achieved_mufu = mufu / (scan_ms * 1e-3) / 1e9
+    launches = max(1, int(work["launches"]) // 2)  # scan kernel + reduction per launch
+    traffic = (HEADLINE_TRAFFIC_PER_UNIT * work["units"] / launches
+               if args.workload == "config2" and args.numerics == "accurate" else None)
     roof = {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_tf, "unit": "TFLOP/s",
-            "frac": achieved_tf / fp32_tf, "traffic": None,
+            "frac": achieved_tf / fp32_tf, "traffic": traffic,
+            "traffic_note": "bytes per scan-kernel launch (%d per scan), scaled by spin*pool*steps from one ncu "
+                            "capture of the first 2 TRs; the algorithmic output is the signal alone" % launches
+                            if traffic is not None else None,
+            "fp32_pipe": {"bloch_flops_per_scan": bloch,
+                          "achieved": bloch / (scan_ms * 1e-3) / 1e12,
+                          "frac": bloch / (scan_ms * 1e-3) / 1e12 / fp32_tf,
+                          "note": "the Bloch integration's op-table flops alone (the receive row counted per "
+                                  "spin*pool*coil runs on the tensor pipe after the spin sum)"},
             "mufu": {"achieved": achieved_mufu, "peak": mufu_g, "unit": "Gop/s", "frac": achieved_mufu / mufu_g},
             "peak_source": "measured on this GPU by libmrl_peaks.so (the larger of FFMA and packed f32x2 FFMA "
                            "chains; MUFU.SIN chains)", "peak_detail": _PEAKS.get("detail"),
