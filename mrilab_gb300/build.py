@@ -56,6 +56,7 @@ UNITS = {
     "adjoint.cu": [],
     "scan_fast_exact.cu": [],
     "scan_fast_exact_bound.cu": [],
+    "scan_fast_tc.cu": [],
     "sar.cu": [],
     "recon.cu": [],
     "decode.cpp": None,  # host C++

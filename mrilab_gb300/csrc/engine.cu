@@ -299,7 +299,15 @@ struct DevBuf {
 inline int split_source(int km, int P, bool all_free) { return km == KM_EXCH && all_free && P <= 3 ? 1 : 0; }
 
 cudaError_t launch_fast(int km, int P, int NS, bool all_free, dim3 grid, size_t smem, cudaStream_t st,
-                        const FastGrid &g, int co = 0) {
+                        const FastGrid &g, int co = 0, bool tc = false) {
+    if (tc) {  // the instantiations with the tcgen05 receive
+        FastKernel k = select_fast_tc(km, co, P, NS, all_free);
+        if (!k) return cudaErrorInvalidValue;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<grid, kBlock, smem, st>>>(g.descs, g.items, g.n_items, g.counter);
+        return cudaGetLastError();
+    }
     if (co) return launch_scan_fast_tab(co, P, NS, all_free, grid, smem, st, g);
     switch (km) {
     case KM_NORMAL: return launch_scan_fast_normal(P, NS, all_free, grid, smem, st, g);
@@ -309,7 +317,15 @@ cudaError_t launch_fast(int km, int P, int NS, bool all_free, dim3 grid, size_t 
     }
 }
 
-int occupancy_fast(int km, int P, int NS, bool all_free, size_t smem, int co = 0) {
+int occupancy_fast(int km, int P, int NS, bool all_free, size_t smem, int co = 0, bool tc = false) {
+    if (tc) {
+        FastKernel k = select_fast_tc(km, co, P, NS, all_free);
+        int n = 0;
+        if (!k || cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kBlock, smem) != cudaSuccess)
+            return 0;
+        return n;
+    }
     if (co) return occupancy_scan_fast_tab(co, P, NS, all_free, smem);
     switch (km) {
     case KM_NORMAL: return occupancy_scan_fast_normal(P, NS, all_free, smem);
@@ -439,6 +455,18 @@ struct Scanner {
     }
     // layout of the exchange channels for the table kernels: 0 ME, 1 GM, 2 MT, 3 CEST
     int k_layout() const { return mtc_exact ? (km_obj == KM_MT ? 2 : 3) : (mi.gm ? 1 : 0); }
+
+    // the accurate kernel contracts the receive on tcgen05: 17 to 32 coils,
+    // 1, 2 or 4 threads per voxel, and an instantiation built for it
+    // (MRL_RECEIVE_TC=0 keeps the warp-level TF32 contraction, for comparison)
+    bool tc_receive() const {
+        const char *e = getenv("MRL_RECEIVE_TC");
+        if (e && strcmp(e, "0") == 0) return false;
+        return fast && tc_receive_ok((RX + 3) & ~3, tpv) &&
+               select_fast_tc(mi.km, coef, P, NS, all_free() != 0) != nullptr;
+    }
+    // dynamic shared memory of an accurate-kernel launch of this scan
+    size_t fast_smem() const { return scan_fast_smem_bytes(stride4, RX, P, NS, tc_receive() ? tpv : 0); }
 
     // every pool of an exchange model is a free pool (ME, or GM without bound pools)
     int all_free() const {
@@ -904,6 +932,7 @@ struct Scanner {
         F.omega = d_f2.p + o_om;
         F.txc = d_f2.p + o_txc;
         F.all_free = all_free();
+        F.tc = tc_receive() ? 1 : 0;
         set_sampling(F, L, P);
         if (mtc_exact) {  // MT / CEST sample pool 0 only (BlochKernelMT.cuh:230)
             F.n_samp = 1;
@@ -963,7 +992,7 @@ struct Scanner {
         if (ls.empty()) return MRL_OK;
         const int nblk = (int)n_blocks();
         const size_t smem =
-            fast ? scan_fast_smem_bytes(stride4, RX, P, NS) : scan_smem_bytes(stride4, mi.nsamp);
+            fast ? fast_smem() : scan_smem_bytes(stride4, mi.nsamp);
         const double cr = std::cos(-rf_ref), sr = std::sin(-rf_ref);
         cudaError_t e;
         int rc;
@@ -982,7 +1011,7 @@ struct Scanner {
                 dim3 grid(nblk);
                 if (fast) {
                     const FastGrid g{d_desc.p + li, nullptr, nblk, nullptr};
-                    e = launch_fast(mi.km, P, NS, all_free() != 0, grid, smem, stream, g, coef);
+                    e = launch_fast(mi.km, P, NS, all_free() != 0, grid, smem, stream, g, coef, tc_receive());
                 } else {
                     switch (mi.km) {
                     case KM_NORMAL: e = launch_scan_ref_normal(P, NS, grid, smem, stream, L); break;
@@ -1320,6 +1349,7 @@ struct mrl_batch {
     struct Group {
         int km = 0, P = 0, NS = 1;
         bool free = false;
+        bool tc = false;                             // the tcgen05 receive instantiation
         int cap = 0;                                 // resident blocks per SM (0: occupancy)
         std::vector<int> inst;
         size_t smem = 0;
@@ -1379,16 +1409,17 @@ FastLaunch batch_desc(mrl_batch &b, mrl_batch::Inst &it, long long max_steps) {
 int batch_build(mrl_batch &b, long long max_steps) {
     std::vector<int> caps;
     for (auto &g : b.groups) caps.push_back(g.cap);
-    std::vector<std::tuple<int, int, int, bool, int>> keys;
-    for (auto &g : b.groups) keys.emplace_back(g.km, g.P, g.NS, g.free, g.cap);
+    std::vector<std::tuple<int, int, int, bool, bool, int>> keys;
+    for (auto &g : b.groups) keys.emplace_back(g.km, g.P, g.NS, g.free, g.tc, g.cap);
     b.drop_groups();
     for (size_t i = 0; i < b.in.size(); ++i) {
         Scanner &sc = *b.in[i].sc;
         const bool fr = sc.all_free() != 0;
+        const bool tc = sc.tc_receive();
         int gi = -1;
         for (size_t k = 0; k < b.groups.size(); ++k) {
             const auto &g = b.groups[k];
-            if (g.km == sc.mi.km && g.P == sc.P && g.NS == sc.NS && g.free == fr) gi = (int)k;
+            if (g.km == sc.mi.km && g.P == sc.P && g.NS == sc.NS && g.free == fr && g.tc == tc) gi = (int)k;
         }
         if (gi < 0) {
             mrl_batch::Group g;
@@ -1396,10 +1427,11 @@ int batch_build(mrl_batch &b, long long max_steps) {
             g.P = sc.P;
             g.NS = sc.NS;
             g.free = fr;
+            g.tc = tc;
             for (auto &k : keys)  // keep a tuned resident-block cap
                 if (std::get<0>(k) == g.km && std::get<1>(k) == g.P && std::get<2>(k) == g.NS &&
-                    std::get<3>(k) == g.free)
-                    g.cap = std::get<4>(k);
+                    std::get<3>(k) == g.free && std::get<4>(k) == g.tc)
+                    g.cap = std::get<5>(k);
             b.groups.push_back(std::move(g));
             gi = (int)b.groups.size() - 1;
         }
@@ -1415,7 +1447,7 @@ int batch_build(mrl_batch &b, long long max_steps) {
             mrl_batch::Inst &it = b.in[i];
             Scanner &sc = *it.sc;
             h.push_back(batch_desc(b, it, max_steps));
-            g.smem = std::max(g.smem, scan_fast_smem_bytes(sc.stride4, sc.RX, sc.P, sc.NS));
+            g.smem = std::max(g.smem, sc.fast_smem());
             const long long steps = max_steps >= 0 ? std::min(it.steps, max_steps) : it.steps;
             const long long cost = steps + 3 * std::min(it.rf_steps, steps);  // an rf step costs ~4 free steps
             const int nblk = sc.n_act > 0 ? (int)sc.n_blocks() : 0;
@@ -1439,7 +1471,7 @@ int batch_build(mrl_batch &b, long long max_steps) {
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b.st);
         if (e != cudaSuccess) return set_err("batch setup: %s", cudaGetErrorString(e)), MRL_ERR_CUDA;
-        const int occ = occupancy_fast(g.km, g.P, g.NS, g.free, g.smem, split_source(g.km, g.P, g.free));
+        const int occ = occupancy_fast(g.km, g.P, g.NS, g.free, g.smem, split_source(g.km, g.P, g.free), g.tc);
         if (occ < 1) return set_err("batch: kernel does not fit (%zu bytes of shared memory)", g.smem), MRL_ERR_UNSUPPORTED;
         const int per_sm = g.cap > 0 ? std::min(g.cap, occ) : occ;
         g.grid = std::max(1, std::min(g.n_items, per_sm * b.sms));
@@ -1489,7 +1521,8 @@ int batch_record(mrl_batch &b, cudaStream_t s, bool reduce) {
         e = cudaStreamWaitEvent(g.st, b.fork, 0);
         if (e == cudaSuccess && g.n_items > 0)
             e = launch_fast(g.km, g.P, g.NS, g.free, dim3(g.grid), g.smem, g.st,
-                            FastGrid{g.descs.p, g.items.p, g.n_items, g.counter.p}, split_source(g.km, g.P, g.free));
+                            FastGrid{g.descs.p, g.items.p, g.n_items, g.counter.p}, split_source(g.km, g.P, g.free),
+                            g.tc);
         if (e == cudaSuccess) e = cudaEventRecord(g.done, g.st);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g.done, 0);
     }
@@ -1817,8 +1850,9 @@ int mrl_batch_execute(mrl_batch *b, int mode, void *stream) {
             e = cudaMemcpyAsync(sc.d_m.p, it.d_m0.p, it.d_m0.n * sizeof(float), cudaMemcpyDeviceToDevice, s);
         if (e != cudaSuccess || sc.n_act == 0) continue;
         const int nblk = (int)sc.n_blocks();
-        e = launch_fast(g.km, g.P, g.NS, g.free, dim3(nblk), scan_fast_smem_bytes(sc.stride4, sc.RX, sc.P, sc.NS), s,
-                        FastGrid{g.descs.p + it.slot, nullptr, nblk, nullptr}, split_source(g.km, g.P, g.free));
+        e = launch_fast(g.km, g.P, g.NS, g.free, dim3(nblk), sc.fast_smem(), s,
+                        FastGrid{g.descs.p + it.slot, nullptr, nblk, nullptr}, split_source(g.km, g.P, g.free),
+                        g.tc);
         const mrl::Scanner::LaunchDesc &d = it.ls[0];
         if (e == cudaSuccess && d.a_count > 0) {
             const int npairs = sc.mi.nsamp * sc.RX;
@@ -1865,7 +1899,7 @@ int mrl_batch_tune(mrl_batch *b, void *stream) {
             }
             if ((rc = batch_build(*b, kTrialSteps))) break;
             mrl_batch::Group &g = b->groups[b->in[set[0]].group];
-            const int occ = occupancy_fast(g.km, g.P, g.NS, g.free, g.smem, split_source(g.km, g.P, g.free));
+            const int occ = occupancy_fast(g.km, g.P, g.NS, g.free, g.smem, split_source(g.km, g.P, g.free), g.tc);
             for (int cap : {occ, occ - 1}) {
                 if (cap < 1 || g.n_items == 0) continue;
                 const int grid = std::max(1, std::min(g.n_items, cap * b->sms));
@@ -1879,7 +1913,8 @@ int mrl_batch_tune(mrl_batch *b, void *stream) {
                     if (e == cudaSuccess) e = cudaEventRecord(e0, b->st);
                     if (e == cudaSuccess)
                         e = launch_fast(g.km, g.P, g.NS, g.free, dim3(grid), g.smem, b->st,
-                                        FastGrid{g.descs.p, g.items.p, g.n_items, g.counter.p}, split_source(g.km, g.P, g.free));
+                                        FastGrid{g.descs.p, g.items.p, g.n_items, g.counter.p}, split_source(g.km, g.P, g.free),
+                            g.tc);
                     if (e == cudaSuccess) e = cudaEventRecord(e1, b->st);
                     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
                     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);

@@ -32,6 +32,7 @@
 
 #include "decode.h"
 #include "scan_kernel.cuh"
+#include "tc_util.cuh"
 
 namespace mrl {
 
@@ -53,8 +54,33 @@ struct FastLaunch {
     // a sample, or -1 for a bound pool (its signal is zero)
     int n_samp;
     int samp_rank[kMaxPool];
+    // receive contraction on the fifth-generation tensor cores (tcgen05,
+    // tc_receive_ok): 17 to 32 coils, 1, 2 or 4 threads per voxel; launched
+    // with the instantiations built for it (select_fast_tc)
+    int tc;
 };
 static_assert(sizeof(FastLaunch) % 4 == 0, "FastLaunch is copied to shared memory as 32-bit words");
+
+// tcgen05 receive: the coil operand has 128 rows -- Re R_c (TF32 big part),
+// Im R_c (big), Re R_c (small part), Im R_c (small) for 32 coil slots -- and
+// K = the block's voxels; the magnetisation operand has 16 rows (sample x
+// sampled pool) in four parts Re m (big), Re m (small), Im m (big), Im m
+// (small).  Both K-major with the 128-byte swizzle (tc_util.cuh).  Tensor
+// memory: 32 columns, Re m products in 0..15, Im m products in 16..31.
+constexpr int kTcRows = 128, kTcN = 16, kTcCoils = 32, kTcCols = 32;
+__host__ __device__ constexpr bool tc_receive_ok(int c4, int tpv) {
+    return c4 > 16 && c4 <= kTcCoils && (tpv == 1 || tpv == 2 || tpv == 4);
+}
+// voxels of a block (the contraction's K) and the byte sizes of the
+// operands: coil operand, one magnetisation part, the magnetisation region
+// (also the epilogue's per-warp sums, [warp][16][32] float2)
+__host__ __device__ constexpr int tc_kv(int tpv) { return kBlock / tpv; }
+__host__ __device__ constexpr int tc_a_bytes(int tpv) { return kTcRows * tc_kv(tpv) * 4; }
+__host__ __device__ constexpr int tc_part_bytes(int tpv) { return kTcN * tc_kv(tpv) * 4; }
+__host__ __device__ constexpr int tc_b_bytes(int tpv) {
+    return 4 * tc_part_bytes(tpv) > (kBlock / 32) * kTcN * kTcCoils * 8 ? 4 * tc_part_bytes(tpv)
+                                                                        : (kBlock / 32) * kTcN * kTcCoils * 8;
+}
 
 // Coil sensitivities in shared memory: up to 16 coils (C4 <= 16) already
 // split into TF32 (big, small) pairs for the receive contraction; beyond,
@@ -305,11 +331,17 @@ __host__ __device__ constexpr int fast_min_blocks() {
 // described by F, over F's step range.  kbase counts the record chunks this
 // block has staged before (it picks the buffer and mbarrier phase).
 // Returns false, block-uniformly, when a wait ran out (status word raised).
+// TC (F.tc): the receive contraction runs on tcgen05 into the tensor memory
+// whose address the kernel keeps at smem + 24 (32 columns held by the
+// block); the 32-bit word at smem + 28 counts the block's contractions (the
+// phase of their completion mbarrier bar[2]) and the one at smem + 32 is
+// raised when a contraction's wait ran out.  (Kept in shared memory, not in
+// registers: the step loop's instantiations sit at their register limit.)
 // Coefficient source CO of the relaxation / exchange step: 0 computed in the
 // kernel at each dt change; 1 the same split-exchange coefficients from a
 // table per (dt, voxel) computed in FP64 (fewer live registers: no rates or
 // relaxation rates held); 2 the exact propagator's table (EXACT).
-template <int MODEL, int P, int NS, bool FREE, int CO = 0>
+template <int MODEL, int P, int NS, bool FREE, int CO = 0, bool TC = false>
 __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigned char *smem, uint32_t &kbase) {
     constexpr bool EXACT = CO == 2;
     static_assert(CO == 0 || (MODEL == KM_EXCH && (FREE || CO == 2)),
@@ -341,7 +373,19 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     uint2 *rsq = reinterpret_cast<uint2 *>(mtile + 16 * kTRow);
     float2 *rsf = reinterpret_cast<float2 *>(rsq);
     float *wstage = reinterpret_cast<float *>(rsq + (presplit ? 2 : 1) * C4 * kTRow);  // [warp][16][2*C4]
-    float2 *dwsm = reinterpret_cast<float2 *>(wstage + kWarps * 16 * 2 * C4);     // [NQ][P][kBlock] spin pairs
+    // tcgen05 receive instead (F.tc): the coil and magnetisation operands
+    // from the first 1024-byte boundary after the records
+    // a compile-time choice: the instantiations without it keep their step
+    // loop as small as before (the headline's is bound by instruction fetch)
+    constexpr bool tcr = TC;
+#define TPV (L.tpv)
+    // the coil operand at the first 1024-byte boundary after the records
+    // (the magnetisation operand follows it)
+#define TCA (reinterpret_cast<unsigned char *>(mtile) + ((1024u - (smem_u32(mtile) & 1023u)) & 1023u))
+#define TCB (TCA + tc_a_bytes(TPV))
+    volatile uint32_t *tc_word = reinterpret_cast<volatile uint32_t *>(smem + 24);  // [0] tmem, [1] kmma, [2] fail
+    float2 *dwsm = tcr ? reinterpret_cast<float2 *>(TCB + tc_b_bytes(TPV))
+                       : reinterpret_cast<float2 *>(wstage + kWarps * 16 * 2 * C4);  // [NQ][P][kBlock] spin pairs
     float *omlo = reinterpret_cast<float *>(dwsm + NQ * P * kBlock);              // [4][kBlock]
 
     const int tid = threadIdx.x;
@@ -461,7 +505,31 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
             if (L.kind[t] != 0) tvo &= ~(1u << t);
     }
     // stage this thread's voxel's coil sensitivities (zero beyond the coil count)
-    for (int c = 0; c < C4; ++c) {
+    if constexpr (tcr) {
+        // one thread per voxel writes its column of the coil operand (all
+        // 32 coil slots: the 128 rows of the MMA)
+        if (sg == 0) {
+            const int kv = tid / TPV;
+            for (int c = 0; c < kTcCoils; ++c) {
+                float2 r = make_float2(0.f, 0.f);
+                if (active && c < L.rx) {
+                    if (L.rx_default)
+                        r = make_float2(1.f, 0.f);
+                    else if (F.direct)
+                        r = make_float2(F.rx_x[(long long)c * n + v], F.rx_y[(long long)c * n + v]);
+                    else
+                        r = L.rxc[(long long)c * n + v];
+                }
+                const float bx = __uint_as_float(tf32_rn(r.x)), by = __uint_as_float(tf32_rn(r.y));
+                const float q[4] = {bx, by, __uint_as_float(tf32_rn(r.x - bx)), __uint_as_float(tf32_rn(r.y - by))};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    *reinterpret_cast<float *>(TCA + tc::sw128_offset(i * kTcCoils + c, kv, kTcRows)) = q[i];
+            }
+        }
+        tc::fence_async_smem();
+    }
+    for (int c = 0; c < (tcr ? 0 : C4); ++c) {
         float2 r = make_float2(0.f, 0.f);
         if (active && c < L.rx) {
             if (L.rx_default)
@@ -492,12 +560,17 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 #pragma unroll
         for (int p = 0; p < P; ++p) fin[t][p] = 0.f;
     }
-    // packed free steps (two spins per f32x2 operation): the all-free exchange
-    // model with the split scheme and an even spin count per thread
-    constexpr bool kPack = MODEL == KM_EXCH && FREE && !EXACT && NS % 2 == 0;
+    // packed free steps (two spins per f32x2 operation): the exchange model
+    // with the split scheme and an even spin count per thread.  With bound
+    // pools (FREE false) the free step is the same arithmetic: a bound pool's
+    // increment is its frame's step back (held in the lab), the transverse
+    // inflow from a bound pool is zero in fr, and saturation acts on rf steps
+    // only
+    constexpr bool kPack = MODEL == KM_EXCH && !EXACT && NS % 2 == 0;
     // rf steps packed too while a thread's state is small (with 8 isochromat-
     // pools the packed rf step's temporaries spill; rf steps are rare there)
-    constexpr bool kPackRf = kPack && NS * P <= 4;
+    // and every pool is free (no saturation)
+    constexpr bool kPackRf = kPack && FREE && NS * P <= 4;
     bool selfx = false;  // some pool of this voxel exchanges with itself (a nonzero K diagonal)
     float mt_y1k = 0.f, mt_y21 = 0.f, mt_y1bk = 0.f, mt_y1b = 0.f, mt_y12 = 0.f;
     LineshapeCache lc;
@@ -623,8 +696,99 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         a_fill = 0;
         __syncthreads();
     };
+    // the flush on tcgen05 (F.tc): D = R x m^T, R the 128-row coil operand
+    // and m the 16-row sample tile, K = the block's voxels; the products of
+    // Re m go to tensor-memory columns 0..15, of Im m to 16..31.  Each of the
+    // two sums adds the big and the small part of m (R's rows carry R's big
+    // and small parts), so the row sums give R m with FP32-level accuracy
+    // (big*big + big*small + small*big + small*small).  One thread issues the
+    // MMAs; the block waits (bounded) for their completion, and each warp
+    // reads its 32 tensor-memory lanes: warp 0 Re R big, 1 Im R big, 2 Re R
+    // small, 3 Im R small, one lane per coil slot.
+    auto flush_tc = [&]() {
+        tc::fence_async_smem();  // this thread's tile writes, for the tensor core
+        tc::fence_before_sync();
+        __syncthreads();
+        const int kv = tc_kv(TPV);
+        const int pbytes = tc_part_bytes(TPV);
+        const uint32_t tmem = tc_word[0], kmma = tc_word[1];
+        __syncthreads();  // every thread has read the counter
+        if (tid == 0) {
+            tc_word[1] = kmma + 1u;
+            tc::fence_after_sync();
+            // descriptors of the operands' bases; a K step adds its byte offset / 16
+            // to the start-address field (shared addresses stay below 2^18)
+            const uint64_t da = tc::sw128_desc(smem_u32(TCA)), db = tc::sw128_desc(smem_u32(TCB));
+            constexpr uint32_t idesc = tc::idesc_tf32(kTcRows, kTcN);
+            for (int xy = 0; xy < 2; ++xy) {
+#pragma unroll
+                for (int bs = 0; bs < 2; ++bs) {
+                    const uint64_t dbp = db + (uint64_t)(((2 * xy + bs) * pbytes) >> 4);
+#pragma unroll 4
+                    for (int ks = 0; ks < kv / 8; ++ks) {
+                        const uint32_t ao = (uint32_t)((ks >> 2) * kTcRows * 128 + (ks & 3) * 32) >> 4;
+                        const uint32_t bo = (uint32_t)((ks >> 2) * kTcN * 128 + (ks & 3) * 32) >> 4;
+                        tc::mma_tf32(tmem + (uint32_t)(xy * kTcN), da + ao, dbp + bo, idesc, bs > 0 || ks > 0);
+                    }
+                }
+            }
+            tc::mma_commit(&bar[2]);
+        }
+        if (!mbar_wait_bounded(&bar[2], kmma & 1u, L.err)) {
+            // a second bounded wait for the MMAs still in flight before the
+            // block gives up (the tensor memory is freed at kernel exit)
+            mbar_wait_bounded(&bar[2], kmma & 1u, L.err);
+            tc_word[2] = 1u;
+        }
+        tc::fence_after_sync();
+        // per warp (S_x, S_y) of each (row, coil slot), S = m conj(R), over the
+        // consumed tile ([warp][16][32] float2): Re R rows give (Re m, Im m)
+        // products to (x, y), Im R rows (Im m, -Re m); read 8 columns at a time
+        float2 *stg = reinterpret_cast<float2 *>(TCB);
+        float *stw = reinterpret_cast<float *>(stg + warp * kTcN * kTcCoils + lane);
+        const bool imr = (warp & 1) != 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float d[8];
+            tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(8 * q), d);
+            const bool im_m = q >= 2;  // columns 16..31: Im m products
+            const int comp = (im_m != imr) ? 1 : 0;
+            const float sgn = (imr && !im_m) ? -1.f : 1.f;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) stw[((q & 1) * 8 + j) * kTcCoils * 2 + comp] = sgn * d[j];
+        }
+        __syncthreads();
+        const int nout = a_fill * kNSampP * L.rx;
+        for (int o = tid; o < nout; o += kBlock) {
+            const int pr = o / L.rx;  // = a * kNSampP + t
+            const int c = o - pr * L.rx;
+            const int a = pr / kNSampP, t = pr - a * kNSampP;
+            const int rank = kRank ? F.samp_rank[t] : t;
+            float sx = 0.f, sy = 0.f;
+            if (rank >= 0) {
+                const int row = a * nsp + rank;
+#pragma unroll
+                for (int w = 0; w < kWarps; ++w) {
+                    const float2 q = stg[(w * kTcN + row) * kTcCoils + c];
+                    sx += q.x;
+                    sy += q.y;
+                }
+            }
+            if (L.dsx) {
+                direct_add(L, a_base + a, t, c, sx, sy);
+            } else {
+                L.partial[((long long)tile * L.a_launch + a_base + a) * L.npairs + t * L.rx + c] = make_float2(sx, sy);
+            }
+        }
+        a_base += a_fill;
+        a_fill = 0;
+        tc::fence_before_sync();
+        __syncthreads();
+    };
     auto flush = [&]() {
-        if (presplit)
+        if constexpr (tcr)
+            flush_tc();
+        else if (presplit)
             flush_form(BoolTag<true>{});
         else
             flush_form(BoolTag<false>{});
@@ -633,7 +797,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     for (int k = 0; k < nchunks; ++k) {
         if (tid == 0 && k + 1 < nchunks) issue(k + 1);
         const uint32_t kk = kbase + k;
-        bool ok = mbar_wait_bounded(&bar[kk & 1], (kk >> 1) & 1, L.err);
+        bool ok = mbar_wait_bounded(&bar[kk & 1], (kk >> 1) & 1, L.err) && (!TC || tc_word[2] == 0u);
         ok = __syncthreads_and(ok) != 0;
         if (!ok) {
             // wait (bounded) for the copies still in flight: this chunk and the next
@@ -820,7 +984,26 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     float2 m = cmul(make_float2(sx, sy), Pc[t]);
                     if (!active) m = make_float2(0.f, 0.f);
                     const int rank = kRank ? F.samp_rank[t] : t;
-                    if (rank >= 0) mtile[(a_fill * nsp + rank) * kTRow + tid] = m;
+                    if constexpr (tcr) {
+                        // the voxel's sum over its threads, written by its first
+                        // thread as the TF32 big and small parts of Re and Im
+                        for (int o = 1; o < TPV; o <<= 1) {
+                            m.x += __shfl_xor_sync(0xffffffffu, m.x, o);
+                            m.y += __shfl_xor_sync(0xffffffffu, m.y, o);
+                        }
+                        if (rank >= 0 && sg == 0) {
+                            const float bx = __uint_as_float(tf32_rn(m.x)), by = __uint_as_float(tf32_rn(m.y));
+                            const uint32_t off = tc::sw128_offset(a_fill * nsp + rank, tid / TPV, kTcN);
+                            const int pb = tc_part_bytes(TPV);
+                            unsigned char *tb = TCB + off;
+                            *reinterpret_cast<float *>(tb) = bx;
+                            *reinterpret_cast<float *>(tb + pb) = __uint_as_float(tf32_rn(m.x - bx));
+                            *reinterpret_cast<float *>(tb + 2 * pb) = by;
+                            *reinterpret_cast<float *>(tb + 3 * pb) = __uint_as_float(tf32_rn(m.y - by));
+                        }
+                    } else if (rank >= 0) {
+                        mtile[(a_fill * nsp + rank) * kTRow + tid] = m;
+                    }
                 }
                 if (++a_fill == ktile) flush();
             }
@@ -877,6 +1060,12 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 #pragma unroll
                     for (int p = 0; p < P; ++p) {
                         if (kPack && p == t && !selfx) {  // fin[t][t] = 0: no self-exchange
+                            fr[t][p] = make_float2(0.f, 0.f);
+                            continue;
+                        }
+                        // no transverse exchange with or of a bound pool, and none of a
+                        // general-model pool with itself (block-uniform tests)
+                        if (!FREE && !EXACT && (L.kind[p] != 0 || L.kind[t] != 0 || (L.exch_gm && p == t))) {
                             fr[t][p] = make_float2(0.f, 0.f);
                             continue;
                         }
@@ -976,6 +1165,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 #pragma unroll
                                 for (int p = 0; p < P; ++p) {
                                     if (p == t && !kSelf) continue;
+                                    if (!FREE && (L.kind[p] != 0 || L.kind[t] != 0)) continue;  // fr is zero
                                     const float2 f1 = make_float2(fr[t][p].x, fr[t][p].x);
                                     const float2 f2 = make_float2(fr[t][p].y, fr[t][p].y);
                                     ax = __ffma2_rn(f1, PAIR(Xs, qq, p), ax);
@@ -1266,6 +1456,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         __syncthreads();
     }
     if (a_fill > 0) flush();
+    if (TC && __syncthreads_or(tc_word[2] != 0u)) return false;
 
     if (active) {
 #pragma unroll
@@ -1285,6 +1476,9 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     }
     kbase += (uint32_t)nchunks;
     return true;
+#undef TCA
+#undef TCB
+#undef TPV
 #undef XS
 #undef YS
 #undef ZS
@@ -1300,32 +1494,50 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 // block per tile); otherwise it is persistent and, after item blockIdx.x,
 // takes items gridDim.x, gridDim.x + 1, ... from *counter (the batched
 // form: the tiles of many scans, ordered longest first).  Each item's
-// descriptor is copied from descs into shared memory.
-template <int MODEL, int P, int NS, bool FREE, int CO = 0>
+// descriptor is copied from descs into shared memory.  A block whose items
+// contract the receive on tcgen05 allocates 32 tensor-memory columns at its
+// first such item and frees them before it exits.
+template <int MODEL, int P, int NS, bool FREE, int CO = 0, bool TC = false>
 __global__ void __launch_bounds__(kBlock, fast_min_blocks<P, NS>())
     scan_fast_kernel(const FastLaunch *__restrict__ descs, const int2 *__restrict__ items, int n_items, int *counter) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ FastLaunch fs;
     __shared__ int next_item;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);  // [0], [1] record chunks, [2] receive MMAs
+    uint32_t *tc_word = reinterpret_cast<uint32_t *>(smem + 24);  // tensor memory, contractions, failure
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], 1);
         fence_mbar_init();
+        tc_word[1] = tc_word[2] = 0u;
     }
     uint32_t kbase = 0;
+    bool tmem_held = false;
     for (int it = blockIdx.x; it < n_items;) {
         const int2 item = items ? items[it] : make_int2(0, it);
         const int *src = reinterpret_cast<const int *>(descs + item.x);
         int *dst = reinterpret_cast<int *>(&fs);
         for (int w = threadIdx.x; w < (int)(sizeof(FastLaunch) / 4); w += blockDim.x) dst[w] = src[w];
         __syncthreads();
-        if (!scan_item<MODEL, P, NS, FREE, CO>(fs, item.y, smem, kbase)) return;
+        if (TC && !tmem_held) {
+            if (threadIdx.x < 32) tc::tmem_alloc(&tc_word[0], kTcCols);
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            tmem_held = true;
+        }
+        if (!scan_item<MODEL, P, NS, FREE, CO, TC>(fs, item.y, smem, kbase)) break;
         if (counter == nullptr) break;
         __syncthreads();  // every thread is done with fs and the item's shared memory
         if (threadIdx.x == 0) next_item = atomicAdd(counter, 1) + (int)gridDim.x;
         __syncthreads();
         it = next_item;
+    }
+    if (TC && tmem_held) {
+        tc::fence_before_sync();
+        __syncthreads();
+        if (threadIdx.x < 32) tc::tmem_dealloc(tc_word[0], kTcCols);
     }
 }
 

@@ -33,13 +33,17 @@ inline int partial_slices(bool fast) {
     return 1;
 }
 
-inline size_t scan_fast_smem_bytes(int stride4, int rx, int P, int NS) {
+// tc_tpv > 0: the receive contraction on tcgen05 (FastLaunch::tc) with
+// tc_tpv threads per voxel -- the coil and magnetisation operands from a
+// 1024-byte boundary instead of the tile, coil maps and per-warp sums.
+inline size_t scan_fast_smem_bytes(int stride4, int rx, int P, int NS, int tc_tpv = 0) {
     const size_t c4 = (size_t)((rx + 3) & ~3);
     const size_t row = kBlock + 2;
+    const size_t recv = tc_tpv > 0 ? 1024 + (size_t)tc_a_bytes(tc_tpv) + (size_t)tc_b_bytes(tc_tpv)
+                                   : 16 * row * 8 + c4 * row * (coil_presplit((int)c4) ? 16 : 8)  // tile, coil maps
+                                         + (kBlock / 32) * 16 * 2 * c4 * 4;  // per-warp receive sums
     return 128 + (size_t)2 * kFastChunk * stride4 * 16  // staged step records
-           + 16 * row * 8 + c4 * row * (coil_presplit((int)c4) ? 16 : 8)  // receive tile, coil maps
-           + (kBlock / 32) * 16 * 2 * c4 * 4        // per-warp receive sums
-           + ((size_t)2 * ((NS + 1) / 2) * P + 4) * kBlock * 4;  // dWRnd (spin pairs), low parts of omega
+           + recv + ((size_t)2 * ((NS + 1) / 2) * P + 4) * kBlock * 4;  // dWRnd (spin pairs), low parts of omega
 }
 
 // One launch of the accurate kernel: n_items work items (instance, tile)
@@ -84,6 +88,9 @@ cudaError_t launch_scan_fast_tab(int co, int P, int NS, bool all_free, dim3 grid
 int occupancy_scan_fast_tab(int co, int P, int NS, bool all_free, size_t smem);
 using FastKernel = void (*)(const FastLaunch *, const int2 *, int, int *);
 FastKernel select_exact_bound(int P, int NS);  // scan_fast_exact_bound.cu
+// the instantiations with the tcgen05 receive contraction (scan_fast_tc.cu),
+// nullptr where none is built: km, coefficient source co (0 or 1), P, NS
+FastKernel select_fast_tc(int km, int co, int P, int NS, bool all_free);
 cudaError_t launch_split_table(int P, const float *dts, int n_dt, int n_act, int gm, const float *rho,
                                const float *t1, const float *t2, const float *kch, float *tab, cudaStream_t st);
 // tab[(d * exact_fields(P) + f) * n_act + v] for the n_dt values dts[]

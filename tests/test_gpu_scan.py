@@ -456,3 +456,35 @@ def test_many_coil_receive_matches_fp64_oracle(built):
     err = rel_l2(signal(out), signal(ref))
     print(f"20 coils: relative L2 {err:.2e}")
     assert err <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("spins_per_thread", ["2", "1"])
+def test_tcgen05_receive_mt_epi_32_coils(built, monkeypatch, spins_per_thread):
+    """The receive contraction on tcgen05 (17 to 32 coils): the MT + exchange
+    EPI's model (general model, bound pool, 4 spins) with 32 Rx coils, two
+    and four threads per voxel (the voxels' spin sums are the contraction's
+    K).  Against the all-FP64 oracle (the MT EPI bound, 2e-5) and against
+    the warp-level TF32 contraction (MRL_RECEIVE_TC=0); the two results are
+    not bit-identical, so both contractions ran."""
+    from mrilab_gb300 import engine, phantoms
+    import oracle
+
+    sc = phantoms.config5_mt_epi(seed=7, nx=12, ny=12, nz=3, spins=4, n_coils=32, n_read=16, n_pe=16)
+    assert int(sc.VCoi["RxCoilNum"]) == 32
+    monkeypatch.setenv("MRL_SPINS_PER_THREAD", spins_per_thread)
+    ref = oracle.run_port(sc, "f64")
+    out_tc = engine.scan(sc)
+    monkeypatch.setenv("MRL_RECEIVE_TC", "0")
+    out_mma = engine.scan(sc)
+    e_tc = rel_l2(signal(out_tc), signal(ref))
+    e_mma = rel_l2(signal(out_mma), signal(ref))
+    e_between = rel_l2(signal(out_tc), signal(out_mma))
+    port32 = rel_l2(signal(oracle.run_port(sc, "f32")), signal(ref))
+    print(f"32 coils, {spins_per_thread} spin(s) per thread: tcgen05 {e_tc:.2e}, warp-level {e_mma:.2e}, "
+          f"between {e_between:.2e} (reference algorithm in FP32: {port32:.2e})")
+    assert e_tc <= 2e-5 and e_tc < port32
+    assert e_between <= 5e-6
+    assert not np.array_equal(signal(out_tc), signal(out_mma))
+    for k in ("Mx", "My", "Mz"):  # the final state does not depend on the receive
+        np.testing.assert_array_equal(out_tc[k], out_mma[k])
