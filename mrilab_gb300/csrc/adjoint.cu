@@ -123,6 +123,54 @@ __device__ __forceinline__ float3 jl_t(const Rot &r, float3 u) {
                        u.z - r.s.y * vu.z + c2 * vvu.z);
 }
 
+// Two pools of one isochromat as the lanes of f32x2 values (the packed
+// two-pool path of the kernel): a 3-vector per pool, lane t = pool t.
+struct V2 {
+    float2 x, y, z;
+};
+__device__ __forceinline__ float2 bc(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 swp(float2 a) { return make_float2(a.y, a.x); }  // the other pool's lane
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+// a x b per lane
+__device__ __forceinline__ V2 cross2(const V2 &a, const V2 &b) {
+    return {fma2(a.y, b.z, neg2(mul2(a.z, b.y))), fma2(a.z, b.x, neg2(mul2(a.x, b.z))),
+            fma2(a.x, b.y, neg2(mul2(a.y, b.x)))};
+}
+__device__ __forceinline__ float2 dot2(const V2 &a, const V2 &b) { return fma2(a.x, b.x, fma2(a.y, b.y, mul2(a.z, b.z))); }
+// (sin a / a, (1 - cos a) / a^2) per lane: the Taylor series of rot_coeffs
+// on both lanes at once when both angles are below 0.25
+__device__ __forceinline__ void rot_coeffs2(float2 a2, float2 &s1, float2 &s2) {
+    if (a2.x < 0.0625f && a2.y < 0.0625f) {
+        s1 = fma2(fma2(fma2(a2, bc(-1.f / 5040.f), bc(1.f / 120.f)), a2, bc(-1.f / 6.f)), a2, bc(1.f));
+        s2 = fma2(fma2(fma2(a2, bc(-1.f / 40320.f), bc(1.f / 720.f)), a2, bc(-1.f / 24.f)), a2, bc(0.5f));
+    } else {
+        const float2 c0 = rot_coeffs(a2.x), c1 = rot_coeffs(a2.y);
+        s1 = make_float2(c0.x, c1.x);
+        s2 = make_float2(c0.y, c1.y);
+    }
+}
+// exp([v]x) m per lane (Rodrigues' formula, as rot_exp)
+__device__ __forceinline__ V2 rot2(const V2 &v, float2 s1, float2 s2, const V2 &m) {
+    const V2 c = cross2(v, m), e = cross2(v, c);
+    return {add2(m.x, fma2(s1, c.x, mul2(s2, e.x))), add2(m.y, fma2(s1, c.y, mul2(s2, e.y))),
+            add2(m.z, fma2(s1, c.z, mul2(s2, e.z)))};
+}
+// J_l(v)^T u per lane (jl_t)
+__device__ __forceinline__ V2 jlt2(const V2 &v, float2 a2, float2 s1, float2 s2, const V2 &u) {
+    float2 c2;
+    if (a2.x < 0.0625f && a2.y < 0.0625f)
+        c2 = fma2(fma2(fma2(a2, bc(-1.f / 362880.f), bc(1.f / 5040.f)), a2, bc(-1.f / 120.f)), a2, bc(1.f / 6.f));
+    else
+        c2 = make_float2(jl_c2(a2.x, s1.x), jl_c2(a2.y, s1.y));
+    const V2 vu = cross2(v, u), vvu = cross2(v, vu);
+    const float2 ns2 = neg2(s2);
+    return {fma2(c2, vvu.x, fma2(ns2, vu.x, u.x)), fma2(c2, vvu.y, fma2(ns2, vu.y, u.y)),
+            fma2(c2, vvu.z, fma2(ns2, vu.z, u.z))};
+}
+
 // compensated running sum (window sums added to a float total)
 struct KSum {
     float s = 0.f, c = 0.f;
@@ -235,6 +283,9 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     // map: d2, d1, cc, fin; gradient: hT1 (of l.z mr.z), hR (of l.z), hT2 (of
     // l.xy mr.xy), e2, e1 (outflow rates, of l.xy mr.xy and l.z mr.z), ffin
     float d1[P], d2[P], y1[P], fin[P][P], hT1[P], hR[P], hT2[P], e1[P], e2[P];
+    // packed two-pool path: (1 - f_tp) dt of each inflow, zero for a pool that is off
+    constexpr bool kPk = P == 2 && !BOUND;
+    float gin[kPk ? P : 1][kPk ? P : 1];
     float dtc = 0.f;  // dt of these coefficients
     auto set_dt = [&](float dt) {
 #pragma unroll
@@ -266,6 +317,11 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             hT2[t] = -(1.f - yot_t) * fT2;
             e2[t] = -(1.f - y2t) * (1.f - yot_t) * dt;
             e1[t] = -(1.f - y1t) * fyo;
+            if (!on[t]) d1[t] = d2[t] = e1[t] = e2[t] = 0.f;  // (an off pool is left alone)
+            if constexpr (kPk) {
+#pragma unroll
+                for (int p = 0; p < P; ++p) gin[t][p] = on[t] && !(GM && p == t) ? (1.f - fin[t][p]) * dt : 0.f;
+            }
         }
         dtc = dt;
     };
@@ -284,6 +340,31 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     };
     // one forward step, m -> F(m)
     auto fwd = [&](float dt, float4 r0, float4 r1, bool rf) {
+        if constexpr (kPk) {  // both pools at once (lanes = pools)
+            const V2 mm = {make_float2(m[0].x, m[1].x), make_float2(m[0].y, m[1].y), make_float2(m[0].z, m[1].z)};
+            V2 mr;
+            if (rf) {
+                const float2 vxy = rf_vxy(dt, r1);
+                const float wz = wcom(r0) + r1.z;
+                const V2 v = {bc(vxy.x), bc(vxy.y), make_float2(-dt * (wz + wres[0]), -dt * (wz + wres[1]))};
+                const float2 a2 = fma2(v.z, v.z, bc(fmaf(vxy.x, vxy.x, vxy.y * vxy.y)));
+                float2 s1, s2;
+                rot_coeffs2(a2, s1, s2);
+                mr = rot2(v, s1, s2, mm);
+            } else {
+                const float2 c = make_float2(cth[0], cth[1]), sn = make_float2(sth[0], sth[1]);
+                mr = {fma2(mm.x, c, mul2(mm.y, sn)), fma2(neg2(mm.x), sn, mul2(mm.y, c)), mm.z};
+            }
+            const float2 D2 = make_float2(d2[0], d2[1]), D1 = make_float2(d1[0], d1[1]);
+            const float2 fd = make_float2(fin[0][0], fin[1][1]), fx = make_float2(fin[0][1], fin[1][0]);
+            const float2 cz = make_float2(rhoS[0] * y1[0], rhoS[1] * y1[1]);
+            const float2 ax = fma2(fx, swp(mm.x), fma2(fd, mm.x, mul2(D2, mr.x)));
+            const float2 ay = fma2(fx, swp(mm.y), fma2(fd, mm.y, mul2(D2, mr.y)));
+            const float2 az = fma2(fx, swp(mm.z), fma2(fd, mm.z, fma2(D1, mr.z, cz)));
+            if (on[0]) m[0] = make_float3(ax.x, ay.x, az.x);
+            if (on[1]) m[1] = make_float3(ax.y, ay.y, az.y);
+            return;
+        }
         float3 mr[P];
         if (rf) {
             const float2 vxy = rf_vxy(dt, r1);
@@ -470,8 +551,72 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             for (int t = 0; t < P; ++t) nl[t] = make_float3(0.f, 0.f, 0.f);
             float2 gv = make_float2(0.f, 0.f);  // dL/d(vx, vy) of the step, summed over the pools
             float2 gs = make_float2(0.f, 0.f);  // dL/dA through the bound pools' saturation
+            if constexpr (kPk) {
+                // both pools at once (lanes = pools); a pool that is off has zero
+                // relaxation, exchange and gradient coefficients (set_dt) and
+                // passes its adjoint through
+                const V2 M = {make_float2(mk[0].x, mk[1].x), make_float2(mk[0].y, mk[1].y),
+                              make_float2(mk[0].z, mk[1].z)};
+                const V2 l = {make_float2(lam[0].x, lam[1].x), make_float2(lam[0].y, lam[1].y),
+                              make_float2(lam[0].z, lam[1].z)};
+                V2 v{}, mr;
+                float2 a2 = bc(0.f), s1 = bc(0.f), s2 = bc(0.f);
+                const float2 c = make_float2(cth[0], cth[1]), sn = make_float2(sth[0], sth[1]);
+                if (rf) {
+                    v = {bc(vxy.x), bc(vxy.y), make_float2(-dt * (wz + wres[0]), -dt * (wz + wres[1]))};
+                    a2 = fma2(v.z, v.z, bc(fmaf(vxy.x, vxy.x, vxy.y * vxy.y)));
+                    rot_coeffs2(a2, s1, s2);
+                    mr = rot2(v, s1, s2, M);
+                } else {
+                    mr = {fma2(M.x, c, mul2(M.y, sn)), fma2(neg2(M.x), sn, mul2(M.y, c)), M.z};
+                }
+                // relaxation / recovery parameters
+                const float2 gd2 = fma2(l.x, mr.x, mul2(l.y, mr.y)), gd1 = mul2(l.z, mr.z);
+                const float2 t1w = fma2(gd1, make_float2(hT1[0], hT1[1]),
+                                        fma2(l.z, make_float2(hR[0], hR[1]), make_float2(wT1[0], wT1[1])));
+                const float2 t2w = fma2(gd2, make_float2(hT2[0], hT2[1]), make_float2(wT2[0], wT2[1]));
+                const float2 rw = fma2(l.z, make_float2(y1[0], y1[1]), make_float2(wrho[0], wrho[1]));
+                wT1[0] = t1w.x, wT1[1] = t1w.y, wT2[0] = t2w.x, wT2[1] = t2w.y, wrho[0] = rw.x, wrho[1] = rw.y;
+                // exchange rates: the outflow of each pool (every channel out of it)
+                // and the inflow to it from the magnetisation before the step
+                const float2 go = fma2(gd1, make_float2(e1[0], e1[1]), mul2(gd2, make_float2(e2[0], e2[1])));
+                const float2 lx = dot2(l, V2{swp(M.x), swp(M.y), swp(M.z)});  // l_t . m_other
+                if (!GM) {
+                    const float2 ls = dot2(l, M);
+                    wk[ch(0, 0)] += fmaf(ls.x, gin[0][0], go.x);
+                    wk[ch(1, 1)] += fmaf(ls.y, gin[1][1], go.y);
+                }
+                wk[ch(0, 1)] += fmaf(lx.y, gin[1][0], go.x);
+                wk[ch(1, 0)] += fmaf(lx.x, gin[0][1], go.y);
+                const float2 fd = make_float2(fin[0][0], fin[1][1]), fx = make_float2(fin[0][1], fin[1][0]);
+                V2 n2 = {fma2(fd, l.x, swp(mul2(fx, l.x))), fma2(fd, l.y, swp(mul2(fx, l.y))),
+                         fma2(fd, l.z, swp(mul2(fx, l.z)))};
+                // adjoint with respect to the rotated magnetisation
+                const float2 D2 = make_float2(d2[0], d2[1]), D1 = make_float2(d1[0], d1[1]);
+                const V2 lr = {mul2(D2, l.x), mul2(D2, l.y), mul2(D1, l.z)};
+                const V2 u = cross2(mr, lr);
+                float2 wwv = make_float2(ww[0], ww[1]);
+                if (rf) {
+                    const V2 g = jlt2(v, a2, s1, s2, u);
+                    wwv = fma2(bc(-dt), g.z, wwv);
+                    gv.x += g.x.x + g.x.y;
+                    gv.y += g.y.x + g.y.y;
+                    const V2 b = rot2(V2{neg2(v.x), neg2(v.y), neg2(v.z)}, s1, s2, lr);
+                    n2 = {add2(n2.x, b.x), add2(n2.y, b.y), add2(n2.z, b.z)};
+                } else {
+                    wwv = fma2(bc(-dt), u.z, wwv);
+                    n2.x = add2(n2.x, fma2(c, lr.x, neg2(mul2(sn, lr.y))));
+                    n2.y = add2(n2.y, fma2(sn, lr.x, mul2(c, lr.y)));
+                    n2.z = add2(n2.z, lr.z);
+                }
+                ww[0] = wwv.x, ww[1] = wwv.y;
+                const float2 off = make_float2(on[0] ? 0.f : 1.f, on[1] ? 0.f : 1.f);
+                n2 = {fma2(off, l.x, n2.x), fma2(off, l.y, n2.y), fma2(off, l.z, n2.z)};
+                nl[0] = make_float3(n2.x.x, n2.y.x, n2.z.x);
+                nl[1] = make_float3(n2.x.y, n2.y.y, n2.z.y);
+            }
 #pragma unroll
-            for (int t = 0; t < P; ++t) {
+            for (int t = 0; t < (kPk ? 0 : P); ++t) {
                 if (!on[t]) {
                     nl[t].x += lam[t].x;
                     nl[t].y += lam[t].y;
@@ -614,15 +759,15 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 const float sc = -dt * L.gyro;
                 float2 gA = make_float2(fmaf(sc, fmaf(txc.x, gv.x, txc.y * gv.y), gs.x),
                                         fmaf(sc, fmaf(txc.x, gv.y, -txc.y * gv.x), gs.y));
+                // both components in one reduction: the first exchange leaves
+                // lanes 0-15 with partial sums of x and lanes 16-31 with those
+                // of y, four more exchanges finish each half (lane 0: x, 16: y)
+                const bool hi = (lane & 16) != 0;
+                float part = hi ? gA.y : gA.x;
+                part += __shfl_xor_sync(0xffffffffu, hi ? gA.x : gA.y, 16);
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    gA.x += __shfl_xor_sync(0xffffffffu, gA.x, o);
-                    gA.y += __shfl_xor_sync(0xffffffffu, gA.y, o);
-                }
-                if (lane == 0) {
-                    rfp[(j * kWarps + warp) * 2 + 0] = gA.x;
-                    rfp[(j * kWarps + warp) * 2 + 1] = gA.y;
-                }
+                for (int o = 8; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                if ((lane & 15) == 0) rfp[(j * kWarps + warp) * 2 + (hi ? 1 : 0)] = part;
             }
         }
 #pragma unroll
