@@ -20,10 +20,12 @@ water exchanging, 8 Rx coils, 6 echoes; 32 x 8 phase/partition encodes of
   where it is built (from the reference tree, or the kernel headers staged
   into ``oracle/_ref/stage``), else the single-precision oracle port; on a
   bounded sample of the same workload (whole TRs on a subset of voxel rows).
-* ``parity``, ``reference_order``, ``batched``, ``fwd_adjoint``: the
-  full-length parity of the headline scan on a voxel subset, the reference-
-  order integrator's rate, and the metric's other two parts (config 3
-  batched vs plain, config 4 fwd+adjoint), timed in the same run.
+* ``parity``, ``reference_order``, ``batched``, ``fwd_adjoint``,
+  ``many_coil``: the full-length parity of the headline scan on a voxel
+  subset, the reference-order integrator's rate, the metric's other two
+  parts (config 3 batched vs plain, config 4 fwd+adjoint), and the 32-coil
+  MT + exchange EPI at 128 x 128 x 32 voxels (receive contraction on
+  tcgen05), timed in the same run.
 
 ``--impl reference`` times that CPU implementation alone (the reference's
 own CPU path; there is no GPU reference on this path) and prints its line.
@@ -418,13 +420,18 @@ def run_config5(args):
         "roofline": {"bound": "fp32", "kernel": "scan kernel (op table: Bloch + receive contraction)",
                      "achieved": ach, "peak": fp32_tf, "unit": "TFLOP/s", "frac": ach / fp32_tf, "traffic": None,
                      "flops_bloch": flops_bloch, "flops_receive": flops_recv,
+                     "fp32_pipe": {"frac": flops_bloch / (ms * 1e-3) / 1e12 / fp32_tf,
+                                   "note": "the Bloch integration's op-table flops alone (the receive contraction "
+                                           "runs on tcgen05 from 17 coils)"},
+                     "receive": "tcgen05 (kind::tf32, 128 coil rows x 16 sample rows per MMA, FP32 accumulator "
+                                "in tensor memory)" if 16 < rx <= 32 else "warp-level TF32 mma.sync",
                      "mufu": {"achieved": mufu / (ms * 1e-3) / 1e9, "peak": mufu_g, "unit": "Gop/s",
                               "frac": mufu / (ms * 1e-3) / 1e9 / mufu_g}},
         "clocks": clk.summary(),
     }
     if args.c5_adjoint:
         line["fwd_adjoint"] = config5_adjoint(sc, args)
-    print(json.dumps(line))
+    return line
 
 
 def config5_adjoint(sc, args):
@@ -540,7 +547,9 @@ def reference_order_rate(gpu, n_tr=32, steps=2):
 def extras(args):
     """The metric's other two parts, timed in the same run on the same GPU:
     batched vs plain (config 3's 256 CEST instances) and fwd+adjoint ms/iter
-    (config 4's bSSFP), each with fewer timed steps than the headline."""
+    (config 4's bSSFP), each with fewer timed steps than the headline; and
+    the 32-coil MT + exchange EPI (config 5's model at 128 x 128 x 32
+    voxels), whose receive contraction runs on tcgen05."""
     sub = argparse.Namespace(**vars(args))
     sub.steps = max(1, min(args.steps, 3))
     sub.warmup = 3
@@ -568,6 +577,19 @@ def extras(args):
             "checkpoint_gb": c4["config"]["checkpoint_gb"], "clocks": c4["clocks"]}
     except Exception as e:
         out["fwd_adjoint"] = {"error": repr(e)}
+    try:
+        # the 32-coil MT + exchange EPI at 1/16 of its voxels: the receive
+        # contraction on tcgen05 in the recorded line
+        sub5 = argparse.Namespace(**vars(sub))
+        sub5.c5_size, sub5.c5_adjoint = "128x128x32", False
+        c5 = run_config5(sub5)
+        out["many_coil"] = {
+            "workload": c5["config"]["workload"], "steps": sub5.steps, "ms_per_step": c5["ms_per_step"],
+            "value": c5["value"], "unit": UNIT, "e2e_value": c5["e2e"]["value"],
+            "roofline_frac": c5["roofline"]["frac"], "fp32_pipe_frac": c5["roofline"]["fp32_pipe"]["frac"],
+            "receive": c5["roofline"]["receive"], "clocks": c5["clocks"]}
+    except Exception as e:
+        out["many_coil"] = {"error": repr(e)}
     return out
 
 
@@ -681,7 +703,7 @@ def main():
         print(json.dumps(run_config4(args)))
         return
     if args.workload == "config5" and args.impl == "ours":
-        run_config5(args)
+        print(json.dumps(run_config5(args)))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
