@@ -370,7 +370,8 @@ def run_config5(args):
     torch.cuda.set_device(0)
     nx, ny, nz = (int(v) for v in args.c5_size.split("x"))
     t0 = time.perf_counter()
-    sc = phantoms.config5_mt_epi(seed=0, nx=nx, ny=ny, nz=nz)
+    spins, coils = getattr(args, "c5_spins", 4), getattr(args, "c5_coils", 32)
+    sc = phantoms.config5_mt_epi(seed=0, nx=nx, ny=ny, nz=nz, spins=spins, n_coils=coils)
     build_s = time.perf_counter() - t0
     plan = engine.Plan(sc)
     work = plan.work()
@@ -408,8 +409,9 @@ def run_config5(args):
         "metric": METRIC, "value": work["units"] / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "MT + exchange 3D EPI: %dx%dx%d voxels, 4 spins, 3 pools (free, myelin, bound "
-                               "MT), 32 Rx, 128x128 single-shot EPI at 250 kHz after an 8 ms MT pulse" % (ny, nx, nz),
+        "config": {"workload": "MT + exchange 3D EPI: %dx%dx%d voxels, %d spins, 3 pools (free, myelin, bound "
+                               "MT), %d Rx, 128x128 single-shot EPI at 250 kHz after an 8 ms MT pulse"
+                               % (ny, nx, nz, spins, coils),
                    "units_per_step": work["units"], "steps_per_scan": work["steps"], "samples": work["samples"],
                    "active_voxels": vox, "phantom_build_s": build_s,
                    "l2": "flushed between timed scans (256 MiB write); the working set (state, coil maps) "
@@ -688,6 +690,8 @@ def main():
     ap.add_argument("--vox-scale", type=float, default=1.0, help="config3: scale of the instance voxel counts")
     ap.add_argument("--c5-size", default="256x256x128", help="config5: voxels NXxNYxNZ")
     ap.add_argument("--c5-adjoint", action="store_true", help="config5: also time fwd+adjoint")
+    ap.add_argument("--c5-spins", type=int, default=4, help="config5: spins per voxel")
+    ap.add_argument("--c5-coils", type=int, default=32, help="config5: Rx coils")
     ap.add_argument("--n-tr", type=int, default=None, help="TRs of the workload (default: all)")
     ap.add_argument("--numerics", default="accurate", choices=["accurate", "reference", "exact"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")

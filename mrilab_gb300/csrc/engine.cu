@@ -457,11 +457,16 @@ struct Scanner {
     int k_layout() const { return mtc_exact ? (km_obj == KM_MT ? 2 : 3) : (mi.gm ? 1 : 0); }
 
     // the accurate kernel contracts the receive on tcgen05: 17 to 32 coils,
-    // 1, 2 or 4 threads per voxel, and an instantiation built for it
-    // (MRL_RECEIVE_TC=0 keeps the warp-level TF32 contraction, for comparison)
+    // 2 or 4 threads per voxel (64 or 32 voxels per block: the MMAs' K), and
+    // an instantiation built for it.  With one thread per voxel (K = 128) the
+    // warp-level TF32 form measured faster (MT EPI, 32 coils, 1 spin: 103 ms
+    // against 132 ms) and stays the default.  MRL_RECEIVE_TC=1 takes tcgen05
+    // wherever it can run (also with one thread per voxel), 0 never.
     bool tc_receive() const {
         const char *e = getenv("MRL_RECEIVE_TC");
         if (e && strcmp(e, "0") == 0) return false;
+        const bool force = e && strcmp(e, "1") == 0;
+        if (!force && tpv < 2) return false;
         return fast && tc_receive_ok((RX + 3) & ~3, tpv) &&
                select_fast_tc(mi.km, coef, P, NS, all_free() != 0) != nullptr;
     }

@@ -63,11 +63,12 @@ static_assert(sizeof(FastLaunch) % 4 == 0, "FastLaunch is copied to shared memor
 
 // tcgen05 receive: the coil operand has 128 rows -- Re R_c (TF32 big part),
 // Im R_c (big), Re R_c (small part), Im R_c (small) for 32 coil slots -- and
-// K = the block's voxels; the magnetisation operand has 16 rows (sample x
-// sampled pool) in four parts Re m (big), Re m (small), Im m (big), Im m
-// (small).  Both K-major with the 128-byte swizzle (tc_util.cuh).  Tensor
-// memory: 32 columns, Re m products in 0..15, Im m products in 16..31.
-constexpr int kTcRows = 128, kTcN = 16, kTcCoils = 32, kTcCols = 32;
+// K = the block's voxels; the magnetisation operand has 64 rows, 16 (sample
+// x sampled pool) in each of four parts: Re m (big), Im m (big), Re m
+// (small), Im m (small).  Both K-major with the 128-byte swizzle
+// (tc_util.cuh).  One MMA per K step (M = 128, N = 64: an MMA's cost barely
+// depends on N) into 64 tensor-memory columns, one per magnetisation row.
+constexpr int kTcRows = 128, kTcN = 16, kTcBRows = 4 * kTcN, kTcCoils = 32, kTcCols = 64;
 __host__ __device__ constexpr bool tc_receive_ok(int c4, int tpv) {
     return c4 > 16 && c4 <= kTcCoils && (tpv == 1 || tpv == 2 || tpv == 4);
 }
@@ -76,10 +77,9 @@ __host__ __device__ constexpr bool tc_receive_ok(int c4, int tpv) {
 // (also the epilogue's per-warp sums, [warp][16][32] float2)
 __host__ __device__ constexpr int tc_kv(int tpv) { return kBlock / tpv; }
 __host__ __device__ constexpr int tc_a_bytes(int tpv) { return kTcRows * tc_kv(tpv) * 4; }
-__host__ __device__ constexpr int tc_part_bytes(int tpv) { return kTcN * tc_kv(tpv) * 4; }
 __host__ __device__ constexpr int tc_b_bytes(int tpv) {
-    return 4 * tc_part_bytes(tpv) > (kBlock / 32) * kTcN * kTcCoils * 8 ? 4 * tc_part_bytes(tpv)
-                                                                        : (kBlock / 32) * kTcN * kTcCoils * 8;
+    return kTcBRows * tc_kv(tpv) * 4 > (kBlock / 32) * kTcN * kTcCoils * 8 ? kTcBRows * tc_kv(tpv) * 4
+                                                                          : (kBlock / 32) * kTcN * kTcCoils * 8;
 }
 
 // Coil sensitivities in shared memory: up to 16 coils (C4 <= 16) already
@@ -710,7 +710,6 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         tc::fence_before_sync();
         __syncthreads();
         const int kv = tc_kv(TPV);
-        const int pbytes = tc_part_bytes(TPV);
         const uint32_t tmem = tc_word[0], kmma = tc_word[1];
         __syncthreads();  // every thread has read the counter
         if (tid == 0) {
@@ -719,18 +718,12 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
             // descriptors of the operands' bases; a K step adds its byte offset / 16
             // to the start-address field (shared addresses stay below 2^18)
             const uint64_t da = tc::sw128_desc(smem_u32(TCA)), db = tc::sw128_desc(smem_u32(TCB));
-            constexpr uint32_t idesc = tc::idesc_tf32(kTcRows, kTcN);
-            for (int xy = 0; xy < 2; ++xy) {
-#pragma unroll
-                for (int bs = 0; bs < 2; ++bs) {
-                    const uint64_t dbp = db + (uint64_t)(((2 * xy + bs) * pbytes) >> 4);
+            constexpr uint32_t idesc = tc::idesc_tf32(kTcRows, kTcBRows);
 #pragma unroll 4
-                    for (int ks = 0; ks < kv / 8; ++ks) {
-                        const uint32_t ao = (uint32_t)((ks >> 2) * kTcRows * 128 + (ks & 3) * 32) >> 4;
-                        const uint32_t bo = (uint32_t)((ks >> 2) * kTcN * 128 + (ks & 3) * 32) >> 4;
-                        tc::mma_tf32(tmem + (uint32_t)(xy * kTcN), da + ao, dbp + bo, idesc, bs > 0 || ks > 0);
-                    }
-                }
+            for (int ks = 0; ks < kv / 8; ++ks) {
+                const uint32_t ao = (uint32_t)((ks >> 2) * kTcRows * 128 + (ks & 3) * 32) >> 4;
+                const uint32_t bo = (uint32_t)((ks >> 2) * kTcBRows * 128 + (ks & 3) * 32) >> 4;
+                tc::mma_tf32(tmem, da + ao, db + bo, idesc, ks > 0);
             }
             tc::mma_commit(&bar[2]);
         }
@@ -743,14 +736,18 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         tc::fence_after_sync();
         // per warp (S_x, S_y) of each (row, coil slot), S = m conj(R), over the
         // consumed tile ([warp][16][32] float2): Re R rows give (Re m, Im m)
-        // products to (x, y), Im R rows (Im m, -Re m); read 8 columns at a time
+        // products to (x, y), Im R rows (Im m, -Re m); read 8 columns of the big
+        // parts and their 8 small-part columns (32 further) at a time
         float2 *stg = reinterpret_cast<float2 *>(TCB);
         float *stw = reinterpret_cast<float *>(stg + warp * kTcN * kTcCoils + lane);
         const bool imr = (warp & 1) != 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            float d[8];
+            float d[8], e[8];
             tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(8 * q), d);
+            tc::tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(2 * kTcN + 8 * q), e);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) d[j] += e[j];
             const bool im_m = q >= 2;  // columns 16..31: Im m products
             const int comp = (im_m != imr) ? 1 : 0;
             const float sgn = (imr && !im_m) ? -1.f : 1.f;
@@ -993,13 +990,15 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                         }
                         if (rank >= 0 && sg == 0) {
                             const float bx = __uint_as_float(tf32_rn(m.x)), by = __uint_as_float(tf32_rn(m.y));
-                            const uint32_t off = tc::sw128_offset(a_fill * nsp + rank, tid / TPV, kTcN);
-                            const int pb = tc_part_bytes(TPV);
-                            unsigned char *tb = TCB + off;
-                            *reinterpret_cast<float *>(tb) = bx;
-                            *reinterpret_cast<float *>(tb + pb) = __uint_as_float(tf32_rn(m.x - bx));
-                            *reinterpret_cast<float *>(tb + 2 * pb) = by;
-                            *reinterpret_cast<float *>(tb + 3 * pb) = __uint_as_float(tf32_rn(m.y - by));
+                            // rows r, 16 + r, 32 + r, 48 + r: Re and Im, big then small
+                            const int r = a_fill * nsp + rank, kv = tid / TPV;
+                            unsigned char *tb = TCB;
+                            *reinterpret_cast<float *>(tb + tc::sw128_offset(r, kv, kTcBRows)) = bx;
+                            *reinterpret_cast<float *>(tb + tc::sw128_offset(kTcN + r, kv, kTcBRows)) = by;
+                            *reinterpret_cast<float *>(tb + tc::sw128_offset(2 * kTcN + r, kv, kTcBRows)) =
+                                __uint_as_float(tf32_rn(m.x - bx));
+                            *reinterpret_cast<float *>(tb + tc::sw128_offset(3 * kTcN + r, kv, kTcBRows)) =
+                                __uint_as_float(tf32_rn(m.y - by));
                         }
                     } else if (rank >= 0) {
                         mtile[(a_fill * nsp + rank) * kTRow + tid] = m;

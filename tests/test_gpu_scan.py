@@ -232,8 +232,9 @@ def test_config2_full_length_subset(built):
     and two FP32 evaluations of the reference algorithm that differ only in
     their transcendental functions' rounding (the reference-order integrator
     on the GPU and the kernel on the host) end 1.5e-4 apart.  The accurate
-    integrator ends 2.4e-5 from FP64: at least five times closer than the
-    reference itself, above the 1e-5 bar the short trains meet (bound 3e-5)."""
+    integrator rounds each isochromat's longitudinal state once per step
+    (increment form) and ends 8.8e-6 from FP64, inside the 1e-5 bar (three
+    roundings per step had walked to 2.4e-5)."""
     sc, g = load_golden("config2_full_length_subset")
     keep = g["sample_index"]
     P, C, A = int(sc.VObj["TypeNum"]), int(sc.VCoi["RxCoilNum"]), sc.signal_num
@@ -248,7 +249,7 @@ def test_config2_full_length_subset(built):
           f"reference order vs reference kernel {e_ro:.3e}, reference order vs FP64 {rel_l2(s_ref, g['f64_S']):.3e}; "
           f"reference kernel vs FP64 {float(g['full_ref_vs_f64']):.3e}")
     ref_err = float(g["full_ref_vs_f64"])
-    assert e64 <= 3e-5 and e64 <= 0.2 * ref_err
+    assert e64 <= 1e-5 and e64 <= 0.1 * ref_err
     # the reference-order integrator stays within the FP32 algorithm's own
     # spread around the reference kernel
     assert e_ro <= ref_err
@@ -459,20 +460,24 @@ def test_many_coil_receive_matches_fp64_oracle(built):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("spins_per_thread", ["2", "1"])
+@pytest.mark.parametrize("spins_per_thread", ["2", "1", "4"])
 def test_tcgen05_receive_mt_epi_32_coils(built, monkeypatch, spins_per_thread):
     """The receive contraction on tcgen05 (17 to 32 coils): the MT + exchange
-    EPI's model (general model, bound pool, 4 spins) with 32 Rx coils, two
-    and four threads per voxel (the voxels' spin sums are the contraction's
-    K).  Against the all-FP64 oracle (the MT EPI bound, 2e-5) and against
-    the warp-level TF32 contraction (MRL_RECEIVE_TC=0); the two results are
-    not bit-identical, so both contractions ran."""
+    EPI's model (general model, bound pool, 4 spins) with 32 Rx coils, two,
+    four and one thread(s) per voxel (the voxels' spin sums are the
+    contraction's K: 64, 32 and 128 voxels per block; the last taken on
+    tcgen05 only when asked, MRL_RECEIVE_TC=1).  Against the all-FP64 oracle
+    (the MT EPI bound, 2e-5) and against the warp-level TF32 contraction
+    (MRL_RECEIVE_TC=0); the two results are not bit-identical, so both
+    contractions ran."""
     from mrilab_gb300 import engine, phantoms
     import oracle
 
     sc = phantoms.config5_mt_epi(seed=7, nx=12, ny=12, nz=3, spins=4, n_coils=32, n_read=16, n_pe=16)
     assert int(sc.VCoi["RxCoilNum"]) == 32
     monkeypatch.setenv("MRL_SPINS_PER_THREAD", spins_per_thread)
+    if spins_per_thread == "4":
+        monkeypatch.setenv("MRL_RECEIVE_TC", "1")
     ref = oracle.run_port(sc, "f64")
     out_tc = engine.scan(sc)
     monkeypatch.setenv("MRL_RECEIVE_TC", "0")
