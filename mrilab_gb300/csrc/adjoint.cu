@@ -152,11 +152,12 @@ __device__ __forceinline__ void rot_coeffs2(float2 a2, float2 &s1, float2 &s2) {
         s2 = make_float2(c0.y, c1.y);
     }
 }
-// exp([v]x) m per lane (Rodrigues' formula, as rot_exp)
+// exp([v]x) m per lane (Rodrigues' formula, m + s1 c + s2 e as two fused
+// steps: the window recompute restarts from a checkpoint every 16 steps)
 __device__ __forceinline__ V2 rot2(const V2 &v, float2 s1, float2 s2, const V2 &m) {
     const V2 c = cross2(v, m), e = cross2(v, c);
-    return {add2(m.x, fma2(s1, c.x, mul2(s2, e.x))), add2(m.y, fma2(s1, c.y, mul2(s2, e.y))),
-            add2(m.z, fma2(s1, c.z, mul2(s2, e.z)))};
+    return {fma2(s2, e.x, fma2(s1, c.x, m.x)), fma2(s2, e.y, fma2(s1, c.y, m.y)),
+            fma2(s2, e.z, fma2(s1, c.z, m.z))};
 }
 // J_l(v)^T u per lane (jl_t)
 __device__ __forceinline__ V2 jlt2(const V2 &v, float2 a2, float2 s1, float2 s2, const V2 &u) {
@@ -286,6 +287,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     // packed two-pool path: (1 - f_tp) dt of each inflow, zero for a pool that is off
     constexpr bool kPk = P == 2 && !BOUND;
     float gin[kPk ? P : 1][kPk ? P : 1];
+    bool selfx = false;  // (packed path) some pool of the voxel exchanges with itself
     float dtc = 0.f;  // dt of these coefficients
     auto set_dt = [&](float dt) {
 #pragma unroll
@@ -323,6 +325,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 for (int p = 0; p < P; ++p) gin[t][p] = on[t] && !(GM && p == t) ? (1.f - fin[t][p]) * dt : 0.f;
             }
         }
+        if constexpr (kPk) selfx = !GM && (fin[0][0] != 0.f || fin[1][1] != 0.f);
         dtc = dt;
     };
     // ---- per-state rotation of free steps -----------------------------------
@@ -358,9 +361,14 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             const float2 D2 = make_float2(d2[0], d2[1]), D1 = make_float2(d1[0], d1[1]);
             const float2 fd = make_float2(fin[0][0], fin[1][1]), fx = make_float2(fin[0][1], fin[1][0]);
             const float2 cz = make_float2(rhoS[0] * y1[0], rhoS[1] * y1[1]);
-            const float2 ax = fma2(fx, swp(mm.x), fma2(fd, mm.x, mul2(D2, mr.x)));
-            const float2 ay = fma2(fx, swp(mm.y), fma2(fd, mm.y, mul2(D2, mr.y)));
-            const float2 az = fma2(fx, swp(mm.z), fma2(fd, mm.z, fma2(D1, mr.z, cz)));
+            float2 ax = fma2(fx, swp(mm.x), mul2(D2, mr.x));
+            float2 ay = fma2(fx, swp(mm.y), mul2(D2, mr.y));
+            float2 az = fma2(fx, swp(mm.z), fma2(D1, mr.z, cz));
+            if (selfx) {  // a pool's inflow from itself (a nonzero K diagonal)
+                ax = fma2(fd, mm.x, ax);
+                ay = fma2(fd, mm.y, ay);
+                az = fma2(fd, mm.z, az);
+            }
             if (on[0]) m[0] = make_float3(ax.x, ay.x, az.x);
             if (on[1]) m[1] = make_float3(ax.y, ay.y, az.y);
             return;
@@ -582,6 +590,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 const float2 go = fma2(gd1, make_float2(e1[0], e1[1]), mul2(gd2, make_float2(e2[0], e2[1])));
                 const float2 lx = dot2(l, V2{swp(M.x), swp(M.y), swp(M.z)});  // l_t . m_other
                 if (!GM) {
+                    // the diagonal channels: the outflow, and the inflow from itself
+                    // (its derivative (1 - f) dt is nonzero at a zero rate too)
                     const float2 ls = dot2(l, M);
                     wk[ch(0, 0)] += fmaf(ls.x, gin[0][0], go.x);
                     wk[ch(1, 1)] += fmaf(ls.y, gin[1][1], go.y);
@@ -589,8 +599,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 wk[ch(0, 1)] += fmaf(lx.y, gin[1][0], go.x);
                 wk[ch(1, 0)] += fmaf(lx.x, gin[0][1], go.y);
                 const float2 fd = make_float2(fin[0][0], fin[1][1]), fx = make_float2(fin[0][1], fin[1][0]);
-                V2 n2 = {fma2(fd, l.x, swp(mul2(fx, l.x))), fma2(fd, l.y, swp(mul2(fx, l.y))),
-                         fma2(fd, l.z, swp(mul2(fx, l.z)))};
+                V2 n2 = {swp(mul2(fx, l.x)), swp(mul2(fx, l.y)), swp(mul2(fx, l.z))};
+                if (selfx) n2 = {fma2(fd, l.x, n2.x), fma2(fd, l.y, n2.y), fma2(fd, l.z, n2.z)};
                 // adjoint with respect to the rotated magnetisation
                 const float2 D2 = make_float2(d2[0], d2[1]), D1 = make_float2(d1[0], d1[1]);
                 const V2 lr = {mul2(D2, l.x), mul2(D2, l.y), mul2(D1, l.z)};

@@ -991,14 +991,14 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                         if (rank >= 0 && sg == 0) {
                             const float bx = __uint_as_float(tf32_rn(m.x)), by = __uint_as_float(tf32_rn(m.y));
                             // rows r, 16 + r, 32 + r, 48 + r: Re and Im, big then small
-                            const int r = a_fill * nsp + rank, kv = tid / TPV;
-                            unsigned char *tb = TCB;
-                            *reinterpret_cast<float *>(tb + tc::sw128_offset(r, kv, kTcBRows)) = bx;
-                            *reinterpret_cast<float *>(tb + tc::sw128_offset(kTcN + r, kv, kTcBRows)) = by;
-                            *reinterpret_cast<float *>(tb + tc::sw128_offset(2 * kTcN + r, kv, kTcBRows)) =
-                                __uint_as_float(tf32_rn(m.x - bx));
-                            *reinterpret_cast<float *>(tb + tc::sw128_offset(3 * kTcN + r, kv, kTcBRows)) =
-                                __uint_as_float(tf32_rn(m.y - by));
+                            // (16 rows = two 1024-byte atoms further, the same swizzle)
+                            const int r = a_fill * nsp + rank;
+                            float *tb = reinterpret_cast<float *>(TCB + tc::sw128_offset(r, tid / TPV, kTcBRows));
+                            constexpr int kPartF = kTcN / 8 * 1024 / 4;  // floats between parts
+                            tb[0] = bx;
+                            tb[kPartF] = by;
+                            tb[2 * kPartF] = __uint_as_float(tf32_rn(m.x - bx));
+                            tb[3 * kPartF] = __uint_as_float(tf32_rn(m.y - by));
                         }
                     } else if (rank >= 0) {
                         mtile[(a_fill * nsp + rank) * kTRow + tid] = m;
