@@ -233,8 +233,9 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n);
  * Scope: the normal, ME, GM, MT and CEST models (GM pools free or bound,
  * MT / CEST pool 1 bound: a bound pool's saturation is differentiated
  * through its lineshape, so g_t2 of a bound pool is dL/dT2b and g_db0
- * includes the lineshape's shift; g_k in each model's own channels), one Tx
- * coil, RunMode 0, no Ext events, TypeNum <= 3, up to 32 Rx coils.
+ * includes the lineshape's shift; g_k in each model's own channels), up to
+ * 4 Tx coils (one with bound pools), RunMode 0, no Ext events,
+ * TypeNum <= 3, up to 32 Rx coils.
  * Host arrays (NULL: not wanted), V voxels, layouts as in mrl_scan_args:
  *   grad_sx, grad_sy  [P][Rx][A]   inputs
  *   g_t1, g_t2, g_rho [P][V]       dL/dT1, dL/dT2, dL/dRho (the recovery
@@ -242,9 +243,12 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n);
  *   g_db0             [V]          dL/d dB0
  *   g_k               [nK][V]      dL/dK, the model's exchange channels
  *   g_mx0, g_my0, g_mz0 [P][S][V]  dL/d(initial Mx, My, Mz)
- *   g_rf              [rf_capacity][2] dL/dRe A, dL/dIm A of every rf-on
- *                                  step in sequence order (A = rfAmp e^{i rfPhase})
- *   rf_a              [rf_capacity][2] Re A, Im A of each of those steps
+ *   g_rf              [rf_capacity][Tx][2] dL/dRe A, dL/dIm A of every
+ *                                  rf-on step in sequence order, per Tx coil
+ *                                  (A = rfAmp e^{i rfPhase} of that coil;
+ *                                  zero for a coil that is off at the step:
+ *                                  it is not part of that step's field)
+ *   rf_a              [rf_capacity][Tx][2] Re A, Im A of each of those steps
  *   rf_step_uts       [rf_capacity] the uts index of each of those steps
  *   g_rf_amp_line, g_rf_phase_line [n_rf of the sequence] dL/d VSeq.rfAmpLine
  *                                  and dL/d VSeq.rfPhaseLine: each step holds
@@ -252,7 +256,8 @@ int mrl_scan_batched(mrl_scan_args *const *args, int n);
  *                                  interval (separately for amplitude and
  *                                  phase), so each step's share goes to the
  *                                  entry it held (entries at a tie of
- *                                  magnitudes have a one-sided derivative)
+ *                                  magnitudes have a one-sided derivative);
+ *                                  each coil's share to its own entries
  * n_rf_steps receives the number of rf-on steps (g_rf, rf_a and rf_step_uts
  * are filled only if they fit rf_capacity). */
 typedef struct {

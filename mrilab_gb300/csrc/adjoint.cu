@@ -186,13 +186,15 @@ struct KSum {
 template <int P, bool GM, bool BOUND>
 __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoint_kernel(AdjLaunch L) {
     extern __shared__ __align__(16) float adj_sm[];
+    constexpr int kWarps = kAdjBlock / 32;
+    const int TXN = L.tx, RS = adjoint_record_f4(L.tx);             // Tx coils, float4 per step record
     float *win = adj_sm;                                            // [kAdjWin][3P][kAdjBlock]
-    float *rfp = adj_sm + kAdjWin * 3 * P * kAdjBlock;              // [kAdjWin][warp][2]
-    float4 *wrec = reinterpret_cast<float4 *>(rfp + kAdjWin * (kAdjBlock / 32) * 2);  // [kAdjWin][3]
-    float2 *rxs = reinterpret_cast<float2 *>(wrec + kAdjWin * 3);                     // [rx][kAdjBlock]
+    float *rfp = adj_sm + kAdjWin * 3 * P * kAdjBlock;              // [kAdjWin][warp][tx][2]
+    float4 *wrec = reinterpret_cast<float4 *>(rfp + kAdjWin * kWarps * 2 * TXN);  // [kAdjWin][RS]
+    float2 *rxs = reinterpret_cast<float2 *>(wrec + kAdjWin * RS);                // [rx][kAdjBlock]
     const int PR = P * L.rx;                                        // dL/dS values of one sample
     float2 *gbuf = rxs + L.rx * kAdjBlock;                          // [warp][2][PR]
-    constexpr int kWarps = kAdjBlock / 32;
+    float2 *txs = gbuf + kWarps * 2 * PR;                           // [tx-1][kAdjBlock] TxCoil of coils >= 1
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long iso = (long long)blockIdx.x * kAdjBlock + tid;
     const bool active = iso < L.n_iso;
@@ -242,6 +244,9 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     // this thread's receive sensitivities, read once: every ADC step uses them
     for (int c = 0; c < L.rx; ++c)
         rxs[c * kAdjBlock + tid] = (active && L.rxc) ? L.rxc[(long long)c * n + v] : make_float2(1.f, 0.f);
+    // and the further transmit coils' TxCoilmg exp(i TxCoilpe) (rf steps)
+    for (int c = 1; c < TXN; ++c)
+        txs[(c - 1) * kAdjBlock + tid] = active ? L.txc[(long long)c * n + v] : make_float2(0.f, 0.f);
     // a pool with T1, T2 or Rho zero is left alone (BlochKernel.cuh:103)
     bool on[P], bnd[P];
 #pragma unroll
@@ -336,18 +341,27 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
 #pragma unroll
         for (int t = 0; t < P; ++t) sincos_cw((wc + wres[t]) * dt, sth[t], cth[t]);
     };
-    // rotation vector of an rf step: -dt (gamma Bx, gamma By, w_t)
-    auto rf_vxy = [&](float dt, float4 r1) {
+    // rotation vector of an rf step (step j of the window): -dt (gamma Bx,
+    // gamma By, w_t), B = sum over the Tx coils of TxCoil_c A_c (a coil that
+    // is off has A_c = 0)
+    auto rf_vxy = [&](float dt, float4 r1, int j) {
         const float sc = -dt * L.gyro;
-        return make_float2(sc * (txc.x * r1.x - txc.y * r1.y), sc * (txc.x * r1.y + txc.y * r1.x));
+        float bx = fmaf(txc.x, r1.x, -txc.y * r1.y), by = fmaf(txc.x, r1.y, txc.y * r1.x);
+        for (int c = 1; c < TXN; ++c) {
+            const float2 tc = txs[(c - 1) * kAdjBlock + tid];
+            const float4 ra = wrec[RS * j + 3 + (c - 1)];
+            bx = fmaf(tc.x, ra.x, fmaf(-tc.y, ra.y, bx));
+            by = fmaf(tc.x, ra.y, fmaf(tc.y, ra.x, by));
+        }
+        return make_float2(sc * bx, sc * by);
     };
-    // one forward step, m -> F(m)
-    auto fwd = [&](float dt, float4 r0, float4 r1, bool rf) {
+    // one forward step, m -> F(m) (step j of the window)
+    auto fwd = [&](float dt, float4 r0, float4 r1, bool rf, int j) {
         if constexpr (kPk) {  // both pools at once (lanes = pools)
             const V2 mm = {make_float2(m[0].x, m[1].x), make_float2(m[0].y, m[1].y), make_float2(m[0].z, m[1].z)};
             V2 mr;
             if (rf) {
-                const float2 vxy = rf_vxy(dt, r1);
+                const float2 vxy = rf_vxy(dt, r1, j);
                 const float wz = wcom(r0) + r1.z;
                 const V2 v = {bc(vxy.x), bc(vxy.y), make_float2(-dt * (wz + wres[0]), -dt * (wz + wres[1]))};
                 const float2 a2 = fma2(v.z, v.z, bc(fmaf(vxy.x, vxy.x, vxy.y * vxy.y)));
@@ -375,7 +389,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
         }
         float3 mr[P];
         if (rf) {
-            const float2 vxy = rf_vxy(dt, r1);
+            const float2 vxy = rf_vxy(dt, r1, j);
             const float wz = wcom(r0) + r1.z;
             float wg = 0.f;
             if (BOUND) {
@@ -428,7 +442,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     // taken (the backward walk starts from it); without, every step taken
     auto recompute = [&](int nk, float *states) {
         for (int j = 0; j < nk; ++j) {
-            const float4 r0 = wrec[3 * j], r1 = wrec[3 * j + 1];
+            const float4 r0 = wrec[RS * j], r1 = wrec[RS * j + 1];
             const int flags = __float_as_int(r1.w);
             const float dt = r0.x;
             if (states) {
@@ -449,7 +463,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 if (flags & kFlagState) set_state(dt, r0);
                 cur = r0;
             }
-            if (!states || j + 1 < nk) fwd(dt, r0, r1, (flags & kFlagRf) != 0);
+            if (!states || j + 1 < nk) fwd(dt, r0, r1, (flags & kFlagRf) != 0, j);
         }
     };
 
@@ -488,7 +502,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                     if (u == w) break;
                     // window u's records, then all its steps (full windows: u < w)
                     __syncthreads();
-                    if (tid < 3 * kAdjWin) wrec[tid] = __ldg(L.rec + u * kAdjWin * 3 + tid);
+                    if (tid < RS * kAdjWin) wrec[tid] = __ldg(L.rec + u * kAdjWin * RS + tid);
                     __syncthreads();
                     recompute(kAdjWin, nullptr);
                 }
@@ -498,11 +512,12 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
         // this window's starting state
         const float *wck = L.seg > 1 ? L.ck2 + (w - wseg) * cs * L.n_iso + iso : L.ckpt + w * cs * L.n_iso + iso;
         // the window's step records, staged in shared memory
-        if (tid < 3 * nk) wrec[tid] = __ldg(L.rec + k0 * 3 + tid);
+        if (tid < RS * nk) wrec[tid] = __ldg(L.rec + k0 * RS + tid);
         __syncthreads();
         // dL/dS of the window's last step (the first one the backward walk
         // takes), fetched while the states are recomputed
-        if (__float_as_int(wrec[3 * (nk - 1) + 2].x) >= 0) prefetch_g(__float_as_int(wrec[3 * (nk - 1) + 2].x), (nk - 1) & 1);
+        if (__float_as_int(wrec[RS * (nk - 1) + 2].x) >= 0)
+            prefetch_g(__float_as_int(wrec[RS * (nk - 1) + 2].x), (nk - 1) & 1);
         // recompute the window's states (before each step) into shared memory
         if (active) {
 #pragma unroll
@@ -518,11 +533,11 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
         for (int i = 0; i < P * P; ++i) wk[i] = 0.f;
         // the coefficients in registers are those of the window's last step
         for (int j = nk - 1; j >= 0; --j) {
-            const float4 r0 = wrec[3 * j], r1 = wrec[3 * j + 1], r2 = wrec[3 * j + 2];
+            const float4 r0 = wrec[RS * j], r1 = wrec[RS * j + 1], r2 = wrec[RS * j + 2];
             const int flags = __float_as_int(r1.w);
             const float dt = r0.x;
             if (j < nk - 1) {  // coefficients of step j, if step j + 1 changed them
-                const int fn = __float_as_int(wrec[3 * j + 4].w);
+                const int fn = __float_as_int(wrec[RS * (j + 1) + 1].w);
                 if (fn & kFlagDt) set_dt(dt);
                 if (fn & kFlagState) set_state(dt, r0);
                 if (fn & (kFlagDt | kFlagState)) cur = r0;
@@ -531,7 +546,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             // buffer step j + 1 read, once every lane of the warp is done with it
             bool pend = false;
             if (j >= 1) {
-                const int an = __float_as_int(wrec[3 * (j - 1) + 2].x);
+                const int an = __float_as_int(wrec[RS * (j - 1) + 2].x);
                 if (an >= 0) {
                     __syncwarp();
                     prefetch_g(an, (j - 1) & 1);
@@ -547,7 +562,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             float2 vxy = make_float2(0.f, 0.f);
             float wz = 0.f, wg = 0.f;
             if (rf) {
-                vxy = rf_vxy(dt, r1);
+                vxy = rf_vxy(dt, r1, j);
                 wz = wcom(r0) + r1.z;
                 if (BOUND) {
                     lineshapes(r1.z);
@@ -767,17 +782,20 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             // share, summed over the warp
             if (rf) {
                 const float sc = -dt * L.gyro;
-                float2 gA = make_float2(fmaf(sc, fmaf(txc.x, gv.x, txc.y * gv.y), gs.x),
-                                        fmaf(sc, fmaf(txc.x, gv.y, -txc.y * gv.x), gs.y));
-                // both components in one reduction: the first exchange leaves
-                // lanes 0-15 with partial sums of x and lanes 16-31 with those
-                // of y, four more exchanges finish each half (lane 0: x, 16: y)
-                const bool hi = (lane & 16) != 0;
-                float part = hi ? gA.y : gA.x;
-                part += __shfl_xor_sync(0xffffffffu, hi ? gA.x : gA.y, 16);
+                for (int c = 0; c < TXN; ++c) {  // dB/dA_c = TxCoil_c
+                    const float2 tc = c == 0 ? txc : txs[(c - 1) * kAdjBlock + tid];
+                    float2 gA = make_float2(sc * fmaf(tc.x, gv.x, tc.y * gv.y), sc * fmaf(tc.x, gv.y, -tc.y * gv.x));
+                    if (c == 0) gA = make_float2(gA.x + gs.x, gA.y + gs.y);
+                    // both components in one reduction: the first exchange leaves
+                    // lanes 0-15 with partial sums of x and lanes 16-31 with those
+                    // of y, four more exchanges finish each half (lane 0: x, 16: y)
+                    const bool hi = (lane & 16) != 0;
+                    float part = hi ? gA.y : gA.x;
+                    part += __shfl_xor_sync(0xffffffffu, hi ? gA.x : gA.y, 16);
 #pragma unroll
-                for (int o = 8; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-                if ((lane & 15) == 0) rfp[(j * kWarps + warp) * 2 + (hi ? 1 : 0)] = part;
+                    for (int o = 8; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                    if ((lane & 15) == 0) rfp[((j * kWarps + warp) * TXN + c) * 2 + (hi ? 1 : 0)] = part;
+                }
             }
         }
 #pragma unroll
@@ -792,16 +810,18 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
         // the window's rf gradients, summed over the block, into their FP64 slots
         __syncthreads();
         if (tid < nk) {
-            const int ri = __float_as_int(wrec[3 * tid + 2].y);
-            if (ri >= 0 && (__float_as_int(wrec[3 * tid + 1].w) & kFlagRf)) {
-                float gx = 0.f, gy = 0.f;
+            const int ri = __float_as_int(wrec[RS * tid + 2].y);
+            if (ri >= 0 && (__float_as_int(wrec[RS * tid + 1].w) & kFlagRf)) {
+                for (int c = 0; c < TXN; ++c) {  // slots [rf step][coil][re, im]
+                    float gx = 0.f, gy = 0.f;
 #pragma unroll
-                for (int q = 0; q < kWarps; ++q) {
-                    gx += rfp[(tid * kWarps + q) * 2 + 0];
-                    gy += rfp[(tid * kWarps + q) * 2 + 1];
+                    for (int q = 0; q < kWarps; ++q) {
+                        gx += rfp[((tid * kWarps + q) * TXN + c) * 2 + 0];
+                        gy += rfp[((tid * kWarps + q) * TXN + c) * 2 + 1];
+                    }
+                    atomicAdd(&L.grf[2 * ((long long)ri * TXN + c)], (double)gx);
+                    atomicAdd(&L.grf[2 * ((long long)ri * TXN + c) + 1], (double)gy);
                 }
-                atomicAdd(&L.grf[2 * ri], (double)gx);
-                atomicAdd(&L.grf[2 * ri + 1], (double)gy);
             }
         }
         __syncthreads();
@@ -841,7 +861,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
 
 template <int P, bool GM, bool BOUND = false>
 cudaError_t go(const AdjLaunch &L, cudaStream_t st) {
-    const size_t smem = adjoint_smem_bytes(P, L.rx);
+    const size_t smem = adjoint_smem_bytes(P, L.rx, L.tx);
     auto k = adjoint_kernel<P, GM, BOUND>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -181,8 +181,10 @@ void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx, double gyro
                 si.freq[c] = c < tx ? s.rf_freq[c] : 0.0;
             }
             si.adc = s.adc == 1 ? s.signali : -1;
-            si.amp_src = s.rf_amp_src[0];
-            si.phase_src = s.rf_phase_src[0];
+            for (int c = 0; c < kMaxTx; ++c) {
+                si.amp_src[c] = c < tx ? s.rf_amp_src[c] : -1;
+                si.phase_src[c] = c < tx ? s.rf_phase_src[c] : -1;
+            }
             out.steps.push_back(si);
             bool rf_on = false;
             for (int c = 0; c < tx; ++c) rf_on |= (float)s.rf_amp[c] != 0.f;

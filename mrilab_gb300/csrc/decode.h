@@ -48,7 +48,8 @@ struct StepInfo {
     double dt, gz, gy, gx;
     double amp[kMaxTx], phase[kMaxTx], freq[kMaxTx];
     int adc;  // ADC sample index, or -1
-    int amp_src, phase_src;  // Tx coil 1: source entries of amp and phase (-1: none)
+    // per Tx coil: the rfAmpLine / rfPhaseLine entries held (-1: none)
+    int amp_src[kMaxTx], phase_src[kMaxTx];
 };
 
 struct DecodeChunk {

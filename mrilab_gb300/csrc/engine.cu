@@ -2026,9 +2026,12 @@ struct mrl_adjoint_plan {
     mrl::DevBuf<float2> d_gs;
     mrl::DevBuf<double> d_rf;
     mrl::AdjLaunch L{};
-    std::vector<int> rf_uts, rf_src;  // per rf step: uts index; rfAmpLine, rfPhaseLine entries held
-    std::vector<double> rf_a;         // per rf step: Re A, Im A
-    int P = 0, S = 0, RX = 0, A = 0, n_rf = 0, ck_every = 0;
+    // per rf step: uts index; per rf step and Tx coil: the rfAmpLine and
+    // rfPhaseLine entries held (-1: none or the coil is off), Re A and Im A,
+    // whether the coil is on
+    std::vector<int> rf_uts, rf_src, rf_on;
+    std::vector<double> rf_a;
+    int P = 0, S = 0, RX = 0, A = 0, TX = 1, n_rf = 0, ck_every = 0;
     long long V = 0, n_iso = 0, N = 0, ck_bytes = 0;
     double rf_ref = 0;
     bool forward_done = false, backward_done = false;
@@ -2057,7 +2060,7 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     const bool mtc = sc.mi.km == KM_MT || sc.mi.km == KM_CEST;
     if (!(sc.mi.km == KM_NORMAL || sc.mi.km == KM_EXCH || mtc))
         return set_err("unknown model for the adjoint"), MRL_ERR_UNSUPPORTED;
-    if (sc.TX != 1) return set_err("the adjoint supports one Tx coil"), MRL_ERR_UNSUPPORTED;
+    if (sc.TX > 4) return set_err("the adjoint supports up to 4 Tx coils"), MRL_ERR_UNSUPPORTED;
     if (sc.P > 3) return set_err("the adjoint supports TypeNum <= 3"), MRL_ERR_UNSUPPORTED;
     if (mtc && sc.P < 2) return set_err("the MT / CEST adjoint needs the bound pool"), MRL_ERR_UNSUPPORTED;
     if (sc.RX > 32) return set_err("the adjoint supports up to 32 Rx coils"), MRL_ERR_UNSUPPORTED;
@@ -2072,13 +2075,17 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
         if (bound == (1u << sc.P) - 1) return set_err("the adjoint needs a free pool"), MRL_ERR_UNSUPPORTED;
     }
     if (mtc) bound = 1u << 1;
-    const int P = sc.P, S = sc.S, RX = sc.RX, A = sc.A;
+    if (bound && sc.TX > 1)
+        return set_err("the adjoint with bound pools supports one Tx coil"), MRL_ERR_UNSUPPORTED;
+    const int P = sc.P, S = sc.S, RX = sc.RX, A = sc.A, TX = sc.TX;
+    p->TX = TX;
     p->P = P, p->S = S, p->RX = RX, p->A = A, p->V = sc.V;
     p->rf_ref = args->var.rf_ref ? *args->var.rf_ref : 0.0;
     // step records of the adjoint
     const long long N = ch.n_steps;
     p->N = N;
-    std::vector<float4> rec((size_t)std::max<long long>(1, N) * 3);
+    const int RS = adjoint_record_f4(TX);
+    std::vector<float4> rec((size_t)std::max<long long>(1, N) * RS);
     std::vector<int> step_uts((size_t)std::max<long long>(1, N), -1);
     for (size_t j = 0; j < ch.point_uts.size(); ++j)
         if (ch.point_dt[j] > 0) step_uts[ch.point_step[j]] = ch.point_uts[j];
@@ -2086,7 +2093,14 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     float last_dt = -1.f, lgx = 0.f, lgy = 0.f, lgz = 0.f;
     for (long long q = 0; q < N; ++q) {
         const StepInfo &si = ch.steps[q];
-        const bool rf = (float)si.amp[0] != 0.f;
+        // an rf step: some Tx coil on; its frequency term sums the coils that are on
+        bool rf = false;
+        double wrf = 0;
+        for (int c = 0; c < TX; ++c)
+            if ((float)si.amp[c] != 0.f) {
+                rf = true;
+                wrf += 2 * kPiRef * si.freq[c];
+            }
         int flags = rf ? kFlagRf : 0;
         const float fdt = (float)si.dt, fgx = (float)si.gx, fgy = (float)si.gy, fgz = (float)si.gz;
         if (fdt != last_dt) flags |= kFlagDt;
@@ -2095,22 +2109,29 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
         float4 r1;
         r1.x = (float)(si.amp[0] * std::cos(si.phase[0]));
         r1.y = (float)(si.amp[0] * std::sin(si.phase[0]));
-        r1.z = (float)(2 * kPiRef * si.freq[0]);
+        r1.z = (float)wrf;
         std::memcpy(&r1.w, &flags, sizeof(int));
         const int ri = rf ? p->n_rf++ : -1;
-        if (rf) {
+        if (rf) {  // per coil: A, and the line entries it came from (-1: the coil is off)
             p->rf_uts.push_back(step_uts[q]);
-            p->rf_a.push_back(si.amp[0] * std::cos(si.phase[0]));
-            p->rf_a.push_back(si.amp[0] * std::sin(si.phase[0]));
-            p->rf_src.push_back(si.amp_src);
-            p->rf_src.push_back(si.phase_src);
+            for (int c = 0; c < TX; ++c) {
+                const bool on = (float)si.amp[c] != 0.f;
+                p->rf_a.push_back(si.amp[c] * std::cos(si.phase[c]));
+                p->rf_a.push_back(si.amp[c] * std::sin(si.phase[c]));
+                p->rf_src.push_back(on ? si.amp_src[c] : -1);
+                p->rf_src.push_back(on ? si.phase_src[c] : -1);
+                p->rf_on.push_back(on ? 1 : 0);
+            }
         }
         float4 r2 = make_float4(0.f, 0.f, 0.f, 0.f);
         std::memcpy(&r2.x, &si.adc, sizeof(int));
         std::memcpy(&r2.y, &ri, sizeof(int));
-        rec[q * 3 + 0] = make_float4((float)si.dt, (float)si.gz, (float)si.gy, (float)si.gx);
-        rec[q * 3 + 1] = r1;
-        rec[q * 3 + 2] = r2;
+        rec[q * RS + 0] = make_float4((float)si.dt, (float)si.gz, (float)si.gy, (float)si.gx);
+        rec[q * RS + 1] = r1;
+        rec[q * RS + 2] = r2;
+        for (int c = 1; c < TX; ++c)
+            rec[q * RS + 2 + c] = make_float4((float)(si.amp[c] * std::cos(si.phase[c])),
+                                              (float)(si.amp[c] * std::sin(si.phase[c])), 0.f, 0.f);
     }
     const int n = std::max(1, sc.n_act);
     const long long n_iso = (long long)sc.n_act * S;
@@ -2134,7 +2155,7 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     if (e == cudaSuccess) e = p->d_ck2.ensure((size_t)std::max(1LL, (M > 1 ? M : 0) * 3 * P * n_iso));
     if (e == cudaSuccess) e = p->d_g.ensure((size_t)nf * std::max(1LL, n_iso));
     if (e == cudaSuccess) e = p->d_gs.ensure((size_t)P * RX * std::max(A, 1));
-    if (e == cudaSuccess) e = p->d_rf.ensure((size_t)2 * std::max(1, p->n_rf));
+    if (e == cudaSuccess) e = p->d_rf.ensure((size_t)2 * TX * std::max(1, p->n_rf));
     if (e == cudaSuccess && mtc) {
         e = p->d_kgm.ensure((size_t)P * P * std::max(1, sc.n_act));
         if (e == cudaSuccess)
@@ -2149,6 +2170,7 @@ int mrl_adjoint_plan_create(const mrl_scan_args *args, mrl_adjoint_plan **out) {
     L.n_act = sc.n_act;
     L.S = S;
     L.rx = RX;
+    L.tx = TX;
     L.A = std::max(A, 1);
     L.exch_gm = (sc.mi.gm || mtc) ? 1 : 0;
     L.bound = bound;
@@ -2280,17 +2302,22 @@ int mrl_adjoint_plan_gradients(mrl_adjoint_plan *p, mrl_adjoint_args *adj) {
             }
         }
     }
+    // a coil that is off at an rf step is not part of its field: no gradient
+    const int TX = p->TX;
+    for (int i = 0; i < n_rf * TX; ++i)
+        if (!p->rf_on[i]) grf[2 * i] = grf[2 * i + 1] = 0.0;
     if (n_rf <= adj->rf_capacity) {
-        if (adj->g_rf) std::copy(grf.begin(), grf.begin() + 2 * n_rf, adj->g_rf);
+        if (adj->g_rf) std::copy(grf.begin(), grf.begin() + 2 * (size_t)n_rf * TX, adj->g_rf);
         if (adj->rf_step_uts) std::copy(p->rf_uts.begin(), p->rf_uts.end(), adj->rf_step_uts);
         if (adj->rf_a) std::copy(p->rf_a.begin(), p->rf_a.end(), adj->rf_a);
     }
     // onto the waveform lines: A = a e^{i phi} with a = rfAmpLine[ja] (a
-    // negative a is the same A as |a| at phi + pi), phi = rfPhaseLine[jp]
+    // negative a is the same A as |a| at phi + pi), phi = rfPhaseLine[jp];
+    // each coil's entries are its own (rfCoilLine)
     const int n_line = args->seq.n_rf;
     if (adj->g_rf_amp_line) std::fill(adj->g_rf_amp_line, adj->g_rf_amp_line + n_line, 0.0);
     if (adj->g_rf_phase_line) std::fill(adj->g_rf_phase_line, adj->g_rf_phase_line + n_line, 0.0);
-    for (int i = 0; i < n_rf; ++i) {
+    for (int i = 0; i < n_rf * TX; ++i) {
         const double gx = grf[2 * i], gy = grf[2 * i + 1], ax = p->rf_a[2 * i], ay = p->rf_a[2 * i + 1];
         const int ja = p->rf_src[2 * i], jp = p->rf_src[2 * i + 1];
         if (adj->g_rf_amp_line && ja >= 0 && ja < n_line) {

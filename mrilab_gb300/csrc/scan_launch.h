@@ -102,11 +102,13 @@ cudaError_t launch_exact_table(int P, const float *dts, int n_dt, int n_act, int
 // ---- adjoint (adjoint.cu) ----------------------------------------------------
 constexpr int kAdjBlock = 128;  // threads (isochromats) per block
 
-// Step record of the adjoint: {dt, Gz, Gy, Gx}, {Re A, Im A, 2 pi f_rf,
-// flags (kFlagRf, kFlagState, kFlagDt)}, {ADC sample (int bits) or -1, rf
-// step index (int bits) or -1, 0, 0}.
+// Step record of the adjoint: {dt, Gz, Gy, Gx}, {Re A_0, Im A_0, 2 pi times
+// the sum of the active Tx coils' rf frequencies, flags (kFlagRf, kFlagState,
+// kFlagDt)}, {ADC sample (int bits) or -1, rf step index (int bits) or -1,
+// 0, 0}, then {Re A_c, Im A_c, 0, 0} for every further Tx coil c.
 struct AdjLaunch {
     int n_act, S, rx, A, exch_gm;
+    int tx;  // Tx coils (txc: [tx][n_act]; records adjoint_record_f4(tx) float4; grf [n_rf][tx][2])
     unsigned bound;  // GM bound pools (TypeFlag 1), one bit per pool
     // MT / CEST (pool 1 bound, kch remapped to the GM layout): a free pool's
     // transverse magnetisation does not flow out to the bound pool, and only
@@ -119,22 +121,27 @@ struct AdjLaunch {
     const float *kch;                    // [P*P][n_act] exchange channels, or null
     const float *dwrnd;                  // [P][S][n_act]
     const float2 *rxc;                   // [rx][n_act], null: the default coil
-    const float2 *txc;                   // [n_act] TxCoilmg exp(i TxCoilpe)
+    const float2 *txc;                   // [tx][n_act] TxCoilmg exp(i TxCoilpe)
     float cs2pi[kMaxPool];
-    const float4 *rec;                   // [n_steps][3]
+    const float4 *rec;                   // [n_steps][adjoint_record_f4(tx)]
     long long n_steps;
     const float *ckpt;                   // [slot][3P][n_iso], every seg windows, written by the forward scan
     int seg;                             // windows (of kAdjWin steps) per stored checkpoint
     float *ck2;                          // seg > 1: [seg][3P][n_iso] the current segment's window checkpoints
     const float2 *gsig;                  // [A][P][rx] dL/dSx + i dL/dSy, one sample's values together
     float *giso;                         // [fields][n_iso]: T1[P] T2[P] Rho[P] dB0 K[P*P] Mx0[P] My0[P] Mz0[P]
-    double *grf;                         // [n_rf][2]
+    double *grf;                         // [n_rf][tx][2]
 };
-// window states, rf partials, window records, the block's receive
-// sensitivities, and per warp two buffers of one sample's dL/dS
-inline size_t adjoint_smem_bytes(int P, int rx) {
-    return (size_t)kAdjWin * 3 * P * kAdjBlock * 4 + (size_t)kAdjWin * (kAdjBlock / 32) * 2 * 4 +
-           (size_t)kAdjWin * 3 * 16 + (size_t)rx * kAdjBlock * 8 + (size_t)(kAdjBlock / 32) * 2 * P * rx * 8;
+// float4 of an adjoint step record: the three above, then {Re A_c, Im A_c,
+// 0, 0} for every further Tx coil c
+__host__ __device__ inline int adjoint_record_f4(int tx) { return 2 + tx; }
+// window states, rf partials (per Tx coil), window records, the block's
+// receive sensitivities, per warp two buffers of one sample's dL/dS, and the
+// further Tx coils' sensitivities
+inline size_t adjoint_smem_bytes(int P, int rx, int tx) {
+    return (size_t)kAdjWin * 3 * P * kAdjBlock * 4 + (size_t)kAdjWin * (kAdjBlock / 32) * 2 * tx * 4 +
+           (size_t)kAdjWin * adjoint_record_f4(tx) * 16 + (size_t)rx * kAdjBlock * 8 +
+           (size_t)(kAdjBlock / 32) * 2 * P * rx * 8 + (size_t)(tx - 1) * kAdjBlock * 8;
 }
 inline int adjoint_fields(int P) { return 3 * P + 1 + P * P + 3 * P; }
 cudaError_t launch_adjoint(int P, const AdjLaunch &L, cudaStream_t st);

@@ -373,10 +373,12 @@ def _adjoint_outputs(sc, rf_capacity: Optional[int]):
     if rf_capacity is None:
         rf_capacity = int(np.count_nonzero(np.diff(sc.VSeq["utsLine"]) > 0))
     n_line = max(int(np.size(sc.VSeq["rfAmpLine"])), 1)
+    tx = int(sc.VCoi["TxCoilNum"])
+    rf_shape = (max(rf_capacity, 1), 2) if tx == 1 else (max(rf_capacity, 1), tx, 2)  # [step][coil][re, im]
     out = dict(T1=np.zeros(P * V, np.float32), T2=np.zeros(P * V, np.float32), Rho=np.zeros(P * V, np.float32),
                dB0=np.zeros(V, np.float32), Mx0=np.zeros(P * S * V, np.float32),
                My0=np.zeros(P * S * V, np.float32), Mz0=np.zeros(P * S * V, np.float32),
-               rf=np.zeros((max(rf_capacity, 1), 2)), rf_a=np.zeros((max(rf_capacity, 1), 2)),
+               rf=np.zeros(rf_shape), rf_a=np.zeros(rf_shape),
                rf_uts=np.zeros(max(rf_capacity, 1), np.int32),
                rf_amp_line=np.zeros(n_line), rf_phase_line=np.zeros(n_line))
     if "K" in o:
@@ -403,9 +405,10 @@ def adjoint(sc, grad_sx, grad_sy, gpu_index: int = 0, rf_capacity: Optional[int]
     """``mrl_adjoint``: gradients of a loss L of the signal of ``sc`` given
     dL/dSx, dL/dSy (flat [P][Rx][A]).  Returns T1, T2, Rho ([P*V]), dB0
     ([V]), K ([nK*V], exchange models), Mx0/My0/Mz0 ([P*S*V]), rf ([n_rf, 2]:
-    dL/dRe A, dL/dIm A per rf-on step), rf_a (their A), rf_uts (their uts
-    indices) and rf_amp_line, rf_phase_line (dL/d VSeq.rfAmpLine and
-    dL/d VSeq.rfPhaseLine)."""
+    dL/dRe A, dL/dIm A per rf-on step; [n_rf, Tx, 2] per Tx coil with
+    several, zero for a coil that is off at that step), rf_a (their A),
+    rf_uts (their uts indices) and rf_amp_line, rf_phase_line (dL/d
+    VSeq.rfAmpLine and dL/d VSeq.rfPhaseLine, each coil's entries)."""
     lib = library()
     lib.mrl_adjoint.argtypes = [ctypes.POINTER(ScanArgs), ctypes.POINTER(AdjointArgs)]
     lib.mrl_adjoint.restype = ctypes.c_int

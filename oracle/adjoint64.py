@@ -15,7 +15,11 @@ the same step list.  The autograd graph holds every step: small cases only.
 Models: normal, ME and GM (GM pools of TypeFlag 0 and 1) as the adjoint
 kernel covers them, and MT and CEST (``BlochKernelMT.cuh:180-411``,
 ``BlochKernelCEST.cuh:280-606``: pool 0 free water, pool 1 the bound pool,
-CEST pools exchanging with pool 0); one transmit coil.
+CEST pools exchanging with pool 0).  Several transmit coils (free-pool
+models): an rf step's field is the sum over the coils that are on of
+TxCoil_c A_c and its frequency term the sum of their frequencies
+(``BlochKernel.h:57-122``; the port's ``rotate``); the rf gradient is per
+step and coil.
 """
 from __future__ import annotations
 
@@ -110,16 +114,18 @@ def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
     """dL/dtheta of L = sum(grad_sx * Sx + grad_sy * Sy) over the scan's
     signal (so its gradient is the adjoint's for those dL/dS), in the
     adjoint's layouts: T1, T2, Rho [P*V], dB0 [V], K [nK*V], Mx0, My0, Mz0
-    [P*S*V], rf [n_rf, 2] (dL/dRe A, dL/dIm A of each rf-on step), plus
-    Sx, Sy (the signal of the restated map)."""
+    [P*S*V], rf [n_rf, 2] (dL/dRe A, dL/dIm A of each rf-on step; [n_rf,
+    Tx, 2] with several Tx coils), plus Sx, Sy (the signal of the restated
+    map)."""
     o, mag, coil, ctl = sc.VObj, sc.VMag, sc.VCoi, sc.VCtl
     model = sc.model
     if model not in ("normal", "me", "gm", "mt", "cest"):
         raise ValueError("unknown model")
     P, S = int(o["TypeNum"]), int(o["SpinNum"])
     TX, RX = int(coil["TxCoilNum"]), int(coil["RxCoilNum"])
-    if TX != 1:
-        raise ValueError("one transmit coil")
+    if TX > 1 and (model in ("mt", "cest") or
+                   (model == "gm" and np.any(np.asarray(o["TypeFlag"], np.float64).ravel() == 1))):
+        raise ValueError("several transmit coils: free-pool models only")
     A = int(sc.VSig["SignalNum"])
     V = int(np.asarray(o["Rho"]).size // P)
     gyro = float(o["Gyro"])
@@ -139,14 +145,20 @@ def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
     My0 = leaf(_flat(o["My"]).reshape(P, S, V))
     Mz0 = leaf(_flat(o["Mz"]).reshape(P, S, V))
     rf_on = rec[:, 7] != 0
-    amp, ph = rec[rf_on, 4], rec[rf_on, 5]
-    rfa = leaf(np.stack([amp * np.cos(ph), amp * np.sin(ph)], 1))
+    # per rf step and coil: amplitude, phase, frequency (coil 0 in columns
+    # 4-6, coil c >= 1 in 10 + 3 (c - 1) ...)
+    cols = [(4, 5, 6)] + [(10 + 3 * (c - 1), 11 + 3 * (c - 1), 12 + 3 * (c - 1)) for c in range(1, TX)]
+    amp = np.stack([rec[rf_on, ca] for ca, _, _ in cols], 1)  # [n_rf, TX]
+    ph = np.stack([rec[rf_on, cp] for _, cp, _ in cols], 1)
+    frq = np.stack([rec[rf_on, cf] for _, _, cf in cols], 1)
+    rfa = leaf(np.stack([amp * np.cos(ph), amp * np.sin(ph)], 2))  # [n_rf, TX, 2]
 
     t = lambda a: torch.tensor(a, dtype=torch.float64)
     dwr = t(_flat(mag["dWRnd"]).reshape(P, S, V))
     gzg, gyg, gxg = (t(_flat(mag[k])) for k in ("Gzgrid", "Gygrid", "Gxgrid"))
-    mg, pe = t(_flat(coil["TxCoilmg"])[:V]), t(_flat(coil["TxCoilpe"])[:V])
-    txc_re, txc_im = mg * torch.cos(pe), mg * torch.sin(pe)
+    mg_all, pe_all = t(_flat(coil["TxCoilmg"]).reshape(-1, V)), t(_flat(coil["TxCoilpe"]).reshape(-1, V))
+    mg, pe = mg_all[0], pe_all[0]
+    txc_re_all, txc_im_all = mg_all * torch.cos(pe_all), mg_all * torch.sin(pe_all)  # [TX, V]
     if float(coil["RxCoilDefault"]) == 0:
         rxr, rxi = t(_flat(coil["RxCoilx"]).reshape(RX, V)), t(_flat(coil["RxCoily"]).reshape(RX, V))
     else:
@@ -174,7 +186,7 @@ def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
     cr, sr = np.cos(-rf_ref), np.sin(-rf_ref)
     ri = 0
     for r in rec:
-        dt, gz, gy, gx, _, _, freq, rf_sum, adc, sidx = (float(q) for q in r)
+        dt, gz, gy, gx, _, _, freq, rf_sum, adc, sidx = (float(q) for q in r[:10])
         if adc and int(sidx) < A:
             # receive before the step: sum over spins and voxels of m conj(R_c)
             for tp in range(P):
@@ -193,11 +205,22 @@ def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
             + (gzg * (gz * gyro) + gyg * (gy * gyro) + gxg * (gx * gyro))[None, None]
         rf = rf_sum != 0
         if rf:
-            Ar, Ai = rfa[ri, 0], rfa[ri, 1]
+            # the field of the coils that are on (TX = 1: coil 0, on whenever rf is)
+            bre = torch.zeros(V, dtype=torch.float64)
+            bim = torch.zeros(V, dtype=torch.float64)
+            fsum = 0.0
+            for c in range(TX):
+                if TX > 1 and amp[ri, c] == 0:
+                    continue
+                Arc, Aic = rfa[ri, c, 0], rfa[ri, c, 1]
+                bre = bre + txc_re_all[c] * Arc - txc_im_all[c] * Aic
+                bim = bim + txc_re_all[c] * Aic + txc_im_all[c] * Arc
+                fsum += float(frq[ri, c])
+            Ar, Ai = rfa[ri, 0, 0], rfa[ri, 0, 1]
             ri += 1
-            vx = (-dt * gyro) * (txc_re * Ar - txc_im * Ai)
-            vy = (-dt * gyro) * (txc_re * Ai + txc_im * Ar)
-            vz = -dt * (w + 2 * PI * freq)
+            vx = (-dt * gyro) * bre
+            vy = (-dt * gyro) * bim
+            vz = -dt * (w + 2 * PI * fsum)
             xr, yr, zr = _rotate(X, Y, Z, vx[None, None].expand_as(X), vy[None, None].expand_as(X), vz)
         else:
             zero = torch.zeros_like(X)
@@ -252,7 +275,8 @@ def gradients(sc, grad_sx, grad_sy) -> Dict[str, np.ndarray]:
         return np.zeros(0) if x is None or x.grad is None else x.grad.numpy().ravel().copy()
 
     out = dict(T1=g(T1), T2=g(T2), Rho=g(Rho), dB0=g(dB0), Mx0=g(Mx0), My0=g(My0), Mz0=g(Mz0),
-               rf=rfa.grad.numpy().copy() if rfa.grad is not None else np.zeros((0, 2)),
+               rf=(rfa.grad.numpy().copy() if rfa.grad is not None else np.zeros((0, TX, 2))) if TX > 1 else
+               (rfa.grad.numpy()[:, 0].copy() if rfa.grad is not None else np.zeros((0, 2))),
                Sx=sig_x.numpy().ravel(), Sy=sig_y.numpy().ravel())
     if has_k:
         out["K"] = g(K)

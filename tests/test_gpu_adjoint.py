@@ -214,7 +214,7 @@ def test_adjoint_two_level_checkpoints(built, monkeypatch):
             assert err <= 1e-4
 
 
-@pytest.mark.parametrize("case", ["gre", "me3", "gm_bound", "bssfp", "mt", "cest3"])
+@pytest.mark.parametrize("case", ["gre", "me3", "gm_bound", "bssfp", "mt", "cest3", "tx2", "tx3"])
 def test_adjoint_vs_fp64_adjoint(built, case):
     """The FP32 adjoint kernel against the FP64 reference gradient
     (oracle.adjoint64: the oracle's map in float64, differentiated by
@@ -233,7 +233,10 @@ def test_adjoint_vs_fp64_adjoint(built, case):
           # 0 received
           "mt": lambda: phantoms.small_multipool("mt", seed=45, n=4, pools=2, spins=2, coils=2, n_tr=2, seq="sat"),
           "cest3": lambda: phantoms.small_multipool("cest", seed=46, n=4, pools=3, spins=1, coils=2, n_tr=2,
-                                                    seq="sat")}[case]()
+                                                    seq="sat"),
+          # several transmit coils: B = sum of TxCoil_c A_c, the rf gradient per coil
+          "tx2": lambda: phantoms.multi_tx_gre(seed=47, n=6, n_tr=2, tx_coils=2, rx_coils=2),
+          "tx3": lambda: phantoms.multi_tx_gre(seed=48, n=6, n_tr=2, tx_coils=3, rx_coils=3)}[case]()
     sc = _phase_modulated(sc, 12)
     tx, ty = _target(sc)
     _, gx, gy = _loss(sc, (tx, ty))
@@ -255,6 +258,52 @@ def test_adjoint_vs_fp64_adjoint(built, case):
     err = float(np.linalg.norm(g["rf"] - ref["rf"]) / np.linalg.norm(ref["rf"]))
     print(f"{case} rf: relative error {err:.2e} over {ref['rf'].shape[0]} steps")
     assert err <= TOL
+
+
+@pytest.mark.parametrize("tx", [2, 3])
+def test_adjoint_multi_tx(built, tx):
+    """Several transmit coils (BlochKernel.h:57-122: the rf field is the sum
+    of TxCoil_c A_c): the tissue gradients and, per coil, the rf gradient
+    against central differences of the FP64 oracle's loss -- scaling one
+    coil's amplitudes, shifting one coil's phases, and single entries of
+    that coil's VSeq.rfAmpLine / rfPhaseLine."""
+    sc = _phase_modulated(phantoms.multi_tx_gre(seed=50 + tx, n=6, n_tr=2, tx_coils=tx, rx_coils=2), 7)
+    target = _target(sc)
+    _, gsx, gsy = _loss(sc, target)
+    g = engine.adjoint(sc, gsx, gsy)
+    o = sc.VObj
+    act = ((o["Rho"] != 0) & (o["T1"] != 0) & (o["T2"] != 0)).ravel(order="F")
+    idx = np.flatnonzero(act)
+    for key in ("T1", "T2"):
+        p = np.asarray(o[key], np.float64).ravel(order="F")
+        _check(key, g[key][idx], _fd_gradient(sc, target, "VObj", key, idx, H * np.abs(p[idx])))
+    _check("dB0", g["dB0"][idx], _fd_gradient(sc, target, "VMag", "dB0", idx, np.full(idx.size, DB0_STEP)))
+    a, grf = g["rf_a"], g["rf"]
+    assert grf.shape[1:] == (tx, 2)
+    coil = np.asarray(sc.VSeq["rfCoilLine"]).ravel()
+    amp = np.asarray(sc.VSeq["rfAmpLine"], np.float64).ravel()
+    ph = np.asarray(sc.VSeq["rfPhaseLine"], np.float64).ravel()
+    rng = np.random.default_rng(13)
+    for c in range(tx):
+        mine = coil == c + 1
+        lp, _, _ = _loss(_with(sc, "VSeq", "rfAmpLine", np.where(mine, amp * (1 + H), amp)), target)
+        lm, _, _ = _loss(_with(sc, "VSeq", "rfAmpLine", np.where(mine, amp * (1 - H), amp)), target)
+        fd = (lp - lm) / (2 * H)
+        adj = float(np.sum(grf[:, c, 0] * a[:, c, 0] + grf[:, c, 1] * a[:, c, 1]))
+        print(f"coil {c} rf amplitude: adjoint {adj:.6e}, finite difference {fd:.6e}")
+        assert abs(adj - fd) <= TOL * abs(fd)
+        lp, _, _ = _loss(_with(sc, "VSeq", "rfPhaseLine", np.where(mine, ph + H, ph)), target)
+        lm, _, _ = _loss(_with(sc, "VSeq", "rfPhaseLine", np.where(mine, ph - H, ph)), target)
+        fd = (lp - lm) / (2 * H)
+        adj = float(np.sum(-grf[:, c, 0] * a[:, c, 1] + grf[:, c, 1] * a[:, c, 0]))
+        print(f"coil {c} rf phase: adjoint {adj:.6e}, finite difference {fd:.6e}")
+        assert abs(adj - fd) <= TOL * abs(fd)
+        # single entries of this coil's lines
+        cand = _untied(amp, 4 * H * np.abs(amp))
+        cand = cand[mine[cand] & (np.abs(amp[cand]) > 1e-3 * np.abs(amp).max())]
+        pick = np.sort(rng.choice(cand, min(8, cand.size), replace=False))
+        _check(f"coil {c} rfAmpLine", g["rf_amp_line"][pick],
+               _fd_gradient(sc, target, "VSeq", "rfAmpLine", pick, H * np.abs(amp[pick])))
 
 
 def test_adjoint_rejects_four_cest_pools(built):

@@ -243,10 +243,13 @@ def _fp64_adjoint_case(name):
         "mt": lambda: phantoms.small_multipool("mt", seed=61, n=4, pools=2, spins=2, coils=2, n_tr=2, seq="sat"),
         "cest4": lambda: phantoms.small_multipool("cest", seed=62, n=4, pools=4, spins=1, coils=2, n_tr=2,
                                                   seq="sat"),
+        # several transmit coils: the field is the sum of TxCoil_c A_c
+        "tx2": lambda: phantoms.multi_tx_gre(seed=63, n=5, n_tr=2, tx_coils=2, rx_coils=2),
+        "tx3": lambda: phantoms.multi_tx_gre(seed=64, n=5, n_tr=2, tx_coils=3, rx_coils=2),
     }[name]()
 
 
-@pytest.mark.parametrize("name", ["me2", "gm_bound", "mt", "cest4"])
+@pytest.mark.parametrize("name", ["me2", "gm_bound", "mt", "cest4", "tx2", "tx3"])
 def test_fp64_adjoint_pinned(name):
     """The FP64 reference gradient (oracle.adjoint64: the oracle's map
     restated in float64 PyTorch, differentiated by autograd) is pinned to
@@ -269,6 +272,8 @@ def test_fp64_adjoint_pinned(name):
         return float(np.dot(gx, o["Sx"]) + np.dot(gy, o["Sy"]))
 
     for struct, key in (("VObj", "T1"), ("VObj", "T2"), ("VObj", "Rho"), ("VMag", "dB0"), ("VObj", "K")):
+        if key not in getattr(sc, struct):
+            continue
         arr = getattr(sc, struct)[key]
         base = np.asarray(arr, np.float64).ravel(order="F")
         nz = np.flatnonzero(base)
@@ -285,3 +290,23 @@ def test_fp64_adjoint_pinned(name):
             fd = (out[0][0] - out[1][0]) / (out[0][1] - out[1][1])
             # (the differences' own truncation reaches 1e-5 for a bound pool's T2)
             assert abs(g[key][i] - fd) <= 5e-5 * abs(fd) + 1e-12, (key, i, g[key][i], fd)
+    tx = int(sc.VCoi["TxCoilNum"])
+    if tx > 1:
+        # per coil: scale that coil's rf amplitudes by (1 + h), dA_c/dh = A_c at
+        # the steps it is on (the rf steps' A from the port's step records)
+        rec = oracle.run_port(sc, "f64", step_records=oracle.run_port(sc, "f64")["steps"])["records"]
+        rec = rec[rec[:, 7] != 0]
+        coil = np.asarray(sc.VSeq["rfCoilLine"]).ravel()
+        amp = np.asarray(sc.VSeq["rfAmpLine"], np.float64).ravel()
+        assert g["rf"].shape == (rec.shape[0], tx, 2)
+        for c in range(tx):
+            ca, cp = (4, 5) if c == 0 else (10 + 3 * (c - 1), 11 + 3 * (c - 1))
+            a_re, a_im = rec[:, ca] * np.cos(rec[:, cp]), rec[:, ca] * np.sin(rec[:, cp])
+            adj = float(np.sum(g["rf"][:, c, 0] * a_re + g["rf"][:, c, 1] * a_im))
+            out = []
+            for sgn in (1, -1):
+                s2 = sc.copy()
+                s2.VSeq["rfAmpLine"] = np.where(coil == c + 1, amp * (1 + sgn * 1e-4), amp)
+                out.append(loss(s2))
+            fd = (out[0] - out[1]) / 2e-4
+            assert abs(adj - fd) <= 1e-5 * abs(fd), (c, adj, fd)
