@@ -570,7 +570,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     // rf steps packed too while a thread's state is small (with 8 isochromat-
     // pools the packed rf step's temporaries spill; rf steps are rare there)
     // and every pool is free (no saturation)
-    constexpr bool kPackRf = kPack && FREE && NS * P <= 4;
+    constexpr bool kPackRf = kPack && FREE && NS * P <= 8;
     bool selfx = false;  // some pool of this voxel exchanges with itself (a nonzero K diagonal)
     float mt_y1k = 0.f, mt_y21 = 0.f, mt_y1bk = 0.f, mt_y1b = 0.f, mt_y12 = 0.f;
     LineshapeCache lc;
@@ -1269,11 +1269,14 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                                     iy = __ffma2_rn(f1, PAIR(Ys, qq, p), iy);
                                     iy = __ffma2_rn(f2, PAIR(Xs, qq, p), iy);
                                 }
-                                const float2 ny2 = make_float2(-y2[t], -y2[t]), nyo = make_float2(-yo[t], -yo[t]);
-                                const float2 x1 = __ffma2_rn(ny2, rx[t], rx[t]);
-                                const float2 y1v = __ffma2_rn(ny2, ry[t], ry[t]);
-                                nx[t] = __fadd2_rn(__ffma2_rn(nyo, x1, x1), fsub2_rn(ax, bx));
-                                ny[t] = __fadd2_rn(__ffma2_rn(nyo, y1v, y1v), iy);
+                                // relaxation in increment form, one rounding of the state:
+                                // m + (inflow - y m), y = 1 - (1 - y2)(1 - yo) transverse,
+                                // 1 - (1 - y1)(1 - yo) longitudinal
+                                const float ya = fmaf(-y2[t], yo[t], y2[t] + yo[t]);
+                                const float yd = fmaf(-y1[t], yo[t], y1[t] + yo[t]);
+                                const float2 nya = make_float2(-ya, -ya), nyd = make_float2(-yd, -yd);
+                                nx[t] = __fadd2_rn(rx[t], __ffma2_rn(nya, rx[t], fsub2_rn(ax, bx)));
+                                ny[t] = __fadd2_rn(ry[t], __ffma2_rn(nya, ry[t], iy));
                                 const float c = rhoS[t] * y1[t];
                                 float2 iz = make_float2(c, c);
 #pragma unroll
@@ -1281,8 +1284,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                                     if (p == t && !kSelf) continue;
                                     iz = __ffma2_rn(make_float2(fin[t][p], fin[t][p]), PAIR(Zs, qq, p), iz);
                                 }
-                                const float2 z1 = __ffma2_rn(make_float2(-y1[t], -y1[t]), rz[t], rz[t]);
-                                nz[t] = __fadd2_rn(__ffma2_rn(nyo, z1, z1), iz);
+                                nz[t] = __fadd2_rn(rz[t], __ffma2_rn(nyd, rz[t], iz));
                             }
 #pragma unroll
                             for (int t = 0; t < P; ++t) {
