@@ -129,7 +129,6 @@ struct V2 {
     float2 x, y, z;
 };
 __device__ __forceinline__ float2 bc(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 swp(float2 a) { return make_float2(a.y, a.x); }  // the other pool's lane
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
@@ -183,11 +182,13 @@ struct KSum {
     }
 };
 
-template <int P, bool GM, bool BOUND>
+// MTX: several Tx coils (L.tx of them); without, one (the instantiations of
+// the common case carry no per-coil loops: they cost registers and spills)
+template <int P, bool GM, bool BOUND, bool MTX>
 __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoint_kernel(AdjLaunch L) {
     extern __shared__ __align__(16) float adj_sm[];
     constexpr int kWarps = kAdjBlock / 32;
-    const int TXN = L.tx, RS = adjoint_record_f4(L.tx);             // Tx coils, float4 per step record
+    const int TXN = MTX ? L.tx : 1, RS = adjoint_record_f4(TXN);    // Tx coils, float4 per step record
     float *win = adj_sm;                                            // [kAdjWin][3P][kAdjBlock]
     float *rfp = adj_sm + kAdjWin * 3 * P * kAdjBlock;              // [kAdjWin][warp][tx][2]
     float4 *wrec = reinterpret_cast<float4 *>(rfp + kAdjWin * kWarps * 2 * TXN);  // [kAdjWin][RS]
@@ -254,6 +255,9 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
         on[t] = active && t1[t] != 0.f && t2[t] != 0.f && rhoS[t] != 0.f;
         bnd[t] = BOUND && (L.bound >> t & 1u);
     }
+    bool anyoff = false;
+#pragma unroll
+    for (int t = 0; t < P; ++t) anyoff = anyoff || !on[t];
     // bound pools: (gamma |TxCoil|)^2, and the lineshape G, its slope dG/da
     // and a at the rf frequency lsw (2 pi f) of the last rf step
     const float gtx2 = L.gyro * L.gyro * fmaf(txc.x, txc.x, txc.y * txc.y);
@@ -287,8 +291,18 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
 
     // ---- per-dt coefficients ------------------------------------------------
     // map: d2, d1, cc, fin; gradient: hT1 (of l.z mr.z), hR (of l.z), hT2 (of
-    // l.xy mr.xy), e2, e1 (outflow rates, of l.xy mr.xy and l.z mr.z), ffin
+    // l.xy mr.xy), e2, e1 (outflow rates, of l.xy mr.xy and l.z mr.z), ffin.
+    // Without bound pools T1, T2 and K enter only here (dt changes are rare):
+    // read again from global memory, they hold no registers in the step loop
+    constexpr bool kLazy = !BOUND;
+    auto par_t1 = [&](int t) { return kLazy ? (active ? __ldg(L.t1 + (long long)t * n + v) : 0.f) : t1[t]; };
+    auto par_t2 = [&](int t) { return kLazy ? (active ? __ldg(L.t2 + (long long)t * n + v) : 0.f) : t2[t]; };
+    auto par_k = [&](int i) { return kLazy ? ((active && L.kch) ? __ldg(L.kch + (long long)i * n + v) : 0.f) : kc[i]; };
     float d1[P], d2[P], y1[P], fin[P][P], hT1[P], hR[P], hT2[P], e1[P], e2[P];
+    // one Tx coil, no bound pools: the coil's sensitivity scaled by -dt gamma
+    // (dv_xy / dA of an rf step), set with dt
+    constexpr bool kTcs = !MTX && !BOUND;
+    float2 tcs = make_float2(0.f, 0.f);
     // packed two-pool path: (1 - f_tp) dt of each inflow, zero for a pool that is off
     constexpr bool kPk = P == 2 && !BOUND;
     float gin[kPk ? P : 1][kPk ? P : 1];
@@ -297,14 +311,15 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     auto set_dt = [&](float dt) {
 #pragma unroll
         for (int t = 0; t < P; ++t) {
-            const float y1t = on[t] ? one_minus_exp(dt / t1[t]) : 0.f;
-            const float y2t = on[t] ? one_minus_exp(dt / t2[t]) : 0.f;
+            const float t1t = par_t1(t), t2t = par_t2(t);
+            const float y1t = on[t] ? one_minus_exp(dt / t1t) : 0.f;
+            const float y2t = on[t] ? one_minus_exp(dt / t2t) : 0.f;
             float ksum = 0.f, ksum_t = 0.f;  // outflow: all partners, transverse partners
 #pragma unroll
             for (int p = 0; p < P; ++p) {
                 fin[t][p] = 0.f;
                 if (GM && p == t) continue;
-                const float kgo = kc[ch(t, p)], kin = kc[ch(p, t)];
+                const float kgo = par_k(ch(t, p)), kin = par_k(ch(p, t));
                 ksum += kgo;
                 if (!(L.mtc && bnd[p])) ksum_t += kgo;
                 if (on[t] && kin != 0.f) fin[t][p] = one_minus_exp(dt * kin);
@@ -316,8 +331,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             d1[t] = (1.f - yot) * (1.f - y1t);
             d2[t] = (1.f - yot_t) * (1.f - y2t);
             // dy1/dT1 = -(1 - y1) dt / T1^2, dyo/dk = (1 - yo) dt
-            const float fT1 = on[t] ? -(1.f - y1t) * dt / (t1[t] * t1[t]) : 0.f;
-            const float fT2 = on[t] ? -(1.f - y2t) * dt / (t2[t] * t2[t]) : 0.f;
+            const float fT1 = on[t] ? -(1.f - y1t) * dt / (t1t * t1t) : 0.f;
+            const float fT2 = on[t] ? -(1.f - y2t) * dt / (t2t * t2t) : 0.f;
             const float fyo = (1.f - yot) * dt;
             hT1[t] = -(1.f - yot) * fT1;
             hR[t] = rhoS[t] * fT1;
@@ -331,13 +346,22 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             }
         }
         if constexpr (kPk) selfx = !GM && (fin[0][0] != 0.f || fin[1][1] != 0.f);
+        if constexpr (kTcs) {
+            const float2 tc = active ? __ldg(L.txc + v) : make_float2(0.f, 0.f);
+            const float sc = -dt * L.gyro;
+            tcs = make_float2(sc * tc.x, sc * tc.y);
+        }
         dtc = dt;
     };
     // ---- per-state rotation of free steps -----------------------------------
     float cth[P], sth[P];
-    auto wcom = [&](float4 r0) { return fmaf(om[3], r0.y, fmaf(om[2], r0.z, fmaf(om[1], r0.w, om[0]))); };
+    // off-resonance of the step's gradients, gamma (dB0 + G.r), set with them
+    // (dB0 and r stay in registers: reading them again at every gradient
+    // change stalled the loop more than the registers cost)
+    float wcc = 0.f;
     auto set_state = [&](float dt, float4 r0) {
-        const float wc = wcom(r0);
+        const float wc = fmaf(om[3], r0.y, fmaf(om[2], r0.z, fmaf(om[1], r0.w, om[0])));
+        wcc = wc;
 #pragma unroll
         for (int t = 0; t < P; ++t) sincos_cw((wc + wres[t]) * dt, sth[t], cth[t]);
     };
@@ -345,6 +369,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     // gamma By, w_t), B = sum over the Tx coils of TxCoil_c A_c (a coil that
     // is off has A_c = 0)
     auto rf_vxy = [&](float dt, float4 r1, int j) {
+        if constexpr (kTcs)
+            return make_float2(fmaf(tcs.x, r1.x, -tcs.y * r1.y), fmaf(tcs.x, r1.y, tcs.y * r1.x));
         const float sc = -dt * L.gyro;
         float bx = fmaf(txc.x, r1.x, -txc.y * r1.y), by = fmaf(txc.x, r1.y, txc.y * r1.x);
         for (int c = 1; c < TXN; ++c) {
@@ -362,7 +388,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             V2 mr;
             if (rf) {
                 const float2 vxy = rf_vxy(dt, r1, j);
-                const float wz = wcom(r0) + r1.z;
+                const float wz = wcc + r1.z;
                 const V2 v = {bc(vxy.x), bc(vxy.y), make_float2(-dt * (wz + wres[0]), -dt * (wz + wres[1]))};
                 const float2 a2 = fma2(v.z, v.z, bc(fmaf(vxy.x, vxy.x, vxy.y * vxy.y)));
                 float2 s1, s2;
@@ -373,11 +399,16 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 mr = {fma2(mm.x, c, mul2(mm.y, sn)), fma2(neg2(mm.x), sn, mul2(mm.y, c)), mm.z};
             }
             const float2 D2 = make_float2(d2[0], d2[1]), D1 = make_float2(d1[0], d1[1]);
-            const float2 fd = make_float2(fin[0][0], fin[1][1]), fx = make_float2(fin[0][1], fin[1][0]);
+            const float2 fd = make_float2(fin[0][0], fin[1][1]);
             const float2 cz = make_float2(rhoS[0] * y1[0], rhoS[1] * y1[1]);
-            float2 ax = fma2(fx, swp(mm.x), mul2(D2, mr.x));
-            float2 ay = fma2(fx, swp(mm.y), mul2(D2, mr.y));
-            float2 az = fma2(fx, swp(mm.z), fma2(D1, mr.z, cz));
+            // the partner's inflow f_tp m_p per lane as scalar fused multiply-adds
+            // (a packed operand with its lanes swapped costs two moves)
+            auto inflow = [&](float2 a, float2 mp) {
+                return make_float2(fmaf(fin[0][1], mp.y, a.x), fmaf(fin[1][0], mp.x, a.y));
+            };
+            float2 ax = inflow(mul2(D2, mr.x), mm.x);
+            float2 ay = inflow(mul2(D2, mr.y), mm.y);
+            float2 az = inflow(fma2(D1, mr.z, cz), mm.z);
             if (selfx) {  // a pool's inflow from itself (a nonzero K diagonal)
                 ax = fma2(fd, mm.x, ax);
                 ay = fma2(fd, mm.y, ay);
@@ -390,7 +421,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
         float3 mr[P];
         if (rf) {
             const float2 vxy = rf_vxy(dt, r1, j);
-            const float wz = wcom(r0) + r1.z;
+            const float wz = wcc + r1.z;
             float wg = 0.f;
             if (BOUND) {
                 lineshapes(r1.z);
@@ -445,7 +476,12 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
             const float4 r0 = wrec[RS * j], r1 = wrec[RS * j + 1];
             const int flags = __float_as_int(r1.w);
             const float dt = r0.x;
-            if (states) {
+            if (states && kPk) {  // packed: (pool 0, pool 1) of a component as one float2
+                float2 *ws = reinterpret_cast<float2 *>(states + j * 3 * P * kAdjBlock) + tid;
+                ws[0] = make_float2(m[0].x, m[1].x);
+                ws[kAdjBlock] = make_float2(m[0].y, m[1].y);
+                ws[2 * kAdjBlock] = make_float2(m[0].z, m[1].z);
+            } else if (states) {
                 float *ws = states + j * 3 * P * kAdjBlock + tid;
 #pragma unroll
                 for (int t = 0; t < P; ++t) {
@@ -532,16 +568,18 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
 #pragma unroll
         for (int i = 0; i < P * P; ++i) wk[i] = 0.f;
         // the coefficients in registers are those of the window's last step
+        int fnext = 0;  // flags of step j + 1 (the step before in this walk)
         for (int j = nk - 1; j >= 0; --j) {
             const float4 r0 = wrec[RS * j], r1 = wrec[RS * j + 1], r2 = wrec[RS * j + 2];
             const int flags = __float_as_int(r1.w);
             const float dt = r0.x;
             if (j < nk - 1) {  // coefficients of step j, if step j + 1 changed them
-                const int fn = __float_as_int(wrec[RS * (j + 1) + 1].w);
+                const int fn = fnext;
                 if (fn & kFlagDt) set_dt(dt);
                 if (fn & kFlagState) set_state(dt, r0);
                 if (fn & (kFlagDt | kFlagState)) cur = r0;
             }
+            fnext = flags;
             // dL/dS of step j - 1 (the next step back), if it samples: into the
             // buffer step j + 1 read, once every lane of the warp is done with it
             bool pend = false;
@@ -554,16 +592,23 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 }
             }
             const bool rf = (flags & kFlagRf) != 0;
-            const float *ws = win + j * 3 * P * kAdjBlock + tid;
             float3 mk[P];
+            V2 Mk{};  // packed path: the state before the step, lanes = pools
+            if constexpr (kPk) {
+                const float2 *ws = reinterpret_cast<const float2 *>(win + j * 3 * P * kAdjBlock) + tid;
+                Mk = {ws[0], ws[kAdjBlock], ws[2 * kAdjBlock]};
+            } else {
+                const float *ws = win + j * 3 * P * kAdjBlock + tid;
 #pragma unroll
-            for (int t = 0; t < P; ++t)
-                mk[t] = make_float3(ws[(3 * t + 0) * kAdjBlock], ws[(3 * t + 1) * kAdjBlock], ws[(3 * t + 2) * kAdjBlock]);
+                for (int t = 0; t < P; ++t)
+                    mk[t] = make_float3(ws[(3 * t + 0) * kAdjBlock], ws[(3 * t + 1) * kAdjBlock],
+                                        ws[(3 * t + 2) * kAdjBlock]);
+            }
             float2 vxy = make_float2(0.f, 0.f);
             float wz = 0.f, wg = 0.f;
             if (rf) {
                 vxy = rf_vxy(dt, r1, j);
-                wz = wcom(r0) + r1.z;
+                wz = wcc + r1.z;
                 if (BOUND) {
                     lineshapes(r1.z);
                     wg = sat_wg(r1);
@@ -578,8 +623,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 // both pools at once (lanes = pools); a pool that is off has zero
                 // relaxation, exchange and gradient coefficients (set_dt) and
                 // passes its adjoint through
-                const V2 M = {make_float2(mk[0].x, mk[1].x), make_float2(mk[0].y, mk[1].y),
-                              make_float2(mk[0].z, mk[1].z)};
+                const V2 M = Mk;
                 const V2 l = {make_float2(lam[0].x, lam[1].x), make_float2(lam[0].y, lam[1].y),
                               make_float2(lam[0].z, lam[1].z)};
                 V2 v{}, mr;
@@ -603,7 +647,9 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 // exchange rates: the outflow of each pool (every channel out of it)
                 // and the inflow to it from the magnetisation before the step
                 const float2 go = fma2(gd1, make_float2(e1[0], e1[1]), mul2(gd2, make_float2(e2[0], e2[1])));
-                const float2 lx = dot2(l, V2{swp(M.x), swp(M.y), swp(M.z)});  // l_t . m_other
+                // l_t . m_other per lane (scalar: no swapped operands)
+                const float2 lx = make_float2(fmaf(l.x.x, M.x.y, fmaf(l.y.x, M.y.y, l.z.x * M.z.y)),
+                                              fmaf(l.x.y, M.x.x, fmaf(l.y.y, M.y.x, l.z.y * M.z.x)));
                 if (!GM) {
                     // the diagonal channels: the outflow, and the inflow from itself
                     // (its derivative (1 - f) dt is nonzero at a zero rate too)
@@ -613,8 +659,11 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 }
                 wk[ch(0, 1)] += fmaf(lx.y, gin[1][0], go.x);
                 wk[ch(1, 0)] += fmaf(lx.x, gin[0][1], go.y);
-                const float2 fd = make_float2(fin[0][0], fin[1][1]), fx = make_float2(fin[0][1], fin[1][0]);
-                V2 n2 = {swp(mul2(fx, l.x)), swp(mul2(fx, l.y)), swp(mul2(fx, l.z))};
+                const float2 fd = make_float2(fin[0][0], fin[1][1]);
+                // the partner's inflow adjoint: lane t takes f_pt lambda_p
+                V2 n2 = {make_float2(fin[1][0] * l.x.y, fin[0][1] * l.x.x),
+                         make_float2(fin[1][0] * l.y.y, fin[0][1] * l.y.x),
+                         make_float2(fin[1][0] * l.z.y, fin[0][1] * l.z.x)};
                 if (selfx) n2 = {fma2(fd, l.x, n2.x), fma2(fd, l.y, n2.y), fma2(fd, l.z, n2.z)};
                 // adjoint with respect to the rotated magnetisation
                 const float2 D2 = make_float2(d2[0], d2[1]), D1 = make_float2(d1[0], d1[1]);
@@ -635,8 +684,10 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                     n2.z = add2(n2.z, lr.z);
                 }
                 ww[0] = wwv.x, ww[1] = wwv.y;
-                const float2 off = make_float2(on[0] ? 0.f : 1.f, on[1] ? 0.f : 1.f);
-                n2 = {fma2(off, l.x, n2.x), fma2(off, l.y, n2.y), fma2(off, l.z, n2.z)};
+                if (anyoff) {  // a pool that is off passes its adjoint through
+                    const float2 off = make_float2(on[0] ? 0.f : 1.f, on[1] ? 0.f : 1.f);
+                    n2 = {fma2(off, l.x, n2.x), fma2(off, l.y, n2.y), fma2(off, l.z, n2.z)};
+                }
                 nl[0] = make_float3(n2.x.x, n2.y.x, n2.z.x);
                 nl[1] = make_float3(n2.x.y, n2.y.y, n2.z.y);
             }
@@ -775,8 +826,10 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                     nl[t].y += src[t].y + src[t].w;
                 }
             }
+            // (an inactive thread's adjoint stays zero: its pools are off, its
+            // state and coefficients zero, and it takes no receive term)
 #pragma unroll
-            for (int t = 0; t < P; ++t) lam[t] = active ? nl[t] : make_float3(0.f, 0.f, 0.f);
+            for (int t = 0; t < P; ++t) lam[t] = nl[t];
             // rf gradient of this step: dB/dA = TxCoil, dv/dB = -dt gamma, so
             // dL/dA = -dt gamma conj(TxCoil) (gvx + i gvy) + the saturation's
             // share, summed over the warp
@@ -784,8 +837,9 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 const float sc = -dt * L.gyro;
                 for (int c = 0; c < TXN; ++c) {  // dB/dA_c = TxCoil_c
                     const float2 tc = c == 0 ? txc : txs[(c - 1) * kAdjBlock + tid];
-                    float2 gA = make_float2(sc * fmaf(tc.x, gv.x, tc.y * gv.y), sc * fmaf(tc.x, gv.y, -tc.y * gv.x));
-                    if (c == 0) gA = make_float2(gA.x + gs.x, gA.y + gs.y);
+                    float2 gA = kTcs ? make_float2(fmaf(tcs.x, gv.x, tcs.y * gv.y), fmaf(tcs.x, gv.y, -tcs.y * gv.x))
+                                     : make_float2(sc * fmaf(tc.x, gv.x, tc.y * gv.y), sc * fmaf(tc.x, gv.y, -tc.y * gv.x));
+                    if (BOUND && c == 0) gA = make_float2(gA.x + gs.x, gA.y + gs.y);
                     // both components in one reduction: the first exchange leaves
                     // lanes 0-15 with partial sums of x and lanes 16-31 with those
                     // of y, four more exchanges finish each half (lane 0: x, 16: y)
@@ -862,7 +916,8 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
 template <int P, bool GM, bool BOUND = false>
 cudaError_t go(const AdjLaunch &L, cudaStream_t st) {
     const size_t smem = adjoint_smem_bytes(P, L.rx, L.tx);
-    auto k = adjoint_kernel<P, GM, BOUND>;
+    // (bound pools run with one Tx coil only: the plan refuses more)
+    auto k = (!BOUND && L.tx > 1) ? adjoint_kernel<P, GM, BOUND, !BOUND> : adjoint_kernel<P, GM, BOUND, false>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const long long blocks = (L.n_iso + kAdjBlock - 1) / kAdjBlock;
