@@ -115,16 +115,25 @@ _WRITTEN = frozenset({"mx", "my", "mz", "sx", "sy", "skz", "sky", "skx", "hmx", 
 
 
 class HostScan:
-    """Column-major host copies of a Scan's arrays, bound into ScanArgs."""
+    """Column-major host copies of a Scan's arrays, bound into ScanArgs.
 
-    def __init__(self, sc, model: Optional[str] = None, numerics: str = "accurate", gpu_index: int = 0):
+    ``inplace``: the engine writes the final magnetisation and the signal
+    into the caller's arrays themselves, as the reference engines write the
+    MATLAB globals (``DoScanAtGPU.cu:124-214`` binds them with
+    ``mxGetPr``); arrays without the engine's type and column-major layout
+    are still copied.  By default every written array is a copy, so a scan
+    leaves the caller's structs unchanged."""
+
+    def __init__(self, sc, model: Optional[str] = None, numerics: str = "accurate", gpu_index: int = 0,
+                 inplace: bool = False):
         self.sc = sc
         o, m, c, ctl, q, v, sig = sc.VObj, sc.VMag, sc.VCoi, sc.VCtl, sc.VSeq, sc.VVar, sc.VSig
         self.keep = {}
         K = self.keep
         # inputs the engine only reads may alias the caller's arrays
-        f32 = lambda k, a: K.setdefault(k, _flat(a, np.float32, copy=k in _WRITTEN))
-        f64 = lambda k, a: K.setdefault(k, _flat(a, np.float64, copy=k in _WRITTEN or k.startswith("var_")))
+        wr = lambda k: k in _WRITTEN and not inplace
+        f32 = lambda k, a: K.setdefault(k, _flat(a, np.float32, copy=wr(k)))
+        f64 = lambda k, a: K.setdefault(k, _flat(a, np.float64, copy=wr(k) or k.startswith("var_")))
         i32 = lambda k, a: K.setdefault(k, _flat(a, np.int32, copy=True))
         p = lambda a, t: a.ctypes.data_as(t)
         a = ScanArgs()
@@ -214,10 +223,12 @@ def run(hs: HostScan, ext: Optional[Callable[[ScanArgs, int], int]] = None) -> D
 
 
 def scan(sc, model: Optional[str] = None, numerics: str = "accurate", gpu_index: int = 0,
-         ext: Optional[Callable[[ScanArgs, int], int]] = None) -> Dict[str, np.ndarray]:
+         ext: Optional[Callable[[ScanArgs, int], int]] = None, inplace: bool = False) -> Dict[str, np.ndarray]:
     """Run ``sc`` (a phantoms.Scan) on the GPU; returns Sx, Sy, Kx, Ky, Kz and
-    the final Mx, My, Mz (flattened column-major), leaving ``sc`` unchanged."""
-    return run(HostScan(sc, model=model, numerics=numerics, gpu_index=gpu_index), ext)
+    the final Mx, My, Mz (flattened column-major), leaving ``sc`` unchanged
+    unless ``inplace`` (then the final state and the signal are written into
+    ``sc``'s own arrays, as the mex entry points write the MATLAB globals)."""
+    return run(HostScan(sc, model=model, numerics=numerics, gpu_index=gpu_index, inplace=inplace), ext)
 
 
 def decode(sc) -> np.ndarray:
@@ -345,12 +356,12 @@ class Batch:
             pass
 
 
-def scan_batched(scans, numerics: str = "accurate", gpu_index: int = 0):
+def scan_batched(scans, numerics: str = "accurate", gpu_index: int = 0, inplace: bool = False):
     """``mrl_scan_batched``: every scan of ``scans`` in one batched pass;
-    returns their outputs like ``scan``."""
+    returns their outputs like ``scan`` (``inplace`` as there)."""
     lib = library()
     lib.mrl_scan_batched.argtypes = [ctypes.POINTER(ctypes.POINTER(ScanArgs)), ctypes.c_int]
-    hosts = [HostScan(sc, numerics=numerics, gpu_index=gpu_index) for sc in scans]
+    hosts = [HostScan(sc, numerics=numerics, gpu_index=gpu_index, inplace=inplace) for sc in scans]
     arr = (ctypes.POINTER(ScanArgs) * len(hosts))(*[ctypes.pointer(h.args) for h in hosts])
     rc = lib.mrl_scan_batched(arr, len(hosts))
     if rc != 0:

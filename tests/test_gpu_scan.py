@@ -116,6 +116,22 @@ def test_plan_matches_scan_and_reruns(built):
     plan.close()
 
 
+def test_inplace_scan_writes_the_callers_arrays(built):
+    """scan(..., inplace=True) writes the final state and the signal into the
+    caller's own arrays (as the mex entry points write the MATLAB globals)
+    and gives the same outputs as the copying call."""
+    sc, g = load_golden("mp_me_p2_s2_c2")
+    ref = engine.scan(sc)
+    assert not np.shares_memory(ref["Mx"], sc.VObj["Mx"])
+    run = sc.copy()
+    out = engine.scan(run, inplace=True)
+    assert np.shares_memory(out["Sx"], run.VSig["Sx"]) and np.shares_memory(out["Mz"], run.VObj["Mz"])
+    for k in ("Sx", "Sy", "Mx", "My", "Mz"):
+        np.testing.assert_array_equal(out[k], ref[k])
+    np.testing.assert_array_equal(np.asarray(run.VSig["Sx"]).reshape(-1, order="F"), ref["Sx"])
+    np.testing.assert_array_equal(np.asarray(run.VObj["Mz"]).reshape(-1, order="F"), ref["Mz"])
+
+
 def test_ext_plugin_callback(built):
     """An Ext plugin that spoils the transverse magnetisation (DoExtPlugin
     case 6) sees the state after the step that starts at the Ext sample."""
