@@ -64,12 +64,29 @@ void record_timing(const double t[8]) {
 namespace {
 
 // Receive reduction: Sx/Sy[pool][coil][signal] = sum over blocks of the
-// per-block partial sums, in FP64, then demodulated by rfRef
-// (BlochKernel.cuh:160-170 applies the same rotation per isochromat).
-// A block takes 32 consecutive (sample, pool, coil) outputs; its 8 warps
-// split the scan blocks (warp w sums blocks w, w + 8, ...; 256-byte loads)
-// and their sums are added in a fixed order, so results are reproducible.
+// per-block partial sums, then demodulated by rfRef (BlochKernel.cuh:160-170
+// applies the same rotation per isochromat).  A block takes 32 consecutive
+// (sample, pool, coil) outputs; its 8 warps split the scan blocks (warp w
+// sums blocks w, w + 8, ...; 256-byte loads) and their sums are added in a
+// fixed order, so results are reproducible.  A lane sums in double-float
+// arithmetic (a float sum and the float sum of its exact rounding errors,
+// Knuth's two-sum: FP64-level accuracy on the FP32 pipe -- this GPU's FP64
+// rate made plain double adds the bound of the reduction), four independent
+// chains per component; the warps' sums and the rotation are in FP64.
 constexpr int kRedWarps = 8;
+
+// a + b = s + e exactly (Knuth's two-sum; additions only, so nothing is
+// contracted into a fused multiply-add)
+struct DFSum {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float b) {
+        const float s = hi + b;
+        const float bb = s - hi;
+        lo += (hi - (s - bb)) + (b - bb);
+        hi = s;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 __device__ __forceinline__ void reduce_block(int bx, const float2 *__restrict__ partial, int nblk, int a_launch,
                                              int npairs, int rx, const int *__restrict__ amap, int A, double *sx,
                                              double *sy, double cr, double sr) {
@@ -81,24 +98,25 @@ __device__ __forceinline__ void reduce_block(int bx, const float2 *__restrict__ 
     if (o < tot) {
         const size_t stride = (size_t)a_launch * npairs;
         const float2 *p = partial + o;
+        DFSum sx4[4], sy4[4];
         int b = w;
         for (; b + 3 * kRedWarps < nblk; b += 4 * kRedWarps) {
-            const float2 p0 = p[(size_t)b * stride], p1 = p[(size_t)(b + kRedWarps) * stride];
-            const float2 p2 = p[(size_t)(b + 2 * kRedWarps) * stride], p3 = p[(size_t)(b + 3 * kRedWarps) * stride];
-            x += (double)p0.x;
-            y += (double)p0.y;
-            x += (double)p1.x;
-            y += (double)p1.y;
-            x += (double)p2.x;
-            y += (double)p2.y;
-            x += (double)p3.x;
-            y += (double)p3.y;
+            float2 q[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) q[u] = p[(size_t)(b + u * kRedWarps) * stride];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                sx4[u].add(q[u].x);
+                sy4[u].add(q[u].y);
+            }
         }
         for (; b < nblk; b += kRedWarps) {
             const float2 q = p[(size_t)b * stride];
-            x += (double)q.x;
-            y += (double)q.y;
+            sx4[0].add(q.x);
+            sy4[0].add(q.y);
         }
+        x = (sx4[0].value() + sx4[1].value()) + (sx4[2].value() + sx4[3].value());
+        y = (sy4[0].value() + sy4[1].value()) + (sy4[2].value() + sy4[3].value());
     }
     red[w][lane] = make_double2(x, y);
     __syncthreads();
