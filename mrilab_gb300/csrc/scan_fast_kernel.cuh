@@ -392,6 +392,12 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     const long long gt = (long long)tile * kBlock + tid;
     const int v = (int)(gt / L.tpv);
     const int sg = (int)(gt % L.tpv);
+    // tcgen05 receive: the magnetisation operand's base and this thread's
+    // column in it (its voxel), fixed for the item -- derived from the
+    // launch's threads per voxel once, not at every sample
+    const int tpv_r = tcr ? L.tpv : 1;
+    unsigned char *const tcb_base = tcr ? TCB : nullptr;
+    const int tc_col = tcr ? tid / tpv_r : 0;
     bool active = v < L.n_act;
     const int n = L.n_act;
 
@@ -671,10 +677,17 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         }
         __syncthreads();
         const float *red = wstage;
-        const int nout = a_fill * kNSampP * L.rx;
-        for (int o = tid; o < nout; o += kBlock) {
-            const int pr = o / L.rx;  // = a * kNSampP + t
-            const int c = o - pr * L.rx;
+        const int rxn = L.rx;
+        const int nout = a_fill * kNSampP * rxn;
+        // output o = pr * rx + c, pr = a * kNSampP + t: (pr, c) advanced by
+        // kBlock outputs per pass (two divisions per flush, not one per output)
+        const int dpr = kBlock / rxn, dc = kBlock - dpr * rxn;
+        int pr = tid / rxn, c = tid - pr * rxn;
+        for (int o = tid; o < nout; o += kBlock, pr += dpr, c += dc) {
+            if (c >= rxn) {
+                c -= rxn;
+                ++pr;
+            }
             const int a = pr / kNSampP, t = pr - a * kNSampP;
             const int rank = kRank ? F.samp_rank[t] : t;
             float sx = 0.f, sy = 0.f;
@@ -755,10 +768,17 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
             for (int j = 0; j < 8; ++j) stw[((q & 1) * 8 + j) * kTcCoils * 2 + comp] = sgn * d[j];
         }
         __syncthreads();
-        const int nout = a_fill * kNSampP * L.rx;
-        for (int o = tid; o < nout; o += kBlock) {
-            const int pr = o / L.rx;  // = a * kNSampP + t
-            const int c = o - pr * L.rx;
+        const int rxn = L.rx;
+        const int nout = a_fill * kNSampP * rxn;
+        // output o = pr * rx + c, pr = a * kNSampP + t: (pr, c) advanced by
+        // kBlock outputs per pass (two divisions per flush, not one per output)
+        const int dpr = kBlock / rxn, dc = kBlock - dpr * rxn;
+        int pr = tid / rxn, c = tid - pr * rxn;
+        for (int o = tid; o < nout; o += kBlock, pr += dpr, c += dc) {
+            if (c >= rxn) {
+                c -= rxn;
+                ++pr;
+            }
             const int a = pr / kNSampP, t = pr - a * kNSampP;
             const int rank = kRank ? F.samp_rank[t] : t;
             float sx = 0.f, sy = 0.f;
@@ -984,7 +1004,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     if constexpr (tcr) {
                         // the voxel's sum over its threads, written by its first
                         // thread as the TF32 big and small parts of Re and Im
-                        for (int o = 1; o < TPV; o <<= 1) {
+                        for (int o = 1; o < tpv_r; o <<= 1) {
                             m.x += __shfl_xor_sync(0xffffffffu, m.x, o);
                             m.y += __shfl_xor_sync(0xffffffffu, m.y, o);
                         }
@@ -993,7 +1013,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                             // rows r, 16 + r, 32 + r, 48 + r: Re and Im, big then small
                             // (16 rows = two 1024-byte atoms further, the same swizzle)
                             const int r = a_fill * nsp + rank;
-                            float *tb = reinterpret_cast<float *>(TCB + tc::sw128_offset(r, tid / TPV, kTcBRows));
+                            float *tb = reinterpret_cast<float *>(tcb_base + tc::sw128_offset(r, tc_col, kTcBRows));
                             constexpr int kPartF = kTcN / 8 * 1024 / 4;  // floats between parts
                             tb[0] = bx;
                             tb[kPartF] = by;
