@@ -271,8 +271,9 @@ void pack_fast_records(const DecodeChunk &ch, int tx, FrameMoments &fm, std::vec
         r[1] = (float)si.gz;
         r[2] = (float)si.gy;
         r[3] = (float)si.gx;
-        r[4] = (float)(si.amp[0] * std::cos(si.phase[0]));
-        r[5] = (float)(si.amp[0] * std::sin(si.phase[0]));
+        // (steps without rf: no cosine or sine; the kernels read A only on rf steps)
+        r[4] = si.amp[0] != 0 ? (float)(si.amp[0] * std::cos(si.phase[0])) : 0.f;
+        r[5] = si.amp[0] != 0 ? (float)(si.amp[0] * std::sin(si.phase[0])) : 0.f;
         r[6] = (float)dw_rf;
         std::memcpy(&r[7], &flags, sizeof(int));
         split(fm.t, r[8], r[9]);

@@ -381,6 +381,69 @@ bool voxel_active(const mrl_scan_args &a, int km, long long v, long long V) {
     return false;
 }
 
+// ---- host staging of large copies --------------------------------------------
+// The caller's arrays are pageable memory (MATLAB's, numpy's); copies of the
+// object and of the results go through a pinned buffer of the calling
+// thread instead: its host side is copied by several threads at once and
+// the DMA runs from pinned memory (pageable copies of the 150 MB object and
+// 100 MB of results took 20-30 ms each way).  Below kStageMin bytes a copy
+// goes directly.
+constexpr size_t kStageMin = 8u << 20;
+struct HostCopy {
+    void *dst;
+    const void *src;
+    size_t bytes;
+};
+// the host copies of `jobs`, split into pieces of about equal size over up to
+// eight threads
+void parallel_copy(const std::vector<HostCopy> &jobs) {
+    size_t total = 0;
+    for (const HostCopy &j : jobs) total += j.bytes;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nth = (int)std::min<size_t>(std::min(8u, hw), std::max<size_t>(1, total / (4u << 20)));
+    if (nth <= 1) {
+        for (const HostCopy &j : jobs) memcpy(j.dst, j.src, j.bytes);
+        return;
+    }
+    const size_t share = (total + nth - 1) / nth;
+    auto run = [&](int t) {  // bytes [t * share, (t + 1) * share) of the concatenated jobs
+        size_t lo = (size_t)t * share, hi = std::min(total, lo + share), base = 0;
+        for (const HostCopy &j : jobs) {
+            const size_t a = std::max(lo, base), b = std::min(hi, base + j.bytes);
+            if (a < b)
+                memcpy(static_cast<char *>(j.dst) + (a - base), static_cast<const char *>(j.src) + (a - base), b - a);
+            base += j.bytes;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nth; ++t) pool.emplace_back(run, t);
+    run(0);
+    for (std::thread &t : pool) t.join();
+}
+// the calling thread's pinned staging buffer, grown to `bytes` (null if
+// pinned memory cannot be had: the copies then go directly)
+struct PinnedStage {
+    void *p = nullptr;
+    size_t cap = 0;
+    ~PinnedStage() {
+        if (p) cudaFreeHost(p);
+    }
+    void *get(size_t bytes) {
+        if (bytes <= cap) return p;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
+            cudaGetLastError();  // clear the error; fall back to direct copies
+            p = nullptr;
+            return nullptr;
+        }
+        cap = bytes;
+        return p;
+    }
+};
+thread_local PinnedStage t_stage;
+
 struct Scanner {
     mrl_scan_args *args;
     mrl_ext_fn ext;
@@ -677,10 +740,24 @@ struct Scanner {
         if ((e = d_rx.ensure(rxmap ? n * RX : 1)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(coils)");
         if (fast && (e = d_f2.ensure(o_txc + (size_t)TX * n)) != cudaSuccess) return fail_cuda(e, "cudaMalloc(frame)");
         auto t0 = std::chrono::steady_clock::now();
+        // large objects: the pieces copied into the pinned stage in place (one
+        // DMA of the whole raw buffer; the stage is free again after the
+        // synchronisation below)
+        float *stage = rtot * sizeof(float) >= kStageMin ? static_cast<float *>(t_stage.get(rtot * sizeof(float)))
+                                                         : nullptr;
+        if (stage) {
+            std::vector<HostCopy> jobs;
+            for (int q = 0; q < kPieces; ++q)
+                if (pieces[q].host && pieces[q].count > 0)
+                    jobs.push_back({stage + roff[q], pieces[q].host, pieces[q].count * sizeof(float)});
+            parallel_copy(jobs);
+            if ((e = cudaMemcpyAsync(d_raw.p, stage, rtot * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+                return fail_cuda(e, "upload object");
+        }
         for (int q = 0; q < kPieces; ++q) {
             if (!pieces[q].host || pieces[q].count == 0) continue;
-            if ((e = cudaMemcpyAsync(d_raw.p + roff[q], pieces[q].host, pieces[q].count * sizeof(float),
-                                     cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            if (!stage && (e = cudaMemcpyAsync(d_raw.p + roff[q], pieces[q].host, pieces[q].count * sizeof(float),
+                                               cudaMemcpyHostToDevice, st)) != cudaSuccess)
                 return fail_cuda(e, "upload object");
             h2d_bytes += (double)pieces[q].count * sizeof(float);
         }
@@ -746,11 +823,25 @@ struct Scanner {
         scatter_state<<<(n_act + 255) / 256, 256, 0, st>>>(d_m.p, d_act.p, n_act, (int)n, P * S, V, raw.mx, raw.my,
                                                           raw.mz);
         cudaError_t e = cudaGetLastError();
-        if (e == cudaSuccess) e = cudaMemcpyAsync(a.obj.mx, raw.mx, PSV * sizeof(float), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(a.obj.my, raw.my, PSV * sizeof(float), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(a.obj.mz, raw.mz, PSV * sizeof(float), cudaMemcpyDeviceToHost, st);
+        // large states: the three (padded, consecutive) raw arrays in one DMA
+        // into the pinned stage, then copied out on several threads
+        const size_t span = (size_t)(raw.mz + PSV - raw.mx);
+        float *stage = 3 * PSV * sizeof(float) >= kStageMin ? static_cast<float *>(t_stage.get(span * sizeof(float)))
+                                                            : nullptr;
+        if (stage) {
+            if (e == cudaSuccess) e = cudaMemcpyAsync(stage, raw.mx, span * sizeof(float), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e == cudaSuccess)
+                parallel_copy({{a.obj.mx, stage, PSV * sizeof(float)},
+                               {a.obj.my, stage + (raw.my - raw.mx), PSV * sizeof(float)},
+                               {a.obj.mz, stage + (raw.mz - raw.mx), PSV * sizeof(float)}});
+        } else {
+            if (e == cudaSuccess) e = cudaMemcpyAsync(a.obj.mx, raw.mx, PSV * sizeof(float), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(a.obj.my, raw.my, PSV * sizeof(float), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(a.obj.mz, raw.mz, PSV * sizeof(float), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        }
         d2h_bytes += 3.0 * PSV * sizeof(float);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return fail_cuda(e, "download state");
         d2h_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         return MRL_OK;
@@ -765,12 +856,30 @@ struct Scanner {
         const size_t pitch = (size_t)A * sizeof(double);
         d2h_bytes += 2.0 * (a1 - a0) * sizeof(double) * P * RX;
         auto t0 = std::chrono::steady_clock::now();
-        cudaError_t e = cudaMemcpy2DAsync(a.sig.sx + a0, pitch, d_sx.p + a0, pitch, (size_t)(a1 - a0) * sizeof(double),
-                                          (size_t)P * RX, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess)
-            e = cudaMemcpy2DAsync(a.sig.sy + a0, pitch, d_sy.p + a0, pitch, (size_t)(a1 - a0) * sizeof(double),
-                                  (size_t)P * RX, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        const size_t rows = (size_t)P * RX, wb = (size_t)(a1 - a0) * sizeof(double);
+        // large signals: both into the pinned stage ([Sx rows][Sy rows], packed),
+        // then copied out on several threads
+        char *stage = 2 * rows * wb >= kStageMin ? static_cast<char *>(t_stage.get(2 * rows * wb)) : nullptr;
+        cudaError_t e;
+        if (stage) {
+            e = cudaMemcpy2DAsync(stage, wb, d_sx.p + a0, pitch, wb, rows, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpy2DAsync(stage + rows * wb, wb, d_sy.p + a0, pitch, wb, rows, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e == cudaSuccess) {
+                std::vector<HostCopy> jobs;
+                for (size_t r = 0; r < rows; ++r) {
+                    jobs.push_back({a.sig.sx + r * A + a0, stage + r * wb, wb});
+                    jobs.push_back({a.sig.sy + r * A + a0, stage + (rows + r) * wb, wb});
+                }
+                parallel_copy(jobs);
+            }
+        } else {
+            e = cudaMemcpy2DAsync(a.sig.sx + a0, pitch, d_sx.p + a0, pitch, wb, rows, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpy2DAsync(a.sig.sy + a0, pitch, d_sy.p + a0, pitch, wb, rows, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        }
         if (e != cudaSuccess) return fail_cuda(e, "download signal");
         d2h_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         return MRL_OK;
