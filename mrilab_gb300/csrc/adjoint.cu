@@ -197,11 +197,22 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
     float2 *gbuf = rxs + L.rx * kAdjBlock;                          // [warp][2][PR]
     float2 *txs = gbuf + kWarps * 2 * PR;                           // [tx-1][kAdjBlock] TxCoil of coils >= 1
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const long long iso = (long long)blockIdx.x * kAdjBlock + tid;
-    const bool active = iso < L.n_iso;
+    // lanes of a voxel that split its receive term (8 coils or more): the
+    // largest power of two dividing the spin count, at most a warp (groups
+    // never straddle a warp); with fewer coils the split costs more than it
+    // saves.  Not in the packed two-pool instantiation (its registers are
+    // at the launch bound)
+    constexpr bool kGroup = !(P == 2 && !BOUND);
+    const int GS = kGroup && L.rx >= 8 ? min(L.S & -L.S, 32) : 1, gl = tid & (GS - 1);
+    // with groups the threads take the isochromats spin-minor (a voxel's
+    // spins on adjacent lanes), else voxel-minor (coalesced checkpoint
+    // reads); iso indexes the [spin][voxel] arrays (checkpoints, gradients)
+    const long long ithr = (long long)blockIdx.x * kAdjBlock + tid;
+    const bool active = ithr < L.n_iso;
     const int n = L.n_act;
-    const int v = active ? (int)(iso % n) : 0;
-    const int s = active ? (int)(iso / n) : 0;
+    const int v = active ? (int)(GS > 1 ? ithr / L.S : ithr % n) : 0;
+    const int s = active ? (int)(GS > 1 ? ithr % L.S : ithr / n) : 0;
+    const long long iso = GS > 1 ? (long long)s * n + v : ithr;  // (voxel-minor: the thread index itself)
     // exchange channel of the rate from pool a to pool b (ME: a*P+b, GM: b*P+a)
     auto ch = [](int a, int b) { return GM ? b * P + a : a * P + b; };
 
@@ -793,7 +804,7 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                     cp_async_wait<0>();
                 __syncwarp();
             }
-            if (a >= 0 && active) {  // (bound pools are not received)
+            if (!kGroup && a >= 0 && active) {  // (bound pools are not received)
                 // per pool: sum_c G R_c as four independent partial sums
                 // (re and im of the even and of the odd coils)
                 const float2 *ga = gbuf + (warp * 2 + (j & 1)) * PR;
@@ -824,6 +835,56 @@ __global__ void __launch_bounds__(kAdjBlock, P <= 2 ? (BOUND ? 3 : 4) : 2) adjoi
                 for (int t = 0; t < P; ++t) {
                     nl[t].x += src[t].x + src[t].z;
                     nl[t].y += src[t].y + src[t].w;
+                }
+            }
+            if (kGroup && a >= 0) {  // (bound pools are not received)
+                // per pool sum_c G R_c: it depends on the voxel and the sample,
+                // not on the spin, so lane gl of a voxel's group of GS lanes
+                // sums coils gl, gl + GS, ... (two independent partial sums,
+                // re and im) and the group adds its partial sums with shuffles
+                const float2 *ga = gbuf + (warp * 2 + (j & 1)) * PR;
+                const int rxn = L.rx;
+                float4 src[P];
+#pragma unroll
+                for (int t = 0; t < P; ++t) src[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+                auto coil = [&](int c, bool second) {
+                    const float2 rc = rxs[c * kAdjBlock + tid];
+#pragma unroll
+                    for (int t = 0; t < P; ++t) {
+                        if (bnd[t] || (L.mtc && t != 0)) continue;  // MT / CEST receive pool 0
+                        const float2 g = ga[t * rxn + c];
+                        if (second) {
+                            src[t].z = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src[t].z));
+                            src[t].w = fmaf(g.x, rc.y, fmaf(g.y, rc.x, src[t].w));
+                        } else {
+                            src[t].x = fmaf(g.x, rc.x, fmaf(-g.y, rc.y, src[t].x));
+                            src[t].y = fmaf(g.x, rc.y, fmaf(g.y, rc.x, src[t].y));
+                        }
+                    }
+                };
+                if (active) {
+#pragma unroll 1
+                    for (int c0 = gl; c0 < rxn; c0 += 8 * GS) {
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            const int c = c0 + k * GS;
+                            if (c >= rxn) break;
+                            coil(c, (k & 1) != 0);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < P; ++t) {
+                    if (bnd[t] || (L.mtc && t != 0)) continue;
+                    float sx = src[t].x + src[t].z, sy = src[t].y + src[t].w;
+                    for (int o = 1; o < GS; o <<= 1) {  // (block-uniform: every lane of the warp takes part)
+                        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+                        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+                    }
+                    if (active) {
+                        nl[t].x += sx;
+                        nl[t].y += sy;
+                    }
                 }
             }
             // (an inactive thread's adjoint stays zero: its pools are off, its

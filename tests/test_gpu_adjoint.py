@@ -214,7 +214,7 @@ def test_adjoint_two_level_checkpoints(built, monkeypatch):
             assert err <= 1e-4
 
 
-@pytest.mark.parametrize("case", ["gre", "me3", "gm_bound", "bssfp", "mt", "cest3", "tx2", "tx3"])
+@pytest.mark.parametrize("case", ["gre", "me3", "gm_bound", "bssfp", "mt", "cest3", "tx2", "tx3", "mt_epi_s4"])
 def test_adjoint_vs_fp64_adjoint(built, case):
     """The FP32 adjoint kernel against the FP64 reference gradient
     (oracle.adjoint64: the oracle's map in float64, differentiated by
@@ -236,7 +236,10 @@ def test_adjoint_vs_fp64_adjoint(built, case):
                                                     seq="sat"),
           # several transmit coils: B = sum of TxCoil_c A_c, the rf gradient per coil
           "tx2": lambda: phantoms.multi_tx_gre(seed=47, n=6, n_tr=2, tx_coils=2, rx_coils=2),
-          "tx3": lambda: phantoms.multi_tx_gre(seed=48, n=6, n_tr=2, tx_coils=3, rx_coils=3)}[case]()
+          "tx3": lambda: phantoms.multi_tx_gre(seed=48, n=6, n_tr=2, tx_coils=3, rx_coils=3),
+          # 4 spins, 12 coils: the four lanes of a voxel split its receive term
+          "mt_epi_s4": lambda: phantoms.config5_mt_epi(seed=49, nx=4, ny=4, nz=1, spins=4, n_coils=12, n_read=8,
+                                                       n_pe=8)}[case]()
     sc = _phase_modulated(sc, 12)
     tx, ty = _target(sc)
     _, gx, gy = _loss(sc, (tx, ty))
