@@ -416,7 +416,12 @@ void parallel_copy(const std::vector<HostCopy> &jobs) {
         }
     };
     std::vector<std::thread> pool;
-    for (int t = 1; t < nth; ++t) pool.emplace_back(run, t);
+    int started = 1;
+    try {  // (no exception crosses the C ABI: threads that cannot start are run here)
+        for (; started < nth; ++started) pool.emplace_back(run, started);
+    } catch (...) {
+    }
+    for (int t = started; t < nth; ++t) run(t);
     run(0);
     for (std::thread &t : pool) t.join();
 }
@@ -429,6 +434,14 @@ struct PinnedStage {
         if (p) cudaFreeHost(p);
     }
     void *get(size_t bytes) {
+        if (p) {  // a device reset frees pinned allocations: then forget this one
+            cudaPointerAttributes at{};
+            if (cudaPointerGetAttributes(&at, p) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+                cudaGetLastError();
+                p = nullptr;
+                cap = 0;
+            }
+        }
         if (bytes <= cap) return p;
         if (p) cudaFreeHost(p);
         p = nullptr;

@@ -573,10 +573,11 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
     // inflow from a bound pool is zero in fr, and saturation acts on rf steps
     // only
     constexpr bool kPack = MODEL == KM_EXCH && !EXACT && NS % 2 == 0;
-    // rf steps packed too while a thread's state is small (with 8 isochromat-
-    // pools the packed rf step's temporaries spill; rf steps are rare there)
-    // and every pool is free (no saturation)
-    constexpr bool kPackRf = kPack && FREE && NS * P <= 8;
+    // rf steps packed too while a thread's state is small (beyond 8
+    // isochromat-pools, or 6 with bound pools, the packed rf step's
+    // temporaries spill); a bound pool takes its saturation instead of the
+    // rotation there
+    constexpr bool kPackRf = kPack && NS * P <= (FREE ? 8 : 6);
     bool selfx = false;  // some pool of this voxel exchanges with itself (a nonzero K diagonal)
     float mt_y1k = 0.f, mt_y21 = 0.f, mt_y1bk = 0.f, mt_y1b = 0.f, mt_y12 = 0.f;
     LineshapeCache lc;
@@ -1235,6 +1236,14 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 #pragma unroll
                             for (int t = 0; t < P; ++t) {
                                 const float2 x = PAIR(Xs, qq, t), y = PAIR(Ys, qq, t), z = PAIR(Zs, qq, t);
+                                if (!FREE && L.kind[t] != 0) {
+                                    // a bound pool (block-uniform): no rotation; its
+                                    // longitudinal magnetisation saturated
+                                    rx[t] = x;
+                                    ry[t] = y;
+                                    rz[t] = __ffma2_rn(make_float2(-sat[t], -sat[t]), z, z);
+                                    continue;
+                                }
                                 const float w0 = wc + F.cs_hi[t] + wrf;
                                 const float2 dwp = dwsm[qq * P * kBlock + t * kBlock + tid];
                                 // nvz = -v_z = dt dW per spin
@@ -1282,6 +1291,7 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
 #pragma unroll
                                 for (int p = 0; p < P; ++p) {
                                     if (p == t && !kSelf) continue;
+                                    if (!FREE && (L.kind[p] != 0 || L.kind[t] != 0)) continue;  // fr is zero
                                     const float2 f1 = make_float2(fr[t][p].x, fr[t][p].x);
                                     const float2 f2 = make_float2(fr[t][p].y, fr[t][p].y);
                                     ax = __ffma2_rn(f1, PAIR(Xs, qq, p), ax);
