@@ -683,6 +683,12 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         // output o = pr * rx + c, pr = a * kNSampP + t: (pr, c) advanced by
         // kBlock outputs per pass (two divisions per flush, not one per output)
         const int dpr = kBlock / rxn, dc = kBlock - dpr * rxn;
+        // the launch's fields in registers (the stores below go through a
+        // generic pointer: the compiler would reload them from shared memory
+        // for every output)
+        const bool direct = L.dsx != nullptr;
+        const int npairs = L.npairs;
+        float2 *const pbase = direct ? nullptr : L.partial + ((long long)tile * L.a_launch + a_base) * npairs;
         int pr = tid / rxn, c = tid - pr * rxn;
         for (int o = tid; o < nout; o += kBlock, pr += dpr, c += dc) {
             if (c >= rxn) {
@@ -700,10 +706,10 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     sy += red[(w * 16 + row) * (2 * C4) + 2 * c + 1];
                 }
             }
-            if (L.dsx) {
+            if (direct) {
                 direct_add(L, a_base + a, t, c, sx, sy);
             } else {
-                L.partial[((long long)tile * L.a_launch + a_base + a) * L.npairs + t * L.rx + c] = make_float2(sx, sy);
+                pbase[(long long)a * npairs + t * rxn + c] = make_float2(sx, sy);
             }
         }
         a_base += a_fill;
@@ -774,6 +780,12 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
         // output o = pr * rx + c, pr = a * kNSampP + t: (pr, c) advanced by
         // kBlock outputs per pass (two divisions per flush, not one per output)
         const int dpr = kBlock / rxn, dc = kBlock - dpr * rxn;
+        // the launch's fields in registers (the stores below go through a
+        // generic pointer: the compiler would reload them from shared memory
+        // for every output)
+        const bool direct = L.dsx != nullptr;
+        const int npairs = L.npairs;
+        float2 *const pbase = direct ? nullptr : L.partial + ((long long)tile * L.a_launch + a_base) * npairs;
         int pr = tid / rxn, c = tid - pr * rxn;
         for (int o = tid; o < nout; o += kBlock, pr += dpr, c += dc) {
             if (c >= rxn) {
@@ -792,10 +804,10 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     sy += q.y;
                 }
             }
-            if (L.dsx) {
+            if (direct) {
                 direct_add(L, a_base + a, t, c, sx, sy);
             } else {
-                L.partial[((long long)tile * L.a_launch + a_base + a) * L.npairs + t * L.rx + c] = make_float2(sx, sy);
+                pbase[(long long)a * npairs + t * rxn + c] = make_float2(sx, sy);
             }
         }
         a_base += a_fill;
