@@ -78,6 +78,16 @@ void decode_until_ext(DecodeState &s, const mrl_sequence &q, int tx, double gyro
     out.point_uts.clear();
     out.point_step.clear();
     out.point_dt.clear();
+    {  // at most one step and one time point per remaining sequence entry:
+       // reserving avoids regrowing (and copying) the step list many times
+        const size_t left = (size_t)std::max(0, q.n_ts - s.i) + 1;
+        out.records.reserve(left * (size_t)stride);
+        out.steps.reserve(left);
+        out.step_adc.reserve(left);
+        out.point_uts.reserve(left);
+        out.point_step.reserve(left);
+        out.point_dt.reserve(left);
+    }
     if (s.pend_active) {
         finish_time_point(s, tx, s.pend_ext, s.pend_flag_sum, s.pend_dt);
         s.pend_active = false;
