@@ -1344,158 +1344,162 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                 }
             }
 
+            // (the unpacked step: the packed paths above take every step when
+            // both the free and the rf step are packed)
+            if constexpr (!(kPack && kPackRf)) {
 #pragma unroll
-            for (int s = 0; s < NS; ++s) {
-                float px[P], py[P], pz[P];
-#pragma unroll
-                for (int t = 0; t < P; ++t) {
-                    px[t] = XS(s, t);
-                    py[t] = YS(s, t);
-                    pz[t] = ZS(s, t);
-                }
-                // ---- transverse ----------------------------------------------
-                if (rf) {
+                for (int s = 0; s < NS; ++s) {
+                    float px[P], py[P], pz[P];
 #pragma unroll
                     for (int t = 0; t < P; ++t) {
-                        if (!has_frame<MODEL>(t)) continue;
-                        float x = px[t], y = py[t], z = pz[t];
-                        const float dW = wc + DWS(s, t) + F.cs_hi[t] + wrf;
-                        const float vz = -dt * dW;
-                        rot_exp(x, y, z, vt[t].x, vt[t].y, vz, rot_coeffs(fmaf(vz, vz, fmaf(vt[t].x, vt[t].x, vt[t].y * vt[t].y))));
-                        const bool on = tvo >> t & 1u;
-                        XS(s, t) = on ? x : px[t];
-                        YS(s, t) = on ? y : py[t];
-                        ZS(s, t) = on ? z : pz[t];
+                        px[t] = XS(s, t);
+                        py[t] = YS(s, t);
+                        pz[t] = ZS(s, t);
                     }
-                    // relaxation and inflow after the rotation (the frames hold still);
-                    // the exact propagator takes the partners after their rotation,
-                    // and bound pools after their saturation (sat is zero for the others)
-                    if constexpr (EXACT) {
-#pragma unroll
-                        for (int t = 0; t < P; ++t) {
-                            if constexpr (!FREE) ZS(s, t) = fmaf(-sat[t], ZS(s, t), ZS(s, t));
-                            px[t] = XS(s, t);
-                            py[t] = YS(s, t);
-                            pz[t] = ZS(s, t);
-                        }
-                    }
-                    if constexpr (MODEL == KM_NORMAL || MODEL == KM_MT) {
+                    // ---- transverse ----------------------------------------------
+                    if (rf) {
 #pragma unroll
                         for (int t = 0; t < P; ++t) {
                             if (!has_frame<MODEL>(t)) continue;
-                            XS(s, t) = fmaf(-y2[t], XS(s, t), XS(s, t));
-                            YS(s, t) = fmaf(-y2[t], YS(s, t), YS(s, t));
+                            float x = px[t], y = py[t], z = pz[t];
+                            const float dW = wc + DWS(s, t) + F.cs_hi[t] + wrf;
+                            const float vz = -dt * dW;
+                            rot_exp(x, y, z, vt[t].x, vt[t].y, vz, rot_coeffs(fmaf(vz, vz, fmaf(vt[t].x, vt[t].x, vt[t].y * vt[t].y))));
+                            const bool on = tvo >> t & 1u;
+                            XS(s, t) = on ? x : px[t];
+                            YS(s, t) = on ? y : py[t];
+                            ZS(s, t) = on ? z : pz[t];
+                        }
+                        // relaxation and inflow after the rotation (the frames hold still);
+                        // the exact propagator takes the partners after their rotation,
+                        // and bound pools after their saturation (sat is zero for the others)
+                        if constexpr (EXACT) {
+#pragma unroll
+                            for (int t = 0; t < P; ++t) {
+                                if constexpr (!FREE) ZS(s, t) = fmaf(-sat[t], ZS(s, t), ZS(s, t));
+                                px[t] = XS(s, t);
+                                py[t] = YS(s, t);
+                                pz[t] = ZS(s, t);
+                            }
+                        }
+                        if constexpr (MODEL == KM_NORMAL || MODEL == KM_MT) {
+#pragma unroll
+                            for (int t = 0; t < P; ++t) {
+                                if (!has_frame<MODEL>(t)) continue;
+                                XS(s, t) = fmaf(-y2[t], XS(s, t), XS(s, t));
+                                YS(s, t) = fmaf(-y2[t], YS(s, t), YS(s, t));
+                            }
+                        } else {
+#pragma unroll
+                            for (int t = 0; t < P; ++t) {
+                                if (!has_frame<MODEL>(t)) continue;
+                                float ix = 0.f, iy = 0.f;
+#pragma unroll
+                                for (int p = 0; p < P; ++p) {
+                                    if (MODEL == KM_CEST && !((t == 0 && p >= 2) || (t >= 2 && p == 0))) continue;
+                                    const float2 f = fr[t][p];
+                                    ix = fmaf(f.x, px[p], fmaf(-f.y, py[p], ix));
+                                    iy = fmaf(f.x, py[p], fmaf(f.y, px[p], iy));
+                                }
+                                const float x = fmaf(-y2[t], XS(s, t), XS(s, t));
+                                const float y = fmaf(-y2[t], YS(s, t), YS(s, t));
+                                XS(s, t) = fmaf(-yo[t], x, x) + ix;
+                                YS(s, t) = fmaf(-yo[t], y, y) + iy;
+                            }
+                        }
+                    } else if constexpr (EXACT) {
+                        // every pool turns by its own step, then the exact propagator
+                        float wx[P], wy[P];
+#pragma unroll
+                        for (int t = 0; t < P; ++t) {
+                            const float2 d = make_float2(DMX(s, t), DMY(s, t));
+                            wx[t] = px[t] + fmaf(d.x, px[t], -d.y * py[t]);
+                            wy[t] = py[t] + fmaf(d.x, py[t], d.y * px[t]);
+                        }
+#pragma unroll
+                        for (int t = 0; t < P; ++t) {
+                            float ix = 0.f, iy = 0.f;
+#pragma unroll
+                            for (int p = 0; p < P; ++p) {
+                                if (p == t) continue;
+                                const float2 f = fr[t][p];
+                                ix = fmaf(f.x, wx[p], fmaf(-f.y, wy[p], ix));
+                                iy = fmaf(f.x, wy[p], fmaf(f.y, wx[p], iy));
+                            }
+                            XS(s, t) = fmaf(-y2[t], wx[t], wx[t]) + ix;
+                            YS(s, t) = fmaf(-y2[t], wy[t], wy[t]) + iy;
                         }
                     } else {
 #pragma unroll
                         for (int t = 0; t < P; ++t) {
                             if (!has_frame<MODEL>(t)) continue;
-                            float ix = 0.f, iy = 0.f;
+                            float2 d = make_float2(DMX(s, t), DMY(s, t));
+                            if (MODEL == KM_EXCH) {  // self exchange (a nonzero K diagonal)
+                                d.x += fr[t][t].x;
+                                d.y += fr[t][t].y;
+                            }
+                            float ix = fmaf(d.x, px[t], -d.y * py[t]);
+                            float iy = fmaf(d.x, py[t], d.y * px[t]);
 #pragma unroll
                             for (int p = 0; p < P; ++p) {
+                                if (p == t || !has_frame<MODEL>(p)) continue;
+                                if (MODEL == KM_NORMAL || MODEL == KM_MT) continue;
                                 if (MODEL == KM_CEST && !((t == 0 && p >= 2) || (t >= 2 && p == 0))) continue;
                                 const float2 f = fr[t][p];
                                 ix = fmaf(f.x, px[p], fmaf(-f.y, py[p], ix));
                                 iy = fmaf(f.x, py[p], fmaf(f.y, px[p], iy));
                             }
-                            const float x = fmaf(-y2[t], XS(s, t), XS(s, t));
-                            const float y = fmaf(-y2[t], YS(s, t), YS(s, t));
-                            XS(s, t) = fmaf(-yo[t], x, x) + ix;
-                            YS(s, t) = fmaf(-yo[t], y, y) + iy;
+                            XS(s, t) = px[t] + ix;
+                            YS(s, t) = py[t] + iy;
                         }
                     }
-                } else if constexpr (EXACT) {
-                    // every pool turns by its own step, then the exact propagator
-                    float wx[P], wy[P];
+                    // ---- longitudinal (and the bound pools) -----------------------
+                    if (MODEL == KM_NORMAL) {
 #pragma unroll
-                    for (int t = 0; t < P; ++t) {
-                        const float2 d = make_float2(DMX(s, t), DMY(s, t));
-                        wx[t] = px[t] + fmaf(d.x, px[t], -d.y * py[t]);
-                        wy[t] = py[t] + fmaf(d.x, py[t], d.y * px[t]);
-                    }
+                        for (int t = 0; t < P; ++t) ZS(s, t) = fmaf(y1[t], rhoS[t] - ZS(s, t), ZS(s, t));
+                    } else if (MODEL == KM_EXCH && EXACT) {
 #pragma unroll
-                    for (int t = 0; t < P; ++t) {
-                        float ix = 0.f, iy = 0.f;
+                        for (int t = 0; t < kXP; ++t) {
+                            float iz = 0.f;
 #pragma unroll
-                        for (int p = 0; p < P; ++p) {
-                            if (p == t) continue;
-                            const float2 f = fr[t][p];
-                            ix = fmaf(f.x, wx[p], fmaf(-f.y, wy[p], ix));
-                            iy = fmaf(f.x, wy[p], fmaf(f.y, wx[p], iy));
+                            for (int p = 0; p < kXP; ++p) iz = fmaf(fL[t][p], pz[p], iz);
+                            const float z = ZS(s, t);
+                            ZS(s, t) = fmaf(-y1[t], z, z) + iz + cL[t];
                         }
-                        XS(s, t) = fmaf(-y2[t], wx[t], wx[t]) + ix;
-                        YS(s, t) = fmaf(-y2[t], wy[t], wy[t]) + iy;
-                    }
-                } else {
+                    } else if (MODEL == KM_EXCH) {
 #pragma unroll
-                    for (int t = 0; t < P; ++t) {
-                        if (!has_frame<MODEL>(t)) continue;
-                        float2 d = make_float2(DMX(s, t), DMY(s, t));
-                        if (MODEL == KM_EXCH) {  // self exchange (a nonzero K diagonal)
-                            d.x += fr[t][t].x;
-                            d.y += fr[t][t].y;
+                        for (int t = 0; t < P; ++t) {
+                            float iz = 0.f;
+#pragma unroll
+                            for (int p = 0; p < P; ++p) iz = fmaf(fin[t][p], pz[p], iz);
+                            float z = ZS(s, t);
+                            if (!FREE && rf) z = fmaf(-sat[t], z, z);
+                            // one rounding of the state (as the packed free step)
+                            const float yd = fmaf(-y1[t], yo[t], y1[t] + yo[t]);
+                            ZS(s, t) = z + fmaf(-yd, z, fmaf(rhoS[t], y1[t], iz));
                         }
-                        float ix = fmaf(d.x, px[t], -d.y * py[t]);
-                        float iy = fmaf(d.x, py[t], d.y * px[t]);
+                    } else {  // MT / CEST
+                        const float zb0 = pz[1], z0 = pz[0];
+                        float z = ZS(s, 0);
+                        if (MODEL == KM_MT) {
+                            z = fmaf(-mt_y1k, z, z) + rhoS[0] * y1[0] + zb0 * mt_y21;
+                        } else {
+                            float iz = 0.f;
 #pragma unroll
-                        for (int p = 0; p < P; ++p) {
-                            if (p == t || !has_frame<MODEL>(p)) continue;
-                            if (MODEL == KM_NORMAL || MODEL == KM_MT) continue;
-                            if (MODEL == KM_CEST && !((t == 0 && p >= 2) || (t >= 2 && p == 0))) continue;
-                            const float2 f = fr[t][p];
-                            ix = fmaf(f.x, px[p], fmaf(-f.y, py[p], ix));
-                            iy = fmaf(f.x, py[p], fmaf(f.y, px[p], iy));
+                            for (int t = 2; t < P; ++t) iz = fmaf(fin[0][t], pz[t], iz);
+                            z = fmaf(-mt_y1k, z, z);
+                            z = fmaf(-yo[0], z, z) + iz + zb0 * mt_y21 + rhoS[0] * y1[0];
+#pragma unroll
+                            for (int t = 2; t < P; ++t) {
+                                const float cz = fmaf(-y1[t], ZS(s, t), ZS(s, t));
+                                ZS(s, t) = fmaf(-yo[t], cz, cz) + fin[t][0] * z0 + rhoS[t] * y1[t];
+                            }
                         }
-                        XS(s, t) = px[t] + ix;
-                        YS(s, t) = py[t] + iy;
+                        float bz = zb0;
+                        if (rf) bz = fmaf(-sat[1], bz, bz);
+                        ZS(s, 1) = fmaf(-mt_y1bk, bz, bz) + rhoS[1] * mt_y1b + z0 * mt_y12;
+                        ZS(s, 0) = z;
                     }
-                }
-                // ---- longitudinal (and the bound pools) -----------------------
-                if (MODEL == KM_NORMAL) {
-#pragma unroll
-                    for (int t = 0; t < P; ++t) ZS(s, t) = fmaf(y1[t], rhoS[t] - ZS(s, t), ZS(s, t));
-                } else if (MODEL == KM_EXCH && EXACT) {
-#pragma unroll
-                    for (int t = 0; t < kXP; ++t) {
-                        float iz = 0.f;
-#pragma unroll
-                        for (int p = 0; p < kXP; ++p) iz = fmaf(fL[t][p], pz[p], iz);
-                        const float z = ZS(s, t);
-                        ZS(s, t) = fmaf(-y1[t], z, z) + iz + cL[t];
-                    }
-                } else if (MODEL == KM_EXCH) {
-#pragma unroll
-                    for (int t = 0; t < P; ++t) {
-                        float iz = 0.f;
-#pragma unroll
-                        for (int p = 0; p < P; ++p) iz = fmaf(fin[t][p], pz[p], iz);
-                        float z = ZS(s, t);
-                        if (!FREE && rf) z = fmaf(-sat[t], z, z);
-                        // one rounding of the state (as the packed free step)
-                        const float yd = fmaf(-y1[t], yo[t], y1[t] + yo[t]);
-                        ZS(s, t) = z + fmaf(-yd, z, fmaf(rhoS[t], y1[t], iz));
-                    }
-                } else {  // MT / CEST
-                    const float zb0 = pz[1], z0 = pz[0];
-                    float z = ZS(s, 0);
-                    if (MODEL == KM_MT) {
-                        z = fmaf(-mt_y1k, z, z) + rhoS[0] * y1[0] + zb0 * mt_y21;
-                    } else {
-                        float iz = 0.f;
-#pragma unroll
-                        for (int t = 2; t < P; ++t) iz = fmaf(fin[0][t], pz[t], iz);
-                        z = fmaf(-mt_y1k, z, z);
-                        z = fmaf(-yo[0], z, z) + iz + zb0 * mt_y21 + rhoS[0] * y1[0];
-#pragma unroll
-                        for (int t = 2; t < P; ++t) {
-                            const float cz = fmaf(-y1[t], ZS(s, t), ZS(s, t));
-                            ZS(s, t) = fmaf(-yo[t], cz, cz) + fin[t][0] * z0 + rhoS[t] * y1[t];
-                        }
-                    }
-                    float bz = zb0;
-                    if (rf) bz = fmaf(-sat[1], bz, bz);
-                    ZS(s, 1) = fmaf(-mt_y1bk, bz, bz) + rhoS[1] * mt_y1b + z0 * mt_y12;
-                    ZS(s, 0) = z;
                 }
             }
         }
