@@ -386,9 +386,12 @@ bool voxel_active(const mrl_scan_args &a, int km, long long v, long long V) {
 // object and of the results go through a pinned buffer of the calling
 // thread instead: its host side is copied by several threads at once and
 // the DMA runs from pinned memory (pageable copies of the 150 MB object and
-// 100 MB of results took 20-30 ms each way).  Below kStageMin bytes a copy
-// goes directly.
-constexpr size_t kStageMin = 8u << 20;
+// 100 MB of results took 20-30 ms each way).  Below stage_min() bytes (8 MB,
+// or MRL_STAGE_MIN_MB) a copy goes directly.
+size_t stage_min() {
+    const char *e = getenv("MRL_STAGE_MIN_MB");
+    return e ? (size_t)(std::max(0.0, atof(e)) * 1048576.0) : (size_t)(8u << 20);
+}
 struct HostCopy {
     void *dst;
     const void *src;
@@ -756,7 +759,7 @@ struct Scanner {
         // large objects: the pieces copied into the pinned stage in place (one
         // DMA of the whole raw buffer; the stage is free again after the
         // synchronisation below)
-        float *stage = rtot * sizeof(float) >= kStageMin ? static_cast<float *>(t_stage.get(rtot * sizeof(float)))
+        float *stage = rtot * sizeof(float) >= stage_min() ? static_cast<float *>(t_stage.get(rtot * sizeof(float)))
                                                          : nullptr;
         if (stage) {
             std::vector<HostCopy> jobs;
@@ -839,7 +842,7 @@ struct Scanner {
         // large states: the three (padded, consecutive) raw arrays in one DMA
         // into the pinned stage, then copied out on several threads
         const size_t span = (size_t)(raw.mz + PSV - raw.mx);
-        float *stage = 3 * PSV * sizeof(float) >= kStageMin ? static_cast<float *>(t_stage.get(span * sizeof(float)))
+        float *stage = 3 * PSV * sizeof(float) >= stage_min() ? static_cast<float *>(t_stage.get(span * sizeof(float)))
                                                             : nullptr;
         if (stage) {
             if (e == cudaSuccess) e = cudaMemcpyAsync(stage, raw.mx, span * sizeof(float), cudaMemcpyDeviceToHost, st);
@@ -872,7 +875,7 @@ struct Scanner {
         const size_t rows = (size_t)P * RX, wb = (size_t)(a1 - a0) * sizeof(double);
         // large signals: both into the pinned stage ([Sx rows][Sy rows], packed),
         // then copied out on several threads
-        char *stage = 2 * rows * wb >= kStageMin ? static_cast<char *>(t_stage.get(2 * rows * wb)) : nullptr;
+        char *stage = 2 * rows * wb >= stage_min() ? static_cast<char *>(t_stage.get(2 * rows * wb)) : nullptr;
         cudaError_t e;
         if (stage) {
             e = cudaMemcpy2DAsync(stage, wb, d_sx.p + a0, pitch, wb, rows, cudaMemcpyDeviceToHost, st);

@@ -132,6 +132,22 @@ def test_inplace_scan_writes_the_callers_arrays(built):
     np.testing.assert_array_equal(np.asarray(run.VObj["Mz"]).reshape(-1, order="F"), ref["Mz"])
 
 
+def test_pinned_staging_matches_direct_copies(built, monkeypatch):
+    """Objects and results above MRL_STAGE_MIN_MB (8 MB by default) travel
+    through the calling thread's pinned buffer; staged and direct copies give
+    the same outputs, also when that buffer grows between calls."""
+    small = phantoms.small_multipool("me", seed=7, n=8, pools=2, spins=2, coils=3, n_tr=2)
+    large = phantoms.small_multipool("me", seed=8, n=16, nz=2, pools=2, spins=2, coils=3, n_tr=2)
+    monkeypatch.setenv("MRL_STAGE_MIN_MB", "100000")  # every copy direct
+    ref = [engine.scan(sc) for sc in (small, large)]
+    monkeypatch.setenv("MRL_STAGE_MIN_MB", "0")  # every copy staged
+    for _ in range(2):
+        for sc, r in zip((small, large), ref):
+            out = engine.scan(sc)
+            for k in ("Sx", "Sy", "Kx", "Mx", "My", "Mz"):
+                np.testing.assert_array_equal(out[k], r[k])
+
+
 def test_ext_plugin_callback(built):
     """An Ext plugin that spoils the transverse magnetisation (DoExtPlugin
     case 6) sees the state after the step that starts at the Ext sample."""
