@@ -1005,6 +1005,8 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
             if (flags & kFlagAdc) {
 #pragma unroll
                 for (int t = 0; t < kNSampP; ++t) {
+                    const int rank = kRank ? F.samp_rank[t] : t;
+                    if (kRank && rank < 0) continue;  // a pool with no tile row (block-uniform)
                     float sx = 0.f, sy = 0.f;
 #pragma unroll
                     for (int s = 0; s < NS; ++s) {
@@ -1013,7 +1015,6 @@ __device__ __forceinline__ bool scan_item(const FastLaunch &F, int tile, unsigne
                     }
                     float2 m = cmul(make_float2(sx, sy), Pc[t]);
                     if (!active) m = make_float2(0.f, 0.f);
-                    const int rank = kRank ? F.samp_rank[t] : t;
                     if constexpr (tcr) {
                         // the voxel's sum over its threads, written by its first
                         // thread as the TF32 big and small parts of Re and Im
