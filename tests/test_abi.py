@@ -142,3 +142,18 @@ def test_adjoint_without_gpu_fails_loudly(built):
     with pytest.raises(engine.ScanError) as e:
         engine.adjoint(sc, np.zeros(1), np.zeros(1))
     assert e.value.status in (-7, -2)
+
+
+def test_inplace_host_scan_aliases_the_callers_arrays(built):
+    """HostScan(inplace=True) binds the caller's own state and signal arrays
+    (the engine writes them, as the mex layer writes the MATLAB globals);
+    the default binds copies and leaves the caller's arrays alone."""
+    sc = phantoms.small_multipool("me", seed=3, n=4, pools=2, spins=2, coils=2, n_tr=1)
+    hs = engine.HostScan(sc, inplace=True)
+    for key, arr in (("mx", sc.VObj["Mx"]), ("mz", sc.VObj["Mz"]), ("sx", sc.VSig["Sx"]), ("sy", sc.VSig["Sy"])):
+        assert np.shares_memory(hs.keep[key], arr), key
+    hc = engine.HostScan(sc)
+    for key, arr in (("mx", sc.VObj["Mx"]), ("sx", sc.VSig["Sx"])):
+        assert not np.shares_memory(hc.keep[key], arr), key
+    # read-only inputs alias the caller's arrays either way
+    assert np.shares_memory(hc.keep["rho"], sc.VObj["Rho"])
