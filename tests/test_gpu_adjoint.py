@@ -214,7 +214,8 @@ def test_adjoint_two_level_checkpoints(built, monkeypatch):
             assert err <= 1e-4
 
 
-@pytest.mark.parametrize("case", ["gre", "me3", "gm_bound", "bssfp", "mt", "cest3", "tx2", "tx3", "mt_epi_s4"])
+@pytest.mark.parametrize("case", ["gre", "me3", "gm_bound", "bssfp", "mt", "cest3", "tx2", "tx3", "mt_epi_s4",
+                                  "me3_s2_rx8", "me1_s4_rx8"])
 def test_adjoint_vs_fp64_adjoint(built, case):
     """The FP32 adjoint kernel against the FP64 reference gradient
     (oracle.adjoint64: the oracle's map in float64, differentiated by
@@ -239,7 +240,10 @@ def test_adjoint_vs_fp64_adjoint(built, case):
           "tx3": lambda: phantoms.multi_tx_gre(seed=48, n=6, n_tr=2, tx_coils=3, rx_coils=3),
           # 4 spins, 12 coils: the four lanes of a voxel split its receive term
           "mt_epi_s4": lambda: phantoms.config5_mt_epi(seed=49, nx=4, ny=4, nz=1, spins=4, n_coils=12, n_read=8,
-                                                       n_pe=8)}[case]()
+                                                       n_pe=8),
+          # the split in the free three-pool and one-pool instantiations
+          "me3_s2_rx8": lambda: phantoms.small_multipool("me", seed=50, n=4, pools=3, spins=2, coils=8, n_tr=2),
+          "me1_s4_rx8": lambda: phantoms.small_multipool("me", seed=51, n=4, pools=1, spins=4, coils=8, n_tr=2)}[case]()
     sc = _phase_modulated(sc, 12)
     tx, ty = _target(sc)
     _, gx, gy = _loss(sc, (tx, ty))
